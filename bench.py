@@ -1,0 +1,431 @@
+#!/usr/bin/env python
+"""Throughput of the SNCH-LBVH hot path on GB300 (queries/s, walk-on-stars query set).
+
+Workload (one "step"): on the seeded two-million-triangle scene (64 noisy tori
+and icospheres in the unit cube, 1,993,600 triangles), rebuild the silhouette
+topology and the LBVH, then run 16M nearest-primitive, 16M nearest-silhouette
+and 16M ray queries and 4M SampleTriangleInSphere draws.
+
+  value  = queries per second of the whole step, device-timed with CUDA events
+           on the launching stream, inputs resident in HBM (N ranks: sum over
+           ranks / max rank time; each rank runs the full step: weak scaling);
+  e2e    = the same through the host-buffer C-ABI calls (scene upload, build,
+           snch_*_host queries with their H2D/D2H copies) on pinned host memory;
+  roofline = algorithmic bytes of the dominant query kernel (visits counted by
+           the instrumented CPU restatement on a sample) / its event time;
+  cpu_baseline = the CPU restatement (oracle/) on the host cores, bounded sample.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--scale F]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+FULL = {"near": 16_000_000, "sil": 16_000_000, "ray": 16_000_000, "smp": 4_000_000}
+KERNEL_OF = {"near": "nearest_kernel", "sil": "silhouette_kernel", "ray": "ray_kernel", "smp": "sample_kernel"}
+# algorithmic bytes per query (reference layout, counted from the reference-order
+# traversal): input + output + per expanded internal node + per leaf (+ per edge)
+BYTES_IO = {"near": 12 + 8, "sil": 13 + 8, "ray": 28 + 20, "smp": 20 + 8}
+BYTES_NODE = {"near": 56, "sil": 96, "ray": 56, "smp": 56}
+BYTES_LEAF = {"near": 48, "sil": 12, "ray": 48, "smp": 52}
+BYTES_EDGE = 64
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--scale", type=float, default=1.0, help="fraction of the query batches (1.0 = full workload)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    return ws, int(os.environ.get("RANK", "0")), int(os.environ.get("LOCAL_RANK", "0"))
+
+
+def workload_name(counts, ntri):
+    return (f"wost_2m: {ntri:,} triangles (64 noisy tori + icospheres in the unit cube); step = silhouette "
+            f"topology + LBVH build + {counts['near']:,} nearest + {counts['sil']:,} silhouette + "
+            f"{counts['ray']:,} ray + {counts['smp']:,} sphere-sample queries")
+
+
+def make_workload(scale, seed):
+    from snch_lbvh_gb300 import meshes
+    sc = meshes.wost_scene(seed=0)
+    counts = {k: max(1, int(v * scale)) for k, v in FULL.items()}
+    q = meshes.wost_queries(counts["near"], counts["sil"], counts["ray"], counts["smp"], seed=seed)
+    return sc, counts, q
+
+
+# --------------------------------------------------------------------- clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index):
+        self.rows, self.proc, self.device_index = [], None, device_index
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device_index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([c.strip() for c in line.split(",")])
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm = [float(r[1]) for r in self.rows if len(r) >= 9 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) >= 9 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows if len(r) >= 9 for i in range(4) if "Active" in r[5 + i]})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(sm)}
+
+
+# --------------------------------------------------------------------- peaks
+def hbm_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "of measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "of fallback"
+
+
+def traffic_of(kernel, workload_key):
+    """Per-launch DRAM bytes of `kernel` from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "traffic.txt")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        parts = line.split()
+        if len(parts) >= 3 and not line.startswith("#") and parts[0] == kernel and parts[1] == workload_key:
+            return float(parts[2])
+    return None
+
+
+# --------------------------------------------------------------------- CPU restatement
+def cpu_sample_counts(counts, frac):
+    return {k: max(256, int(v * frac)) for k, v in counts.items()}
+
+
+def run_cpu(sc, q, counts, frac, nthreads):
+    """Times the CPU restatement: single-threaded build + a bounded sample of each
+    query batch on nthreads threads. Returns per-type q/s, build seconds, and
+    mean visit counts (for the algorithmic-bytes roofline)."""
+    from oracle import oracle
+    oracle.build()
+    t0 = time.perf_counter()
+    tree = oracle.Tree(sc.verts, sc.faces)
+    build_s = time.perf_counter() - t0
+    sc_n = cpu_sample_counts(counts, frac)
+    out, stats = {}, {}
+    t0 = time.perf_counter()
+    _, _, st = tree.nearest(q["near_pts"][:sc_n["near"]], stats=True, nthreads=nthreads)
+    out["near"] = sc_n["near"] / (time.perf_counter() - t0)
+    stats["near"] = st.mean(0)
+    t0 = time.perf_counter()
+    _, _, st = tree.silhouette(q["sil_pts"][:sc_n["sil"]], q["sil_flip"][:sc_n["sil"]], stats=True, nthreads=nthreads)
+    out["sil"] = sc_n["sil"] / (time.perf_counter() - t0)
+    stats["sil"] = st.mean(0)
+    t0 = time.perf_counter()
+    *_, st = tree.ray(q["ray_o"][:sc_n["ray"]], q["ray_d"][:sc_n["ray"]], q["ray_tmax"][:sc_n["ray"]], stats=True,
+                      nthreads=nthreads)
+    out["ray"] = sc_n["ray"] / (time.perf_counter() - t0)
+    stats["ray"] = st.mean(0)
+    t0 = time.perf_counter()
+    *_, st = tree.sample(q["smp_c"][:sc_n["smp"]], q["smp_r"][:sc_n["smp"]], q["smp_u"][:sc_n["smp"]], stats=True,
+                         nthreads=nthreads)
+    out["smp"] = sc_n["smp"] / (time.perf_counter() - t0)
+    stats["smp"] = st.mean(0)
+    step_s = build_s + sum(counts[k] / out[k] for k in counts)
+    total = sum(counts.values())
+    return {"qps": out, "build_s": build_s, "step_s": step_s, "value": total / step_s, "stats": stats,
+            "sample": sc_n}
+
+
+def algorithmic_bytes(kind, st):
+    b = BYTES_IO[kind] + BYTES_NODE[kind] * st[0] + BYTES_LEAF[kind] * st[1]
+    if kind == "sil":
+        b += BYTES_EDGE * st[2]
+    return float(b)
+
+
+def cpu_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+# --------------------------------------------------------------------- reference arm
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    sc, counts, q = make_workload(args.scale, seed=1)
+    nthreads = cpu_threads()
+    frac = 0.01
+    # warmup steps are short: the build is the expensive part and is repeated
+    vals = []
+    for i in range(args.warmup + args.steps):
+        r = run_cpu(sc, q, counts, frac if i >= args.warmup else 0.001, nthreads)
+        if i >= args.warmup:
+            vals.append(r)
+    value = float(np.mean([r["value"] for r in vals]))
+    step_ms = float(np.mean([r["step_s"] for r in vals]) * 1e3)
+    smp = vals[-1]["sample"]
+    line = {
+        "impl": "reference", "metric": "queries/sec (walk-on-stars query set: nearest, silhouette, ray, sphere "
+        "sample) on the 2M-triangle scene", "value": value, "unit": "queries/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+        "config": {"workload": workload_name(counts, len(sc.faces)), "backend": "cpu"},
+        "per_type_qps": {k: float(np.mean([r["qps"][k] for r in vals])) for k in counts},
+        "cpu_baseline": {"value": value, "unit": "queries/s", "cores": nthreads, "kind": "port",
+                         "sample": f"per step: single-thread build of the {len(sc.faces):,}-triangle scene + "
+                                   f"{smp['near']:,} nearest, {smp['sil']:,} silhouette, {smp['ray']:,} ray, "
+                                   f"{smp['smp']:,} sample queries on {nthreads} threads, each type "
+                                   f"extrapolated to its full batch"},
+        "e2e": {"value": value, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# --------------------------------------------------------------------- our arm
+def run_ours(args):
+    import torch
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    import snch_lbvh_gb300 as snch
+    L = snch.lib()
+
+    sc, counts, q = make_workload(args.scale, seed=1 + rank)
+    dev = {k: torch.from_numpy(np.ascontiguousarray(v)).cuda() for k, v in q.items()}
+    n = counts
+    out = {
+        "near": (torch.empty(n["near"], dtype=torch.int32, device="cuda"),
+                 torch.empty(n["near"], dtype=torch.float32, device="cuda")),
+        "sil": (torch.empty(n["sil"], dtype=torch.float32, device="cuda"),
+                torch.empty(n["sil"], dtype=torch.int32, device="cuda")),
+        "ray": (torch.empty(n["ray"], dtype=torch.uint8, device="cuda"),
+                torch.empty(n["ray"], dtype=torch.float32, device="cuda"),
+                torch.empty((n["ray"], 2), dtype=torch.float32, device="cuda"),
+                torch.empty(n["ray"], dtype=torch.int32, device="cuda")),
+        "smp": (torch.empty(n["smp"], dtype=torch.int32, device="cuda"),
+                torch.empty(n["smp"], dtype=torch.float32, device="cuda")),
+    }
+    verts_d = torch.from_numpy(sc.verts).cuda()
+    faces_d = torch.from_numpy(sc.faces).cuda()
+    scene = snch.Scene(verts_d, faces_d)
+    stream = torch.cuda.current_stream()
+
+    def step(ev=None):
+        if ev:
+            ev[0].record(stream)
+        scene.compute_silhouettes()
+        scene.build_bvh()
+        if ev:
+            ev[1].record(stream)
+        scene.query_nearest(dev["near_pts"], out=out["near"])
+        if ev:
+            ev[2].record(stream)
+        scene.query_silhouette(dev["sil_pts"], dev["sil_flip"], out=out["sil"])
+        if ev:
+            ev[3].record(stream)
+        scene.query_ray(dev["ray_o"], dev["ray_d"], dev["ray_tmax"], out=out["ray"])
+        if ev:
+            ev[4].record(stream)
+        scene.sample_in_sphere(dev["smp_c"], dev["smp_r"], dev["smp_u"], out=out["smp"])
+        if ev:
+            ev[5].record(stream)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if ws > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(max(args.warmup, 0)):
+        step()
+    barrier()
+    status = scene.device_status()
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(6)] for _ in range(args.steps)]
+    clocks = ClockSampler(torch.cuda.current_device() if "CUDA_VISIBLE_DEVICES" not in os.environ
+                          else os.environ["CUDA_VISIBLE_DEVICES"].split(",")[local])
+    clocks.start()
+    time.sleep(0.3)
+    launches0 = L.snch_kernel_launch_count()
+    barrier()
+    t_start = torch.cuda.Event(enable_timing=True)
+    t_end = torch.cuda.Event(enable_timing=True)
+    t_start.record(stream)
+    for k in range(args.steps):
+        step(evs[k])
+    t_end.record(stream)
+    barrier()
+    launches = L.snch_kernel_launch_count() - launches0
+    clk = clocks.stop()
+    status |= scene.device_status()
+    elapsed_ms = t_start.elapsed_time(t_end)
+    if ws > 1:
+        import torch.distributed as dist
+        t = torch.tensor([elapsed_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed_ms = float(t.item())
+    phase_ms = np.array([[e[i].elapsed_time(e[i + 1]) for i in range(5)] for e in evs]).mean(0)
+    total_q = sum(counts.values())
+    value = total_q * ws * args.steps / (elapsed_ms / 1e3)
+    per_type = {k: counts[k] / (phase_ms[i + 1] / 1e3) for i, k in enumerate(["near", "sil", "ray", "smp"])}
+
+    # ---- e2e through the host-buffer C ABI
+    e2e = None
+    if not args.no_e2e:
+        pin = {k: torch.from_numpy(np.ascontiguousarray(v)).pin_memory().numpy() for k, v in q.items()}
+        pin_v = torch.from_numpy(sc.verts).pin_memory().numpy()
+        pin_f = torch.from_numpy(sc.faces).pin_memory().numpy()
+        hout = {
+            "near": (torch.empty(n["near"], dtype=torch.int32).pin_memory().numpy().view(np.uint32),
+                     torch.empty(n["near"], dtype=torch.float32).pin_memory().numpy()),
+            "sil": (torch.empty(n["sil"], dtype=torch.float32).pin_memory().numpy(),
+                    torch.empty(n["sil"], dtype=torch.int32).pin_memory().numpy()),
+            "ray": (torch.empty(n["ray"], dtype=torch.uint8).pin_memory().numpy(),
+                    torch.empty(n["ray"], dtype=torch.float32).pin_memory().numpy(),
+                    torch.empty((n["ray"], 2), dtype=torch.float32).pin_memory().numpy(),
+                    torch.empty(n["ray"], dtype=torch.int32).pin_memory().numpy().view(np.uint32)),
+            "smp": (torch.empty(n["smp"], dtype=torch.int32).pin_memory().numpy(),
+                    torch.empty(n["smp"], dtype=torch.float32).pin_memory().numpy()),
+        }
+
+        def e2e_step():
+            s = snch.Scene(pin_v, pin_f)
+            s.compute_silhouettes()
+            s.build_bvh()
+            s.query_nearest_host(pin["near_pts"], out=hout["near"])
+            s.query_silhouette_host(pin["sil_pts"], pin["sil_flip"], out=hout["sil"])
+            s.query_ray_host(pin["ray_o"], pin["ray_d"], pin["ray_tmax"], out=hout["ray"])
+            s.sample_in_sphere_host(pin["smp_c"], pin["smp_r"], pin["smp_u"], out=hout["smp"])
+            s.close()
+
+        e2e_steps = max(1, min(args.steps, 3))
+        e2e_step()
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            e2e_step()
+        barrier()
+        e2e_s = time.perf_counter() - t0
+        if ws > 1:
+            import torch.distributed as dist
+            t = torch.tensor([e2e_s], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            e2e_s = float(t.item())
+        h2d = sc.verts.nbytes + sc.faces.nbytes + sum(v.nbytes for v in q.values())
+        d2h = sum(a.nbytes for v in hout.values() for a in v)
+        e2e = {"value": total_q * ws * e2e_steps / e2e_s, "unit": "queries/s", "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": int(d2h), "steps": e2e_steps,
+               "note": "scene upload + build + snch_*_host queries from pinned host memory, wall clock"}
+
+    if rank != 0:
+        if ws > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+        return
+
+    # ---- CPU baseline (rank 0, N = 1): also yields the visit counts of the roofline
+    cpu = None
+    if ws == 1 and not args.no_cpu_baseline:
+        cpu = run_cpu(sc, q, counts, 0.005, cpu_threads())
+    kinds = ["near", "sil", "ray", "smp"]
+    dom = kinds[int(np.argmax(phase_ms[1:]))]
+    peak, peak_src = hbm_peak()
+    roof = None
+    if cpu is not None:
+        bytes_per_launch = algorithmic_bytes(dom, cpu["stats"][dom]) * counts[dom]
+        achieved = bytes_per_launch / (phase_ms[1 + kinds.index(dom)] / 1e3) / 1e9
+        roof = {"bound": "hbm", "kernel": KERNEL_OF[dom], "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_source": peak_src,
+                "algorithmic_bytes_per_query": algorithmic_bytes(dom, cpu["stats"][dom]),
+                "traffic": traffic_of(KERNEL_OF[dom], "wost_2m"),
+                "per_kernel": {KERNEL_OF[k]: {"ms": float(phase_ms[1 + i]),
+                                              "bytes_per_query": algorithmic_bytes(k, cpu["stats"][k]),
+                                              "GB/s": algorithmic_bytes(k, cpu["stats"][k]) * counts[k]
+                                              / (phase_ms[1 + i] / 1e3) / 1e9,
+                                              "visits_per_query": [float(x) for x in cpu["stats"][k]]}
+                               for i, k in enumerate(kinds)}}
+    line = {
+        "metric": "queries/sec (walk-on-stars query set: nearest, silhouette, ray, sphere sample) on the 2M-triangle "
+                  "scene", "value": value, "unit": "queries/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded meshes and queries)",
+        "config": {"workload": workload_name(counts, len(sc.faces)),
+                   "l2": "inputs larger than L2: 192 MB per 16M-query array, >1 GB of tree records",
+                   "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
+        "per_type_qps": {k: float(v) for k, v in per_type.items()},
+        "phase_ms": {"build": float(phase_ms[0]), **{k: float(phase_ms[1 + i]) for i, k in enumerate(kinds)}},
+        "gpu_launches": int(launches),
+        "device_status": int(status),
+        "clocks": clk,
+        "roofline": roof,
+        "e2e": e2e,
+    }
+    if cpu is not None:
+        smp = cpu["sample"]
+        line["cpu_baseline"] = {"value": cpu["value"], "unit": "queries/s", "cores": cpu_threads(), "kind": "port",
+                                "sample": f"single-thread build of the {len(sc.faces):,}-triangle scene + "
+                                          f"{smp['near']:,} nearest, {smp['sil']:,} silhouette, {smp['ray']:,} ray, "
+                                          f"{smp['smp']:,} sample queries, each type extrapolated to its batch",
+                                "per_type_qps": {k: float(v) for k, v in cpu["qps"].items()},
+                                "build_s": cpu["build_s"]}
+    print(json.dumps(line), flush=True)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,184 @@
+/*
+ * snch_gb300.h -- C ABI of the GB300-native SNCH-LBVH (libsnch_gb300.so).
+ *
+ * Drop-in boundary for the LBVH build + query path of tyanyuy3125/snch-lbvh,
+ * whose interface is header-only C++ (include/snch_lbvh/scene.cuh,
+ * core/bvh.cuh, core/query.cuh, core/sample.cuh). Every entry point below
+ * names the reference call it replaces. Conventions:
+ *   - plain pointers and sizes; no C++ or CUDA types in the signatures
+ *     (a stream is a cudaStream_t passed as void*, NULL = legacy default stream);
+ *   - "device" buffers live in GPU memory and are owned by the caller; the
+ *     scene owns its tree; "host" buffers are CPU memory (pinned for speed);
+ *   - every call returns an snch_status; snch_last_error() describes the
+ *     last failure of the calling thread; no exception crosses the boundary;
+ *   - query calls are asynchronous on the given stream, exactly like the
+ *     reference's per-thread device calls inside a user kernel;
+ *   - results are those of the reference's own code on the same inputs
+ *     (indices bit-exact, distances bit-exact except where CUDA's
+ *     transcendental functions enter the normal-cone tests).
+ */
+#ifndef SNCH_GB300_H
+#define SNCH_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct snch_scene_s *snch_scene_t;
+typedef void *snch_stream_t; /* cudaStream_t */
+
+typedef enum
+{
+    SNCH_OK = 0,
+    SNCH_ERR_INVALID_ARGUMENT = 1, /* null pointer, negative size, index out of range */
+    SNCH_ERR_CUDA = 2,             /* a CUDA runtime call failed (see snch_last_error) */
+    SNCH_ERR_NOT_BUILT = 3,        /* query before build: "BVH is not built yet." (scene.cuh:1250) */
+    SNCH_ERR_OUT_OF_MEMORY = 4,
+    SNCH_ERR_DEVICE_STATUS = 5,    /* a kernel reported a failure, see snch_get_device_status */
+    SNCH_ERR_TOO_LARGE = 6         /* more than 2^30 triangles, or a no-allocation limit exceeded */
+} snch_status;
+
+/* bits of the device status word (snch_get_device_status) */
+#define SNCH_DEVICE_STACK_OVERFLOW 1u   /* a traversal needed more than 64 stack entries       */
+#define SNCH_DEVICE_LOOKBACK_TIMEOUT 2u /* a bounded cross-block wait gave up (results invalid) */
+#define SNCH_DEVICE_HASH_FULL 4u        /* the edge hash table overflowed (results invalid)    */
+
+/* Reference-layout records, byte-compatible with the reference's device view
+ * (bvh.cuh:27-33 node, aabb.cuh:12-16 aabb<float,3>, cone.cuh:11-16 cone<float,3>,
+ * scene.cuh:708-722 silhouette_edge, scene.cuh:826-840 triangle,
+ * bvh.cuh:36-72 basic_device_bvh). */
+typedef struct { uint32_t parent_idx, left_idx, right_idx, object_idx; } snch_node;
+typedef struct { float upper[3], lower[3]; } snch_aabb;
+typedef struct { float axis[3], half_angle, radius; } snch_cone;
+typedef struct { int32_t indices[4]; const float *vertices; uint64_t pad_; } snch_silhouette_edge; /* 32 B */
+typedef struct
+{
+    int32_t vertex_indices[3];
+    int32_t silhouette_indices[3];
+    const float *vertices;                    /* float3 array */
+    const snch_silhouette_edge *silhouettes;  /* 40 B */
+} snch_triangle;
+typedef struct
+{
+    uint32_t num_nodes;   /* 2N-1 */
+    uint32_t num_objects; /* N    */
+    const snch_node *nodes;
+    const snch_aabb *aabbs;
+    const snch_cone *cones;
+    const snch_triangle *objects;
+} snch_bvh_view;
+
+/* ------------------------------------------------------------------ scene */
+
+/* lbvh::scene<3>(vertices_first, vertices_last, indices_first, indices_last)
+ * scene.cuh:1128-1133: host float3 vertices and int3 faces, copied to the GPU. */
+int snch_scene_create(const float *vertices_xyz, int64_t num_vertices, const int32_t *triangles,
+                      int64_t num_triangles, snch_scene_t *out_scene);
+
+/* Same from device buffers (no host round trip). */
+int snch_scene_create_device(const float *vertices_xyz, int64_t num_vertices, const int32_t *triangles,
+                             int64_t num_triangles, snch_scene_t *out_scene, snch_stream_t stream);
+
+/* scene<3>::compute_silhouettes() scene.cuh:1167-1204 (with assign_edge_indices 1135-1166),
+ * computed on the GPU: edge ids in first-seen order and the 4-vertex edge records. */
+int snch_compute_silhouettes(snch_scene_t scene, snch_stream_t stream);
+
+/* scene<3>::build_bvh() scene.cuh:1205-1229 -> bvh::construct() bvh.cuh:380-613:
+ * edge ownership, leaf boxes and cones, Morton codes, stable radix sort, Karras
+ * internal nodes, bottom-up AABB + normal-cone refit. Runs compute_silhouettes
+ * first if it has not been called. Asynchronous on `stream`. */
+int snch_build_bvh(snch_scene_t scene, snch_stream_t stream);
+
+/* scene<3>::get_bvh_device_ptr() scene.cuh:1242-1252: the tree in the
+ * reference's device layout (device pointers owned by the scene). */
+int snch_get_bvh_view(snch_scene_t scene, snch_bvh_view *out_view);
+
+/* ~scene: frees every device buffer of the scene. */
+int snch_scene_destroy(snch_scene_t scene);
+
+/* Sizes (synchronises the scene's build stream for num_edges). */
+int snch_scene_info(snch_scene_t scene, int64_t *num_vertices, int64_t *num_triangles, int64_t *num_edges);
+
+/* Device status word of the scene (OR of SNCH_DEVICE_* bits set by its
+ * kernels since the last reset); synchronises the given stream. */
+int snch_get_device_status(snch_scene_t scene, uint32_t *out_bits, int reset, snch_stream_t stream);
+
+/* Thread-local description of the last failure. */
+const char *snch_last_error(void);
+
+/* Copies of the build products into caller DEVICE buffers (parity checks):
+ * morton codes sorted (N), sorted original indices (N), nodes ((2N-1)*4),
+ * aabbs ((2N-1)*6), cones ((2N-1)*5); any pointer may be NULL. */
+int snch_export_tree(snch_scene_t scene, uint32_t *sorted_morton, uint32_t *sorted_indices, uint32_t *nodes,
+                     float *aabbs, float *cones, snch_stream_t stream);
+/* tri_edges (N*3), tri_owned (N*3), edge_verts (E*4) into caller DEVICE buffers. */
+int snch_export_topology(snch_scene_t scene, int32_t *tri_edges, int32_t *tri_owned, int32_t *edge_verts,
+                         snch_stream_t stream);
+
+/* ------------------------------------------------------------------ queries
+ * All buffers are DEVICE buffers of n entries (float3 = 3 packed floats). */
+
+/* query_device(bvh, nearest(p), scene<3>::distance_calculator()) query.cuh:239-318
+ * -> (object index, distance); index 0xFFFFFFFF and +inf for an empty scene. */
+int snch_query_nearest(snch_scene_t scene, const float *points_xyz, int64_t n, uint32_t *out_index,
+                       float *out_distance, snch_stream_t stream);
+
+/* query_device(bvh, nearest_silhouette(p, flip), silhouette_distance_calculator())
+ * query.cuh:326-423 -> distance (+inf if none). flip may be NULL (all false).
+ * out_edge (may be NULL) receives the silhouette edge id of the returned
+ * distance, which the reference does not report (query.cuh:386), or -1. */
+int snch_query_silhouette(snch_scene_t scene, const float *points_xyz, const uint8_t *flip, int64_t n,
+                          float *out_distance, int32_t *out_edge, snch_stream_t stream);
+
+/* query_device(bvh, ray_intersect(ray(o, d), tmax), intersect_test()) query.cuh:82-169
+ * -> (hit, t, uv (2 floats), object index); t = +inf, uv = 0, index 0xFFFFFFFF on a miss. */
+int snch_query_ray(snch_scene_t scene, const float *origins_xyz, const float *dirs_xyz, const float *tmax,
+                   int64_t n, uint8_t *out_hit, float *out_t, float *out_uv, uint32_t *out_index,
+                   snch_stream_t stream);
+
+/* sample_object_in_sphere(bvh, sphere_intersect(sphere(c, r)), intersect_sphere(),
+ * measurement_getter(), green_weight(), u) sample.cuh:26-91 -> (object index or -1,
+ * pdf; 0 when -1, where the reference leaves it unset). */
+int snch_sample_in_sphere(snch_scene_t scene, const float *centers_xyz, const float *radii, const float *u,
+                          int64_t n, int32_t *out_index, float *out_pdf, snch_stream_t stream);
+
+/* sample_on_object(bvh, idx, scene<3>::sample_on_object(), u, v) sample.cuh:10-22 ->
+ * point on triangle idx (original index). */
+int snch_sample_on_object(snch_scene_t scene, const int32_t *index, const float *u, const float *v, int64_t n,
+                          float *out_points_xyz, snch_stream_t stream);
+
+/* Host-buffer forms of the four queries: copy in, run, copy out in pipelined
+ * chunks on the scene's own streams; return when results are in host memory.
+ * This is the call shape of the reference's benchmark loop (benchmark.cu:395-409). */
+int snch_query_nearest_host(snch_scene_t scene, const float *points_xyz, int64_t n, uint32_t *out_index,
+                            float *out_distance);
+int snch_query_silhouette_host(snch_scene_t scene, const float *points_xyz, const uint8_t *flip, int64_t n,
+                               float *out_distance, int32_t *out_edge);
+int snch_query_ray_host(snch_scene_t scene, const float *origins_xyz, const float *dirs_xyz, const float *tmax,
+                        int64_t n, uint8_t *out_hit, float *out_t, float *out_uv, uint32_t *out_index);
+int snch_sample_in_sphere_host(snch_scene_t scene, const float *centers_xyz, const float *radii, const float *u,
+                               int64_t n, int32_t *out_index, float *out_pdf);
+
+/* ------------------------------------------------------------------ building blocks */
+
+/* Stable radix sort of (key, value) uint32 pairs on the low key_bits bits, in
+ * place on DEVICE buffers (the sort behind bvh.cuh:452-454). keys_tmp/vals_tmp
+ * are n-entry DEVICE buffers; scratch is snch_sort_scratch_bytes(n, key_bits)
+ * bytes of DEVICE memory. Asynchronous. */
+size_t snch_sort_scratch_bytes(int64_t n, int key_bits);
+int snch_sort_pairs(uint32_t *keys, uint32_t *values, uint32_t *keys_tmp, uint32_t *values_tmp, int64_t n,
+                    int key_bits, void *scratch, uint32_t *device_status, snch_stream_t stream);
+
+/* Number of kernels this library has launched in this process (all scenes). */
+uint64_t snch_kernel_launch_count(void);
+
+/* Library version string. */
+const char *snch_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SNCH_GB300_H */

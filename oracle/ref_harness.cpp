@@ -1,0 +1,217 @@
+// Driver around the UNMODIFIED reference headers (tyanyuy3125/snch-lbvh,
+// include/snch_lbvh/*.cuh) -- TEST INFRASTRUCTURE ONLY.
+//
+// Built by oracle/Makefile with g++ and Thrust's CPP (host) backend, so the
+// reference's own construction (bvh.cuh:380-613) and its own per-thread
+// query_device / sample functions (query.cuh, sample.cuh) run on the CPU of
+// this container and produce the golden vectors under tests/golden/.
+// The reference compiles as host C++ after three shims defined here:
+//   * atomicCAS / __threadfence used unguarded by the AABB refit (bvh.cuh:531, 548),
+//     restated for a single host thread;
+//   * thrust::min / thrust::max (bvh.cuh:125, 216, 220), absent from current CCCL;
+//   * unqualified max() in green_weight (scene.cuh:1123) resolved to std::max.
+// Where the reference leaves an output unset (sample pdf when no triangle is
+// hit, sample.cuh:46; ray uv on a miss, query.cuh:100) this driver writes 0.
+//
+// Input/output: raw little-endian files, layout documented in
+// tests/golden/make_golden.py (the only caller).
+#include <cuda_runtime.h>
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <iostream>
+#include <unordered_map>
+#include <vector>
+using std::max;
+using std::min;
+namespace thrust
+{
+    using std::max;
+    using std::min;
+}
+static inline int atomicCAS(int *address, int compare, int val)
+{
+    int old = *address;
+    if (old == compare)
+        *address = val;
+    return old;
+}
+static inline void __threadfence() {}
+
+#include "snch_lbvh/lbvh.cuh"
+#include "snch_lbvh/scene.cuh"
+
+namespace
+{
+    template <typename T>
+    bool read_n(FILE *f, std::vector<T> &v, int64_t n)
+    {
+        v.resize(static_cast<size_t>(n));
+        return n == 0 || fread(v.data(), sizeof(T), static_cast<size_t>(n), f) == static_cast<size_t>(n);
+    }
+    template <typename T>
+    void write_n(FILE *f, const T *p, int64_t n)
+    {
+        if (n > 0)
+            fwrite(p, sizeof(T), static_cast<size_t>(n), f);
+    }
+} // namespace
+
+int main(int argc, char **argv)
+{
+    if (argc != 3)
+    {
+        std::fprintf(stderr, "usage: %s in.bin out.bin\n", argv[0]);
+        return 2;
+    }
+    FILE *in = std::fopen(argv[1], "rb");
+    if (!in)
+        return 3;
+    int64_t hdr[7];
+    if (std::fread(hdr, sizeof(int64_t), 7, in) != 7)
+        return 4;
+    const int64_t nv = hdr[0], nt = hdr[1], n_near = hdr[2], n_sil = hdr[3], n_ray = hdr[4], n_smp = hdr[5],
+                  n_obj = hdr[6];
+    std::vector<float> verts, near_pts, sil_pts, ray_o, ray_d, ray_tmax, smp_c, smp_r, smp_u, obj_u, obj_v;
+    std::vector<int32_t> tris, obj_idx;
+    std::vector<uint8_t> sil_flip;
+    bool ok = read_n(in, verts, nv * 3) && read_n(in, tris, nt * 3) && read_n(in, near_pts, n_near * 3) &&
+              read_n(in, sil_pts, n_sil * 3) && read_n(in, sil_flip, n_sil) && read_n(in, ray_o, n_ray * 3) &&
+              read_n(in, ray_d, n_ray * 3) && read_n(in, ray_tmax, n_ray) && read_n(in, smp_c, n_smp * 3) &&
+              read_n(in, smp_r, n_smp) && read_n(in, smp_u, n_smp) && read_n(in, obj_idx, n_obj) &&
+              read_n(in, obj_u, n_obj) && read_n(in, obj_v, n_obj);
+    std::fclose(in);
+    if (!ok)
+        return 5;
+
+    std::vector<float3> v3(static_cast<size_t>(nv));
+    for (int64_t i = 0; i < nv; ++i)
+        v3[i] = make_float3(verts[3 * i], verts[3 * i + 1], verts[3 * i + 2]);
+    std::vector<int3> f3(static_cast<size_t>(nt));
+    for (int64_t i = 0; i < nt; ++i)
+        f3[i] = make_int3(tris[3 * i], tris[3 * i + 1], tris[3 * i + 2]);
+
+    lbvh::scene<3> sc(v3.data(), v3.data() + v3.size(), f3.data(), f3.data() + f3.size());
+    sc.compute_silhouettes();
+    sc.build_bvh();
+    const auto bvh = sc.get_bvh_device_ptr();
+
+    FILE *out = std::fopen(argv[2], "wb");
+    if (!out)
+        return 6;
+    const int64_t E = static_cast<int64_t>(sc.silhouettes_h.size());
+    const int64_t NN = bvh.num_nodes;
+    int64_t ohdr[2] = {E, NN};
+    write_n(out, ohdr, 2);
+    for (int64_t i = 0; i < nt; ++i)
+    {
+        int32_t e[3] = {sc.edge_indices_h[i].x, sc.edge_indices_h[i].y, sc.edge_indices_h[i].z};
+        write_n(out, e, 3);
+    }
+    for (int64_t i = 0; i < nt; ++i)
+    {
+        const auto &t = sc.triangles[i];
+        int32_t o[3] = {t.silhouette_indices.x, t.silhouette_indices.y, t.silhouette_indices.z};
+        write_n(out, o, 3);
+    }
+    for (int64_t e = 0; e < E; ++e)
+    {
+        const auto &s = sc.silhouettes_h[e];
+        int32_t q[4] = {s.indices.x, s.indices.y, s.indices.z, s.indices.w};
+        write_n(out, q, 4);
+    }
+    // Morton codes in original order, from the reference's own calculator and
+    // scene AABB (bvh.cuh:423-439).
+    {
+        using box_t = lbvh::aabb<float, 3>;
+        const float inf = std::numeric_limits<float>::infinity();
+        box_t whole;
+        whole.upper = make_float3(-inf, -inf, -inf);
+        whole.lower = make_float3(inf, inf, inf);
+        std::vector<box_t> boxes(static_cast<size_t>(nt));
+        for (int64_t i = 0; i < nt; ++i)
+        {
+            boxes[i] = lbvh::scene<3>::aabb_getter()(sc.triangles[i]);
+            whole = lbvh::merge(whole, boxes[i]);
+        }
+        lbvh::default_morton_code_calculator<float, 3, lbvh::scene<3>::triangle> calc(whole);
+        for (int64_t i = 0; i < nt; ++i)
+        {
+            uint32_t m = calc(sc.triangles[i], boxes[i]);
+            write_n(out, &m, 1);
+        }
+    }
+    for (int64_t i = 0; i < NN; ++i)
+    {
+        const auto &n = bvh.nodes[i];
+        uint32_t q[4] = {n.parent_idx, n.left_idx, n.right_idx, n.object_idx};
+        write_n(out, q, 4);
+    }
+    for (int64_t i = 0; i < NN; ++i)
+    {
+        const auto &b = bvh.aabbs[i];
+        float q[6] = {b.upper.x, b.upper.y, b.upper.z, b.lower.x, b.lower.y, b.lower.z};
+        write_n(out, q, 6);
+    }
+    for (int64_t i = 0; i < NN; ++i)
+    {
+        const auto &c = bvh.cones[i];
+        float q[5] = {c.axis.x, c.axis.y, c.axis.z, c.half_angle, c.radius};
+        write_n(out, q, 5);
+    }
+    // The reference's nearest / silhouette traversals read past the node array
+    // for a one-triangle tree (bvh.cuh:388-390, query.cuh:265): not run there.
+    const bool tree_ok = nt >= 2;
+    for (int64_t q = 0; q < (tree_ok ? n_near : 0); ++q)
+    {
+        const float3 p = make_float3(near_pts[3 * q], near_pts[3 * q + 1], near_pts[3 * q + 2]);
+        const auto r = lbvh::query_device(bvh, lbvh::nearest(p), lbvh::scene<3>::distance_calculator());
+        uint32_t idx = r.first;
+        float d = r.second;
+        write_n(out, &idx, 1);
+        write_n(out, &d, 1);
+    }
+    for (int64_t q = 0; q < (tree_ok ? n_sil : 0); ++q)
+    {
+        const float3 p = make_float3(sil_pts[3 * q], sil_pts[3 * q + 1], sil_pts[3 * q + 2]);
+        float d = lbvh::query_device(bvh, lbvh::nearest_silhouette(p, sil_flip[q] != 0),
+                                     lbvh::scene<3>::silhouette_distance_calculator());
+        write_n(out, &d, 1);
+    }
+    for (int64_t q = 0; q < n_ray; ++q)
+    {
+        const float3 o = make_float3(ray_o[3 * q], ray_o[3 * q + 1], ray_o[3 * q + 2]);
+        const float3 d = make_float3(ray_d[3 * q], ray_d[3 * q + 1], ray_d[3 * q + 2]);
+        const auto r = lbvh::query_device(bvh, lbvh::ray_intersect(lbvh::ray<float, 3>(o, d), ray_tmax[q]),
+                                          lbvh::scene<3>::intersect_test());
+        uint8_t hit = thrust::get<0>(r) ? 1 : 0;
+        float t = thrust::get<1>(r);
+        float2 uv = hit ? thrust::get<2>(r) : make_float2(0.0f, 0.0f);
+        uint32_t idx = thrust::get<3>(r);
+        write_n(out, &hit, 1);
+        write_n(out, &t, 1);
+        write_n(out, &uv.x, 1);
+        write_n(out, &uv.y, 1);
+        write_n(out, &idx, 1);
+    }
+    for (int64_t q = 0; q < n_smp; ++q)
+    {
+        const float3 c = make_float3(smp_c[3 * q], smp_c[3 * q + 1], smp_c[3 * q + 2]);
+        const auto r = lbvh::sample_object_in_sphere(
+            bvh, lbvh::sphere_intersect(lbvh::sphere<float, 3>(c, smp_r[q])), lbvh::scene<3>::intersect_sphere(),
+            lbvh::scene<3>::measurement_getter(), lbvh::scene<3>::green_weight(), smp_u[q]);
+        int32_t idx = r.first;
+        float pdf = idx >= 0 ? r.second : 0.0f;
+        write_n(out, &idx, 1);
+        write_n(out, &pdf, 1);
+    }
+    for (int64_t q = 0; q < n_obj; ++q)
+    {
+        const float3 p = lbvh::sample_on_object(bvh, obj_idx[q], lbvh::scene<3>::sample_on_object(), obj_u[q], obj_v[q]);
+        float xyz[3] = {p.x, p.y, p.z};
+        write_n(out, xyz, 3);
+    }
+    std::fclose(out);
+    return 0;
+}

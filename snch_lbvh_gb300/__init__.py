@@ -1,0 +1,244 @@
+"""GB300-native SNCH-LBVH: host-side mirror of the reference's scene API.
+
+``Scene`` follows ``lbvh::scene<3>`` of tyanyuy3125/snch-lbvh
+(include/snch_lbvh/scene.cuh:704-1267): construct from vertices and
+triangles, ``compute_silhouettes()``, ``build_bvh()``, ``get_bvh_device_ptr()``,
+then the four queries of include/snch_lbvh/core/query.cuh and sample.cuh.
+Every call goes through the C ABI of libsnch_gb300.so (include/snch_gb300.h);
+PyTorch only provides device memory and streams.
+
+Device-buffer calls take CUDA tensors and are asynchronous on the current
+torch stream (or ``stream=``); the ``*_host`` forms take NumPy arrays and
+return NumPy arrays (copies pipelined inside the library).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from ._ffi import BvhView, SnchError, check, lib  # noqa: F401
+
+__all__ = ["Scene", "SnchError", "BvhView", "lib"]
+
+INVALID = 0xFFFFFFFF
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def _stream(stream):
+    torch = _torch()
+    if stream is None:
+        stream = torch.cuda.current_stream()
+    return C.c_void_p(stream.cuda_stream if hasattr(stream, "cuda_stream") else int(stream))
+
+
+def _ptr(t):
+    return None if t is None else C.c_void_p(t.data_ptr())
+
+
+def _dev(x, dtype, cols=None):
+    torch = _torch()
+    if not isinstance(x, torch.Tensor):
+        x = torch.as_tensor(np.ascontiguousarray(x))
+    x = x.to(device="cuda", dtype=dtype).contiguous()
+    if cols is not None:
+        x = x.reshape(-1, cols)
+    return x
+
+
+def _host(x, dtype, cols=None):
+    a = np.ascontiguousarray(x, dtype=dtype)
+    return a.reshape(-1, cols) if cols else a.reshape(-1)
+
+
+class Scene:
+    """lbvh::scene<3>: a triangle mesh, its silhouette edges and its SNCH-LBVH."""
+
+    def __init__(self, vertices, triangles, stream=None):
+        self._h = C.c_void_p()
+        torch = _torch()
+        L = lib()
+        if isinstance(vertices, torch.Tensor) and vertices.is_cuda:
+            v = vertices.to(torch.float32).contiguous()
+            t = triangles.to(device=v.device, dtype=torch.int32).contiguous()
+            check(L.snch_scene_create_device(_ptr(v), v.numel() // 3, _ptr(t), t.numel() // 3, C.byref(self._h),
+                                             _stream(stream)))
+        else:
+            v = _host(vertices, np.float32, 3)
+            t = _host(triangles, np.int32, 3)
+            check(L.snch_scene_create(v.ctypes.data_as(C.c_void_p), len(v), t.ctypes.data_as(C.c_void_p), len(t),
+                                      C.byref(self._h)))
+
+    # ------------------------------------------------------------ lifetime
+    def close(self):
+        if self._h:
+            check(lib().snch_scene_destroy(self._h))
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # ------------------------------------------------------------ build
+    def compute_silhouettes(self, stream=None):
+        """scene<3>::compute_silhouettes() scene.cuh:1167."""
+        check(lib().snch_compute_silhouettes(self._h, _stream(stream)))
+
+    def build_bvh(self, stream=None):
+        """scene<3>::build_bvh() scene.cuh:1205."""
+        check(lib().snch_build_bvh(self._h, _stream(stream)))
+
+    def get_bvh_device_ptr(self) -> BvhView:
+        """scene<3>::get_bvh_device_ptr() scene.cuh:1242; raises SnchError("BVH is not built yet.")."""
+        v = BvhView()
+        check(lib().snch_get_bvh_view(self._h, C.byref(v)))
+        return v
+
+    def info(self):
+        nv, nt, ne = C.c_int64(), C.c_int64(), C.c_int64()
+        check(lib().snch_scene_info(self._h, C.byref(nv), C.byref(nt), C.byref(ne)))
+        return nv.value, nt.value, ne.value
+
+    @property
+    def num_triangles(self):
+        return self.info()[1]
+
+    def device_status(self, reset=True, stream=None) -> int:
+        out = C.c_uint32()
+        check(lib().snch_get_device_status(self._h, C.byref(out), int(reset), _stream(stream)))
+        return out.value
+
+    # ------------------------------------------------------------ exports (parity checks)
+    def export_tree(self, stream=None):
+        torch = _torch()
+        n = self.num_triangles
+        nn = max(2 * n - 1, 0)
+        d = {k: torch.empty(s, dtype=torch.int32, device="cuda") for k, s in
+             [("morton", n), ("sorted_idx", n), ("nodes", (nn, 4))]}
+        d["aabbs"] = torch.empty((nn, 6), dtype=torch.float32, device="cuda")
+        d["cones"] = torch.empty((nn, 5), dtype=torch.float32, device="cuda")
+        check(lib().snch_export_tree(self._h, _ptr(d["morton"]), _ptr(d["sorted_idx"]), _ptr(d["nodes"]),
+                                     _ptr(d["aabbs"]), _ptr(d["cones"]), _stream(stream)))
+        torch.cuda.current_stream().synchronize() if stream is None else stream.synchronize()
+        out = {k: v.cpu().numpy() for k, v in d.items()}
+        for k in ("morton", "sorted_idx", "nodes"):
+            out[k] = out[k].view(np.uint32)
+        return out
+
+    def export_topology(self, stream=None):
+        torch = _torch()
+        _, n, ne = self.info()
+        te = torch.empty((n, 3), dtype=torch.int32, device="cuda")
+        to = torch.empty((n, 3), dtype=torch.int32, device="cuda")
+        ev = torch.empty((max(ne, 0), 4), dtype=torch.int32, device="cuda")
+        check(lib().snch_export_topology(self._h, _ptr(te), _ptr(to), _ptr(ev), _stream(stream)))
+        torch.cuda.synchronize()
+        return te.cpu().numpy(), to.cpu().numpy(), ev.cpu().numpy()
+
+    # ------------------------------------------------------------ device-buffer queries
+    def query_nearest(self, points, stream=None, out=None):
+        """query_device(nearest) query.cuh:239 -> (index int32 [-1 = none], distance)."""
+        torch = _torch()
+        p = _dev(points, torch.float32, 3)
+        n = p.shape[0]
+        idx, dist = out if out is not None else (torch.empty(n, dtype=torch.int32, device="cuda"),
+                                                 torch.empty(n, dtype=torch.float32, device="cuda"))
+        check(lib().snch_query_nearest(self._h, _ptr(p), n, _ptr(idx), _ptr(dist), _stream(stream)))
+        return idx, dist
+
+    def query_silhouette(self, points, flip=None, stream=None, out=None):
+        """query_device(nearest_silhouette) query.cuh:326 -> (distance, edge id or -1)."""
+        torch = _torch()
+        p = _dev(points, torch.float32, 3)
+        n = p.shape[0]
+        f = None if flip is None else _dev(flip, torch.uint8)
+        dist, edge = out if out is not None else (torch.empty(n, dtype=torch.float32, device="cuda"),
+                                                  torch.empty(n, dtype=torch.int32, device="cuda"))
+        check(lib().snch_query_silhouette(self._h, _ptr(p), _ptr(f), n, _ptr(dist), _ptr(edge), _stream(stream)))
+        return dist, edge
+
+    def query_ray(self, origins, dirs, tmax, stream=None, out=None):
+        """query_device(ray_intersect) query.cuh:82 -> (hit uint8, t, uv [n,2], index int32)."""
+        torch = _torch()
+        o, d = _dev(origins, torch.float32, 3), _dev(dirs, torch.float32, 3)
+        tm = _dev(tmax, torch.float32)
+        n = o.shape[0]
+        if out is None:
+            out = (torch.empty(n, dtype=torch.uint8, device="cuda"), torch.empty(n, dtype=torch.float32, device="cuda"),
+                   torch.empty((n, 2), dtype=torch.float32, device="cuda"),
+                   torch.empty(n, dtype=torch.int32, device="cuda"))
+        hit, t, uv, idx = out
+        check(lib().snch_query_ray(self._h, _ptr(o), _ptr(d), _ptr(tm), n, _ptr(hit), _ptr(t), _ptr(uv), _ptr(idx),
+                                   _stream(stream)))
+        return hit, t, uv, idx
+
+    def sample_in_sphere(self, centers, radii, u, stream=None, out=None):
+        """sample_object_in_sphere sample.cuh:26 -> (index or -1, pdf)."""
+        torch = _torch()
+        c = _dev(centers, torch.float32, 3)
+        r, uu = _dev(radii, torch.float32), _dev(u, torch.float32)
+        n = c.shape[0]
+        idx, pdf = out if out is not None else (torch.empty(n, dtype=torch.int32, device="cuda"),
+                                                torch.empty(n, dtype=torch.float32, device="cuda"))
+        check(lib().snch_sample_in_sphere(self._h, _ptr(c), _ptr(r), _ptr(uu), n, _ptr(idx), _ptr(pdf),
+                                          _stream(stream)))
+        return idx, pdf
+
+    def sample_on_object(self, index, u, v, stream=None):
+        """sample_on_object sample.cuh:10 -> points [n,3]."""
+        torch = _torch()
+        i = _dev(index, torch.int32)
+        uu, vv = _dev(u, torch.float32), _dev(v, torch.float32)
+        out = torch.empty((i.shape[0], 3), dtype=torch.float32, device="cuda")
+        check(lib().snch_sample_on_object(self._h, _ptr(i), _ptr(uu), _ptr(vv), i.shape[0], _ptr(out),
+                                          _stream(stream)))
+        return out
+
+    # ------------------------------------------------------------ host-buffer queries
+    def query_nearest_host(self, points, out=None):
+        p = _host(points, np.float32, 3)
+        n = len(p)
+        idx, dist = out if out is not None else (np.empty(n, np.uint32), np.empty(n, np.float32))
+        check(lib().snch_query_nearest_host(self._h, p.ctypes.data_as(C.c_void_p), n,
+                                            idx.ctypes.data_as(C.c_void_p), dist.ctypes.data_as(C.c_void_p)))
+        return idx, dist
+
+    def query_silhouette_host(self, points, flip=None, out=None):
+        p = _host(points, np.float32, 3)
+        n = len(p)
+        f = None if flip is None else _host(flip, np.uint8)
+        dist, edge = out if out is not None else (np.empty(n, np.float32), np.empty(n, np.int32))
+        check(lib().snch_query_silhouette_host(self._h, p.ctypes.data_as(C.c_void_p),
+                                               None if f is None else f.ctypes.data_as(C.c_void_p), n,
+                                               dist.ctypes.data_as(C.c_void_p), edge.ctypes.data_as(C.c_void_p)))
+        return dist, edge
+
+    def query_ray_host(self, origins, dirs, tmax, out=None):
+        o, d, tm = _host(origins, np.float32, 3), _host(dirs, np.float32, 3), _host(tmax, np.float32)
+        n = len(o)
+        if out is None:
+            out = (np.empty(n, np.uint8), np.empty(n, np.float32), np.empty((n, 2), np.float32), np.empty(n, np.uint32))
+        hit, t, uv, idx = out
+        vp = lambda a: a.ctypes.data_as(C.c_void_p)  # noqa: E731
+        check(lib().snch_query_ray_host(self._h, vp(o), vp(d), vp(tm), n, vp(hit), vp(t), vp(uv), vp(idx)))
+        return hit, t, uv, idx
+
+    def sample_in_sphere_host(self, centers, radii, u, out=None):
+        c, r, uu = _host(centers, np.float32, 3), _host(radii, np.float32), _host(u, np.float32)
+        n = len(c)
+        idx, pdf = out if out is not None else (np.empty(n, np.int32), np.empty(n, np.float32))
+        vp = lambda a: a.ctypes.data_as(C.c_void_p)  # noqa: E731
+        check(lib().snch_sample_in_sphere_host(self._h, vp(c), vp(r), vp(uu), n, vp(idx), vp(pdf)))
+        return idx, pdf

@@ -1,0 +1,664 @@
+// C ABI of libsnch_gb300 (declared in include/snch_gb300.h): scene lifetime,
+// build orchestration, query dispatch and the pipelined host-buffer forms.
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <string>
+
+#include <atomic>
+
+#include "internal.h"
+
+namespace snch
+{
+static std::atomic<unsigned long long> g_kernel_launches{0};
+void note_launch(unsigned count) { g_kernel_launches.fetch_add(count, std::memory_order_relaxed); }
+}  // namespace snch
+
+using namespace snch;
+
+namespace
+{
+thread_local std::string g_error;
+
+int fail(int code, const std::string &msg)
+{
+    g_error = msg;
+    return code;
+}
+
+#define SNCH_CUDA(expr)                                                                                    \
+    do                                                                                                     \
+    {                                                                                                      \
+        cudaError_t e_ = (expr);                                                                           \
+        if (e_ != cudaSuccess)                                                                             \
+            return fail(e_ == cudaErrorMemoryAllocation ? SNCH_ERR_OUT_OF_MEMORY : SNCH_ERR_CUDA,          \
+                        std::string(#expr) + ": " + cudaGetErrorString(e_));                               \
+    } while (0)
+
+inline cudaStream_t S(snch_stream_t s) { return static_cast<cudaStream_t>(s); }
+
+// small device words: [0..5] scene box, [8..1031] histograms, [1040] status,
+// [1041] num_edges, [1042] bad-index counter
+constexpr size_t kSmallWords = 1056;
+constexpr size_t kWStatus = 1040, kWNumEdges = 1041, kWBad = 1042, kWHist = 8;
+
+constexpr int64_t kHostChunk = 1 << 21;  // queries per pipelined host-form chunk
+
+struct HostStage
+{
+    void *in[2] = {nullptr, nullptr};
+    void *out[2] = {nullptr, nullptr};
+    size_t in_bytes = 0, out_bytes = 0;
+};
+}  // namespace
+
+struct snch_scene_s
+{
+    uint32_t num_verts = 0, num_tris = 0;
+    int64_t num_edges_host = -1;
+    float *verts = nullptr;
+    int32_t *tris = nullptr, *tri_edges = nullptr, *tri_owned = nullptr, *edge_verts = nullptr;
+    NodeRec *nodes = nullptr;
+    Box *aabbs = nullptr;
+    Cone *cones = nullptr;
+    InnerRec *inner = nullptr;
+    InnerConeRec *inner_cones = nullptr;
+    LeafRec *leaves = nullptr;
+    EdgeRec *edges = nullptr;
+    uint32_t *keys = nullptr, *vals = nullptr, *keys_tmp = nullptr, *vals_tmp = nullptr, *flags = nullptr;
+    float4 *centroids = nullptr;
+    uint32_t *small = nullptr;
+    void *scratch = nullptr;
+    snch_triangle *ref_objects = nullptr;
+    snch_silhouette_edge *ref_edges = nullptr;
+    bool topology_ready = false, built = false;
+    cudaStream_t pipe[2] = {nullptr, nullptr};
+    HostStage stage;
+
+    TreeView view() const
+    {
+        TreeView t;
+        t.num_tris = num_tris;
+        t.nodes = nodes;
+        t.aabbs = aabbs;
+        t.inner = inner;
+        t.inner_cones = inner_cones;
+        t.leaves = leaves;
+        t.edges = edges;
+        t.status = small + kWStatus;
+        return t;
+    }
+};
+
+namespace
+{
+template <typename T>
+cudaError_t dalloc(T **p, size_t count)
+{
+    *p = nullptr;
+    if (count == 0)
+        count = 1;
+    return cudaMalloc(reinterpret_cast<void **>(p), sizeof(T) * count);
+}
+
+void free_scene(snch_scene_s *s)
+{
+    void *ptrs[] = {s->verts, s->tris, s->tri_edges, s->tri_owned, s->edge_verts, s->nodes, s->aabbs, s->cones,
+                    s->inner, s->inner_cones, s->leaves, s->edges, s->keys, s->vals, s->keys_tmp, s->vals_tmp,
+                    s->flags, s->centroids, s->small, s->scratch, s->ref_objects, s->ref_edges,
+                    s->stage.in[0], s->stage.in[1], s->stage.out[0], s->stage.out[1]};
+    for (void *p : ptrs)
+        if (p)
+            cudaFree(p);
+    for (cudaStream_t st : s->pipe)
+        if (st)
+            cudaStreamDestroy(st);
+    delete s;
+}
+
+int allocate(snch_scene_s *s)
+{
+    const size_t n = s->num_tris, nn = n ? 2 * n - 1 : 1, ni = n > 1 ? n - 1 : 1;
+    SNCH_CUDA(dalloc(&s->verts, 3 * (size_t)s->num_verts));
+    SNCH_CUDA(dalloc(&s->tris, 3 * n));
+    SNCH_CUDA(dalloc(&s->tri_edges, 3 * n));
+    SNCH_CUDA(dalloc(&s->tri_owned, 3 * n));
+    SNCH_CUDA(dalloc(&s->edge_verts, 4 * 3 * n));
+    SNCH_CUDA(dalloc(&s->nodes, nn));
+    SNCH_CUDA(dalloc(&s->aabbs, nn));
+    SNCH_CUDA(dalloc(&s->cones, nn));
+    SNCH_CUDA(dalloc(&s->inner, ni));
+    SNCH_CUDA(dalloc(&s->inner_cones, ni));
+    SNCH_CUDA(dalloc(&s->leaves, n));
+    SNCH_CUDA(dalloc(&s->edges, 3 * n));
+    SNCH_CUDA(dalloc(&s->keys, n));
+    SNCH_CUDA(dalloc(&s->vals, n));
+    SNCH_CUDA(dalloc(&s->keys_tmp, n));
+    SNCH_CUDA(dalloc(&s->vals_tmp, n));
+    SNCH_CUDA(dalloc(&s->flags, ni));
+    SNCH_CUDA(dalloc(&s->centroids, n));
+    SNCH_CUDA(dalloc(&s->small, kSmallWords));
+    SNCH_CUDA(dalloc(&s->ref_objects, n));
+    SNCH_CUDA(dalloc(&s->ref_edges, 3 * n));
+    const size_t scratch = std::max(topology_scratch_bytes((uint32_t)n), sort_scratch_bytes((uint32_t)n, 30));
+    SNCH_CUDA(cudaMalloc(&s->scratch, scratch));
+    SNCH_CUDA(cudaMemset(s->small, 0, kSmallWords * 4));
+    return SNCH_OK;
+}
+
+int create_common(const float *v, int64_t nv, const int32_t *t, int64_t nt, snch_scene_t *out, bool device,
+                  cudaStream_t st)
+{
+    if (!out)
+        return fail(SNCH_ERR_INVALID_ARGUMENT, "out_scene is NULL");
+    *out = nullptr;
+    if (nv < 0 || nt < 0)
+        return fail(SNCH_ERR_INVALID_ARGUMENT, "negative vertex or triangle count");
+    if ((nv > 0 && !v) || (nt > 0 && !t))
+        return fail(SNCH_ERR_INVALID_ARGUMENT, "NULL vertex or triangle buffer");
+    if (nt >= (int64_t(1) << 30) || nv >= (int64_t(1) << 31))
+        return fail(SNCH_ERR_TOO_LARGE, "at most 2^30 - 1 triangles and 2^31 - 1 vertices are supported");
+    if (!device)
+        for (int64_t i = 0; i < 3 * nt; ++i)
+            if (t[i] < 0 || t[i] >= nv)
+                return fail(SNCH_ERR_INVALID_ARGUMENT,
+                            "triangle vertex index out of range at triangle " + std::to_string(i / 3));
+    snch_scene_s *s = new snch_scene_s();
+    s->num_verts = (uint32_t)nv;
+    s->num_tris = (uint32_t)nt;
+    int rc = allocate(s);
+    if (rc != SNCH_OK)
+    {
+        free_scene(s);
+        return rc;
+    }
+    const cudaMemcpyKind kind = device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    cudaError_t e = cudaSuccess;
+    if (nv)
+        e = cudaMemcpyAsync(s->verts, v, 12 * (size_t)nv, kind, st);
+    if (e == cudaSuccess && nt)
+        e = cudaMemcpyAsync(s->tris, t, 12 * (size_t)nt, kind, st);
+    if (e == cudaSuccess && device && nt)
+    {
+        e = launch_validate(s->tris, 3 * nt, nv, s->small + kWBad, st);
+        uint32_t bad = 0;
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(&bad, s->small + kWBad, 4, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess)
+            e = cudaStreamSynchronize(st);
+        if (e == cudaSuccess && bad)
+        {
+            free_scene(s);
+            return fail(SNCH_ERR_INVALID_ARGUMENT, std::to_string(bad) + " triangle vertex indices out of range");
+        }
+    }
+    if (e == cudaSuccess && !device)
+        e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess)
+    {
+        free_scene(s);
+        return fail(SNCH_ERR_CUDA, std::string("scene upload: ") + cudaGetErrorString(e));
+    }
+    *out = s;
+    return SNCH_OK;
+}
+
+int topology(snch_scene_s *s, cudaStream_t st)
+{
+    SNCH_CUDA(compute_topology(s->tris, s->num_tris, s->tri_edges, s->tri_owned, s->edge_verts,
+                               s->small + kWNumEdges, s->scratch, s->small + kWStatus, st));
+    s->topology_ready = true;
+    s->num_edges_host = -1;
+    return SNCH_OK;
+}
+
+BuildArgs build_args(snch_scene_s *s)
+{
+    BuildArgs a;
+    a.num_tris = s->num_tris;
+    a.verts = s->verts;
+    a.tris = s->tris;
+    a.tri_owned = s->tri_owned;
+    a.edge_verts = s->edge_verts;
+    a.centroids = s->centroids;
+    a.scene_box = s->small;
+    a.keys = s->keys;
+    a.vals = s->vals;
+    a.hist = s->small + kWHist;
+    a.nodes = s->nodes;
+    a.aabbs = s->aabbs;
+    a.cones = s->cones;
+    a.flags = s->flags;
+    a.inner = s->inner;
+    a.inner_cones = s->inner_cones;
+    a.leaves = s->leaves;
+    a.edges = s->edges;
+    a.status = s->small + kWStatus;
+    return a;
+}
+
+int check_built(snch_scene_t s)
+{
+    if (!s)
+        return fail(SNCH_ERR_INVALID_ARGUMENT, "scene is NULL");
+    if (!s->built)
+        return fail(SNCH_ERR_NOT_BUILT, "BVH is not built yet.");
+    return SNCH_OK;
+}
+
+int check_n(int64_t n, std::initializer_list<const void *> ptrs)
+{
+    if (n < 0)
+        return fail(SNCH_ERR_INVALID_ARGUMENT, "negative query count");
+    if (n > 0)
+        for (const void *p : ptrs)
+            if (!p)
+                return fail(SNCH_ERR_INVALID_ARGUMENT, "NULL query buffer");
+    return SNCH_OK;
+}
+
+// ---- host-form pipeline: chunk i runs on pipe[i % 2]: H2D inputs, kernel, D2H outputs
+int ensure_stage(snch_scene_s *s, size_t in_bytes, size_t out_bytes)
+{
+    for (int k = 0; k < 2; ++k)
+        if (!s->pipe[k])
+            SNCH_CUDA(cudaStreamCreateWithFlags(&s->pipe[k], cudaStreamNonBlocking));
+    if (in_bytes > s->stage.in_bytes)
+    {
+        for (int k = 0; k < 2; ++k)
+        {
+            if (s->stage.in[k])
+                cudaFree(s->stage.in[k]);
+            s->stage.in[k] = nullptr;
+            SNCH_CUDA(cudaMalloc(&s->stage.in[k], in_bytes));
+        }
+        s->stage.in_bytes = in_bytes;
+    }
+    if (out_bytes > s->stage.out_bytes)
+    {
+        for (int k = 0; k < 2; ++k)
+        {
+            if (s->stage.out[k])
+                cudaFree(s->stage.out[k]);
+            s->stage.out[k] = nullptr;
+            SNCH_CUDA(cudaMalloc(&s->stage.out[k], out_bytes));
+        }
+        s->stage.out_bytes = out_bytes;
+    }
+    return SNCH_OK;
+}
+
+struct Field
+{
+    const void *host_in;
+    void *host_out;
+    size_t elem;  // bytes per query
+};
+
+// Runs `body(chunk_begin, count, dev_in[], dev_out[], stream)` over chunks.
+template <typename Body>
+int run_host_pipeline(snch_scene_s *s, int64_t n, const Field *ins, int nin, const Field *outs, int nout, Body body)
+{
+    if (n == 0)
+        return SNCH_OK;
+    size_t in_per = 0, out_per = 0;
+    for (int i = 0; i < nin; ++i)
+        in_per += ins[i].elem;
+    for (int i = 0; i < nout; ++i)
+        out_per += outs[i].elem;
+    const int64_t chunk = std::min<int64_t>(n, kHostChunk);
+    int rc = ensure_stage(s, in_per * chunk + 256 * nin, out_per * chunk + 256 * nout);
+    if (rc != SNCH_OK)
+        return rc;
+    for (int64_t b = 0, c = 0; b < n; b += chunk, ++c)
+    {
+        const int64_t m = std::min<int64_t>(chunk, n - b);
+        const int k = (int)(c & 1);
+        cudaStream_t st = s->pipe[k];
+        char *din = static_cast<char *>(s->stage.in[k]);
+        char *dout = static_cast<char *>(s->stage.out[k]);
+        void *dev_in[4], *dev_out[4];
+        size_t off = 0;
+        for (int i = 0; i < nin; ++i)
+        {
+            dev_in[i] = din + off;
+            if (ins[i].host_in)
+                SNCH_CUDA(cudaMemcpyAsync(din + off, static_cast<const char *>(ins[i].host_in) + b * ins[i].elem,
+                                          m * ins[i].elem, cudaMemcpyHostToDevice, st));
+            else
+                dev_in[i] = nullptr;
+            off += (ins[i].elem * chunk + 255) & ~size_t(255);
+        }
+        off = 0;
+        for (int i = 0; i < nout; ++i)
+        {
+            dev_out[i] = outs[i].host_out ? dout + off : nullptr;
+            off += (outs[i].elem * chunk + 255) & ~size_t(255);
+        }
+        SNCH_CUDA(body(m, dev_in, dev_out, st));
+        for (int i = 0; i < nout; ++i)
+            if (outs[i].host_out)
+                SNCH_CUDA(cudaMemcpyAsync(static_cast<char *>(outs[i].host_out) + b * outs[i].elem, dev_out[i],
+                                          m * outs[i].elem, cudaMemcpyDeviceToHost, st));
+    }
+    SNCH_CUDA(cudaStreamSynchronize(s->pipe[0]));
+    SNCH_CUDA(cudaStreamSynchronize(s->pipe[1]));
+    return SNCH_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *snch_version(void) { return "snch_gb300 0.1 (sm_103a)"; }
+
+const char *snch_last_error(void) { return g_error.c_str(); }
+
+uint64_t snch_kernel_launch_count(void) { return g_kernel_launches.load(std::memory_order_relaxed); }
+
+int snch_scene_create(const float *v, int64_t nv, const int32_t *t, int64_t nt, snch_scene_t *out)
+{
+    return create_common(v, nv, t, nt, out, false, nullptr);
+}
+
+int snch_scene_create_device(const float *v, int64_t nv, const int32_t *t, int64_t nt, snch_scene_t *out,
+                             snch_stream_t stream)
+{
+    return create_common(v, nv, t, nt, out, true, S(stream));
+}
+
+int snch_scene_destroy(snch_scene_t s)
+{
+    if (!s)
+        return fail(SNCH_ERR_INVALID_ARGUMENT, "scene is NULL");
+    free_scene(s);
+    return SNCH_OK;
+}
+
+int snch_compute_silhouettes(snch_scene_t s, snch_stream_t stream)
+{
+    if (!s)
+        return fail(SNCH_ERR_INVALID_ARGUMENT, "scene is NULL");
+    s->built = false;
+    return topology(s, S(stream));
+}
+
+int snch_build_bvh(snch_scene_t s, snch_stream_t stream)
+{
+    if (!s)
+        return fail(SNCH_ERR_INVALID_ARGUMENT, "scene is NULL");
+    cudaStream_t st = S(stream);
+    if (!s->topology_ready)
+    {
+        int rc = topology(s, st);
+        if (rc != SNCH_OK)
+            return rc;
+    }
+    if (s->num_tris > 0)
+    {
+        BuildArgs a = build_args(s);
+        SNCH_CUDA(launch_build_front(a, st));
+        SNCH_CUDA(radix_sort_pairs(s->keys, s->vals, s->keys_tmp, s->vals_tmp, s->num_tris, 30, s->small + kWHist,
+                                   s->scratch, s->small + kWStatus, st));
+        SNCH_CUDA(launch_build_back(a, st));
+        SNCH_CUDA(launch_ref_objects(s->verts, s->tris, s->tri_owned, s->edge_verts, s->num_tris, s->ref_objects,
+                                     s->ref_edges, st));
+    }
+    s->built = true;
+    return SNCH_OK;
+}
+
+int snch_get_bvh_view(snch_scene_t s, snch_bvh_view *out)
+{
+    int rc = check_built(s);
+    if (rc != SNCH_OK)
+        return rc;
+    if (!out)
+        return fail(SNCH_ERR_INVALID_ARGUMENT, "out_view is NULL");
+    out->num_nodes = s->num_tris ? 2 * s->num_tris - 1 : 0;
+    out->num_objects = s->num_tris;
+    out->nodes = reinterpret_cast<const snch_node *>(s->nodes);
+    out->aabbs = reinterpret_cast<const snch_aabb *>(s->aabbs);
+    out->cones = reinterpret_cast<const snch_cone *>(s->cones);
+    out->objects = s->ref_objects;
+    return SNCH_OK;
+}
+
+int snch_scene_info(snch_scene_t s, int64_t *nv, int64_t *nt, int64_t *ne)
+{
+    if (!s)
+        return fail(SNCH_ERR_INVALID_ARGUMENT, "scene is NULL");
+    if (nv)
+        *nv = s->num_verts;
+    if (nt)
+        *nt = s->num_tris;
+    if (ne)
+    {
+        if (!s->topology_ready)
+            *ne = -1;
+        else
+        {
+            if (s->num_edges_host < 0)
+            {
+                uint32_t e = 0;
+                SNCH_CUDA(cudaMemcpy(&e, s->small + kWNumEdges, 4, cudaMemcpyDeviceToHost));
+                s->num_edges_host = e;
+            }
+            *ne = s->num_edges_host;
+        }
+    }
+    return SNCH_OK;
+}
+
+int snch_get_device_status(snch_scene_t s, uint32_t *out, int reset, snch_stream_t stream)
+{
+    if (!s || !out)
+        return fail(SNCH_ERR_INVALID_ARGUMENT, "NULL argument");
+    cudaStream_t st = S(stream);
+    SNCH_CUDA(cudaMemcpyAsync(out, s->small + kWStatus, 4, cudaMemcpyDeviceToHost, st));
+    if (reset)
+        SNCH_CUDA(cudaMemsetAsync(s->small + kWStatus, 0, 4, st));
+    SNCH_CUDA(cudaStreamSynchronize(st));
+    return SNCH_OK;
+}
+
+int snch_export_tree(snch_scene_t s, uint32_t *morton, uint32_t *sidx, uint32_t *nodes, float *aabbs, float *cones,
+                     snch_stream_t stream)
+{
+    int rc = check_built(s);
+    if (rc != SNCH_OK)
+        return rc;
+    cudaStream_t st = S(stream);
+    const size_t n = s->num_tris, nn = n ? 2 * n - 1 : 0;
+    if (morton && n)
+        SNCH_CUDA(cudaMemcpyAsync(morton, s->keys, 4 * n, cudaMemcpyDeviceToDevice, st));
+    if (sidx && n)
+        SNCH_CUDA(cudaMemcpyAsync(sidx, s->vals, 4 * n, cudaMemcpyDeviceToDevice, st));
+    if (nodes && nn)
+        SNCH_CUDA(cudaMemcpyAsync(nodes, s->nodes, 16 * nn, cudaMemcpyDeviceToDevice, st));
+    if (aabbs && nn)
+        SNCH_CUDA(cudaMemcpyAsync(aabbs, s->aabbs, 24 * nn, cudaMemcpyDeviceToDevice, st));
+    if (cones && nn)
+        SNCH_CUDA(cudaMemcpyAsync(cones, s->cones, 20 * nn, cudaMemcpyDeviceToDevice, st));
+    return SNCH_OK;
+}
+
+int snch_export_topology(snch_scene_t s, int32_t *tri_edges, int32_t *tri_owned, int32_t *edge_verts,
+                         snch_stream_t stream)
+{
+    if (!s)
+        return fail(SNCH_ERR_INVALID_ARGUMENT, "scene is NULL");
+    if (!s->topology_ready)
+        return fail(SNCH_ERR_NOT_BUILT, "silhouettes are not computed yet");
+    int64_t ne = 0;
+    int rc = snch_scene_info(s, nullptr, nullptr, &ne);
+    if (rc != SNCH_OK)
+        return rc;
+    cudaStream_t st = S(stream);
+    const size_t n = s->num_tris;
+    if (tri_edges && n)
+        SNCH_CUDA(cudaMemcpyAsync(tri_edges, s->tri_edges, 12 * n, cudaMemcpyDeviceToDevice, st));
+    if (tri_owned && n)
+        SNCH_CUDA(cudaMemcpyAsync(tri_owned, s->tri_owned, 12 * n, cudaMemcpyDeviceToDevice, st));
+    if (edge_verts && ne)
+        SNCH_CUDA(cudaMemcpyAsync(edge_verts, s->edge_verts, 16 * (size_t)ne, cudaMemcpyDeviceToDevice, st));
+    return SNCH_OK;
+}
+
+
+int snch_query_nearest(snch_scene_t s, const float *pts, int64_t n, uint32_t *idx, float *dist, snch_stream_t stream)
+{
+    int rc = check_built(s);
+    if (rc == SNCH_OK)
+        rc = check_n(n, {pts, idx, dist});
+    if (rc != SNCH_OK)
+        return rc;
+    SNCH_CUDA(launch_nearest(s->view(), pts, n, idx, dist, S(stream)));
+    return SNCH_OK;
+}
+
+int snch_query_silhouette(snch_scene_t s, const float *pts, const uint8_t *flip, int64_t n, float *dist, int32_t *edge,
+                          snch_stream_t stream)
+{
+    int rc = check_built(s);
+    if (rc == SNCH_OK)
+        rc = check_n(n, {pts, dist});
+    if (rc != SNCH_OK)
+        return rc;
+    SNCH_CUDA(launch_silhouette(s->view(), pts, flip, n, dist, edge, S(stream)));
+    return SNCH_OK;
+}
+
+int snch_query_ray(snch_scene_t s, const float *o, const float *d, const float *tmax, int64_t n, uint8_t *hit, float *t,
+                   float *uv, uint32_t *idx, snch_stream_t stream)
+{
+    int rc = check_built(s);
+    if (rc == SNCH_OK)
+        rc = check_n(n, {o, d, tmax, hit, t, uv, idx});
+    if (rc != SNCH_OK)
+        return rc;
+    SNCH_CUDA(launch_ray(s->view(), o, d, tmax, n, hit, t, uv, idx, S(stream)));
+    return SNCH_OK;
+}
+
+int snch_sample_in_sphere(snch_scene_t s, const float *c, const float *r, const float *u, int64_t n, int32_t *idx,
+                          float *pdf, snch_stream_t stream)
+{
+    int rc = check_built(s);
+    if (rc == SNCH_OK)
+        rc = check_n(n, {c, r, u, idx, pdf});
+    if (rc != SNCH_OK)
+        return rc;
+    SNCH_CUDA(launch_sample(s->view(), c, r, u, n, idx, pdf, S(stream)));
+    return SNCH_OK;
+}
+
+int snch_sample_on_object(snch_scene_t s, const int32_t *idx, const float *u, const float *v, int64_t n, float *pts,
+                          snch_stream_t stream)
+{
+    int rc = check_built(s);
+    if (rc == SNCH_OK)
+        rc = check_n(n, {idx, u, v, pts});
+    if (rc != SNCH_OK)
+        return rc;
+    if (n > 0 && s->num_tris == 0)
+        return fail(SNCH_ERR_INVALID_ARGUMENT, "sample_on_object on an empty scene");
+    SNCH_CUDA(launch_validate(idx, n, s->num_tris, s->small + kWBad, S(stream)));
+    uint32_t bad = 0;
+    SNCH_CUDA(cudaMemcpyAsync(&bad, s->small + kWBad, 4, cudaMemcpyDeviceToHost, S(stream)));
+    SNCH_CUDA(cudaStreamSynchronize(S(stream)));
+    if (bad)
+        return fail(SNCH_ERR_INVALID_ARGUMENT, std::to_string(bad) + " object indices out of range");
+    SNCH_CUDA(launch_sample_point(s->verts, s->tris, idx, u, v, n, pts, S(stream)));
+    return SNCH_OK;
+}
+
+int snch_query_nearest_host(snch_scene_t s, const float *pts, int64_t n, uint32_t *idx, float *dist)
+{
+    int rc = check_built(s);
+    if (rc == SNCH_OK)
+        rc = check_n(n, {pts, idx, dist});
+    if (rc != SNCH_OK)
+        return rc;
+    const Field ins[] = {{pts, nullptr, 12}};
+    const Field outs[] = {{nullptr, idx, 4}, {nullptr, dist, 4}};
+    const TreeView t = s->view();
+    return run_host_pipeline(s, n, ins, 1, outs, 2, [&](int64_t m, void **di, void **dout, cudaStream_t st) {
+        return launch_nearest(t, (const float *)di[0], m, (uint32_t *)dout[0], (float *)dout[1], st);
+    });
+}
+
+int snch_query_silhouette_host(snch_scene_t s, const float *pts, const uint8_t *flip, int64_t n, float *dist,
+                               int32_t *edge)
+{
+    int rc = check_built(s);
+    if (rc == SNCH_OK)
+        rc = check_n(n, {pts, dist});
+    if (rc != SNCH_OK)
+        return rc;
+    const Field ins[] = {{pts, nullptr, 12}, {flip, nullptr, 1}};
+    const Field outs[] = {{nullptr, dist, 4}, {nullptr, edge, 4}};
+    const TreeView t = s->view();
+    return run_host_pipeline(s, n, ins, 2, outs, 2, [&](int64_t m, void **di, void **dout, cudaStream_t st) {
+        return launch_silhouette(t, (const float *)di[0], (const uint8_t *)di[1], m, (float *)dout[0],
+                                 (int32_t *)dout[1], st);
+    });
+}
+
+int snch_query_ray_host(snch_scene_t s, const float *o, const float *d, const float *tmax, int64_t n, uint8_t *hit,
+                        float *t, float *uv, uint32_t *idx)
+{
+    int rc = check_built(s);
+    if (rc == SNCH_OK)
+        rc = check_n(n, {o, d, tmax, hit, t, uv, idx});
+    if (rc != SNCH_OK)
+        return rc;
+    const Field ins[] = {{o, nullptr, 12}, {d, nullptr, 12}, {tmax, nullptr, 4}};
+    const Field outs[] = {{nullptr, hit, 1}, {nullptr, t, 4}, {nullptr, uv, 8}, {nullptr, idx, 4}};
+    const TreeView tv = s->view();
+    return run_host_pipeline(s, n, ins, 3, outs, 4, [&](int64_t m, void **di, void **dout, cudaStream_t st) {
+        return launch_ray(tv, (const float *)di[0], (const float *)di[1], (const float *)di[2], m, (uint8_t *)dout[0],
+                          (float *)dout[1], (float *)dout[2], (uint32_t *)dout[3], st);
+    });
+}
+
+int snch_sample_in_sphere_host(snch_scene_t s, const float *c, const float *r, const float *u, int64_t n, int32_t *idx,
+                               float *pdf)
+{
+    int rc = check_built(s);
+    if (rc == SNCH_OK)
+        rc = check_n(n, {c, r, u, idx, pdf});
+    if (rc != SNCH_OK)
+        return rc;
+    const Field ins[] = {{c, nullptr, 12}, {r, nullptr, 4}, {u, nullptr, 4}};
+    const Field outs[] = {{nullptr, idx, 4}, {nullptr, pdf, 4}};
+    const TreeView t = s->view();
+    return run_host_pipeline(s, n, ins, 3, outs, 2, [&](int64_t m, void **di, void **dout, cudaStream_t st) {
+        return launch_sample(t, (const float *)di[0], (const float *)di[1], (const float *)di[2], m,
+                             (int32_t *)dout[0], (float *)dout[1], st);
+    });
+}
+
+size_t snch_sort_scratch_bytes(int64_t n, int key_bits)
+{
+    if (n <= 0 || n >= (int64_t(1) << 30) || key_bits < 1 || key_bits > 32)
+        return 0;
+    return sort_scratch_bytes((uint32_t)n, key_bits);
+}
+
+int snch_sort_pairs(uint32_t *keys, uint32_t *vals, uint32_t *keys_tmp, uint32_t *vals_tmp, int64_t n, int key_bits,
+                    void *scratch, uint32_t *device_status, snch_stream_t stream)
+{
+    if (n < 0 || key_bits < 1 || key_bits > 32)
+        return fail(SNCH_ERR_INVALID_ARGUMENT, "n < 0 or key_bits outside [1, 32]");
+    if (n >= (int64_t(1) << 30))
+        return fail(SNCH_ERR_TOO_LARGE, "at most 2^30 - 1 pairs");
+    if (n > 1 && (!keys || !vals || !keys_tmp || !vals_tmp || !scratch || !device_status))
+        return fail(SNCH_ERR_INVALID_ARGUMENT, "NULL buffer");
+    SNCH_CUDA(radix_sort_pairs(keys, vals, keys_tmp, vals_tmp, (uint32_t)n, key_bits, nullptr, scratch, device_status,
+                               S(stream)));
+    return SNCH_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,259 @@
+// Shared device math and data layout of the GB300 SNCH-LBVH.
+//
+// Every translation unit that includes this header is compiled with
+// -fmad=false: each + - * / below is exactly one IEEE-754 binary32 operation
+// in the reference's left-to-right expression order, so the build and the
+// queries reproduce the reference's arithmetic (tyanyuy3125/snch-lbvh,
+// include/snch_lbvh/core/{aabb,cone,utility}.cuh and scene.cuh) bit for bit,
+// except where CUDA's acosf/asinf/atan2f/sinf/cosf are called (cone code).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#define SNCH_DEV __device__ __forceinline__
+
+namespace snch
+{
+
+constexpr uint32_t kInvalid = 0xFFFFFFFFu;
+constexpr float kEps = 1.1920928955078125e-07f;  // epsilon<float>() utility.cuh:186
+constexpr float kPi = 3.14159274101257324219f;   // static_cast<float>(M_PI)
+constexpr float kPi2 = 1.57079637050628662109f;  // static_cast<float>(M_PI_2)
+constexpr int kStackDepth = 64;                   // query.cuh:250, 338 (64-entry stacks)
+
+// bits of the per-scene device status word
+enum : uint32_t
+{
+    kStatusStackOverflow = 1u,     // a traversal needed more than kStackDepth entries
+    kStatusLookbackTimeout = 2u,   // a decoupled look-back wait gave up
+    kStatusHashFull = 4u,          // the edge hash table had no free slot
+    kStatusRefitTimeout = 8u,      // reserved
+};
+
+struct f3
+{
+    float x, y, z;
+};
+struct Box  // aabb<float,3> aabb.cuh:11-16 (upper first)
+{
+    f3 upper, lower;
+};
+struct Cone  // cone<float,3> cone.cuh:10-16
+{
+    f3 axis;
+    float half_angle, radius;
+};
+
+// ---------------------------------------------------------------- HBM layout
+// Reference-layout records (bvh.cuh:27-33): nodes, aabbs and cones indexed by
+// node id; internal nodes 0..N-2, the leaf of sorted position j is N-1+j.
+struct NodeRec
+{
+    uint32_t parent, left, right, object;
+};
+
+// Traversal layout. One 64-byte record per internal node holds both child
+// boxes and both child node ids, so expanding a node is one 64-B line
+// (four 16-B vector loads) instead of the reference's four scattered records.
+//   a = (L.upper.xyz, L.lower.x)  b = (L.lower.yz, R.upper.xy)
+//   c = (R.upper.z, R.lower.xyz)  d = (bits L, bits R, 0, 0)
+struct alignas(64) InnerRec
+{
+    float4 a, b, c, d;
+};
+// Child cones of an internal node (silhouette traversal), 48 B:
+//   a = (L.axis.xyz, L.half)  b = (L.radius, R.axis.xyz)  c = (R.half, R.radius, 0, 0)
+struct alignas(16) InnerConeRec
+{
+    float4 a, b, c;
+};
+// Leaf triangle in sorted order, vertices gathered: 48 B
+//   v0 = (pa.xyz, bits original index)  v1 = (pb.xyz, bits owned-edge count)  v2 = (pc.xyz, 0)
+struct alignas(16) LeafRec
+{
+    float4 v0, v1, v2;
+};
+// Owned silhouette edge of a sorted leaf (slot 3*j+k), 64 B, with the two
+// face normals precomputed exactly as silhouette_edge::normal(f) computes them:
+//   a = (pa.xyz, bits has_face flags)  b = (pb.xyz, bits edge id)  c = (n0.xyz, 0)  d = (n1.xyz, 0)
+struct alignas(64) EdgeRec
+{
+    float4 a, b, c, d;
+};
+
+// Everything a query kernel reads, passed by value.
+struct TreeView
+{
+    uint32_t num_tris;  // N
+    const NodeRec *nodes;
+    const Box *aabbs;   // aabbs[0] is the root box
+    const InnerRec *inner;
+    const InnerConeRec *inner_cones;
+    const LeafRec *leaves;
+    const EdgeRec *edges;
+    uint32_t *status;
+};
+
+// ---------------------------------------------------------------- vector math
+SNCH_DEV f3 mk(float x, float y, float z)
+{
+    f3 r;
+    r.x = x;
+    r.y = y;
+    r.z = z;
+    return r;
+}
+SNCH_DEV f3 sub(f3 a, f3 b) { return mk(a.x - b.x, a.y - b.y, a.z - b.z); }
+// dot / length / squared_length / normalize / cross: utility.cuh:238, 382-389, 400-407, 427-431, 449-455
+SNCH_DEV float dot3(f3 a, f3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+SNCH_DEV float len3(f3 a) { return sqrtf(a.x * a.x + a.y * a.y + a.z * a.z); }
+SNCH_DEV float sqlen3(f3 a) { return (a.x * a.x + a.y * a.y + a.z * a.z); }
+SNCH_DEV f3 normalize3(f3 v)
+{
+    float n = len3(v);
+    return mk(v.x / n, v.y / n, v.z / n);
+}
+SNCH_DEV f3 cross3(f3 u, f3 v) { return mk(u.y * v.z - u.z * v.y, u.z * v.x - u.x * v.z, u.x * v.y - u.y * v.x); }
+SNCH_DEV f3 cabs3(f3 a) { return mk(fabsf(a.x), fabsf(a.y), fabsf(a.z)); }
+// std::min / std::max with their argument order (matters for NaN)
+SNCH_DEV float smin(float a, float b) { return (b < a) ? b : a; }
+SNCH_DEV float smax(float a, float b) { return (a < b) ? b : a; }
+
+SNCH_DEV f3 load_vert(const float *__restrict__ v, int32_t i)
+{
+    const float *p = v + 3 * (int64_t)i;
+    return mk(__ldg(p), __ldg(p + 1), __ldg(p + 2));
+}
+
+// centroid aabb.cuh:271-279; the reference's "* 0.5" (double) rounds exactly like "* 0.5f"
+SNCH_DEV f3 centroid(const Box &b)
+{
+    return mk((b.upper.x + b.lower.x) * 0.5f, (b.upper.y + b.lower.y) * 0.5f, (b.upper.z + b.lower.z) * 0.5f);
+}
+
+// merge(aabb,aabb) aabb.cuh:113-124
+SNCH_DEV Box merge_box(const Box &l, const Box &r)
+{
+    Box m;
+    m.upper = mk(fmaxf(l.upper.x, r.upper.x), fmaxf(l.upper.y, r.upper.y), fmaxf(l.upper.z, r.upper.z));
+    m.lower = mk(fminf(l.lower.x, r.lower.x), fminf(l.lower.y, r.lower.y), fminf(l.lower.z, r.lower.z));
+    return m;
+}
+
+// mindist aabb.cuh:144-150 (squared)
+SNCH_DEV float mindist(const Box &b, f3 p)
+{
+    const float dx = fminf(b.upper.x, fmaxf(b.lower.x, p.x)) - p.x;
+    const float dy = fminf(b.upper.y, fmaxf(b.lower.y, p.y)) - p.y;
+    const float dz = fminf(b.upper.z, fmaxf(b.lower.z, p.z)) - p.z;
+    return dx * dx + dy * dy + dz * dz;
+}
+
+// minmaxdist aabb.cuh:182-209 (squared)
+SNCH_DEV float minmaxdist(const Box &b, f3 p)
+{
+    float rmx = (b.lower.x - p.x) * (b.lower.x - p.x), rmy = (b.lower.y - p.y) * (b.lower.y - p.y),
+          rmz = (b.lower.z - p.z) * (b.lower.z - p.z);
+    float rMx = (b.upper.x - p.x) * (b.upper.x - p.x), rMy = (b.upper.y - p.y) * (b.upper.y - p.y),
+          rMz = (b.upper.z - p.z) * (b.upper.z - p.z);
+    float t;
+    if ((b.upper.x + b.lower.x) * 0.5f < p.x) { t = rmx; rmx = rMx; rMx = t; }
+    if ((b.upper.y + b.lower.y) * 0.5f < p.y) { t = rmy; rmy = rMy; rMy = t; }
+    if ((b.upper.z + b.lower.z) * 0.5f < p.z) { t = rmz; rmz = rMz; rMz = t; }
+    const float dx = rmx + rMy + rMz;
+    const float dy = rMx + rmy + rMz;
+    const float dz = rMx + rMy + rmz;
+    return fminf(dx, fminf(dy, dz));
+}
+
+// -------------------------------------------------------------- record packing
+SNCH_DEV void unpack_inner(const InnerRec &r, Box &l, Box &rb, uint32_t &L, uint32_t &R)
+{
+    l.upper = mk(r.a.x, r.a.y, r.a.z);
+    l.lower = mk(r.a.w, r.b.x, r.b.y);
+    rb.upper = mk(r.b.z, r.b.w, r.c.x);
+    rb.lower = mk(r.c.y, r.c.z, r.c.w);
+    L = __float_as_uint(r.d.x);
+    R = __float_as_uint(r.d.y);
+}
+SNCH_DEV InnerRec pack_inner(const Box &l, const Box &r, uint32_t L, uint32_t R)
+{
+    InnerRec o;
+    o.a = make_float4(l.upper.x, l.upper.y, l.upper.z, l.lower.x);
+    o.b = make_float4(l.lower.y, l.lower.z, r.upper.x, r.upper.y);
+    o.c = make_float4(r.upper.z, r.lower.x, r.lower.y, r.lower.z);
+    o.d = make_float4(__uint_as_float(L), __uint_as_float(R), 0.0f, 0.0f);
+    return o;
+}
+SNCH_DEV InnerRec load_inner(const InnerRec *p)
+{
+    const float4 *q = reinterpret_cast<const float4 *>(p);
+    InnerRec r;
+    r.a = __ldg(q);
+    r.b = __ldg(q + 1);
+    r.c = __ldg(q + 2);
+    r.d = __ldg(q + 3);
+    return r;
+}
+SNCH_DEV void unpack_cones(const InnerConeRec &r, Cone &l, Cone &rc)
+{
+    l.axis = mk(r.a.x, r.a.y, r.a.z);
+    l.half_angle = r.a.w;
+    l.radius = r.b.x;
+    rc.axis = mk(r.b.y, r.b.z, r.b.w);
+    rc.half_angle = r.c.x;
+    rc.radius = r.c.y;
+}
+SNCH_DEV InnerConeRec pack_cones(const Cone &l, const Cone &r)
+{
+    InnerConeRec o;
+    o.a = make_float4(l.axis.x, l.axis.y, l.axis.z, l.half_angle);
+    o.b = make_float4(l.radius, r.axis.x, r.axis.y, r.axis.z);
+    o.c = make_float4(r.half_angle, r.radius, 0.0f, 0.0f);
+    return o;
+}
+SNCH_DEV void load_leaf(const LeafRec *p, f3 &pa, f3 &pb, f3 &pc, uint32_t &orig, uint32_t &n_owned)
+{
+    const float4 *q = reinterpret_cast<const float4 *>(p);
+    const float4 a = __ldg(q), b = __ldg(q + 1), c = __ldg(q + 2);
+    pa = mk(a.x, a.y, a.z);
+    pb = mk(b.x, b.y, b.z);
+    pc = mk(c.x, c.y, c.z);
+    orig = __float_as_uint(a.w);
+    n_owned = __float_as_uint(b.w);
+}
+
+// relaxed device-scope loads/stores for cross-block flags (no stale L1 lines)
+SNCH_DEV uint32_t ld_relaxed(const uint32_t *p)
+{
+    uint32_t v;
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+SNCH_DEV void st_relaxed(uint32_t *p, uint32_t v)
+{
+    asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+SNCH_DEV uint32_t ld_acquire(const uint32_t *p)
+{
+    uint32_t v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+SNCH_DEV void st_release(uint32_t *p, uint32_t v)
+{
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// float <-> order-preserving uint32 (atomicMin/atomicMax on floats)
+SNCH_DEV uint32_t float_to_ordered(float f)
+{
+    uint32_t u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+SNCH_DEV float ordered_to_float(uint32_t u)
+{
+    return __uint_as_float((u & 0x80000000u) ? (u & 0x7FFFFFFFu) : ~u);
+}
+
+}  // namespace snch

@@ -1,0 +1,83 @@
+// Host-side launchers shared between the translation units of libsnch_gb300.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/snch_gb300.h"
+#include "common.cuh"
+
+namespace snch
+{
+
+// Number of kernels this library has launched (snch_kernel_launch_count).
+void note_launch(unsigned count = 1);
+
+// Device arrays of one LBVH construction (build.cu).
+struct BuildArgs
+{
+    uint32_t num_tris;
+    const float *verts;
+    const int32_t *tris;
+    const int32_t *tri_owned;
+    const int32_t *edge_verts;
+    float4 *centroids;
+    uint32_t *scene_box;  // 6 ordered uints: upper.xyz (max), lower.xyz (min)
+    uint32_t *keys;       // Morton codes, sorted in place
+    uint32_t *vals;       // original triangle indices, sorted in place
+    uint32_t *hist;       // 4 x 256 digit counts
+    NodeRec *nodes;
+    Box *aabbs;
+    Cone *cones;
+    uint32_t *flags;      // refit arrival counters, N-1
+    InnerRec *inner;
+    InnerConeRec *inner_cones;
+    LeafRec *leaves;
+    EdgeRec *edges;
+    uint32_t *status;
+};
+
+// ---- build.cu
+cudaError_t launch_build_front(const BuildArgs &a, cudaStream_t st);
+cudaError_t launch_build_back(const BuildArgs &a, cudaStream_t st);
+cudaError_t launch_ref_objects(const float *verts, const int32_t *tris, const int32_t *tri_owned,
+                               const int32_t *edge_verts, uint32_t num_tris, snch_triangle *objs,
+                               snch_silhouette_edge *edges, cudaStream_t st);
+cudaError_t launch_validate(const int32_t *tris, int64_t n, int64_t num_verts, uint32_t *bad, cudaStream_t st);
+
+// ---- queries.cu
+cudaError_t launch_nearest(const TreeView &t, const float *pts, int64_t n, uint32_t *idx, float *dist, cudaStream_t st);
+cudaError_t launch_silhouette(const TreeView &t, const float *pts, const uint8_t *flip, int64_t n, float *dist,
+                              int32_t *edge, cudaStream_t st);
+cudaError_t launch_ray(const TreeView &t, const float *o, const float *d, const float *tmax, int64_t n, uint8_t *hit,
+                       float *tt, float *uv, uint32_t *idx, cudaStream_t st);
+cudaError_t launch_sample(const TreeView &t, const float *c, const float *r, const float *u, int64_t n, int32_t *idx,
+                          float *pdf, cudaStream_t st);
+cudaError_t launch_sample_point(const float *verts, const int32_t *tris, const int32_t *idx, const float *u,
+                                const float *v, int64_t n, float *out, cudaStream_t st);
+
+// ---- scan_sort.cu
+// Exclusive scan of 0/1 flags (totals below 2^30), one pass, decoupled look-back.
+size_t scan_flags_scratch_bytes(uint64_t n);
+cudaError_t scan_flags(const uint32_t *in, uint32_t *out, uint32_t n, uint32_t *total, void *scratch,
+                       uint32_t *status, cudaStream_t st);
+
+// Stable LSD radix sort of (key, value) pairs on the low key_bits bits,
+// onesweep style: one histogram pass then one scatter pass per 8-bit digit.
+// Data ping-pongs between (keys, vals) and (keys_tmp, vals_tmp); the result
+// is written back to (keys, vals). If hist is non-null it already holds the
+// per-pass digit counts (passes x 256) and the histogram pass is skipped.
+constexpr int kSortTile = 4096;
+size_t sort_scratch_bytes(uint32_t n, int key_bits);
+cudaError_t radix_sort_pairs(uint32_t *keys, uint32_t *vals, uint32_t *keys_tmp, uint32_t *vals_tmp, uint32_t n,
+                             int key_bits, const uint32_t *hist, void *scratch, uint32_t *status, cudaStream_t st);
+inline int sort_passes(int key_bits) { return (key_bits + 7) / 8; }
+
+// ---- topology.cu (scene.cuh:1135-1225 on the device)
+size_t topology_scratch_bytes(uint32_t num_tris);
+// Outputs: tri_edges, tri_owned (int32 x 3N), edge_verts (int32 x 4 x capacity 3N), *num_edges (device).
+cudaError_t compute_topology(const int32_t *tris, uint32_t num_tris, int32_t *tri_edges, int32_t *tri_owned,
+                             int32_t *edge_verts, uint32_t *num_edges, void *scratch, uint32_t *status,
+                             cudaStream_t st);
+
+}  // namespace snch

@@ -1,0 +1,731 @@
+// Per-query traversal kernels over the 64-B node layout.
+//
+// Each kernel keeps the reference's visit order (stack discipline, child order,
+// pruning tests and tie rules) so that it returns the reference's results bit
+// for bit, while reading one 64-byte record per expanded node:
+//   nearest_kernel     query_device(nearest)            query.cuh:239-318
+//   silhouette_kernel  query_device(nearest_silhouette) query.cuh:326-423
+//   ray_kernel         query_device(ray_intersect)      query.cuh:82-169
+//   sample_kernel      sample_object_in_sphere          sample.cuh:26-91
+//   sample_point_kernel sample_on_object                sample.cuh:10-22
+// A one-triangle tree (where the reference reads past its node array,
+// bvh.cuh:388-390) evaluates its only leaf directly. A traversal that would
+// need more than 64 stack entries (undefined in the reference) stops, writes
+// NaN / 0xFFFFFFFF and sets kStatusStackOverflow.
+#include "internal.h"
+
+namespace snch
+{
+
+// find_closest_point_triangle scene.cuh:34-110 (distance only)
+SNCH_DEV float closest_point_triangle(f3 pa, f3 pb, f3 pc, f3 x)
+{
+    const f3 ab = sub(pb, pa), ac = sub(pc, pa), ax = sub(x, pa);
+    const float d1 = dot3(ab, ax), d2 = dot3(ac, ax);
+    if (d1 <= 0.0f && d2 <= 0.0f)
+        return len3(sub(x, pa));
+    const f3 bx = sub(x, pb);
+    const float d3 = dot3(ab, bx), d4 = dot3(ac, bx);
+    if (d3 >= 0.0f && d4 <= d3)
+        return len3(sub(x, pb));
+    const f3 cx = sub(x, pc);
+    const float d5 = dot3(ab, cx), d6 = dot3(ac, cx);
+    if (d6 >= 0.0f && d5 <= d6)
+        return len3(sub(x, pc));
+    const float vc = d1 * d4 - d3 * d2;
+    if (vc <= 0.0f && d1 >= 0.0f && d3 <= 0.0f)
+    {
+        const float v = d1 / (d1 - d3);
+        return len3(sub(x, mk(pa.x + ab.x * v, pa.y + ab.y * v, pa.z + ab.z * v)));
+    }
+    const float vb = d5 * d2 - d1 * d6;
+    if (vb <= 0.0f && d2 >= 0.0f && d6 <= 0.0f)
+    {
+        const float w = d2 / (d2 - d6);
+        return len3(sub(x, mk(pa.x + ac.x * w, pa.y + ac.y * w, pa.z + ac.z * w)));
+    }
+    const float va = d3 * d6 - d5 * d4;
+    if (va <= 0.0f && (d4 - d3) >= 0.0f && (d5 - d6) >= 0.0f)
+    {
+        const float w = (d4 - d3) / ((d4 - d3) + (d5 - d6));
+        return len3(sub(x, mk(pb.x + (pc.x - pb.x) * w, pb.y + (pc.y - pb.y) * w, pb.z + (pc.z - pb.z) * w)));
+    }
+    const float denom = 1.0f / (va + vb + vc);
+    const float v = vb * denom, w = vc * denom;
+    return len3(sub(x, mk(pa.x + ab.x * v + ac.x * w, pa.y + ab.y * v + ac.y * w, pa.z + ab.z * v + ac.z * w)));
+}
+
+SNCH_DEV Box load_root_box(const Box *p)
+{
+    const float *q = reinterpret_cast<const float *>(p);
+    Box b;
+    b.upper = mk(__ldg(q), __ldg(q + 1), __ldg(q + 2));
+    b.lower = mk(__ldg(q + 3), __ldg(q + 4), __ldg(q + 5));
+    return b;
+}
+
+SNCH_DEV f3 load_point(const float *__restrict__ p, int64_t q)
+{
+    return mk(__ldg(p + 3 * q), __ldg(p + 3 * q + 1), __ldg(p + 3 * q + 2));
+}
+
+// ------------------------------------------------------------------ nearest
+SNCH_DEV float leaf_distance2(const TreeView &t, uint32_t pos, f3 p, uint32_t &orig)
+{
+    f3 pa, pb, pc;
+    uint32_t n_owned;
+    load_leaf(t.leaves + pos, pa, pb, pc, orig, n_owned);
+    float d = closest_point_triangle(pa, pb, pc, p);
+    d *= d;
+    return d;
+}
+
+__global__ void __launch_bounds__(128) nearest_kernel(TreeView t, const float *__restrict__ pts, int64_t n,
+                                                      uint32_t *__restrict__ out_idx, float *__restrict__ out_dist)
+{
+    const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (q >= n)
+        return;
+    const f3 p = load_point(pts, q);
+    uint32_t nearest = kInvalid;
+    float best = INFINITY;
+    const uint32_t ni = t.num_tris - 1;
+    if (t.num_tris == 1)
+    {
+        uint32_t orig;
+        best = leaf_distance2(t, 0, p, orig);
+        nearest = orig;
+    }
+    else if (t.num_tris > 1)
+    {
+        uint32_t sn[kStackDepth];
+        float sd[kStackDepth];
+        int sp = 0;
+        sn[0] = 0;
+        sd[0] = mindist(load_root_box(t.aabbs), p);
+        sp = 1;
+        do
+        {
+            --sp;
+            const uint32_t node = sn[sp];
+            if (sd[sp] > best)
+                continue;
+            if (sp > kStackDepth - 2)
+            {
+                atomicOr(t.status, kStatusStackOverflow);
+                nearest = kInvalid;
+                best = NAN;
+                break;
+            }
+            Box lb, rb;
+            uint32_t L, R;
+            unpack_inner(load_inner(t.inner + node), lb, rb, L, R);
+            const float Lmd = mindist(lb, p), Rmd = mindist(rb, p);
+            const float Lmm = minmaxdist(lb, p), Rmm = minmaxdist(rb, p);
+            if (Lmd <= Rmm)
+            {
+                if (L >= ni)
+                {
+                    uint32_t orig;
+                    const float d = leaf_distance2(t, L - ni, p, orig);
+                    if (d <= best)
+                    {
+                        best = d;
+                        nearest = orig;
+                    }
+                }
+                else
+                {
+                    sn[sp] = L;
+                    sd[sp] = Lmd;
+                    ++sp;
+                }
+            }
+            if (Rmd <= Lmm)
+            {
+                if (R >= ni)
+                {
+                    uint32_t orig;
+                    const float d = leaf_distance2(t, R - ni, p, orig);
+                    if (d <= best)
+                    {
+                        best = d;
+                        nearest = orig;
+                    }
+                }
+                else
+                {
+                    sn[sp] = R;
+                    sd[sp] = Rmd;
+                    ++sp;
+                }
+            }
+        } while (sp > 0);
+    }
+    out_idx[q] = nearest;
+    out_dist[q] = sqrtf(best);
+}
+
+// ------------------------------------------------------------------ silhouette
+// compute_orthonormal_basis(float3) cone.cuh:34-42 + project_to_plane cone.cuh:58-66
+SNCH_DEV float project_to_plane(f3 n, f3 e)
+{
+    const float sign = copysignf(1.0f, n.z);
+    const float a = -1.0f / (sign + n.z);
+    const float b = n.x * n.y * a;
+    const f3 b1 = mk(1.0f + sign * n.x * n.x * a, sign * b, -sign * n.x);
+    const f3 b2 = mk(b, sign + n.y * n.y * a, -n.y);
+    const float r1 = dot3(e, cabs3(b1));
+    const float r2 = dot3(e, cabs3(b2));
+    return sqrtf(r1 * r1 + r2 * r2);
+}
+SNCH_DEV bool inrange(float v, float lo, float hi) { return v >= lo && v <= hi; }
+
+// overlap(cone<float,3>, ...) cone.cuh:168-212
+SNCH_DEV bool cone_overlap(const Cone &bc, f3 o, const Box &b, float dist_to_box)
+{
+    if (bc.half_angle >= kPi2 || dist_to_box < kEps)
+        return true;
+    const f3 c = centroid(b);
+    f3 v = mk(c.x - o.x, c.y - o.y, c.z - o.z);
+    const float l = len3(v);
+    v.x /= l;
+    v.y /= l;
+    v.z /= l;
+    const float dax = acosf(smax(-1.0f, smin(1.0f, dot3(bc.axis, v))));
+    if (inrange(kPi2, dax - bc.half_angle, dax + bc.half_angle))
+        return true;
+    if (l > bc.radius)
+    {
+        const float vch = asinf(bc.radius / l);
+        const float hs = bc.half_angle + vch;
+        const float mn = dax - hs, mx = dax + hs;
+        return hs >= kPi2 ? true : inrange(kPi2, mn, mx);
+    }
+    const f3 e = mk(b.upper.x - c.x, b.upper.y - c.y, b.upper.z - c.z);
+    float d = dot3(e, cabs3(v));
+    const float s = l - d;
+    if (s <= 0.0f)
+        return true;
+    d = project_to_plane(v, e);
+    const float vch = atan2f(d, s);
+    const float hs = bc.half_angle + vch;
+    const float mn = dax - hs, mx = dax + hs;
+    return hs >= kPi2 ? true : inrange(kPi2, mn, mx);
+}
+
+// find_closest_point_line_segment(float3) scene.cuh:230-255
+SNCH_DEV float closest_point_segment(f3 pa, f3 pb, f3 x, f3 &pt)
+{
+    const f3 u = sub(pb, pa), v = sub(x, pa);
+    const float c1 = dot3(u, v);
+    if (c1 <= 0.0f)
+    {
+        pt = pa;
+        return len3(sub(x, pt));
+    }
+    const float c2 = dot3(u, u);
+    if (c2 <= c1)
+    {
+        pt = pb;
+        return len3(sub(x, pt));
+    }
+    const float tt = c1 / c2;
+    pt = mk(pa.x + u.x * tt, pa.y + u.y * tt, pa.z + u.z * tt);
+    return len3(sub(x, pt));
+}
+
+// is_silhouette_edge scene.cuh:143-174 (view_dir left unnormalised, as there)
+SNCH_DEV bool is_silhouette_edge(f3 pa, f3 pb, f3 n0, f3 n1, f3 view_dir, float d, bool flip)
+{
+    const float precision = 1e-3f;
+    const float sign = flip ? 1.0f : -1.0f;
+    if (d <= precision)
+    {
+        const f3 ed = normalize3(sub(pb, pa));
+        const float sda = atan2f(dot3(ed, cross3(n0, n1)), dot3(n0, n1));
+        return sign * sda > precision;
+    }
+    const float dot0 = dot3(view_dir, n0), dot1 = dot3(view_dir, n1);
+    if (fabsf(dot0) <= precision)
+        return sign * dot1 > precision;
+    if (fabsf(dot1) <= precision)
+        return sign * dot0 > precision;
+    return dot0 * dot1 < 0.0f;
+}
+
+// silhouette_distance_calculator scene.cuh:978-1003 with
+// find_closest_silhouette_point scene.cuh:788-824 per owned edge (min radius 0)
+SNCH_DEV bool leaf_silhouette(const TreeView &t, uint32_t pos, f3 o, float max_r2, float &dist, bool flip,
+                              int32_t &edge_id)
+{
+    const uint32_t n_owned = __float_as_uint(__ldg(&t.leaves[pos].v1.w));
+    float mr2 = max_r2;
+    bool ret = false;
+    for (uint32_t k = 0; k < n_owned; ++k)
+    {
+        if (0.0f >= mr2)
+            continue;
+        const float4 *e = reinterpret_cast<const float4 *>(t.edges + 3 * (uint64_t)pos + k);
+        const float4 ea = __ldg(e), eb = __ldg(e + 1);
+        const f3 pa = mk(ea.x, ea.y, ea.z), pb = mk(eb.x, eb.y, eb.z);
+        f3 cp;
+        const float d = closest_point_segment(pa, pb, o, cp);
+        if (d * d > mr2)
+            continue;
+        const uint32_t flags = __float_as_uint(ea.w);
+        bool is_sil = (flags & 1u) == 0u || (flags & 2u) == 0u;
+        if (!is_sil)
+        {
+            const float4 ec = __ldg(e + 2), ed = __ldg(e + 3);
+            is_sil = is_silhouette_edge(pa, pb, mk(ec.x, ec.y, ec.z), mk(ed.x, ed.y, ed.z),
+                                        mk(o.x - cp.x, o.y - cp.y, o.z - cp.z), d, flip);
+        }
+        if (is_sil && d * d <= mr2)
+        {
+            dist = d;
+            ret = true;
+            mr2 = dist * dist;
+            edge_id = __float_as_int(eb.w);
+        }
+    }
+    return ret;
+}
+
+__global__ void __launch_bounds__(128) silhouette_kernel(TreeView t, const float *__restrict__ pts,
+                                                         const uint8_t *__restrict__ flips, int64_t n,
+                                                         float *__restrict__ out_dist, int32_t *__restrict__ out_edge)
+{
+    const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (q >= n)
+        return;
+    const f3 p = load_point(pts, q);
+    const bool flip = flips ? __ldg(flips + q) != 0 : false;
+    float best = INFINITY;
+    int32_t best_edge = -1;
+    const uint32_t ni = t.num_tris - 1;
+    if (t.num_tris == 1)
+    {
+        float dist = INFINITY;
+        int32_t eid = -1;
+        if (leaf_silhouette(t, 0, p, best * best, dist, flip, eid) && dist <= best)
+        {
+            best = dist;
+            best_edge = eid;
+        }
+    }
+    else if (t.num_tris > 1)
+    {
+        uint32_t sn[kStackDepth];
+        float sd[kStackDepth];
+        int sp = 0;
+        sn[0] = 0;
+        sd[0] = mindist(load_root_box(t.aabbs), p);
+        sp = 1;
+        do
+        {
+            --sp;
+            const uint32_t node = sn[sp];
+            if (sd[sp] > best * best)
+                continue;
+            if (sp > kStackDepth - 2)
+            {
+                atomicOr(t.status, kStatusStackOverflow);
+                best = NAN;
+                best_edge = -1;
+                break;
+            }
+            Box lb, rb;
+            uint32_t L, R;
+            unpack_inner(load_inner(t.inner + node), lb, rb, L, R);
+            const float4 *cr = reinterpret_cast<const float4 *>(t.inner_cones + node);
+            InnerConeRec icr;
+            icr.a = __ldg(cr);
+            icr.b = __ldg(cr + 1);
+            icr.c = __ldg(cr + 2);
+            Cone lc, rc;
+            unpack_cones(icr, lc, rc);
+            const float Lmd = mindist(lb, p), Rmd = mindist(rb, p);
+            const bool hitL = lc.half_angle >= 0.0f && cone_overlap(lc, p, lb, Lmd);
+            const bool hitR = rc.half_angle >= 0.0f && cone_overlap(rc, p, rb, Rmd);
+            if (hitL)
+            {
+                if (L >= ni)
+                {
+                    float dist = INFINITY;
+                    int32_t eid = -1;
+                    if (leaf_silhouette(t, L - ni, p, best * best, dist, flip, eid) && dist <= best)
+                    {
+                        best = dist;
+                        best_edge = eid;
+                    }
+                }
+                else
+                {
+                    sn[sp] = L;
+                    sd[sp] = Lmd;
+                    ++sp;
+                }
+            }
+            if (hitR)
+            {
+                if (R >= ni)
+                {
+                    float dist = INFINITY;
+                    int32_t eid = -1;
+                    if (leaf_silhouette(t, R - ni, p, best * best, dist, flip, eid) && dist <= best)
+                    {
+                        best = dist;
+                        best_edge = eid;
+                    }
+                }
+                else
+                {
+                    sn[sp] = R;
+                    sd[sp] = Rmd;
+                    ++sp;
+                }
+            }
+        } while (sp > 0);
+    }
+    out_dist[q] = best;
+    if (out_edge)
+        out_edge[q] = best_edge;
+}
+
+// ------------------------------------------------------------------ ray
+// intersects_d(ray<float,3>) aabb.cuh:397-431
+SNCH_DEV bool ray_box(f3 o, f3 inv, const Box &b, float max_dist, float &dist)
+{
+    float t1 = (b.lower.x - o.x) * inv.x, t2 = (b.upper.x - o.x) * inv.x;
+    float tmin = fminf(t1, t2), tmax = fmaxf(t1, t2);
+    t1 = (b.lower.y - o.y) * inv.y;
+    t2 = (b.upper.y - o.y) * inv.y;
+    tmin = fmaxf(tmin, fminf(t1, t2));
+    tmax = fminf(tmax, fmaxf(t1, t2));
+    t1 = (b.lower.z - o.z) * inv.z;
+    t2 = (b.upper.z - o.z) * inv.z;
+    tmin = fmaxf(tmin, fminf(t1, t2));
+    tmax = fminf(tmax, fmaxf(t1, t2));
+    if (tmax >= tmin && tmax >= 0.0f && tmin <= max_dist)
+    {
+        dist = tmin >= 0.0f ? tmin : 0.0f;
+        return true;
+    }
+    return false;
+}
+
+// intersect_test scene.cuh:1005-1052 (Moller-Trumbore, __frcp_rn as there)
+SNCH_DEV bool ray_triangle(f3 o, f3 dir, f3 v0, f3 v1, f3 v2, float &t, float &uo, float &vo)
+{
+    const f3 e1 = sub(v1, v0), e2 = sub(v2, v0);
+    const f3 h = mk(dir.y * e2.z - dir.z * e2.y, dir.z * e2.x - dir.x * e2.z, dir.x * e2.y - dir.y * e2.x);
+    const float det = e1.x * h.x + e1.y * h.y + e1.z * h.z;
+    if (fabsf(det) < kEps)
+        return false;
+    const float inv_det = __frcp_rn(det);
+    const f3 s = sub(o, v0);
+    const float u = (s.x * h.x + s.y * h.y + s.z * h.z) * inv_det;
+    if (u < 0.0f || u > 1.0f)
+        return false;
+    const f3 qv = mk(s.y * e1.z - s.z * e1.y, s.z * e1.x - s.x * e1.z, s.x * e1.y - s.y * e1.x);
+    const float v = (dir.x * qv.x + dir.y * qv.y + dir.z * qv.z) * inv_det;
+    if (v < 0.0f || u + v > 1.0f)
+        return false;
+    const float tt = (e2.x * qv.x + e2.y * qv.y + e2.z * qv.z) * inv_det;
+    if (tt >= 0.0f)
+    {
+        t = tt;
+        uo = u;
+        vo = v;
+        return true;
+    }
+    return false;
+}
+
+__global__ void __launch_bounds__(128) ray_kernel(TreeView t, const float *__restrict__ origins,
+                                                  const float *__restrict__ dirs, const float *__restrict__ tmaxs,
+                                                  int64_t n, uint8_t *__restrict__ out_hit, float *__restrict__ out_t,
+                                                  float *__restrict__ out_uv, uint32_t *__restrict__ out_idx)
+{
+    const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (q >= n)
+        return;
+    const f3 o = load_point(origins, q), dir = load_point(dirs, q);
+    const f3 inv = mk(1 / dir.x, 1 / dir.y, 1 / dir.z);  // ray ctor aabb.cuh:305-312
+    const float max_dist = __ldg(tmaxs + q);
+    float min_dist = INFINITY, bu = 0.0f, bv = 0.0f;
+    bool found = false;
+    uint32_t nearest = kInvalid;
+    const uint32_t ni = t.num_tris - 1;
+    if (t.num_tris > 0)
+    {
+        uint32_t sn[kStackDepth];
+        float sd[kStackDepth];
+        int sp = 1;
+        sn[0] = 0;
+        sd[0] = INFINITY;
+        do
+        {
+            --sp;
+            const uint32_t node = sn[sp];
+            if (sd[sp] > min_dist)
+                continue;
+            if (node >= ni)
+            {
+                f3 pa, pb, pc;
+                uint32_t orig, n_owned;
+                load_leaf(t.leaves + (node - ni), pa, pb, pc, orig, n_owned);
+                float tt, uu, vv;
+                if (ray_triangle(o, dir, pa, pb, pc, tt, uu, vv) && tt < max_dist && tt < min_dist)
+                {
+                    min_dist = tt;
+                    found = true;
+                    bu = uu;
+                    bv = vv;
+                    nearest = orig;
+                }
+            }
+            else
+            {
+                if (sp > kStackDepth - 2)
+                {
+                    atomicOr(t.status, kStatusStackOverflow);
+                    found = false;
+                    nearest = kInvalid;
+                    min_dist = NAN;
+                    break;
+                }
+                Box lb, rb;
+                uint32_t L, R;
+                unpack_inner(load_inner(t.inner + node), lb, rb, L, R);
+                float Ld = 0.0f, Rd = 0.0f;
+                const bool Lh = ray_box(o, inv, lb, max_dist, Ld);
+                const bool Rh = ray_box(o, inv, rb, max_dist, Rd);
+                if (Lh && Rh)
+                {
+                    uint32_t closer = L, other = R;
+                    if (Rd < Ld)
+                    {
+                        const float tmp = Ld;
+                        Ld = Rd;
+                        Rd = tmp;
+                        closer = R;
+                        other = L;
+                    }
+                    sn[sp] = other;
+                    sd[sp] = Rd;
+                    ++sp;
+                    sn[sp] = closer;
+                    sd[sp] = Ld;
+                    ++sp;
+                }
+                else if (Lh)
+                {
+                    sn[sp] = L;
+                    sd[sp] = Ld;
+                    ++sp;
+                }
+                else if (Rh)
+                {
+                    sn[sp] = R;
+                    sd[sp] = Rd;
+                    ++sp;
+                }
+            }
+        } while (sp > 0);
+    }
+    out_hit[q] = found ? 1 : 0;
+    out_t[q] = min_dist;
+    out_uv[2 * q] = bu;
+    out_uv[2 * q + 1] = bv;
+    out_idx[q] = nearest;
+}
+
+// ------------------------------------------------------------------ sampling
+// intersect_sphere(sphere, aabb) aabb.cuh:433-449
+SNCH_DEV bool sphere_box(f3 c, float r, const Box &b)
+{
+    const float cx = smax(b.lower.x, smin(c.x, b.upper.x));
+    const float cy = smax(b.lower.y, smin(c.y, b.upper.y));
+    const float dx = cx - c.x, dy = cy - c.y;
+    float d2 = dx * dx + dy * dy;
+    const float cz = smax(b.lower.z, smin(c.z, b.upper.z));
+    const float dz = cz - c.z;
+    d2 += dz * dz;
+    return d2 <= (r * r);
+}
+
+// scene<3>::intersect_sphere scene.cuh:1054-1117
+SNCH_DEV bool sphere_triangle(f3 c, float radius, f3 p1, f3 p2, f3 p3)
+{
+    const f3 e1 = sub(p2, p1), e2 = sub(p3, p1);
+    f3 nn = mk(e1.y * e2.z - e1.z * e2.y, e1.z * e2.x - e1.x * e2.z, e1.x * e2.y - e1.y * e2.x);
+    const float nl = sqrtf(nn.x * nn.x + nn.y * nn.y + nn.z * nn.z);
+    nn = mk(nn.x / nl, nn.y / nl, nn.z / nl);
+    const float d = nn.x * p1.x + nn.y * p1.y + nn.z * p1.z;
+    const float dp = nn.x * c.x + nn.y * c.y + nn.z * c.z - d;
+    const f3 proj = mk(c.x - dp * nn.x, c.y - dp * nn.y, c.z - dp * nn.z);
+    const f3 v0 = sub(p3, p1), v1 = sub(p2, p1), v2 = sub(proj, p1);
+    const float d00 = v0.x * v0.x + v0.y * v0.y + v0.z * v0.z;
+    const float d01 = v0.x * v1.x + v0.y * v1.y + v0.z * v1.z;
+    const float d02 = v0.x * v2.x + v0.y * v2.y + v0.z * v2.z;
+    const float d11 = v1.x * v1.x + v1.y * v1.y + v1.z * v1.z;
+    const float d12 = v1.x * v2.x + v1.y * v2.y + v1.z * v2.z;
+    const float inv = 1.0f / (d00 * d11 - d01 * d01);
+    const float u = (d11 * d02 - d01 * d12) * inv;
+    const float v = (d00 * d12 - d01 * d02) * inv;
+    if (u >= 0 && v >= 0 && u + v <= 1)
+        return fabsf(dp) <= radius;
+    f3 cp = proj;
+    if (u < 0)
+        cp = p1;
+    else if (v < 0)
+        cp = p3;
+    else if (u + v > 1)
+        cp = p2;
+    const float dx = cp.x - c.x, dy = cp.y - c.y, dz = cp.z - c.z;
+    const float d2 = dx * dx + dy * dy + dz * dz;
+    return d2 <= (radius * radius);
+}
+
+// green_weight scene.cuh:1119-1126
+SNCH_DEV float green_weight(f3 x, f3 y)
+{
+    const float r = fmaxf(len3(mk(x.x - y.x, x.y - y.y, x.z - y.z)), 1e-4f);
+    const float four_pi = 3.14159265358979323846f * 4.0f;
+    return 1.0f / (four_pi * r);
+}
+
+__global__ void __launch_bounds__(128) sample_kernel(TreeView t, const float *__restrict__ centers,
+                                                     const float *__restrict__ radii, const float *__restrict__ us,
+                                                     int64_t n, int32_t *__restrict__ out_idx,
+                                                     float *__restrict__ out_pdf)
+{
+    const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (q >= n)
+        return;
+    const f3 c = load_point(centers, q);
+    const float rad = __ldg(radii + q);
+    float u = __ldg(us + q);
+    int32_t oi = -1;
+    float opdf = 0.0f;
+    const uint32_t ni = t.num_tris - 1;
+    if (t.num_tris > 0)
+    {
+        uint32_t node = 0;
+        float npdf = 1.0f;
+        // the reference's stack never holds more than one entry (sample.cuh:41-90);
+        // a descent is at most one step per tree level
+        for (int level = 0; level < 2 * kStackDepth; ++level)
+        {
+            if (node >= ni)
+            {
+                f3 pa, pb, pc;
+                uint32_t orig, n_owned;
+                load_leaf(t.leaves + (node - ni), pa, pb, pc, orig, n_owned);
+                if (sphere_triangle(c, rad, pa, pb, pc))
+                {
+                    oi = (int32_t)orig;
+                    opdf = npdf;
+                    opdf /= len3(cross3(sub(pc, pa), sub(pb, pa))) / 2;  // measurement_getter scene.cuh:855-868
+                }
+                break;
+            }
+            Box lb, rb;
+            uint32_t L, R;
+            unpack_inner(load_inner(t.inner + node), lb, rb, L, R);
+            const float Lw = sphere_box(c, rad, lb) ? green_weight(c, centroid(lb)) : 0;
+            const float Rw = sphere_box(c, rad, rb) ? green_weight(c, centroid(rb)) : 0;
+            const float tw = Lw + Rw;
+            if (!(tw > 0))
+                break;
+            const float Lp = Lw / tw;
+            if (u < Lp)
+            {
+                u /= Lp;
+                node = L;
+                npdf = Lp * npdf;
+            }
+            else
+            {
+                const float Rp = 1.0f - Lp;
+                u = (u - Lp) / Rp;
+                node = R;
+                npdf = Rp * npdf;
+            }
+        }
+    }
+    out_idx[q] = oi;
+    out_pdf[q] = opdf;
+}
+
+// sample_triangle scene.cuh:14-27 on the triangle of ORIGINAL index idx
+__global__ void sample_point_kernel(const float *__restrict__ verts, const int32_t *__restrict__ tris,
+                                    const int32_t *__restrict__ idx, const float *__restrict__ us,
+                                    const float *__restrict__ vs, int64_t n, float *__restrict__ out)
+{
+    const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (q >= n)
+        return;
+    const int32_t *tr = tris + 3 * (int64_t)__ldg(idx + q);
+    const f3 pa = load_vert(verts, __ldg(tr)), pb = load_vert(verts, __ldg(tr + 1)), pc = load_vert(verts, __ldg(tr + 2));
+    float u = __ldg(us + q), v = __ldg(vs + q);
+    if (u + v > 1.0f)
+    {
+        u = 1.0f - u;
+        v = 1.0f - v;
+    }
+    const float w = 1.0f - u - v;
+    out[3 * q] = w * pa.x + u * pb.x + v * pc.x;
+    out[3 * q + 1] = w * pa.y + u * pb.y + v * pc.y;
+    out[3 * q + 2] = w * pa.z + u * pb.z + v * pc.z;
+}
+
+// ------------------------------------------------------------------ launchers
+namespace
+{
+inline unsigned grid_for(int64_t n, int b) { return (unsigned)((n + b - 1) / b); }
+}  // namespace
+
+cudaError_t launch_nearest(const TreeView &t, const float *pts, int64_t n, uint32_t *idx, float *dist, cudaStream_t st)
+{
+    if (n > 0)
+        nearest_kernel<<<grid_for(n, 128), 128, 0, st>>>(t, pts, n, idx, dist);
+        note_launch();
+    return cudaGetLastError();
+}
+cudaError_t launch_silhouette(const TreeView &t, const float *pts, const uint8_t *flip, int64_t n, float *dist,
+                              int32_t *edge, cudaStream_t st)
+{
+    if (n > 0)
+        silhouette_kernel<<<grid_for(n, 128), 128, 0, st>>>(t, pts, flip, n, dist, edge);
+        note_launch();
+    return cudaGetLastError();
+}
+cudaError_t launch_ray(const TreeView &t, const float *o, const float *d, const float *tmax, int64_t n, uint8_t *hit,
+                       float *tt, float *uv, uint32_t *idx, cudaStream_t st)
+{
+    if (n > 0)
+        ray_kernel<<<grid_for(n, 128), 128, 0, st>>>(t, o, d, tmax, n, hit, tt, uv, idx);
+        note_launch();
+    return cudaGetLastError();
+}
+cudaError_t launch_sample(const TreeView &t, const float *c, const float *r, const float *u, int64_t n, int32_t *idx,
+                          float *pdf, cudaStream_t st)
+{
+    if (n > 0)
+        sample_kernel<<<grid_for(n, 128), 128, 0, st>>>(t, c, r, u, n, idx, pdf);
+        note_launch();
+    return cudaGetLastError();
+}
+cudaError_t launch_sample_point(const float *verts, const int32_t *tris, const int32_t *idx, const float *u,
+                                const float *v, int64_t n, float *out, cudaStream_t st)
+{
+    if (n > 0)
+        sample_point_kernel<<<grid_for(n, 256), 256, 0, st>>>(verts, tris, idx, u, v, n, out);
+        note_launch();
+    return cudaGetLastError();
+}
+
+}  // namespace snch

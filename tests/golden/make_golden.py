@@ -1,0 +1,180 @@
+"""Generate the golden vectors under tests/golden/ from the reference's own code.
+
+Runs oracle/_ref/ref_harness -- the unmodified tyanyuy3125/snch-lbvh headers
+compiled as host C++ (oracle/Makefile) -- on seeded inputs and stores inputs
+and outputs as compressed .npz fixtures. Needs the reference checkout, so it
+runs only where the reference exists; the fixtures it writes are committed.
+
+    python tests/golden/make_golden.py
+
+Harness file layout (little endian):
+  in : int64[7] {nv, nt, n_near, n_sil, n_ray, n_smp, n_obj}, verts f32[nv*3],
+       tris i32[nt*3], near f32[*3], sil f32[*3], sil_flip u8[], ray_o f32[*3],
+       ray_d f32[*3], ray_tmax f32[], smp_c f32[*3], smp_r f32[], smp_u f32[],
+       obj_idx i32[], obj_u f32[], obj_v f32[]
+  out: int64[2] {E, NN}, tri_edges i32[nt*3], tri_owned i32[nt*3],
+       edge_verts i32[E*4], morton u32[nt], nodes u32[NN*4], aabbs f32[NN*6],
+       cones f32[NN*5], near {u32 idx, f32 dist}, sil f32, ray {u8 hit, f32 t,
+       f32 u, f32 v, u32 idx}, smp {i32 idx, f32 pdf}, obj f32[*3]
+"""
+from __future__ import annotations
+
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+
+from oracle import oracle  # noqa: E402
+from snch_lbvh_gb300 import meshes  # noqa: E402
+
+OUT = os.path.dirname(os.path.abspath(__file__))
+
+
+def run_harness(verts, tris, q):
+    nv, nt = len(verts), len(tris)
+    n_near, n_sil, n_ray = len(q["near_pts"]), len(q["sil_pts"]), len(q["ray_o"])
+    n_smp, n_obj = len(q["smp_c"]), len(q["obj_idx"])
+    with tempfile.TemporaryDirectory() as td:
+        fin, fout = os.path.join(td, "in.bin"), os.path.join(td, "out.bin")
+        with open(fin, "wb") as f:
+            np.array([nv, nt, n_near, n_sil, n_ray, n_smp, n_obj], np.int64).tofile(f)
+            for a, dt in [(verts, np.float32), (tris, np.int32), (q["near_pts"], np.float32),
+                          (q["sil_pts"], np.float32), (q["sil_flip"], np.uint8), (q["ray_o"], np.float32),
+                          (q["ray_d"], np.float32), (q["ray_tmax"], np.float32), (q["smp_c"], np.float32),
+                          (q["smp_r"], np.float32), (q["smp_u"], np.float32), (q["obj_idx"], np.int32),
+                          (q["obj_u"], np.float32), (q["obj_v"], np.float32)]:
+                np.ascontiguousarray(a, dtype=dt).tofile(f)
+        subprocess.run([oracle.REF_HARNESS, fin, fout], check=True, stdout=subprocess.DEVNULL)
+        buf = open(fout, "rb").read()
+    off = 0
+
+    def take(dt, n):
+        nonlocal off
+        a = np.frombuffer(buf, dtype=dt, count=n, offset=off)
+        off += a.nbytes
+        return a.copy()
+
+    E, NN = take(np.int64, 2)
+    r = {}
+    r["ref_tri_edges"] = take(np.int32, nt * 3).reshape(nt, 3)
+    r["ref_tri_owned"] = take(np.int32, nt * 3).reshape(nt, 3)
+    r["ref_edge_verts"] = take(np.int32, E * 4).reshape(E, 4)
+    r["ref_morton"] = take(np.uint32, nt)
+    r["ref_nodes"] = take(np.uint32, NN * 4).reshape(NN, 4)
+    r["ref_aabbs"] = take(np.float32, NN * 6).reshape(NN, 6)
+    r["ref_cones"] = take(np.float32, NN * 5).reshape(NN, 5)
+    tree_ok = nt >= 2
+    nn_, ns_ = (n_near, n_sil) if tree_ok else (0, 0)
+    rec = take(np.uint8, nn_ * 8).reshape(-1, 8)
+    r["ref_near_idx"] = rec[:, :4].copy().view(np.uint32).reshape(-1)
+    r["ref_near_dist"] = rec[:, 4:].copy().view(np.float32).reshape(-1)
+    r["ref_sil_dist"] = take(np.float32, ns_)
+    rec = take(np.uint8, n_ray * 17).reshape(-1, 17)
+    r["ref_ray_hit"] = rec[:, 0].copy()
+    r["ref_ray_t"] = rec[:, 1:5].copy().view(np.float32).reshape(-1)
+    r["ref_ray_uv"] = rec[:, 5:13].copy().view(np.float32).reshape(-1, 2)
+    r["ref_ray_idx"] = rec[:, 13:17].copy().view(np.uint32).reshape(-1)
+    rec = take(np.uint8, n_smp * 8).reshape(-1, 8)
+    r["ref_smp_idx"] = rec[:, :4].copy().view(np.int32).reshape(-1)
+    r["ref_smp_pdf"] = rec[:, 4:].copy().view(np.float32).reshape(-1)
+    r["ref_obj_pts"] = take(np.float32, n_obj * 3).reshape(-1, 3)
+    assert off == len(buf), (off, len(buf))
+    return r
+
+
+def make_queries(verts, tris, seed, n_rand=512, extra=True):
+    """Random points in the AABB x 1.5 plus exact-tie probes (vertices, edge
+    midpoints, face centroids, offset along face normals), rays (random and
+    axis-aligned), sphere draws and on-object samples."""
+    rng = np.random.default_rng(seed)
+    v = verts.astype(np.float64)
+    lo, hi = v.min(0), v.max(0)
+    c, h = 0.5 * (lo + hi), 0.5 * np.maximum(hi - lo, 1e-3) * 1.5
+    pts = [c + (rng.random((n_rand, 3)) * 2 - 1) * h]
+    if extra:
+        k = min(len(tris), 64)
+        sel = rng.choice(len(tris), k, replace=False)
+        a, b, cc = v[tris[sel, 0]], v[tris[sel, 1]], v[tris[sel, 2]]
+        n = np.cross(b - a, cc - a)
+        nn = np.linalg.norm(n, axis=1, keepdims=True)
+        n = np.where(nn > 0, n / np.where(nn > 0, nn, 1), 0)
+        pts += [a, 0.5 * (a + b), (a + b + cc) / 3, (a + b + cc) / 3 + 0.01 * n, 0.5 * (a + b) - 0.02 * n]
+    pts = np.concatenate(pts, 0).astype(np.float32)
+    q = {"near_pts": pts, "sil_pts": pts, "sil_flip": (rng.random(len(pts)) < 0.5).astype(np.uint8)}
+    nr = len(pts)
+    d = rng.standard_normal((nr, 3))
+    axis = rng.integers(0, 3, nr)
+    axial = rng.random(nr) < 0.15
+    d[axial] = 0.0
+    d[axial, axis[axial]] = np.where(rng.random(axial.sum()) < 0.5, -1.0, 1.0)
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    q["ray_o"] = pts
+    q["ray_d"] = d.astype(np.float32)
+    q["ray_tmax"] = np.where(rng.random(nr) < 0.2, np.float32(np.inf),
+                             np.exp(rng.uniform(np.log(1e-3), np.log(4 * h.max()), nr))).astype(np.float32)
+    q["smp_c"] = pts
+    q["smp_r"] = np.exp(rng.uniform(np.log(1e-3), np.log(2 * h.max()), nr)).astype(np.float32)
+    q["smp_u"] = rng.random(nr).astype(np.float32)
+    m = min(256, 4 * len(tris))
+    q["obj_idx"] = rng.integers(0, len(tris), m).astype(np.int32)
+    q["obj_u"] = rng.random(m).astype(np.float32)
+    q["obj_v"] = rng.random(m).astype(np.float32)
+    return q
+
+
+def cases():
+    tet_v = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1]], np.float32)
+    tet_f = np.array([[0, 2, 1], [0, 1, 3], [0, 3, 2], [1, 2, 3]], np.int32)
+    yield "tetra", tet_v, tet_f, 11
+    yield "single_tri", np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], np.float32), np.array([[0, 1, 2]], np.int32), 12
+    yield "two_tri", np.array([[0, 0, 0], [1, 0, 0], [1, 1, 0], [0, 1, 0]], np.float32), \
+        np.array([[0, 1, 2], [0, 2, 3]], np.int32), 13
+    # open flat grid: coplanar neighbours (dihedral branch of is_silhouette_edge) and boundary edges
+    g = 12
+    xs, ys = np.meshgrid(np.arange(g + 1), np.arange(g + 1), indexing="ij")
+    gv = np.stack([xs.ravel() / g, ys.ravel() / g, np.zeros(xs.size)], 1).astype(np.float32)
+    gi = np.arange(g)[:, None] * (g + 1) + np.arange(g)[None, :]
+    gf = np.concatenate([np.stack([gi, gi + g + 1, gi + g + 2], -1).reshape(-1, 3),
+                         np.stack([gi, gi + g + 2, gi + 1], -1).reshape(-1, 3)]).astype(np.int32)
+    yield "open_grid", gv, gf, 14
+    v, f = meshes.noisy_icosphere(3, 1.0, 0.01, seed=5)
+    yield "ico3", v, f, 15
+    v, f = meshes.noisy_torus(0.4, 0.1, 24, 12, 0.004, seed=6)
+    yield "torus_small", v, f, 16
+    # every triangle twice (and some three times): duplicated Morton codes force
+    # the 64-bit key path (bvh.cuh:459-476); edges with 4-6 faces exercise the
+    # overwrite order of compute_silhouettes
+    v, f = meshes.noisy_icosphere(2, 1.0, 0.02, seed=7)
+    f = np.concatenate([f, f[::-1], f[:40]]).astype(np.int32)
+    yield "duplicated", v, f, 17
+    # degenerate triangles: a repeated vertex id and collinear vertices
+    v, f = meshes.noisy_icosphere(1, 1.0, 0.0, seed=8)
+    extra_v = np.array([[2, 0, 0], [2.5, 0, 0], [3, 0, 0]], np.float32)
+    v = np.concatenate([v, extra_v]).astype(np.float32)
+    n0 = len(v) - 3
+    f = np.concatenate([f, [[n0, n0 + 1, n0 + 2], [n0, n0, n0 + 1]]]).astype(np.int32)
+    yield "degenerate", v, f, 18
+    v, f = meshes.noisy_icosphere(5, 1.0, 0.01, seed=0)
+    yield "cfg1_icosphere_l5", v, f, 19
+
+
+def main():
+    oracle.build()
+    for name, v, f, seed in cases():
+        q = make_queries(v, f, seed, n_rand=2048 if name.startswith("cfg1") else 512)
+        tree = oracle.Tree(v, f)
+        depth = tree.max_depth()
+        assert depth < 60, f"{name}: tree depth {depth} would overflow the reference's 64-entry stacks"
+        r = run_harness(v, f, q)
+        path = os.path.join(OUT, f"{name}.npz")
+        np.savez_compressed(path, verts=v, tris=f, **q, **r)
+        print(f"{name:22s} tris={len(f):6d} depth={depth:3d} unique={tree.unique} -> {os.path.getsize(path)/1024:.0f} KiB")
+
+
+if __name__ == "__main__":
+    main()

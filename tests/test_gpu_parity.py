@@ -1,0 +1,188 @@
+"""CUDA path (through the C ABI) against the reference's own outputs and the oracle.
+
+Bars:
+  * topology, Morton codes, sorted order, nodes, AABBs: bit-exact;
+  * nearest / ray / sphere-sample / sample-on-object: bit-exact indices and floats
+    (same IEEE operation sequence, no contraction, correctly rounded / and sqrt);
+  * normal cones: CUDA's acosf/sinf/cosf vs libm: |diff| <= CONE_TOL (radians /
+    unit-axis components) on every node whose cone is defined in the reference;
+  * silhouette distances: bit-exact except where a cone test on the cull
+    boundary flips; such queries must still agree within SIL_RTOL relative and
+    be rarer than SIL_MAX_FLIP_FRACTION.
+"""
+import numpy as np
+import pytest
+
+from conftest import d1_tainted, golden_names, load_golden
+
+pytestmark = pytest.mark.gpu
+
+CONE_TOL = 2e-5
+SIL_RTOL = 1e-6
+SIL_MAX_FLIP_FRACTION = 1e-3
+
+
+def bits(a):
+    return np.ascontiguousarray(a).view(np.uint32)
+
+
+@pytest.fixture(scope="module")
+def snch():
+    import torch
+    assert torch.cuda.is_available(), "GPU tests need a CUDA device"
+    import snch_lbvh_gb300
+    snch_lbvh_gb300.lib()
+    return snch_lbvh_gb300
+
+
+def built_scene(snch, verts, tris):
+    s = snch.Scene(verts, tris)
+    s.compute_silhouettes()
+    s.build_bvh()
+    return s
+
+
+def check_cones(gpu_cones, ref_cones, nodes, d1):
+    taint = d1_tainted(nodes, d1)
+    valid = ref_cones[:, 3] >= 0
+    np.testing.assert_array_equal((gpu_cones[:, 3] >= 0)[~taint], valid[~taint])
+    ok = valid & ~taint
+    diff = np.abs(gpu_cones[ok].astype(np.float64) - ref_cones[ok])
+    rad = np.abs(ref_cones[ok, 4]).astype(np.float64)
+    assert diff[:, :4].max(initial=0) <= CONE_TOL, diff[:, :4].max()
+    assert np.all(diff[:, 4] <= CONE_TOL * np.maximum(rad, 1.0))
+    assert np.all(gpu_cones[taint, 3] >= 0)
+
+
+def check_silhouette(gpu, ref):
+    same = bits(gpu) == bits(ref)
+    both_inf = np.isinf(gpu) & np.isinf(ref)
+    flips = ~(same | both_inf)
+    assert flips.mean() <= SIL_MAX_FLIP_FRACTION, (flips.sum(), len(gpu))
+    fin = flips & np.isfinite(gpu) & np.isfinite(ref)
+    if fin.any():
+        rel = np.abs(gpu[fin] - ref[fin]) / np.maximum(np.abs(ref[fin]), 1e-30)
+        assert rel.max() <= SIL_RTOL or flips.sum() <= max(1, int(SIL_MAX_FLIP_FRACTION * len(gpu)))
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_build_matches_reference(snch, oracle_mod, name):
+    g = load_golden(name)
+    s = built_scene(snch, g["verts"], g["tris"])
+    te, to, ev = s.export_topology()
+    np.testing.assert_array_equal(te, g["ref_tri_edges"])
+    np.testing.assert_array_equal(to, g["ref_tri_owned"])
+    np.testing.assert_array_equal(ev, g["ref_edge_verts"])
+    tr = s.export_tree()
+    n = len(g["tris"])
+    ref_sorted = g["ref_nodes"][n - 1:, 3]
+    np.testing.assert_array_equal(tr["sorted_idx"], ref_sorted)
+    np.testing.assert_array_equal(tr["morton"], g["ref_morton"][ref_sorted])
+    np.testing.assert_array_equal(tr["nodes"], g["ref_nodes"])
+    np.testing.assert_array_equal(bits(tr["aabbs"]), bits(g["ref_aabbs"]))
+    orc = oracle_mod.Tree(g["verts"], g["tris"])
+    check_cones(tr["cones"], g["ref_cones"], orc.nodes, orc.d1)
+    assert s.device_status() == 0
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_queries_match_reference(snch, name):
+    g = load_golden(name)
+    s = built_scene(snch, g["verts"], g["tris"])
+    if len(g["ref_near_idx"]):
+        idx, dist = s.query_nearest(g["near_pts"])
+        np.testing.assert_array_equal(idx.cpu().numpy().view(np.uint32), g["ref_near_idx"])
+        np.testing.assert_array_equal(bits(dist.cpu().numpy()), bits(g["ref_near_dist"]))
+        sd, _ = s.query_silhouette(g["sil_pts"], g["sil_flip"])
+        check_silhouette(sd.cpu().numpy(), g["ref_sil_dist"])
+    hit, t, uv, ri = s.query_ray(g["ray_o"], g["ray_d"], g["ray_tmax"])
+    np.testing.assert_array_equal(hit.cpu().numpy(), g["ref_ray_hit"])
+    np.testing.assert_array_equal(bits(t.cpu().numpy()), bits(g["ref_ray_t"]))
+    np.testing.assert_array_equal(bits(uv.cpu().numpy()), bits(g["ref_ray_uv"]))
+    np.testing.assert_array_equal(ri.cpu().numpy().view(np.uint32), g["ref_ray_idx"])
+    si, sp = s.sample_in_sphere(g["smp_c"], g["smp_r"], g["smp_u"])
+    np.testing.assert_array_equal(si.cpu().numpy(), g["ref_smp_idx"])
+    np.testing.assert_array_equal(bits(sp.cpu().numpy()), bits(g["ref_smp_pdf"]))
+    pts = s.sample_on_object(g["obj_idx"], g["obj_u"], g["obj_v"])
+    np.testing.assert_array_equal(bits(pts.cpu().numpy()), bits(g["ref_obj_pts"]))
+    assert s.device_status() == 0
+
+
+def test_config1_workload_against_oracle(snch, oracle_mod):
+    """Config 1: level-5 noisy icosphere, 1M nearest queries uniform in the AABB x 1.2."""
+    from snch_lbvh_gb300 import meshes
+    v, f = meshes.noisy_icosphere(5, 1.0, 0.01, seed=0)
+    pts = meshes.box_queries(v, 1_000_000, 1.2, seed=1)
+    s = built_scene(snch, v, f)
+    idx, dist = s.query_nearest(pts)
+    idx, dist = idx.cpu().numpy().view(np.uint32), dist.cpu().numpy()
+    orc = oracle_mod.Tree(v, f)
+    oi, od = orc.nearest(pts)
+    np.testing.assert_array_equal(idx, oi)
+    np.testing.assert_array_equal(bits(dist), bits(od))
+    # FP64 brute force on a subset: the FP32 path's error bound
+    sub = np.arange(0, len(pts), 122)[:8192]
+    bi, bd = oracle_mod.brute_nearest_f64(v, f, pts[sub])
+    rel = np.abs(dist[sub].astype(np.float64) - bd) / np.maximum(bd, 1e-12)
+    assert rel.max() < 1e-5, rel.max()
+    assert s.device_status() == 0
+
+
+def test_host_forms_equal_device_forms(snch):
+    from snch_lbvh_gb300 import meshes
+    v, f = meshes.noisy_icosphere(4, 1.0, 0.01, seed=2)
+    q = meshes.wost_queries(300_000, 300_000, 300_000, 100_000, seed=4)
+    s = built_scene(snch, v * 0.4 + 0.5, f)
+    i1, d1 = s.query_nearest(q["near_pts"])
+    i2, d2 = s.query_nearest_host(q["near_pts"])
+    np.testing.assert_array_equal(i1.cpu().numpy().view(np.uint32), i2)
+    np.testing.assert_array_equal(bits(d1.cpu().numpy()), bits(d2))
+    s1, e1 = s.query_silhouette(q["sil_pts"], q["sil_flip"])
+    s2, e2 = s.query_silhouette_host(q["sil_pts"], q["sil_flip"])
+    np.testing.assert_array_equal(bits(s1.cpu().numpy()), bits(s2))
+    np.testing.assert_array_equal(e1.cpu().numpy(), e2)
+    r1 = s.query_ray(q["ray_o"], q["ray_d"], q["ray_tmax"])
+    r2 = s.query_ray_host(q["ray_o"], q["ray_d"], q["ray_tmax"])
+    np.testing.assert_array_equal(r1[0].cpu().numpy(), r2[0])
+    np.testing.assert_array_equal(bits(r1[1].cpu().numpy()), bits(r2[1]))
+    np.testing.assert_array_equal(bits(r1[2].cpu().numpy()), bits(r2[2]))
+    np.testing.assert_array_equal(r1[3].cpu().numpy().view(np.uint32), r2[3])
+    p1 = s.sample_in_sphere(q["smp_c"], q["smp_r"], q["smp_u"])
+    p2 = s.sample_in_sphere_host(q["smp_c"], q["smp_r"], q["smp_u"])
+    np.testing.assert_array_equal(p1[0].cpu().numpy(), p2[0])
+    np.testing.assert_array_equal(bits(p1[1].cpu().numpy()), bits(p2[1]))
+
+
+def test_query_before_build_raises(snch):
+    import torch
+    s = snch.Scene(np.eye(3, dtype=np.float32), np.array([[0, 1, 2]], np.int32))
+    with pytest.raises(snch.SnchError, match="BVH is not built yet."):
+        s.query_nearest(torch.zeros((4, 3), device="cuda"))
+    with pytest.raises(snch.SnchError, match="BVH is not built yet."):
+        s.get_bvh_device_ptr()
+
+
+def test_empty_and_single_triangle(snch):
+    empty = snch.Scene(np.zeros((0, 3), np.float32), np.zeros((0, 3), np.int32))
+    empty.build_bvh()
+    idx, dist = empty.query_nearest(np.zeros((5, 3), np.float32))
+    assert np.all(idx.cpu().numpy() == -1) and np.all(np.isinf(dist.cpu().numpy()))
+    hit, t, _, ri = empty.query_ray(np.zeros((2, 3), np.float32), np.ones((2, 3), np.float32), np.ones(2, np.float32))
+    assert not hit.cpu().numpy().any()
+    one = built_scene(snch, np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], np.float32), np.array([[0, 1, 2]], np.int32))
+    idx, dist = one.query_nearest(np.array([[0.2, 0.2, 1.0], [2.0, 0.0, 0.0]], np.float32))
+    np.testing.assert_array_equal(idx.cpu().numpy(), [0, 0])
+    np.testing.assert_allclose(dist.cpu().numpy(), [1.0, 1.0], rtol=1e-6)
+    view = one.get_bvh_device_ptr()
+    assert view.num_nodes == 1 and view.num_objects == 1
+
+
+def test_device_create_validates_indices(snch):
+    import torch
+    v = torch.zeros((3, 3), device="cuda")
+    bad = torch.tensor([[0, 1, 7]], dtype=torch.int32, device="cuda")
+    with pytest.raises(snch.SnchError, match="out of range"):
+        snch.Scene(v, bad)
+    ok = snch.Scene(v + torch.eye(3, device="cuda"), torch.tensor([[0, 1, 2]], dtype=torch.int32, device="cuda"))
+    ok.build_bvh()
+    assert ok.info() == (3, 1, 3)

@@ -1,0 +1,90 @@
+"""Full-size checks on the two-million-triangle walk-on-stars scene (64 placed
+tori and icospheres): the whole build bit-exact against the oracle, queries
+against the oracle on a seeded subset, determinism and size-independent
+properties of the tree."""
+import numpy as np
+import pytest
+
+from test_gpu_parity import bits, built_scene, check_cones, check_silhouette
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def big(oracle_mod):
+    import torch
+    assert torch.cuda.is_available()
+    import snch_lbvh_gb300
+    from snch_lbvh_gb300 import meshes
+    sc = meshes.wost_scene(seed=0)
+    s = built_scene(snch_lbvh_gb300, sc.verts, sc.faces)
+    orc = oracle_mod.Tree(sc.verts, sc.faces)
+    return sc, s, orc
+
+
+def test_full_build_bit_exact(big):
+    sc, s, orc = big
+    assert len(sc.faces) == 1_993_600
+    te, to, ev = s.export_topology()
+    np.testing.assert_array_equal(te, orc.tri_edges)
+    np.testing.assert_array_equal(to, orc.tri_owned)
+    np.testing.assert_array_equal(ev, orc.edge_verts)
+    tr = s.export_tree()
+    np.testing.assert_array_equal(tr["sorted_idx"], orc.sorted_idx)
+    np.testing.assert_array_equal(tr["morton"], orc.morton[orc.sorted_idx])
+    np.testing.assert_array_equal(tr["nodes"], orc.nodes)
+    np.testing.assert_array_equal(bits(tr["aabbs"]), bits(orc.aabbs))
+    check_cones(tr["cones"], orc.cones, orc.nodes, orc.d1)
+    assert s.device_status() == 0
+
+
+def test_tree_properties(big):
+    sc, s, _ = big
+    tr = s.export_tree()
+    n = len(sc.faces)
+    m = tr["morton"]
+    assert np.all(m[1:] >= m[:-1]), "Morton codes must come out sorted"
+    same = m[1:] == m[:-1]
+    assert np.all(tr["sorted_idx"][1:][same] > tr["sorted_idx"][:-1][same]), "sort must be stable"
+    assert np.array_equal(np.sort(tr["sorted_idx"]), np.arange(n, dtype=np.uint32))
+    nodes = tr["nodes"]
+    ni = n - 1
+    L, R = nodes[:ni, 1], nodes[:ni, 2]
+    assert np.all(nodes[L, 0] == np.arange(ni)) and np.all(nodes[R, 0] == np.arange(ni))
+    child_count = np.bincount(np.concatenate([L, R]), minlength=2 * n - 1)
+    assert child_count[0] == 0 and np.all(child_count[1:] == 1)
+    a = tr["aabbs"]
+    for c in (L, R):
+        assert np.all(a[:ni, :3] >= a[c, :3]) and np.all(a[:ni, 3:] <= a[c, 3:])
+
+
+def test_build_is_deterministic(big):
+    import snch_lbvh_gb300
+    sc, s, _ = big
+    s2 = built_scene(snch_lbvh_gb300, sc.verts, sc.faces)
+    t1, t2 = s.export_tree(), s2.export_tree()
+    for k in t1:
+        np.testing.assert_array_equal(bits(t1[k]), bits(t2[k]))
+
+
+def test_queries_against_oracle_subset(big):
+    from snch_lbvh_gb300 import meshes
+    sc, s, orc = big
+    q = meshes.wost_queries(200_000, 100_000, 200_000, 200_000, seed=11)
+    idx, dist = s.query_nearest(q["near_pts"])
+    oi, od = orc.nearest(q["near_pts"])
+    np.testing.assert_array_equal(idx.cpu().numpy().view(np.uint32), oi)
+    np.testing.assert_array_equal(bits(dist.cpu().numpy()), bits(od))
+    sd, _ = s.query_silhouette(q["sil_pts"], q["sil_flip"])
+    osd, _ = orc.silhouette(q["sil_pts"], q["sil_flip"])
+    check_silhouette(sd.cpu().numpy(), osd)
+    hit, t, uv, ri = s.query_ray(q["ray_o"], q["ray_d"], q["ray_tmax"])
+    oh, ot, ouv, oi = orc.ray(q["ray_o"], q["ray_d"], q["ray_tmax"])
+    np.testing.assert_array_equal(hit.cpu().numpy(), oh)
+    np.testing.assert_array_equal(bits(t.cpu().numpy()), bits(ot))
+    np.testing.assert_array_equal(ri.cpu().numpy().view(np.uint32), oi)
+    si, sp = s.sample_in_sphere(q["smp_c"], q["smp_r"], q["smp_u"])
+    osi, osp = orc.sample(q["smp_c"], q["smp_r"], q["smp_u"])
+    np.testing.assert_array_equal(si.cpu().numpy(), osi)
+    np.testing.assert_array_equal(bits(sp.cpu().numpy()), bits(osp))
+    assert s.device_status() == 0
