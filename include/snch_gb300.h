@@ -118,6 +118,19 @@ int snch_export_tree(snch_scene_t scene, uint32_t *sorted_morton, uint32_t *sort
 int snch_export_topology(snch_scene_t scene, int32_t *tri_edges, int32_t *tri_owned, int32_t *edge_verts,
                          snch_stream_t stream);
 
+/* Traversal order of the nearest-primitive and nearest-silhouette queries.
+ * NEAR_FIRST (default) searches the nearer child first; REFERENCE_ORDER replays
+ * the reference's stack order (query.cuh:256-316, 344-421). Both return the
+ * same indices and distances: exact ties are resolved with each leaf's
+ * position in the reference's depth-first order. */
+#define SNCH_TRAVERSAL_NEAR_FIRST 0
+#define SNCH_TRAVERSAL_REFERENCE_ORDER 1
+int snch_set_traversal(snch_scene_t scene, int mode);
+
+/* Position of each sorted leaf in the reference's depth-first visit order,
+ * copied to a HOST buffer of N entries (synchronous). */
+int snch_export_leaf_ranks(snch_scene_t scene, uint32_t *ranks);
+
 /* ------------------------------------------------------------------ queries
  * All buffers are DEVICE buffers of n entries (float3 = 3 packed floats). */
 
@@ -161,6 +174,15 @@ int snch_query_ray_host(snch_scene_t scene, const float *origins_xyz, const floa
                         int64_t n, uint8_t *out_hit, float *out_t, float *out_uv, uint32_t *out_index);
 int snch_sample_in_sphere_host(snch_scene_t scene, const float *centers_xyz, const float *radii, const float *u,
                                int64_t n, int32_t *out_index, float *out_pdf);
+
+/* Work counters of the traversal these calls run: for each of n queries, 3
+ * words {internal nodes expanded, leaves evaluated, silhouette edges
+ * evaluated} into the DEVICE buffer `visits` (results are discarded). kind:
+ * 0 nearest (in0 = points), 1 silhouette (in0 = points, flip), 2 ray
+ * (in0, in1, in2 = origins, dirs, tmax), 3 sphere sample (centers, radii, u).
+ * Used to count algorithmic bytes; no reference counterpart. */
+int snch_query_visits(snch_scene_t scene, int kind, const float *in0, const float *in1, const float *in2,
+                      const uint8_t *flip, int64_t n, uint32_t *visits, snch_stream_t stream);
 
 /* ------------------------------------------------------------------ building blocks */
 

@@ -63,6 +63,7 @@ def _declare(L):
     L.orc_brute_ray_f64.argtypes = [P, P, I64, P, P, P, I64, P, P, P, I]
     L.orc_max_depth.argtypes = [P, I64]
     L.orc_max_depth.restype = I
+    L.orc_leaf_ranks.argtypes = [P, I64, P]
 
 
 def _p(a: np.ndarray | None):
@@ -107,6 +108,11 @@ class Tree:
     @property
     def num_tris(self):
         return len(self.tris)
+
+    def leaf_ranks(self):
+        r = np.empty(self.num_tris, np.uint32)
+        lib().orc_leaf_ranks(_p(self.nodes), self.num_tris, _p(r))
+        return r
 
     def max_depth(self) -> int:
         return lib().orc_max_depth(_p(self.nodes), self.num_tris)

@@ -497,6 +497,25 @@ int orc_max_depth(const uint32_t *nodes, int64_t nt) {
     return best;
 }
 
+void orc_leaf_ranks(const uint32_t *nodes, int64_t nt, uint32_t *ranks) {
+    if (nt <= 0) return;
+    if (nt == 1) { ranks[0] = 0; return; }
+    const uint32_t NI = (uint32_t)(nt - 1);
+    uint32_t *stk = (uint32_t *)malloc(sizeof(uint32_t) * (size_t)nt);
+    int64_t sp = 0;
+    uint32_t r = 0;
+    stk[sp++] = 0;
+    while (sp > 0) {
+        uint32_t n = stk[--sp];
+        uint32_t L = nodes[4 * n + 1], R = nodes[4 * n + 2];
+        if (L >= NI) ranks[L - NI] = r++;
+        if (R >= NI) ranks[R - NI] = r++;
+        if (L < NI) stk[sp++] = L;
+        if (R < NI) stk[sp++] = R;
+    }
+    free(stk);
+}
+
 /* ----------------------------------------------------------- query math */
 /* mindist aabb.cuh:144-150 */
 static inline float mindist(box3 b, f3 p) {

@@ -102,6 +102,11 @@ void orc_brute_ray_f64(const float *verts, const int32_t *tris, int64_t nt, cons
 
 int orc_max_depth(const uint32_t *nodes, int64_t nt);
 
+/* Position of every sorted leaf in the reference's full depth-first order
+ * (query.cuh:256-316: leaf children evaluated left then right when a node is
+ * expanded; the right child is pushed last and so expanded first). */
+void orc_leaf_ranks(const uint32_t *nodes, int64_t nt, uint32_t *ranks);
+
 #ifdef __cplusplus
 }
 #endif

@@ -22,6 +22,8 @@ from ._ffi import BvhView, SnchError, check, lib  # noqa: F401
 __all__ = ["Scene", "SnchError", "BvhView", "lib"]
 
 INVALID = 0xFFFFFFFF
+TRAVERSAL_NEAR_FIRST = 0
+TRAVERSAL_REFERENCE_ORDER = 1
 
 
 def _torch():
@@ -106,6 +108,16 @@ class Scene:
         check(lib().snch_get_bvh_view(self._h, C.byref(v)))
         return v
 
+    def set_traversal(self, mode: int):
+        """TRAVERSAL_NEAR_FIRST (default) or TRAVERSAL_REFERENCE_ORDER; same results."""
+        check(lib().snch_set_traversal(self._h, int(mode)))
+
+    def leaf_ranks(self):
+        n = self.num_triangles
+        r = np.empty(n, np.uint32)
+        check(lib().snch_export_leaf_ranks(self._h, r.ctypes.data_as(C.c_void_p)))
+        return r
+
     def info(self):
         nv, nt, ne = C.c_int64(), C.c_int64(), C.c_int64()
         check(lib().snch_scene_info(self._h, C.byref(nv), C.byref(nt), C.byref(ne)))
@@ -146,6 +158,21 @@ class Scene:
         check(lib().snch_export_topology(self._h, _ptr(te), _ptr(to), _ptr(ev), _stream(stream)))
         torch.cuda.synchronize()
         return te.cpu().numpy(), to.cpu().numpy(), ev.cpu().numpy()
+
+    def query_visits(self, kind: str, *inputs, flip=None, stream=None):
+        """Per-query work counters {internal nodes, leaves, silhouette edges} of the
+        traversal the library runs, for kind in nearest|silhouette|ray|sample."""
+        torch = _torch()
+        k = {"nearest": 0, "silhouette": 1, "ray": 2, "sample": 3}[kind]
+        cols = {0: [3], 1: [3], 2: [3, 3, None], 3: [3, None, None]}[k]
+        ins = [_dev(x, torch.float32, c) for x, c in zip(inputs, cols)]
+        ins += [None] * (3 - len(ins))
+        n = ins[0].shape[0]
+        f = None if flip is None else _dev(flip, torch.uint8)
+        out = torch.empty((n, 3), dtype=torch.int32, device="cuda")
+        check(lib().snch_query_visits(self._h, k, _ptr(ins[0]), _ptr(ins[1]), _ptr(ins[2]), _ptr(f), n, _ptr(out),
+                                      _stream(stream)))
+        return out.cpu().numpy().view(np.uint32)
 
     # ------------------------------------------------------------ device-buffer queries
     def query_nearest(self, points, stream=None, out=None):

@@ -67,12 +67,14 @@ struct snch_scene_s
     LeafRec *leaves = nullptr;
     EdgeRec *edges = nullptr;
     uint32_t *keys = nullptr, *vals = nullptr, *keys_tmp = nullptr, *vals_tmp = nullptr, *flags = nullptr;
+    uint32_t *sizes = nullptr;
     float4 *centroids = nullptr;
     uint32_t *small = nullptr;
     void *scratch = nullptr;
     snch_triangle *ref_objects = nullptr;
     snch_silhouette_edge *ref_edges = nullptr;
     bool topology_ready = false, built = false;
+    int traversal = SNCH_TRAVERSAL_NEAR_FIRST;
     cudaStream_t pipe[2] = {nullptr, nullptr};
     HostStage stage;
 
@@ -87,6 +89,7 @@ struct snch_scene_s
         t.leaves = leaves;
         t.edges = edges;
         t.status = small + kWStatus;
+        t.near_first = traversal == SNCH_TRAVERSAL_NEAR_FIRST ? 1 : 0;
         return t;
     }
 };
@@ -106,7 +109,7 @@ void free_scene(snch_scene_s *s)
 {
     void *ptrs[] = {s->verts, s->tris, s->tri_edges, s->tri_owned, s->edge_verts, s->nodes, s->aabbs, s->cones,
                     s->inner, s->inner_cones, s->leaves, s->edges, s->keys, s->vals, s->keys_tmp, s->vals_tmp,
-                    s->flags, s->centroids, s->small, s->scratch, s->ref_objects, s->ref_edges,
+                    s->flags, s->sizes, s->centroids, s->small, s->scratch, s->ref_objects, s->ref_edges,
                     s->stage.in[0], s->stage.in[1], s->stage.out[0], s->stage.out[1]};
     for (void *p : ptrs)
         if (p)
@@ -137,6 +140,7 @@ int allocate(snch_scene_s *s)
     SNCH_CUDA(dalloc(&s->keys_tmp, n));
     SNCH_CUDA(dalloc(&s->vals_tmp, n));
     SNCH_CUDA(dalloc(&s->flags, ni));
+    SNCH_CUDA(dalloc(&s->sizes, ni));
     SNCH_CUDA(dalloc(&s->centroids, n));
     SNCH_CUDA(dalloc(&s->small, kSmallWords));
     SNCH_CUDA(dalloc(&s->ref_objects, n));
@@ -230,6 +234,7 @@ BuildArgs build_args(snch_scene_s *s)
     a.aabbs = s->aabbs;
     a.cones = s->cones;
     a.flags = s->flags;
+    a.sizes = s->sizes;
     a.inner = s->inner;
     a.inner_cones = s->inner_cones;
     a.leaves = s->leaves;
@@ -406,6 +411,29 @@ int snch_build_bvh(snch_scene_t s, snch_stream_t stream)
                                      s->ref_edges, st));
     }
     s->built = true;
+    return SNCH_OK;
+}
+
+int snch_set_traversal(snch_scene_t s, int mode)
+{
+    if (!s)
+        return fail(SNCH_ERR_INVALID_ARGUMENT, "scene is NULL");
+    if (mode != SNCH_TRAVERSAL_NEAR_FIRST && mode != SNCH_TRAVERSAL_REFERENCE_ORDER)
+        return fail(SNCH_ERR_INVALID_ARGUMENT, "unknown traversal mode " + std::to_string(mode));
+    s->traversal = mode;
+    return SNCH_OK;
+}
+
+int snch_export_leaf_ranks(snch_scene_t s, uint32_t *ranks)
+{
+    int rc = check_built(s);
+    if (rc != SNCH_OK)
+        return rc;
+    if (!ranks && s->num_tris)
+        return fail(SNCH_ERR_INVALID_ARGUMENT, "ranks is NULL");
+    if (s->num_tris)
+        SNCH_CUDA(cudaMemcpy2D(ranks, 4, reinterpret_cast<const char *>(s->leaves) + 44, sizeof(LeafRec), 4,
+                               s->num_tris, cudaMemcpyDeviceToHost));
     return SNCH_OK;
 }
 
@@ -638,6 +666,48 @@ int snch_sample_in_sphere_host(snch_scene_t s, const float *c, const float *r, c
         return launch_sample(t, (const float *)di[0], (const float *)di[1], (const float *)di[2], m,
                              (int32_t *)dout[0], (float *)dout[1], st);
     });
+}
+
+int snch_query_visits(snch_scene_t s, int kind, const float *in0, const float *in1, const float *in2,
+                      const uint8_t *flip, int64_t n, uint32_t *visits, snch_stream_t stream)
+{
+    int rc = check_built(s);
+    if (rc == SNCH_OK)
+        rc = check_n(n, {in0, visits});
+    if (rc != SNCH_OK)
+        return rc;
+    if (n == 0)
+        return SNCH_OK;
+    if ((kind == 2 || kind == 3) && (!in1 || !in2))
+        return fail(SNCH_ERR_INVALID_ARGUMENT, "NULL query buffer");
+    cudaStream_t st = S(stream);
+    // result buffers of the counted launch (discarded)
+    char *scratch = nullptr;
+    SNCH_CUDA(cudaMallocAsync(reinterpret_cast<void **>(&scratch), 32 * (size_t)n + 256, st));
+    const TreeView t = s->view();
+    cudaError_t e = cudaSuccess;
+    switch (kind)
+    {
+    case 0:
+        e = launch_nearest(t, in0, n, (uint32_t *)scratch, (float *)(scratch + 8 * n), st, visits);
+        break;
+    case 1:
+        e = launch_silhouette(t, in0, flip, n, (float *)scratch, (int32_t *)(scratch + 8 * n), st, visits);
+        break;
+    case 2:
+        e = launch_ray(t, in0, in1, in2, n, (uint8_t *)scratch, (float *)(scratch + 4 * n),
+                       (float *)(scratch + 8 * n), (uint32_t *)(scratch + 16 * n), st, visits);
+        break;
+    case 3:
+        e = launch_sample(t, in0, in1, in2, n, (int32_t *)scratch, (float *)(scratch + 8 * n), st, visits);
+        break;
+    default:
+        cudaFreeAsync(scratch, st);
+        return fail(SNCH_ERR_INVALID_ARGUMENT, "kind must be 0..3");
+    }
+    cudaFreeAsync(scratch, st);
+    SNCH_CUDA(e);
+    return SNCH_OK;
 }
 
 size_t snch_sort_scratch_bytes(int64_t n, int key_bits)

@@ -254,6 +254,7 @@ __global__ void __launch_bounds__(256) karras_kernel(BuildArgs a)
     nodes[idx].left = left;
     nodes[idx].right = right;
     nodes[idx].object = kInvalid;
+    a.sizes[idx] = hi - lo + 1;
     nodes[left].parent = idx;
     nodes[right].parent = idx;
 }
@@ -494,6 +495,35 @@ __global__ void __launch_bounds__(128) refit_kernel(BuildArgs a)
     }
 }
 
+// Position of every leaf in the reference's full depth-first visit order
+// (query.cuh:256-316): expanding node n emits its leaf children (left, then
+// right), then visits the right subtree, then the left one. A leaf's position
+// is the sum, over the path to the root, of the offset of each node within its
+// parent's emission sequence. The near-first traversals use it to resolve exact
+// distance ties the way the reference's visit order does. Stored in LeafRec.v2.w.
+__global__ void __launch_bounds__(256) rank_kernel(BuildArgs a)
+{
+    const uint32_t n = a.num_tris, ni = n - 1;
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n)
+        return;
+    uint32_t node = ni + j, r = 0;
+    for (int level = 0; level < 96 && n > 1; ++level)
+    {
+        const uint32_t p = a.nodes[node].parent;
+        if (p >= ni)
+            break;
+        const uint32_t L = a.nodes[p].left, R = a.nodes[p].right;
+        const uint32_t lleaf = L >= ni ? 1u : 0u, rleaf = R >= ni ? 1u : 0u;
+        if (node == L)
+            r += lleaf ? 0u : lleaf + rleaf + (rleaf ? 0u : a.sizes[R]);
+        else
+            r += rleaf ? lleaf : lleaf + rleaf;
+        node = p;
+    }
+    a.leaves[j].v2.w = __uint_as_float(r);
+}
+
 // Objects in the reference's device layout (scene.cuh:708-722 silhouette_edge,
 // 826-840 triangle) so that snch_get_bvh_view() is a drop-in bvh_device view.
 __global__ void ref_objects_kernel(const float *verts, const int32_t *tris, const int32_t *tri_owned,
@@ -569,6 +599,8 @@ cudaError_t launch_build_back(const BuildArgs &a, cudaStream_t st)
             return e;
     }
     refit_kernel<<<(n + 127) / 128, 128, 0, st>>>(a);
+    note_launch();
+    rank_kernel<<<(n + 255) / 256, 256, 0, st>>>(a);
     note_launch();
     return cudaGetLastError();
 }

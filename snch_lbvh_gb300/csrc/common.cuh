@@ -92,6 +92,7 @@ struct TreeView
     const LeafRec *leaves;
     const EdgeRec *edges;
     uint32_t *status;
+    int near_first;  // 1: near-first nearest/silhouette traversal, 0: the reference's stack order
 };
 
 // ---------------------------------------------------------------- vector math

@@ -30,6 +30,7 @@ struct BuildArgs
     Box *aabbs;
     Cone *cones;
     uint32_t *flags;      // refit arrival counters, N-1
+    uint32_t *sizes;      // leaves under each internal node, N-1
     InnerRec *inner;
     InnerConeRec *inner_cones;
     LeafRec *leaves;
@@ -45,14 +46,15 @@ cudaError_t launch_ref_objects(const float *verts, const int32_t *tris, const in
                                snch_silhouette_edge *edges, cudaStream_t st);
 cudaError_t launch_validate(const int32_t *tris, int64_t n, int64_t num_verts, uint32_t *bad, cudaStream_t st);
 
-// ---- queries.cu
-cudaError_t launch_nearest(const TreeView &t, const float *pts, int64_t n, uint32_t *idx, float *dist, cudaStream_t st);
+// ---- queries.cu (stats != nullptr: per-query work counters, 3 words per query)
+cudaError_t launch_nearest(const TreeView &t, const float *pts, int64_t n, uint32_t *idx, float *dist, cudaStream_t st,
+                           uint32_t *stats = nullptr);
 cudaError_t launch_silhouette(const TreeView &t, const float *pts, const uint8_t *flip, int64_t n, float *dist,
-                              int32_t *edge, cudaStream_t st);
+                              int32_t *edge, cudaStream_t st, uint32_t *stats = nullptr);
 cudaError_t launch_ray(const TreeView &t, const float *o, const float *d, const float *tmax, int64_t n, uint8_t *hit,
-                       float *tt, float *uv, uint32_t *idx, cudaStream_t st);
+                       float *tt, float *uv, uint32_t *idx, cudaStream_t st, uint32_t *stats = nullptr);
 cudaError_t launch_sample(const TreeView &t, const float *c, const float *r, const float *u, int64_t n, int32_t *idx,
-                          float *pdf, cudaStream_t st);
+                          float *pdf, cudaStream_t st, uint32_t *stats = nullptr);
 cudaError_t launch_sample_point(const float *verts, const int32_t *tris, const int32_t *idx, const float *u,
                                 const float *v, int64_t n, float *out, cudaStream_t st);
 

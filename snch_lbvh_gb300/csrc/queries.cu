@@ -393,6 +393,274 @@ __global__ void __launch_bounds__(128) silhouette_kernel(TreeView t, const float
         out_edge[q] = best_edge;
 }
 
+// ------------------------------------------------------------------ near-first forms
+// Same results as nearest_kernel / silhouette_kernel, fewer visits. The
+// reference's answer is a minimum over the leaves its traversal evaluates;
+// the child tests that decide which leaves can be reached (minmaxdist for the
+// nearest query, the normal-cone test for the silhouette query) depend only on
+// the node and the query point, and pruning by the running best never removes
+// a leaf that attains the final minimum. So any visit order reaches the same
+// minimum; only exact ties depend on the order, and those are resolved with
+// the leaf's position in the reference's depth-first order (LeafRec.v2.w):
+//   nearest:    among equal squared distances the reference keeps the leaf it
+//               visits last (query.cuh:286, 304: "<=");
+//   silhouette: among equal distances it keeps the last (edge slot order inside
+//               a leaf, scene.cuh:989-999), except at distance 0, after which
+//               no edge is accepted any more (scene.cuh:791-794) -- the first wins.
+// Children are pushed far-then-near so the nearer subtree is searched first.
+
+SNCH_DEV void leaf_nearest_fast(const TreeView &t, uint32_t pos, f3 p, float &best, uint32_t &best_rank,
+                                uint32_t &nearest)
+{
+    const float4 *q = reinterpret_cast<const float4 *>(t.leaves + pos);
+    const float4 a = __ldg(q), b = __ldg(q + 1), c = __ldg(q + 2);
+    float d = closest_point_triangle(mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), mk(c.x, c.y, c.z), p);
+    d *= d;
+    const uint32_t rank = __float_as_uint(c.w);
+    if (d < best || (d == best && rank > best_rank))
+    {
+        best = d;
+        best_rank = rank;
+        nearest = __float_as_uint(a.w);
+    }
+}
+
+template <bool kStats>
+__global__ void __launch_bounds__(128) nearest_fast_kernel(TreeView t, const float *__restrict__ pts, int64_t n,
+                                                           uint32_t *__restrict__ out_idx, float *__restrict__ out_dist,
+                                                           uint32_t *__restrict__ stats)
+{
+    uint32_t n_int = 0, n_leaf = 0;
+    const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (q >= n)
+        return;
+    const f3 p = load_point(pts, q);
+    uint32_t nearest = kInvalid, best_rank = 0;
+    float best = INFINITY;
+    const uint32_t ni = t.num_tris - 1;
+    if (t.num_tris == 1)
+    {
+        uint32_t orig;
+        best = leaf_distance2(t, 0, p, orig);
+        nearest = orig;
+    }
+    else if (t.num_tris > 1)
+    {
+        uint32_t sn[kStackDepth];
+        float sd[kStackDepth];
+        int sp = 1;
+        sn[0] = 0;
+        sd[0] = mindist(load_root_box(t.aabbs), p);
+        do
+        {
+            --sp;
+            const uint32_t node = sn[sp];
+            if (sd[sp] > best)
+                continue;
+            if (sp > kStackDepth - 2)
+            {
+                atomicOr(t.status, kStatusStackOverflow);
+                nearest = kInvalid;
+                best = NAN;
+                break;
+            }
+            Box lb, rb;
+            uint32_t L, R;
+            unpack_inner(load_inner(t.inner + node), lb, rb, L, R);
+            if (kStats)
+                ++n_int;
+            const float Lmd = mindist(lb, p), Rmd = mindist(rb, p);
+            const float Lmm = minmaxdist(lb, p), Rmm = minmaxdist(rb, p);
+            const bool aL = Lmd <= Rmm, aR = Rmd <= Lmm;  // query.cuh:279, 297
+            if (aL && L >= ni && Lmd <= best)
+            {
+                leaf_nearest_fast(t, L - ni, p, best, best_rank, nearest);
+                if (kStats)
+                    ++n_leaf;
+            }
+            if (aR && R >= ni && Rmd <= best)
+            {
+                leaf_nearest_fast(t, R - ni, p, best, best_rank, nearest);
+                if (kStats)
+                    ++n_leaf;
+            }
+            const bool pL = aL && L < ni && Lmd <= best, pR = aR && R < ni && Rmd <= best;
+            if (pL && pR)
+            {
+                const bool l_first = Lmd <= Rmd;
+                sn[sp] = l_first ? R : L;
+                sd[sp] = l_first ? Rmd : Lmd;
+                sn[sp + 1] = l_first ? L : R;
+                sd[sp + 1] = l_first ? Lmd : Rmd;
+                sp += 2;
+            }
+            else if (pL)
+            {
+                sn[sp] = L;
+                sd[sp] = Lmd;
+                ++sp;
+            }
+            else if (pR)
+            {
+                sn[sp] = R;
+                sd[sp] = Rmd;
+                ++sp;
+            }
+        } while (sp > 0);
+    }
+    if (kStats)
+    {
+        stats[3 * q] = n_int;
+        stats[3 * q + 1] = n_leaf;
+        stats[3 * q + 2] = 0;
+    }
+    out_idx[q] = nearest;
+    out_dist[q] = sqrtf(best);
+}
+
+// one leaf of the silhouette query; key = rank * 4 + slot orders candidates
+// like the reference's visit order
+SNCH_DEV void leaf_silhouette_fast(const TreeView &t, uint32_t pos, f3 o, bool flip, float &best, uint32_t &best_key,
+                                   int32_t &best_edge, uint32_t &n_edge)
+{
+    const float4 *lr = reinterpret_cast<const float4 *>(t.leaves + pos);
+    const uint32_t n_owned = __float_as_uint(__ldg(&lr[1].w));
+    const uint32_t rank = __float_as_uint(__ldg(&lr[2].w));
+    n_edge += n_owned;
+    for (uint32_t k = 0; k < n_owned; ++k)
+    {
+        const float4 *e = reinterpret_cast<const float4 *>(t.edges + 3 * (uint64_t)pos + k);
+        const float4 ea = __ldg(e), eb = __ldg(e + 1);
+        const f3 pa = mk(ea.x, ea.y, ea.z), pb = mk(eb.x, eb.y, eb.z);
+        f3 cp;
+        const float d = closest_point_segment(pa, pb, o, cp);
+        if (d > best)
+            continue;
+        const uint32_t flags = __float_as_uint(ea.w);
+        bool is_sil = (flags & 1u) == 0u || (flags & 2u) == 0u;
+        if (!is_sil)
+        {
+            const float4 ec = __ldg(e + 2), ed = __ldg(e + 3);
+            is_sil = is_silhouette_edge(pa, pb, mk(ec.x, ec.y, ec.z), mk(ed.x, ed.y, ed.z),
+                                        mk(o.x - cp.x, o.y - cp.y, o.z - cp.z), d, flip);
+        }
+        if (!is_sil)
+            continue;
+        const uint32_t key = rank * 4u + k;
+        if (d < best || (d > 0.0f ? key > best_key : key < best_key))
+        {
+            best = d;
+            best_key = key;
+            best_edge = __float_as_int(eb.w);
+        }
+    }
+}
+
+template <bool kStats>
+__global__ void __launch_bounds__(128) silhouette_fast_kernel(TreeView t, const float *__restrict__ pts,
+                                                              const uint8_t *__restrict__ flips, int64_t n,
+                                                              float *__restrict__ out_dist,
+                                                              int32_t *__restrict__ out_edge,
+                                                              uint32_t *__restrict__ stats)
+{
+    uint32_t n_int = 0, n_leaf = 0, n_edge = 0;
+    const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (q >= n)
+        return;
+    const f3 p = load_point(pts, q);
+    const bool flip = flips ? __ldg(flips + q) != 0 : false;
+    float best = INFINITY;
+    uint32_t best_key = 0;
+    int32_t best_edge = -1;
+    const uint32_t ni = t.num_tris - 1;
+    if (t.num_tris == 1)
+    {
+        leaf_silhouette_fast(t, 0, p, flip, best, best_key, best_edge, n_edge);
+    }
+    else if (t.num_tris > 1)
+    {
+        uint32_t sn[kStackDepth];
+        float sd[kStackDepth];
+        int sp = 1;
+        sn[0] = 0;
+        sd[0] = mindist(load_root_box(t.aabbs), p);
+        do
+        {
+            --sp;
+            const uint32_t node = sn[sp];
+            if (sd[sp] > best * best)
+                continue;
+            if (sp > kStackDepth - 2)
+            {
+                atomicOr(t.status, kStatusStackOverflow);
+                best = NAN;
+                best_edge = -1;
+                break;
+            }
+            Box lb, rb;
+            uint32_t L, R;
+            unpack_inner(load_inner(t.inner + node), lb, rb, L, R);
+            const float4 *cr = reinterpret_cast<const float4 *>(t.inner_cones + node);
+            InnerConeRec icr;
+            icr.a = __ldg(cr);
+            icr.b = __ldg(cr + 1);
+            icr.c = __ldg(cr + 2);
+            Cone lc, rc;
+            unpack_cones(icr, lc, rc);
+            const float Lmd = mindist(lb, p), Rmd = mindist(rb, p);
+            const float b2 = best * best;
+            const bool hitL = Lmd <= b2 && lc.half_angle >= 0.0f && cone_overlap(lc, p, lb, Lmd);
+            const bool hitR = Rmd <= b2 && rc.half_angle >= 0.0f && cone_overlap(rc, p, rb, Rmd);
+            if (kStats)
+                ++n_int;
+            if (hitL && L >= ni)
+            {
+                leaf_silhouette_fast(t, L - ni, p, flip, best, best_key, best_edge, n_edge);
+                if (kStats)
+                    ++n_leaf;
+            }
+            if (hitR && R >= ni)
+            {
+                leaf_silhouette_fast(t, R - ni, p, flip, best, best_key, best_edge, n_edge);
+                if (kStats)
+                    ++n_leaf;
+            }
+            const float b2n = best * best;
+            const bool pL = hitL && L < ni && Lmd <= b2n, pR = hitR && R < ni && Rmd <= b2n;
+            if (pL && pR)
+            {
+                const bool l_first = Lmd <= Rmd;
+                sn[sp] = l_first ? R : L;
+                sd[sp] = l_first ? Rmd : Lmd;
+                sn[sp + 1] = l_first ? L : R;
+                sd[sp + 1] = l_first ? Lmd : Rmd;
+                sp += 2;
+            }
+            else if (pL)
+            {
+                sn[sp] = L;
+                sd[sp] = Lmd;
+                ++sp;
+            }
+            else if (pR)
+            {
+                sn[sp] = R;
+                sd[sp] = Rmd;
+                ++sp;
+            }
+        } while (sp > 0);
+    }
+    out_dist[q] = best;
+    if (out_edge)
+        out_edge[q] = best_edge;
+    if (kStats)
+    {
+        stats[3 * q] = n_int;
+        stats[3 * q + 1] = n_leaf;
+        stats[3 * q + 2] = n_edge;
+    }
+}
+
 // ------------------------------------------------------------------ ray
 // intersects_d(ray<float,3>) aabb.cuh:397-431
 SNCH_DEV bool ray_box(f3 o, f3 inv, const Box &b, float max_dist, float &dist)
@@ -443,11 +711,14 @@ SNCH_DEV bool ray_triangle(f3 o, f3 dir, f3 v0, f3 v1, f3 v2, float &t, float &u
     return false;
 }
 
+template <bool kStats>
 __global__ void __launch_bounds__(128) ray_kernel(TreeView t, const float *__restrict__ origins,
                                                   const float *__restrict__ dirs, const float *__restrict__ tmaxs,
                                                   int64_t n, uint8_t *__restrict__ out_hit, float *__restrict__ out_t,
-                                                  float *__restrict__ out_uv, uint32_t *__restrict__ out_idx)
+                                                  float *__restrict__ out_uv, uint32_t *__restrict__ out_idx,
+                                                  uint32_t *__restrict__ stats)
 {
+    uint32_t n_int = 0, n_leaf = 0;
     const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (q >= n)
         return;
@@ -476,6 +747,8 @@ __global__ void __launch_bounds__(128) ray_kernel(TreeView t, const float *__res
                 f3 pa, pb, pc;
                 uint32_t orig, n_owned;
                 load_leaf(t.leaves + (node - ni), pa, pb, pc, orig, n_owned);
+                if (kStats)
+                    ++n_leaf;
                 float tt, uu, vv;
                 if (ray_triangle(o, dir, pa, pb, pc, tt, uu, vv) && tt < max_dist && tt < min_dist)
                 {
@@ -499,6 +772,8 @@ __global__ void __launch_bounds__(128) ray_kernel(TreeView t, const float *__res
                 Box lb, rb;
                 uint32_t L, R;
                 unpack_inner(load_inner(t.inner + node), lb, rb, L, R);
+                if (kStats)
+                    ++n_int;
                 float Ld = 0.0f, Rd = 0.0f;
                 const bool Lh = ray_box(o, inv, lb, max_dist, Ld);
                 const bool Rh = ray_box(o, inv, rb, max_dist, Rd);
@@ -540,6 +815,12 @@ __global__ void __launch_bounds__(128) ray_kernel(TreeView t, const float *__res
     out_uv[2 * q] = bu;
     out_uv[2 * q + 1] = bv;
     out_idx[q] = nearest;
+    if (kStats)
+    {
+        stats[3 * q] = n_int;
+        stats[3 * q + 1] = n_leaf;
+        stats[3 * q + 2] = 0;
+    }
 }
 
 // ------------------------------------------------------------------ sampling
@@ -597,11 +878,13 @@ SNCH_DEV float green_weight(f3 x, f3 y)
     return 1.0f / (four_pi * r);
 }
 
+template <bool kStats>
 __global__ void __launch_bounds__(128) sample_kernel(TreeView t, const float *__restrict__ centers,
                                                      const float *__restrict__ radii, const float *__restrict__ us,
                                                      int64_t n, int32_t *__restrict__ out_idx,
-                                                     float *__restrict__ out_pdf)
+                                                     float *__restrict__ out_pdf, uint32_t *__restrict__ stats)
 {
+    uint32_t n_int = 0, n_leaf = 0;
     const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (q >= n)
         return;
@@ -624,6 +907,8 @@ __global__ void __launch_bounds__(128) sample_kernel(TreeView t, const float *__
                 f3 pa, pb, pc;
                 uint32_t orig, n_owned;
                 load_leaf(t.leaves + (node - ni), pa, pb, pc, orig, n_owned);
+                if (kStats)
+                    ++n_leaf;
                 if (sphere_triangle(c, rad, pa, pb, pc))
                 {
                     oi = (int32_t)orig;
@@ -635,6 +920,8 @@ __global__ void __launch_bounds__(128) sample_kernel(TreeView t, const float *__
             Box lb, rb;
             uint32_t L, R;
             unpack_inner(load_inner(t.inner + node), lb, rb, L, R);
+            if (kStats)
+                ++n_int;
             const float Lw = sphere_box(c, rad, lb) ? green_weight(c, centroid(lb)) : 0;
             const float Rw = sphere_box(c, rad, rb) ? green_weight(c, centroid(rb)) : 0;
             const float tw = Lw + Rw;
@@ -658,6 +945,12 @@ __global__ void __launch_bounds__(128) sample_kernel(TreeView t, const float *__
     }
     out_idx[q] = oi;
     out_pdf[q] = opdf;
+    if (kStats)
+    {
+        stats[3 * q] = n_int;
+        stats[3 * q + 1] = n_leaf;
+        stats[3 * q + 2] = 0;
+    }
 }
 
 // sample_triangle scene.cuh:14-27 on the triangle of ORIGINAL index idx
@@ -688,43 +981,65 @@ namespace
 inline unsigned grid_for(int64_t n, int b) { return (unsigned)((n + b - 1) / b); }
 }  // namespace
 
-cudaError_t launch_nearest(const TreeView &t, const float *pts, int64_t n, uint32_t *idx, float *dist, cudaStream_t st)
+cudaError_t launch_nearest(const TreeView &t, const float *pts, int64_t n, uint32_t *idx, float *dist, cudaStream_t st,
+                           uint32_t *stats)
 {
-    if (n > 0)
+    if (n <= 0)
+        return cudaSuccess;
+    if (stats)
+        nearest_fast_kernel<true><<<grid_for(n, 128), 128, 0, st>>>(t, pts, n, idx, dist, stats);
+    else if (t.near_first)
+        nearest_fast_kernel<false><<<grid_for(n, 128), 128, 0, st>>>(t, pts, n, idx, dist, nullptr);
+    else
         nearest_kernel<<<grid_for(n, 128), 128, 0, st>>>(t, pts, n, idx, dist);
-        note_launch();
+    note_launch();
     return cudaGetLastError();
 }
 cudaError_t launch_silhouette(const TreeView &t, const float *pts, const uint8_t *flip, int64_t n, float *dist,
-                              int32_t *edge, cudaStream_t st)
+                              int32_t *edge, cudaStream_t st, uint32_t *stats)
 {
-    if (n > 0)
+    if (n <= 0)
+        return cudaSuccess;
+    if (stats)
+        silhouette_fast_kernel<true><<<grid_for(n, 128), 128, 0, st>>>(t, pts, flip, n, dist, edge, stats);
+    else if (t.near_first)
+        silhouette_fast_kernel<false><<<grid_for(n, 128), 128, 0, st>>>(t, pts, flip, n, dist, edge, nullptr);
+    else
         silhouette_kernel<<<grid_for(n, 128), 128, 0, st>>>(t, pts, flip, n, dist, edge);
-        note_launch();
+    note_launch();
     return cudaGetLastError();
 }
 cudaError_t launch_ray(const TreeView &t, const float *o, const float *d, const float *tmax, int64_t n, uint8_t *hit,
-                       float *tt, float *uv, uint32_t *idx, cudaStream_t st)
+                       float *tt, float *uv, uint32_t *idx, cudaStream_t st, uint32_t *stats)
 {
-    if (n > 0)
-        ray_kernel<<<grid_for(n, 128), 128, 0, st>>>(t, o, d, tmax, n, hit, tt, uv, idx);
-        note_launch();
+    if (n <= 0)
+        return cudaSuccess;
+    if (stats)
+        ray_kernel<true><<<grid_for(n, 128), 128, 0, st>>>(t, o, d, tmax, n, hit, tt, uv, idx, stats);
+    else
+        ray_kernel<false><<<grid_for(n, 128), 128, 0, st>>>(t, o, d, tmax, n, hit, tt, uv, idx, nullptr);
+    note_launch();
     return cudaGetLastError();
 }
 cudaError_t launch_sample(const TreeView &t, const float *c, const float *r, const float *u, int64_t n, int32_t *idx,
-                          float *pdf, cudaStream_t st)
+                          float *pdf, cudaStream_t st, uint32_t *stats)
 {
-    if (n > 0)
-        sample_kernel<<<grid_for(n, 128), 128, 0, st>>>(t, c, r, u, n, idx, pdf);
-        note_launch();
+    if (n <= 0)
+        return cudaSuccess;
+    if (stats)
+        sample_kernel<true><<<grid_for(n, 128), 128, 0, st>>>(t, c, r, u, n, idx, pdf, stats);
+    else
+        sample_kernel<false><<<grid_for(n, 128), 128, 0, st>>>(t, c, r, u, n, idx, pdf, nullptr);
+    note_launch();
     return cudaGetLastError();
 }
 cudaError_t launch_sample_point(const float *verts, const int32_t *tris, const int32_t *idx, const float *u,
                                 const float *v, int64_t n, float *out, cudaStream_t st)
 {
-    if (n > 0)
-        sample_point_kernel<<<grid_for(n, 256), 256, 0, st>>>(verts, tris, idx, u, v, n, out);
-        note_launch();
+    if (n <= 0)
+        return cudaSuccess;
+    sample_point_kernel<<<grid_for(n, 256), 256, 0, st>>>(verts, tris, idx, u, v, n, out);
+    note_launch();
     return cudaGetLastError();
 }
 

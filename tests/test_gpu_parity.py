@@ -18,6 +18,7 @@ from conftest import d1_tainted, golden_names, load_golden
 pytestmark = pytest.mark.gpu
 
 CONE_TOL = 2e-5
+FP64_ABS_TOL = 2.5e-7  # two float32 ulps at unit coordinates
 SIL_RTOL = 1e-6
 SIL_MAX_FLIP_FRACTION = 1e-3
 
@@ -47,7 +48,10 @@ def check_cones(gpu_cones, ref_cones, nodes, d1):
     valid = ref_cones[:, 3] >= 0
     np.testing.assert_array_equal((gpu_cones[:, 3] >= 0)[~taint], valid[~taint])
     ok = valid & ~taint
-    diff = np.abs(gpu_cones[ok].astype(np.float64) - ref_cones[ok])
+    g64, r64 = gpu_cones[ok].astype(np.float64), ref_cones[ok].astype(np.float64)
+    both_nan = np.isnan(g64) & np.isnan(r64)  # degenerate triangles: 0/0 axes in both
+    diff = np.where(both_nan, 0.0, np.abs(g64 - r64))
+    diff[np.isnan(diff)] = np.inf
     rad = np.abs(ref_cones[ok, 4]).astype(np.float64)
     assert diff[:, :4].max(initial=0) <= CONE_TOL, diff[:, :4].max()
     assert np.all(diff[:, 4] <= CONE_TOL * np.maximum(rad, 1.0))
@@ -120,11 +124,17 @@ def test_config1_workload_against_oracle(snch, oracle_mod):
     oi, od = orc.nearest(pts)
     np.testing.assert_array_equal(idx, oi)
     np.testing.assert_array_equal(bits(dist), bits(od))
-    # FP64 brute force on a subset: the FP32 path's error bound
+    # FP64 brute force on a subset: the reference algorithm's FP32 error. The
+    # chosen triangle is compared through its FP64 distance, because exact ties
+    # (a shared vertex or edge is the nearest feature) are common and brute
+    # force keeps a different tied triangle than the reference's visit order.
     sub = np.arange(0, len(pts), 122)[:8192]
     bi, bd = oracle_mod.brute_nearest_f64(v, f, pts[sub])
-    rel = np.abs(dist[sub].astype(np.float64) - bd) / np.maximum(bd, 1e-12)
-    assert rel.max() < 1e-5, rel.max()
+    err = np.abs(dist[sub].astype(np.float64) - bd)
+    assert err.max() <= FP64_ABS_TOL, err.max()
+    for k in np.nonzero(idx[sub] != bi)[0][:256]:
+        _, dk = oracle_mod.brute_nearest_f64(v, f[idx[sub][k]][None], pts[sub][k][None])
+        assert abs(dk[0] - bd[k]) <= FP64_ABS_TOL
     assert s.device_status() == 0
 
 
@@ -186,3 +196,45 @@ def test_device_create_validates_indices(snch):
     ok = snch.Scene(v + torch.eye(3, device="cuda"), torch.tensor([[0, 1, 2]], dtype=torch.int32, device="cuda"))
     ok.build_bvh()
     assert ok.info() == (3, 1, 3)
+
+
+def run_all(s, q, mode):
+    s.set_traversal(mode)
+    i, d = s.query_nearest(q["near_pts"])
+    sd, se = s.query_silhouette(q["sil_pts"], q["sil_flip"])
+    return [i.cpu().numpy(), bits(d.cpu().numpy()), bits(sd.cpu().numpy()), se.cpu().numpy()]
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_near_first_equals_reference_order_golden(snch, oracle_mod, name):
+    """The near-first traversals return the reference-order results bit for bit,
+    tie winners included (golden inputs hold vertex / edge / face-centre probes)."""
+    g = load_golden(name)
+    s = built_scene(snch, g["verts"], g["tris"])
+    orc = oracle_mod.Tree(g["verts"], g["tris"])
+    np.testing.assert_array_equal(s.leaf_ranks(), orc.leaf_ranks())
+    q = {"near_pts": g["near_pts"], "sil_pts": g["sil_pts"], "sil_flip": g["sil_flip"]}
+    a = run_all(s, q, snch.TRAVERSAL_REFERENCE_ORDER)
+    b = run_all(s, q, snch.TRAVERSAL_NEAR_FIRST)
+    for x, y in zip(a, b):
+        np.testing.assert_array_equal(x, y)
+    if len(g["ref_near_idx"]):
+        np.testing.assert_array_equal(b[0].view(np.uint32), g["ref_near_idx"])
+        np.testing.assert_array_equal(b[1], bits(g["ref_near_dist"]))
+
+
+def test_near_first_equals_reference_order_config1(snch):
+    from snch_lbvh_gb300 import meshes
+    v, f = meshes.noisy_icosphere(5, 1.0, 0.01, seed=0)
+    pts = meshes.box_queries(v, 1_000_000, 1.2, seed=1)
+    # add exact-tie probes: every vertex and every edge midpoint
+    e = np.concatenate([f[:, [0, 1]], f[:, [1, 2]], f[:, [2, 0]]])
+    mids = (0.5 * (v[e[:, 0]].astype(np.float64) + v[e[:, 1]])).astype(np.float32)
+    pts = np.concatenate([pts, v, mids]).astype(np.float32)
+    q = {"near_pts": pts, "sil_pts": pts, "sil_flip": (np.arange(len(pts)) % 2).astype(np.uint8)}
+    s = built_scene(snch, v, f)
+    a = run_all(s, q, snch.TRAVERSAL_REFERENCE_ORDER)
+    b = run_all(s, q, snch.TRAVERSAL_NEAR_FIRST)
+    for x, y in zip(a, b):
+        np.testing.assert_array_equal(x, y)
+    assert s.device_status() == 0

@@ -88,3 +88,17 @@ def test_queries_against_oracle_subset(big):
     np.testing.assert_array_equal(si.cpu().numpy(), osi)
     np.testing.assert_array_equal(bits(sp.cpu().numpy()), bits(osp))
     assert s.device_status() == 0
+
+
+def test_near_first_equals_reference_order_full_scene(big):
+    """On the 2M-triangle scene: 1M nearest + 250k silhouette queries, both orders."""
+    import snch_lbvh_gb300 as snch
+    from snch_lbvh_gb300 import meshes
+    from test_gpu_parity import run_all
+    sc, s, _ = big
+    q = meshes.wost_queries(1_000_000, 250_000, 1, 1, seed=21)
+    a = run_all(s, q, snch.TRAVERSAL_REFERENCE_ORDER)
+    b = run_all(s, q, snch.TRAVERSAL_NEAR_FIRST)
+    for x, y in zip(a, b):
+        np.testing.assert_array_equal(x, y)
+    assert s.device_status() == 0
