@@ -224,7 +224,52 @@ def run_reference(args):
                                    f"extrapolated to its full batch"},
         "e2e": {"value": value, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
+    line["reference_cuda"] = reference_cuda_leg(sc, q, counts)
     print(json.dumps(line), flush=True)
+
+
+def reference_cuda_leg(sc, q, counts, sample=2_000_000):
+    """The reference's own query_device kernels (its headers compiled for sm_103a
+    with its flags, oracle/ref_gpu_kernels.cu) timed on this GPU over a tree
+    built by this library; queries only, a bounded sample of each batch."""
+    try:
+        import torch
+        if not torch.cuda.is_available():
+            return {"unavailable": "no CUDA device"}
+        from oracle import ref_gpu
+        ok, why = ref_gpu.available()
+        if not ok:
+            return {"unavailable": why}
+        import snch_lbvh_gb300 as snch
+        scene = snch.Scene(torch.from_numpy(sc.verts).cuda(), torch.from_numpy(sc.faces).cuda())
+        scene.compute_silhouettes()
+        scene.build_bvh()
+        R = ref_gpu.RefQueries(scene)
+        m = {k: min(sample, counts[k]) for k in counts}
+        d = {k: torch.from_numpy(np.ascontiguousarray(v[:m[{"near_pts": "near", "sil_pts": "sil", "sil_flip": "sil",
+                                                         "ray_o": "ray", "ray_d": "ray", "ray_tmax": "ray",
+                                                         "smp_c": "smp", "smp_r": "smp", "smp_u": "smp"}[k]]]))
+             .cuda() for k, v in q.items()}
+        calls = {"near": lambda: R.nearest(d["near_pts"]), "sil": lambda: R.silhouette(d["sil_pts"], d["sil_flip"]),
+                 "ray": lambda: R.ray(d["ray_o"], d["ray_d"], d["ray_tmax"]),
+                 "smp": lambda: R.sample(d["smp_c"], d["smp_r"], d["smp_u"])}
+        qps = {}
+        for k, f in calls.items():
+            f()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            f()
+            e1.record()
+            torch.cuda.synchronize()
+            qps[k] = m[k] / (e0.elapsed_time(e1) / 1e3)
+        t = sum(counts[k] / qps[k] for k in counts)
+        return {"value": sum(counts.values()) / t, "unit": "queries/s", "per_type_qps": qps,
+                "sample": f"{m['near']:,} nearest, {m['sil']:,} silhouette, {m['ray']:,} ray, {m['smp']:,} sample "
+                          f"queries (input order), each extrapolated to its batch; queries only (the reference's "
+                          f"build is host Thrust code)"}
+    except Exception as exc:  # reported, never fatal for the CPU arm
+        return {"unavailable": f"{type(exc).__name__}: {exc}"}
 
 
 # --------------------------------------------------------------------- our arm

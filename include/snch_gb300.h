@@ -127,6 +127,17 @@ int snch_export_topology(snch_scene_t scene, int32_t *tri_edges, int32_t *tri_ow
 #define SNCH_TRAVERSAL_REFERENCE_ORDER 1
 int snch_set_traversal(snch_scene_t scene, int mode);
 
+/* Scene options (snch_set_option):
+ *   SNCH_OPT_TRAVERSAL        SNCH_TRAVERSAL_NEAR_FIRST (default) / _REFERENCE_ORDER
+ *   SNCH_OPT_QUERY_ORDER      1 (default): batches are answered in the Morton order
+ *                             of their query points (results still land at their
+ *                             input positions and do not change); 0: input order
+ *   SNCH_OPT_ORDER_MIN_BATCH  smallest batch that is reordered (default 65536) */
+#define SNCH_OPT_TRAVERSAL 1
+#define SNCH_OPT_QUERY_ORDER 2
+#define SNCH_OPT_ORDER_MIN_BATCH 3
+int snch_set_option(snch_scene_t scene, int option, int64_t value);
+
 /* Position of each sorted leaf in the reference's depth-first visit order,
  * copied to a HOST buffer of N entries (synchronous). */
 int snch_export_leaf_ranks(snch_scene_t scene, uint32_t *ranks);

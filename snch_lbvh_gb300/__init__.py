@@ -24,6 +24,7 @@ __all__ = ["Scene", "SnchError", "BvhView", "lib"]
 INVALID = 0xFFFFFFFF
 TRAVERSAL_NEAR_FIRST = 0
 TRAVERSAL_REFERENCE_ORDER = 1
+OPT_TRAVERSAL, OPT_QUERY_ORDER, OPT_ORDER_MIN_BATCH = 1, 2, 3
 
 
 def _torch():
@@ -111,6 +112,10 @@ class Scene:
     def set_traversal(self, mode: int):
         """TRAVERSAL_NEAR_FIRST (default) or TRAVERSAL_REFERENCE_ORDER; same results."""
         check(lib().snch_set_traversal(self._h, int(mode)))
+
+    def set_option(self, option: int, value: int):
+        """OPT_TRAVERSAL, OPT_QUERY_ORDER (Morton-sorted batches), OPT_ORDER_MIN_BATCH."""
+        check(lib().snch_set_option(self._h, int(option), int(value)))
 
     def leaf_ranks(self):
         n = self.num_triangles

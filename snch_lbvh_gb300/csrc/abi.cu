@@ -75,6 +75,8 @@ struct snch_scene_s
     snch_silhouette_edge *ref_edges = nullptr;
     bool topology_ready = false, built = false;
     int traversal = SNCH_TRAVERSAL_NEAR_FIRST;
+    int query_order = 1;             // Morton-sort batches of at least order_min queries
+    int64_t order_min = 65536;
     cudaStream_t pipe[2] = {nullptr, nullptr};
     HostStage stage;
 
@@ -263,6 +265,34 @@ int check_n(int64_t n, std::initializer_list<const void *> ptrs)
     return SNCH_OK;
 }
 
+// Tree view for one batch: Morton-sorted query order when enabled (the
+// ordering scratch is stream-ordered memory released after the launch).
+struct BatchView
+{
+    TreeView t;
+    void *scratch = nullptr;
+    cudaStream_t st = nullptr;
+    ~BatchView()
+    {
+        if (scratch)
+            cudaFreeAsync(scratch, st);
+    }
+};
+cudaError_t batch_view(const snch_scene_s *s, const float *keys_from, int64_t n, cudaStream_t st, BatchView &b)
+{
+    b.t = s->view();
+    b.st = st;
+    if (!s->query_order || n < s->order_min || n >= (int64_t(1) << 30) || s->num_tris < 2)
+        return cudaSuccess;
+    cudaError_t e = cudaMallocAsync(&b.scratch, query_order_scratch_bytes(n), st);
+    if (e != cudaSuccess)
+        return e;
+    uint32_t *order = nullptr;
+    e = launch_query_order(b.t, keys_from, n, b.scratch, &order, st);
+    b.t.order = order;
+    return e;
+}
+
 // ---- host-form pipeline: chunk i runs on pipe[i % 2]: H2D inputs, kernel, D2H outputs
 int ensure_stage(snch_scene_s *s, size_t in_bytes, size_t out_bytes)
 {
@@ -424,6 +454,29 @@ int snch_set_traversal(snch_scene_t s, int mode)
     return SNCH_OK;
 }
 
+int snch_set_option(snch_scene_t s, int option, int64_t value)
+{
+    if (!s)
+        return fail(SNCH_ERR_INVALID_ARGUMENT, "scene is NULL");
+    switch (option)
+    {
+    case SNCH_OPT_TRAVERSAL:
+        return snch_set_traversal(s, (int)value);
+    case SNCH_OPT_QUERY_ORDER:
+        if (value != 0 && value != 1)
+            return fail(SNCH_ERR_INVALID_ARGUMENT, "SNCH_OPT_QUERY_ORDER takes 0 or 1");
+        s->query_order = (int)value;
+        return SNCH_OK;
+    case SNCH_OPT_ORDER_MIN_BATCH:
+        if (value < 0)
+            return fail(SNCH_ERR_INVALID_ARGUMENT, "SNCH_OPT_ORDER_MIN_BATCH must be >= 0");
+        s->order_min = value;
+        return SNCH_OK;
+    default:
+        return fail(SNCH_ERR_INVALID_ARGUMENT, "unknown option " + std::to_string(option));
+    }
+}
+
 int snch_export_leaf_ranks(snch_scene_t s, uint32_t *ranks)
 {
     int rc = check_built(s);
@@ -542,7 +595,9 @@ int snch_query_nearest(snch_scene_t s, const float *pts, int64_t n, uint32_t *id
         rc = check_n(n, {pts, idx, dist});
     if (rc != SNCH_OK)
         return rc;
-    SNCH_CUDA(launch_nearest(s->view(), pts, n, idx, dist, S(stream)));
+    BatchView b;
+    SNCH_CUDA(batch_view(s, pts, n, S(stream), b));
+    SNCH_CUDA(launch_nearest(b.t, pts, n, idx, dist, S(stream)));
     return SNCH_OK;
 }
 
@@ -554,7 +609,9 @@ int snch_query_silhouette(snch_scene_t s, const float *pts, const uint8_t *flip,
         rc = check_n(n, {pts, dist});
     if (rc != SNCH_OK)
         return rc;
-    SNCH_CUDA(launch_silhouette(s->view(), pts, flip, n, dist, edge, S(stream)));
+    BatchView b;
+    SNCH_CUDA(batch_view(s, pts, n, S(stream), b));
+    SNCH_CUDA(launch_silhouette(b.t, pts, flip, n, dist, edge, S(stream)));
     return SNCH_OK;
 }
 
@@ -566,7 +623,9 @@ int snch_query_ray(snch_scene_t s, const float *o, const float *d, const float *
         rc = check_n(n, {o, d, tmax, hit, t, uv, idx});
     if (rc != SNCH_OK)
         return rc;
-    SNCH_CUDA(launch_ray(s->view(), o, d, tmax, n, hit, t, uv, idx, S(stream)));
+    BatchView b;
+    SNCH_CUDA(batch_view(s, o, n, S(stream), b));
+    SNCH_CUDA(launch_ray(b.t, o, d, tmax, n, hit, t, uv, idx, S(stream)));
     return SNCH_OK;
 }
 
@@ -578,7 +637,9 @@ int snch_sample_in_sphere(snch_scene_t s, const float *c, const float *r, const 
         rc = check_n(n, {c, r, u, idx, pdf});
     if (rc != SNCH_OK)
         return rc;
-    SNCH_CUDA(launch_sample(s->view(), c, r, u, n, idx, pdf, S(stream)));
+    BatchView b;
+    SNCH_CUDA(batch_view(s, c, n, S(stream), b));
+    SNCH_CUDA(launch_sample(b.t, c, r, u, n, idx, pdf, S(stream)));
     return SNCH_OK;
 }
 
@@ -611,9 +672,11 @@ int snch_query_nearest_host(snch_scene_t s, const float *pts, int64_t n, uint32_
         return rc;
     const Field ins[] = {{pts, nullptr, 12}};
     const Field outs[] = {{nullptr, idx, 4}, {nullptr, dist, 4}};
-    const TreeView t = s->view();
     return run_host_pipeline(s, n, ins, 1, outs, 2, [&](int64_t m, void **di, void **dout, cudaStream_t st) {
-        return launch_nearest(t, (const float *)di[0], m, (uint32_t *)dout[0], (float *)dout[1], st);
+        BatchView b;
+        cudaError_t e = batch_view(s, (const float *)di[0], m, st, b);
+        return e != cudaSuccess ? e : launch_nearest(b.t, (const float *)di[0], m, (uint32_t *)dout[0],
+                                                     (float *)dout[1], st);
     });
 }
 
@@ -627,10 +690,11 @@ int snch_query_silhouette_host(snch_scene_t s, const float *pts, const uint8_t *
         return rc;
     const Field ins[] = {{pts, nullptr, 12}, {flip, nullptr, 1}};
     const Field outs[] = {{nullptr, dist, 4}, {nullptr, edge, 4}};
-    const TreeView t = s->view();
     return run_host_pipeline(s, n, ins, 2, outs, 2, [&](int64_t m, void **di, void **dout, cudaStream_t st) {
-        return launch_silhouette(t, (const float *)di[0], (const uint8_t *)di[1], m, (float *)dout[0],
-                                 (int32_t *)dout[1], st);
+        BatchView b;
+        cudaError_t e = batch_view(s, (const float *)di[0], m, st, b);
+        return e != cudaSuccess ? e : launch_silhouette(b.t, (const float *)di[0], (const uint8_t *)di[1], m,
+                                                        (float *)dout[0], (int32_t *)dout[1], st);
     });
 }
 
@@ -644,10 +708,13 @@ int snch_query_ray_host(snch_scene_t s, const float *o, const float *d, const fl
         return rc;
     const Field ins[] = {{o, nullptr, 12}, {d, nullptr, 12}, {tmax, nullptr, 4}};
     const Field outs[] = {{nullptr, hit, 1}, {nullptr, t, 4}, {nullptr, uv, 8}, {nullptr, idx, 4}};
-    const TreeView tv = s->view();
     return run_host_pipeline(s, n, ins, 3, outs, 4, [&](int64_t m, void **di, void **dout, cudaStream_t st) {
-        return launch_ray(tv, (const float *)di[0], (const float *)di[1], (const float *)di[2], m, (uint8_t *)dout[0],
-                          (float *)dout[1], (float *)dout[2], (uint32_t *)dout[3], st);
+        BatchView b;
+        cudaError_t e = batch_view(s, (const float *)di[0], m, st, b);
+        return e != cudaSuccess ? e
+                                : launch_ray(b.t, (const float *)di[0], (const float *)di[1], (const float *)di[2], m,
+                                             (uint8_t *)dout[0], (float *)dout[1], (float *)dout[2],
+                                             (uint32_t *)dout[3], st);
     });
 }
 
@@ -661,10 +728,11 @@ int snch_sample_in_sphere_host(snch_scene_t s, const float *c, const float *r, c
         return rc;
     const Field ins[] = {{c, nullptr, 12}, {r, nullptr, 4}, {u, nullptr, 4}};
     const Field outs[] = {{nullptr, idx, 4}, {nullptr, pdf, 4}};
-    const TreeView t = s->view();
     return run_host_pipeline(s, n, ins, 3, outs, 2, [&](int64_t m, void **di, void **dout, cudaStream_t st) {
-        return launch_sample(t, (const float *)di[0], (const float *)di[1], (const float *)di[2], m,
-                             (int32_t *)dout[0], (float *)dout[1], st);
+        BatchView b;
+        cudaError_t e = batch_view(s, (const float *)di[0], m, st, b);
+        return e != cudaSuccess ? e : launch_sample(b.t, (const float *)di[0], (const float *)di[1],
+                                                    (const float *)di[2], m, (int32_t *)dout[0], (float *)dout[1], st);
     });
 }
 

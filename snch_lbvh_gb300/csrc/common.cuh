@@ -92,8 +92,12 @@ struct TreeView
     const LeafRec *leaves;
     const EdgeRec *edges;
     uint32_t *status;
-    int near_first;  // 1: near-first nearest/silhouette traversal, 0: the reference's stack order
+    int near_first;         // 1: near-first nearest/silhouette traversal, 0: the reference's stack order
+    const uint32_t *order;  // optional: thread i answers query order[i] (Morton-sorted batches)
 };
+
+// index of the query answered by global thread i
+SNCH_DEV int64_t query_index(const TreeView &t, int64_t i) { return t.order ? (int64_t)__ldg(t.order + i) : i; }
 
 // ---------------------------------------------------------------- vector math
 SNCH_DEV f3 mk(float x, float y, float z)

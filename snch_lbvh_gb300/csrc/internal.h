@@ -55,6 +55,11 @@ cudaError_t launch_ray(const TreeView &t, const float *o, const float *d, const 
                        float *tt, float *uv, uint32_t *idx, cudaStream_t st, uint32_t *stats = nullptr);
 cudaError_t launch_sample(const TreeView &t, const float *c, const float *r, const float *u, int64_t n, int32_t *idx,
                           float *pdf, cudaStream_t st, uint32_t *stats = nullptr);
+// Morton-sorted order of a query batch (thread i answers query order[i]);
+// scratch holds query_order_scratch_bytes(n) bytes and owns *order.
+size_t query_order_scratch_bytes(int64_t n);
+cudaError_t launch_query_order(const TreeView &t, const float *pts, int64_t n, void *scratch, uint32_t **order,
+                               cudaStream_t st);
 cudaError_t launch_sample_point(const float *verts, const int32_t *tris, const int32_t *idx, const float *u,
                                 const float *v, int64_t n, float *out, cudaStream_t st);
 

@@ -83,9 +83,10 @@ SNCH_DEV float leaf_distance2(const TreeView &t, uint32_t pos, f3 p, uint32_t &o
 __global__ void __launch_bounds__(128) nearest_kernel(TreeView t, const float *__restrict__ pts, int64_t n,
                                                       uint32_t *__restrict__ out_idx, float *__restrict__ out_dist)
 {
-    const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (q >= n)
+    const int64_t qi = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (qi >= n)
         return;
+    const int64_t q = query_index(t, qi);
     const f3 p = load_point(pts, q);
     uint32_t nearest = kInvalid;
     float best = INFINITY;
@@ -296,9 +297,10 @@ __global__ void __launch_bounds__(128) silhouette_kernel(TreeView t, const float
                                                          const uint8_t *__restrict__ flips, int64_t n,
                                                          float *__restrict__ out_dist, int32_t *__restrict__ out_edge)
 {
-    const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (q >= n)
+    const int64_t qi = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (qi >= n)
         return;
+    const int64_t q = query_index(t, qi);
     const f3 p = load_point(pts, q);
     const bool flip = flips ? __ldg(flips + q) != 0 : false;
     float best = INFINITY;
@@ -431,9 +433,10 @@ __global__ void __launch_bounds__(128) nearest_fast_kernel(TreeView t, const flo
                                                            uint32_t *__restrict__ stats)
 {
     uint32_t n_int = 0, n_leaf = 0;
-    const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (q >= n)
+    const int64_t qi = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (qi >= n)
         return;
+    const int64_t q = query_index(t, qi);
     const f3 p = load_point(pts, q);
     uint32_t nearest = kInvalid, best_rank = 0;
     float best = INFINITY;
@@ -564,9 +567,10 @@ __global__ void __launch_bounds__(128) silhouette_fast_kernel(TreeView t, const 
                                                               uint32_t *__restrict__ stats)
 {
     uint32_t n_int = 0, n_leaf = 0, n_edge = 0;
-    const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (q >= n)
+    const int64_t qi = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (qi >= n)
         return;
+    const int64_t q = query_index(t, qi);
     const f3 p = load_point(pts, q);
     const bool flip = flips ? __ldg(flips + q) != 0 : false;
     float best = INFINITY;
@@ -719,9 +723,10 @@ __global__ void __launch_bounds__(128) ray_kernel(TreeView t, const float *__res
                                                   uint32_t *__restrict__ stats)
 {
     uint32_t n_int = 0, n_leaf = 0;
-    const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (q >= n)
+    const int64_t qi = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (qi >= n)
         return;
+    const int64_t q = query_index(t, qi);
     const f3 o = load_point(origins, q), dir = load_point(dirs, q);
     const f3 inv = mk(1 / dir.x, 1 / dir.y, 1 / dir.z);  // ray ctor aabb.cuh:305-312
     const float max_dist = __ldg(tmaxs + q);
@@ -885,9 +890,10 @@ __global__ void __launch_bounds__(128) sample_kernel(TreeView t, const float *__
                                                      float *__restrict__ out_pdf, uint32_t *__restrict__ stats)
 {
     uint32_t n_int = 0, n_leaf = 0;
-    const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (q >= n)
+    const int64_t qi = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (qi >= n)
         return;
+    const int64_t q = query_index(t, qi);
     const f3 c = load_point(centers, q);
     const float rad = __ldg(radii + q);
     float u = __ldg(us + q);
@@ -975,6 +981,36 @@ __global__ void sample_point_kernel(const float *__restrict__ verts, const int32
     out[3 * q + 2] = w * pa.z + u * pb.z + v * pc.z;
 }
 
+// ------------------------------------------------------------------ query ordering
+// 30-bit Morton code of each query point inside the root box (same encoding
+// as the leaves, morton_code.cuh:61-70); sorting a batch by it makes the 32
+// queries of a warp spatial neighbours. Results do not depend on the order.
+__global__ void query_keys_kernel(const float *__restrict__ pts, int64_t n, const Box *__restrict__ root,
+                                  uint32_t *__restrict__ keys, uint32_t *__restrict__ vals)
+{
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    const Box b = load_root_box(root);
+    f3 p = load_point(pts, i);
+    p.x = (p.x - b.lower.x) / (b.upper.x - b.lower.x);
+    p.y = (p.y - b.lower.y) / (b.upper.y - b.lower.y);
+    p.z = (p.z - b.lower.z) / (b.upper.z - b.lower.z);
+    const float res = 1024.0f;
+    const uint32_t x = (uint32_t)fminf(fmaxf(p.x * res, 0.0f), res - 1.0f);
+    const uint32_t y = (uint32_t)fminf(fmaxf(p.y * res, 0.0f), res - 1.0f);
+    const uint32_t z = (uint32_t)fminf(fmaxf(p.z * res, 0.0f), res - 1.0f);
+    auto expand = [](uint32_t v) {
+        v = (v | (v << 16)) & 0x070000FFu;
+        v = (v | (v << 8)) & 0x0700F00Fu;
+        v = (v | (v << 4)) & 0x430C30C3u;
+        v = (v | (v << 2)) & 0x49249249u;
+        return v;
+    };
+    keys[i] = expand(x) * 4 + expand(y) * 2 + expand(z);
+    vals[i] = (uint32_t)i;
+}
+
 // ------------------------------------------------------------------ launchers
 namespace
 {
@@ -1033,6 +1069,22 @@ cudaError_t launch_sample(const TreeView &t, const float *c, const float *r, con
     note_launch();
     return cudaGetLastError();
 }
+cudaError_t launch_query_order(const TreeView &t, const float *pts, int64_t n, void *scratch, uint32_t **order,
+                               cudaStream_t st)
+{
+    uint32_t *keys = static_cast<uint32_t *>(scratch);
+    uint32_t *vals = keys + n, *keys_tmp = vals + n, *vals_tmp = keys_tmp + n;
+    void *sort_scratch = vals_tmp + n;
+    query_keys_kernel<<<grid_for(n, 256), 256, 0, st>>>(pts, n, t.aabbs, keys, vals);
+    note_launch();
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess)
+        e = radix_sort_pairs(keys, vals, keys_tmp, vals_tmp, (uint32_t)n, 30, nullptr, sort_scratch, t.status, st);
+    *order = vals;
+    return e;
+}
+size_t query_order_scratch_bytes(int64_t n) { return 16 * (size_t)n + sort_scratch_bytes((uint32_t)n, 30) + 256; }
+
 cudaError_t launch_sample_point(const float *verts, const int32_t *tris, const int32_t *idx, const float *u,
                                 const float *v, int64_t n, float *out, cudaStream_t st)
 {

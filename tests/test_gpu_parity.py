@@ -238,3 +238,28 @@ def test_near_first_equals_reference_order_config1(snch):
     for x, y in zip(a, b):
         np.testing.assert_array_equal(x, y)
     assert s.device_status() == 0
+
+
+def test_query_order_does_not_change_results(snch):
+    """Morton-sorted batches (default for >= 65536 queries) equal input-order batches."""
+    from snch_lbvh_gb300 import meshes
+    v, f = meshes.noisy_icosphere(5, 1.0, 0.01, seed=0)
+    q = meshes.wost_queries(400_000, 200_000, 400_000, 200_000, seed=9)
+    for k in ("near_pts", "sil_pts", "ray_o", "smp_c"):
+        q[k] = (q[k] * 2.4 - 1.2).astype(np.float32)
+    s = built_scene(snch, v, f)
+
+    def everything():
+        i, d = s.query_nearest(q["near_pts"])
+        sd, se = s.query_silhouette(q["sil_pts"], q["sil_flip"])
+        h, t, uv, ri = s.query_ray(q["ray_o"], q["ray_d"], q["ray_tmax"])
+        si, sp = s.sample_in_sphere(q["smp_c"], q["smp_r"], q["smp_u"])
+        return [x.cpu().numpy() for x in (i, d, sd, se, h, t, uv, ri, si, sp)]
+
+    s.set_option(snch.OPT_QUERY_ORDER, 0)
+    a = everything()
+    s.set_option(snch.OPT_QUERY_ORDER, 1)
+    b = everything()
+    for x, y in zip(a, b):
+        np.testing.assert_array_equal(x.view(np.uint8), y.view(np.uint8))
+    assert s.device_status() == 0

@@ -1,0 +1,85 @@
+"""The reference's own CUDA queries (its headers compiled for sm_103a with its own
+flags) run over a tree built by this library through the byte-compatible
+snch_bvh_view, and agree with this library's kernels.
+
+The reference compiles with nvcc's default FMA contraction, this library
+without it, so floats agree to within a few ulps (RTOL) and indices agree
+except where two candidates' distances are that close.
+"""
+import numpy as np
+import pytest
+
+from conftest import golden_names, load_golden
+from test_gpu_parity import built_scene
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-6
+
+
+@pytest.fixture(scope="module")
+def ref():
+    from oracle import ref_gpu
+    ok, why = ref_gpu.available()
+    if not ok:
+        pytest.skip(why)
+    ref_gpu.lib()
+    return ref_gpu
+
+
+def close(a, b, rtol=RTOL):
+    a, b = a.astype(np.float64), b.astype(np.float64)
+    both_inf = np.isinf(a) & np.isinf(b) & (np.sign(a) == np.sign(b))
+    return both_inf | (np.abs(a - b) <= rtol * np.maximum(np.abs(b), 1e-30))
+
+
+def compare_all(snch, ref, s, q):
+    import torch
+    R = ref.RefQueries(s)
+    d = {k: torch.from_numpy(np.ascontiguousarray(v)).cuda() for k, v in q.items()}
+    ri, rd = R.nearest(d["near_pts"])
+    mi, md = s.query_nearest(d["near_pts"])
+    rd, md = rd.cpu().numpy(), md.cpu().numpy()
+    assert close(rd, md).all()
+    same = ri.cpu().numpy() == mi.cpu().numpy()
+    assert same.mean() > 0.999, same.mean()
+    rs = R.silhouette(d["sil_pts"], d["sil_flip"]).cpu().numpy()
+    ms = s.query_silhouette(d["sil_pts"], d["sil_flip"])[0].cpu().numpy()
+    assert close(rs, ms).mean() > 0.999
+    rh, rt, rr = R.ray(d["ray_o"], d["ray_d"], d["ray_tmax"])
+    mh, mt, _, mr = s.query_ray(d["ray_o"], d["ray_d"], d["ray_tmax"])
+    hit_same = rh.cpu().numpy() == mh.cpu().numpy()
+    assert hit_same.mean() > 0.999
+    both = (rh.cpu().numpy() == 1) & hit_same
+    assert close(rt.cpu().numpy()[both], mt.cpu().numpy()[both]).all()
+    rsi, rsp = R.sample(d["smp_c"], d["smp_r"], d["smp_u"])
+    msi, msp = s.sample_in_sphere(d["smp_c"], d["smp_r"], d["smp_u"])
+    assert (rsi.cpu().numpy() == msi.cpu().numpy()).mean() > 0.999
+    torch.cuda.synchronize()
+
+
+@pytest.mark.parametrize("name", [n for n in golden_names() if n not in ("single_tri",)])
+def test_reference_cuda_runs_on_our_tree_golden(ref, name):
+    import snch_lbvh_gb300 as snch
+    g = load_golden(name)
+    s = built_scene(snch, g["verts"], g["tris"])
+    q = {"near_pts": g["near_pts"], "sil_pts": g["sil_pts"], "sil_flip": g["sil_flip"], "ray_o": g["ray_o"],
+         "ray_d": g["ray_d"], "ray_tmax": g["ray_tmax"], "smp_c": g["smp_c"], "smp_r": g["smp_r"],
+         "smp_u": g["smp_u"]}
+    compare_all(snch, ref, s, q)
+    # and the reference's GPU answers match its CPU answers (same algorithm, FMA aside)
+    import torch
+    R = ref.RefQueries(s)
+    ri, rd = R.nearest(torch.from_numpy(g["near_pts"]).cuda())
+    assert close(rd.cpu().numpy(), g["ref_near_dist"]).all()
+
+
+def test_reference_cuda_runs_on_our_tree_config1(ref):
+    import snch_lbvh_gb300 as snch
+    from snch_lbvh_gb300 import meshes
+    v, f = meshes.noisy_icosphere(5, 1.0, 0.01, seed=0)
+    q = meshes.wost_queries(200_000, 100_000, 200_000, 100_000, seed=12)
+    for k in ("near_pts", "sil_pts", "ray_o", "smp_c"):
+        q[k] = (q[k] * 2.4 - 1.2).astype(np.float32)
+    s = built_scene(snch, v, f)
+    compare_all(snch, ref, s, q)
