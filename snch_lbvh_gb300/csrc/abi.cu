@@ -82,7 +82,7 @@ struct snch_scene_s
 
     TreeView view() const
     {
-        TreeView t;
+        TreeView t{};
         t.num_tris = num_tris;
         t.nodes = nodes;
         t.aabbs = aabbs;
@@ -221,7 +221,7 @@ int topology(snch_scene_s *s, cudaStream_t st)
 
 BuildArgs build_args(snch_scene_s *s)
 {
-    BuildArgs a;
+    BuildArgs a{};
     a.num_tris = s->num_tris;
     a.verts = s->verts;
     a.tris = s->tris;

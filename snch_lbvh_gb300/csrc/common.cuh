@@ -84,16 +84,16 @@ struct alignas(64) EdgeRec
 // Everything a query kernel reads, passed by value.
 struct TreeView
 {
-    uint32_t num_tris;  // N
-    const NodeRec *nodes;
-    const Box *aabbs;   // aabbs[0] is the root box
-    const InnerRec *inner;
-    const InnerConeRec *inner_cones;
-    const LeafRec *leaves;
-    const EdgeRec *edges;
-    uint32_t *status;
-    int near_first;         // 1: near-first nearest/silhouette traversal, 0: the reference's stack order
-    const uint32_t *order;  // optional: thread i answers query order[i] (Morton-sorted batches)
+    uint32_t num_tris = 0;  // N
+    const NodeRec *nodes = nullptr;
+    const Box *aabbs = nullptr;  // aabbs[0] is the root box
+    const InnerRec *inner = nullptr;
+    const InnerConeRec *inner_cones = nullptr;
+    const LeafRec *leaves = nullptr;
+    const EdgeRec *edges = nullptr;
+    uint32_t *status = nullptr;
+    int near_first = 1;               // 1: near-first nearest/silhouette traversal, 0: the reference's stack order
+    const uint32_t *order = nullptr;  // optional: thread i answers query order[i] (Morton-sorted batches)
 };
 
 // index of the query answered by global thread i
