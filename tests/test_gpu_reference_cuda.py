@@ -3,8 +3,11 @@ flags) run over a tree built by this library through the byte-compatible
 snch_bvh_view, and agree with this library's kernels.
 
 The reference compiles with nvcc's default FMA contraction, this library
-without it, so floats agree to within a few ulps (RTOL) and indices agree
-except where two candidates' distances are that close.
+without it (and bit-exactly equal to the reference's uncontracted arithmetic,
+tests/test_gpu_parity.py), so floats agree to within RTOL relative or ATOL
+absolute (two float32 ulps at unit coordinates; near-surface distances of
+~0.01 differ by 1-3e-8 between the two builds), and indices agree except
+where two candidates' distances are that close.
 """
 import numpy as np
 import pytest
@@ -15,6 +18,7 @@ from test_gpu_parity import built_scene
 pytestmark = pytest.mark.gpu
 
 RTOL = 1e-6
+ATOL = 2.5e-7
 
 
 @pytest.fixture(scope="module")
@@ -27,10 +31,10 @@ def ref():
     return ref_gpu
 
 
-def close(a, b, rtol=RTOL):
+def close(a, b, rtol=RTOL, atol=ATOL):
     a, b = a.astype(np.float64), b.astype(np.float64)
     both_inf = np.isinf(a) & np.isinf(b) & (np.sign(a) == np.sign(b))
-    return both_inf | (np.abs(a - b) <= rtol * np.maximum(np.abs(b), 1e-30))
+    return both_inf | (np.abs(a - b) <= np.maximum(rtol * np.abs(b), atol))
 
 
 def compare_all(snch, ref, s, q):
