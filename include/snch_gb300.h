@@ -208,6 +208,25 @@ int snch_sort_pairs(uint32_t *keys, uint32_t *values, uint32_t *keys_tmp, uint32
 /* Number of kernels this library has launched in this process (all scenes). */
 uint64_t snch_kernel_launch_count(void);
 
+/* snch_sort_pairs for callers that cannot allocate GPU memory -- a real-time
+ * solver loop that must never stall the device (cudaMalloc/cudaFree can
+ * synchronise it), a host plug-in whose GPU memory belongs to the host
+ * application's allocator. No counterpart in the reference (whose Thrust sort
+ * allocates). Sorts (keys_in, values_in) by the low key_bits bits into
+ * (keys_out, values_out) (in == out is allowed), stably, asynchronously on
+ * `stream`, calling no allocating routine: all other working memory is one
+ * fixed array of about 10 MB that every GPU loading this library holds until
+ * exit. At most SNCH_SORT_NOALLOC_MAX_PAIRS pairs per call (larger n returns
+ * SNCH_ERR_TOO_LARGE). Calls share that array: calls that overlap on the GPU
+ * (other streams, other host threads) race and must be serialised by the
+ * caller. The first call on each device looks up the array's device address
+ * (cudaGetSymbolAddress) -- make it before any stream capture. device_status
+ * (may be NULL) is a caller DEVICE word that receives SNCH_DEVICE_* bits. */
+#define SNCH_SORT_NOALLOC_MAX_PAIRS 1048576
+int snch_sort_pairs_noalloc(const uint32_t *keys_in, const uint32_t *values_in, uint32_t *keys_out,
+                            uint32_t *values_out, int64_t n, int key_bits, uint32_t *device_status,
+                            snch_stream_t stream);
+
 /* Library version string. */
 const char *snch_version(void);
 

@@ -29,6 +29,7 @@ UNITS = [
     ("build.cu", ["-fmad=false"]),
     ("queries.cu", ["-fmad=false"]),
     ("abi.cu", []),
+    ("noalloc_sort.cu", []),
 ]
 HEADERS = ["common.cuh", "internal.h"]
 

@@ -26,6 +26,12 @@ int fail(int code, const std::string &msg)
     g_error = msg;
     return code;
 }
+}  // namespace
+
+int snch::report_error(int code, const std::string &msg) { return fail(code, msg); }
+
+namespace
+{
 
 #define SNCH_CUDA(expr)                                                                                    \
     do                                                                                                     \

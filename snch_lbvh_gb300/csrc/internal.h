@@ -2,6 +2,7 @@
 #pragma once
 #include <cstddef>
 #include <cstdint>
+#include <string>
 #include <cuda_runtime.h>
 
 #include "../../include/snch_gb300.h"
@@ -12,6 +13,9 @@ namespace snch
 
 // Number of kernels this library has launched (snch_kernel_launch_count).
 void note_launch(unsigned count = 1);
+
+// Records msg as the calling thread's snch_last_error() and returns code.
+int report_error(int code, const std::string &msg);
 
 // Device arrays of one LBVH construction (build.cu).
 struct BuildArgs
