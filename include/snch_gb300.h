@@ -174,6 +174,22 @@ int snch_sample_in_sphere(snch_scene_t scene, const float *centers_xyz, const fl
 int snch_sample_on_object(snch_scene_t scene, const int32_t *index, const float *u, const float *v, int64_t n,
                           float *out_points_xyz, snch_stream_t stream);
 
+/* Nearest / silhouette queries with a per-query search radius (DEVICE float[n],
+ * e.g. predicted by snch_mlp_predict_radius): the search starts as if a
+ * primitive at that distance had been found, so only nodes within it are
+ * visited; queries with nothing inside their radius are answered again without
+ * a bound within the same call. Results equal snch_query_nearest /
+ * snch_query_silhouette for any radii (tie winners included); the radius only
+ * changes the work. num_fallback (DEVICE uint32, may be NULL) receives the
+ * number of queries that needed the unbounded pass. No reference counterpart:
+ * the reference always starts unbounded (query.cuh:255, 343). */
+int snch_query_nearest_seeded(snch_scene_t scene, const float *points_xyz, const float *radius, int64_t n,
+                              uint32_t *out_index, float *out_distance, uint32_t *num_fallback,
+                              snch_stream_t stream);
+int snch_query_silhouette_seeded(snch_scene_t scene, const float *points_xyz, const uint8_t *flip,
+                                 const float *radius, int64_t n, float *out_distance, int32_t *out_edge,
+                                 uint32_t *num_fallback, snch_stream_t stream);
+
 /* Host-buffer forms of the four queries: copy in, run, copy out in pipelined
  * chunks on the scene's own streams; return when results are in host memory.
  * This is the call shape of the reference's benchmark loop (benchmark.cu:395-409). */

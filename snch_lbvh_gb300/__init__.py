@@ -190,6 +190,31 @@ class Scene:
         check(lib().snch_query_nearest(self._h, _ptr(p), n, _ptr(idx), _ptr(dist), _stream(stream)))
         return idx, dist
 
+    def query_nearest_seeded(self, points, radius, stream=None, out=None, num_fallback=None):
+        """Nearest query whose search starts at a per-query radius; same results as query_nearest."""
+        torch = _torch()
+        p = _dev(points, torch.float32, 3)
+        r = _dev(radius, torch.float32)
+        n = p.shape[0]
+        idx, dist = out if out is not None else (torch.empty(n, dtype=torch.int32, device="cuda"),
+                                                 torch.empty(n, dtype=torch.float32, device="cuda"))
+        check(lib().snch_query_nearest_seeded(self._h, _ptr(p), _ptr(r), n, _ptr(idx), _ptr(dist), _ptr(num_fallback),
+                                              _stream(stream)))
+        return idx, dist
+
+    def query_silhouette_seeded(self, points, radius, flip=None, stream=None, out=None, num_fallback=None):
+        """Silhouette query whose search starts at a per-query radius; same results as query_silhouette."""
+        torch = _torch()
+        p = _dev(points, torch.float32, 3)
+        r = _dev(radius, torch.float32)
+        n = p.shape[0]
+        f = None if flip is None else _dev(flip, torch.uint8)
+        dist, edge = out if out is not None else (torch.empty(n, dtype=torch.float32, device="cuda"),
+                                                  torch.empty(n, dtype=torch.int32, device="cuda"))
+        check(lib().snch_query_silhouette_seeded(self._h, _ptr(p), _ptr(f), _ptr(r), n, _ptr(dist), _ptr(edge),
+                                                 _ptr(num_fallback), _stream(stream)))
+        return dist, edge
+
     def query_silhouette(self, points, flip=None, stream=None, out=None):
         """query_device(nearest_silhouette) query.cuh:326 -> (distance, edge id or -1)."""
         torch = _torch()

@@ -299,6 +299,42 @@ cudaError_t batch_view(const snch_scene_s *s, const float *keys_from, int64_t n,
     return e;
 }
 
+// Seeded pass over the batch, then the unbounded pass over the queries that
+// found nothing inside their radius (listed by the seeded kernel itself).
+template <typename Launch>
+int run_seeded(snch_scene_s *s, const float *pts, const float *radius, int64_t n, uint32_t *num_fallback,
+               cudaStream_t st, Launch launch)
+{
+    char *scratch = nullptr;
+    SNCH_CUDA(cudaMallocAsync(reinterpret_cast<void **>(&scratch), 4 * (size_t)n + 256, st));
+    uint32_t *count = reinterpret_cast<uint32_t *>(scratch);
+    uint32_t *list = reinterpret_cast<uint32_t *>(scratch + 256);
+    cudaError_t e = cudaMemsetAsync(count, 0, 4, st);
+    if (e == cudaSuccess)
+    {
+        BatchView b;
+        e = batch_view(s, pts, n, st, b);
+        SeedArgs seed;
+        seed.radius = radius;
+        seed.fail_list = list;
+        seed.fail_count = count;
+        if (e == cudaSuccess)
+            e = launch(b.t, seed);
+        if (e == cudaSuccess)
+        {
+            TreeView fallback = s->view();
+            fallback.order = list;
+            fallback.order_count = count;
+            e = launch(fallback, SeedArgs());
+        }
+        if (e == cudaSuccess && num_fallback)
+            e = cudaMemcpyAsync(num_fallback, count, 4, cudaMemcpyDeviceToDevice, st);
+    }
+    cudaFreeAsync(scratch, st);
+    SNCH_CUDA(e);
+    return SNCH_OK;
+}
+
 // ---- host-form pipeline: chunk i runs on pipe[i % 2]: H2D inputs, kernel, D2H outputs
 int ensure_stage(snch_scene_s *s, size_t in_bytes, size_t out_bytes)
 {
@@ -739,6 +775,32 @@ int snch_sample_in_sphere_host(snch_scene_t s, const float *c, const float *r, c
         cudaError_t e = batch_view(s, (const float *)di[0], m, st, b);
         return e != cudaSuccess ? e : launch_sample(b.t, (const float *)di[0], (const float *)di[1],
                                                     (const float *)di[2], m, (int32_t *)dout[0], (float *)dout[1], st);
+    });
+}
+
+int snch_query_nearest_seeded(snch_scene_t s, const float *pts, const float *radius, int64_t n, uint32_t *idx,
+                              float *dist, uint32_t *num_fallback, snch_stream_t stream)
+{
+    int rc = check_built(s);
+    if (rc == SNCH_OK)
+        rc = check_n(n, {pts, radius, idx, dist});
+    if (rc != SNCH_OK || n == 0)
+        return rc;
+    return run_seeded(s, pts, radius, n, num_fallback, S(stream), [&](const TreeView &t, const SeedArgs &seed) {
+        return launch_nearest(t, pts, n, idx, dist, S(stream), nullptr, seed);
+    });
+}
+
+int snch_query_silhouette_seeded(snch_scene_t s, const float *pts, const uint8_t *flip, const float *radius, int64_t n,
+                                 float *dist, int32_t *edge, uint32_t *num_fallback, snch_stream_t stream)
+{
+    int rc = check_built(s);
+    if (rc == SNCH_OK)
+        rc = check_n(n, {pts, radius, dist});
+    if (rc != SNCH_OK || n == 0)
+        return rc;
+    return run_seeded(s, pts, radius, n, num_fallback, S(stream), [&](const TreeView &t, const SeedArgs &seed) {
+        return launch_silhouette(t, pts, flip, n, dist, edge, S(stream), nullptr, seed);
     });
 }
 

@@ -94,10 +94,38 @@ struct TreeView
     uint32_t *status = nullptr;
     int near_first = 1;               // 1: near-first nearest/silhouette traversal, 0: the reference's stack order
     const uint32_t *order = nullptr;  // optional: thread i answers query order[i] (Morton-sorted batches)
+    const uint32_t *order_count = nullptr;  // optional: device count of valid entries of order
+};
+
+// Seeded search: per-query initial radius, and where queries that find
+// nothing inside it are listed for the unbounded fallback pass.
+struct SeedArgs
+{
+    const float *radius = nullptr;   // nullptr: unbounded
+    uint32_t *fail_list = nullptr;   // query indices with an empty seeded result
+    uint32_t *fail_count = nullptr;
 };
 
 // index of the query answered by global thread i
 SNCH_DEV int64_t query_index(const TreeView &t, int64_t i) { return t.order ? (int64_t)__ldg(t.order + i) : i; }
+// number of queries of this launch (the fallback pass reads it from the device)
+SNCH_DEV int64_t query_count(const TreeView &t, int64_t n) { return t.order_count ? (int64_t)*t.order_count : n; }
+
+// warp-aggregated append of q to list (order of the list is irrelevant)
+SNCH_DEV void append_failed(uint32_t *list, uint32_t *count, uint32_t q, bool failed)
+{
+    const uint32_t active = __activemask();
+    const uint32_t mask = __ballot_sync(active, failed);
+    if (!failed)
+        return;
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(mask) - 1;
+    uint32_t base = 0;
+    if (lane == leader)
+        base = atomicAdd(count, (uint32_t)__popc(mask));
+    base = __shfl_sync(mask, base, leader);
+    list[base + __popc(mask & ((1u << lane) - 1u))] = q;
+}
 
 // ---------------------------------------------------------------- vector math
 SNCH_DEV f3 mk(float x, float y, float z)

@@ -84,7 +84,7 @@ __global__ void __launch_bounds__(128) nearest_kernel(TreeView t, const float *_
                                                       uint32_t *__restrict__ out_idx, float *__restrict__ out_dist)
 {
     const int64_t qi = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (qi >= n)
+    if (qi >= query_count(t, n))
         return;
     const int64_t q = query_index(t, qi);
     const f3 p = load_point(pts, q);
@@ -298,7 +298,7 @@ __global__ void __launch_bounds__(128) silhouette_kernel(TreeView t, const float
                                                          float *__restrict__ out_dist, int32_t *__restrict__ out_edge)
 {
     const int64_t qi = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (qi >= n)
+    if (qi >= query_count(t, n))
         return;
     const int64_t q = query_index(t, qi);
     const f3 p = load_point(pts, q);
@@ -419,7 +419,7 @@ SNCH_DEV void leaf_nearest_fast(const TreeView &t, uint32_t pos, f3 p, float &be
     float d = closest_point_triangle(mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), mk(c.x, c.y, c.z), p);
     d *= d;
     const uint32_t rank = __float_as_uint(c.w);
-    if (d < best || (d == best && rank > best_rank))
+    if (d < best || (d == best && (nearest == kInvalid || rank > best_rank)))
     {
         best = d;
         best_rank = rank;
@@ -430,22 +430,31 @@ SNCH_DEV void leaf_nearest_fast(const TreeView &t, uint32_t pos, f3 p, float &be
 template <bool kStats>
 __global__ void __launch_bounds__(128) nearest_fast_kernel(TreeView t, const float *__restrict__ pts, int64_t n,
                                                            uint32_t *__restrict__ out_idx, float *__restrict__ out_dist,
-                                                           uint32_t *__restrict__ stats)
+                                                           uint32_t *__restrict__ stats, SeedArgs seed)
 {
     uint32_t n_int = 0, n_leaf = 0;
     const int64_t qi = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (qi >= n)
+    if (qi >= query_count(t, n))
         return;
     const int64_t q = query_index(t, qi);
     const f3 p = load_point(pts, q);
     uint32_t nearest = kInvalid, best_rank = 0;
     float best = INFINITY;
+    if (seed.radius)
+    {
+        const float r = __ldg(seed.radius + q);
+        best = r * r;
+    }
     const uint32_t ni = t.num_tris - 1;
     if (t.num_tris == 1)
     {
         uint32_t orig;
-        best = leaf_distance2(t, 0, p, orig);
-        nearest = orig;
+        const float d = leaf_distance2(t, 0, p, orig);
+        if (d <= best)
+        {
+            best = d;
+            nearest = orig;
+        }
     }
     else if (t.num_tris > 1)
     {
@@ -517,8 +526,12 @@ __global__ void __launch_bounds__(128) nearest_fast_kernel(TreeView t, const flo
         stats[3 * q + 1] = n_leaf;
         stats[3 * q + 2] = 0;
     }
+    if (seed.radius && nearest == kInvalid)
+        best = INFINITY;  // nothing within the seed radius: the fallback pass answers it
     out_idx[q] = nearest;
     out_dist[q] = sqrtf(best);
+    if (seed.fail_list)
+        append_failed(seed.fail_list, seed.fail_count, (uint32_t)q, nearest == kInvalid);
 }
 
 // one leaf of the silhouette query; key = rank * 4 + slot orders candidates
@@ -550,7 +563,7 @@ SNCH_DEV void leaf_silhouette_fast(const TreeView &t, uint32_t pos, f3 o, bool f
         if (!is_sil)
             continue;
         const uint32_t key = rank * 4u + k;
-        if (d < best || (d > 0.0f ? key > best_key : key < best_key))
+        if (d < best || best_edge < 0 || (d > 0.0f ? key > best_key : key < best_key))
         {
             best = d;
             best_key = key;
@@ -564,16 +577,16 @@ __global__ void __launch_bounds__(128) silhouette_fast_kernel(TreeView t, const 
                                                               const uint8_t *__restrict__ flips, int64_t n,
                                                               float *__restrict__ out_dist,
                                                               int32_t *__restrict__ out_edge,
-                                                              uint32_t *__restrict__ stats)
+                                                              uint32_t *__restrict__ stats, SeedArgs seed)
 {
     uint32_t n_int = 0, n_leaf = 0, n_edge = 0;
     const int64_t qi = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (qi >= n)
+    if (qi >= query_count(t, n))
         return;
     const int64_t q = query_index(t, qi);
     const f3 p = load_point(pts, q);
     const bool flip = flips ? __ldg(flips + q) != 0 : false;
-    float best = INFINITY;
+    float best = seed.radius ? __ldg(seed.radius + q) : INFINITY;
     uint32_t best_key = 0;
     int32_t best_edge = -1;
     const uint32_t ni = t.num_tris - 1;
@@ -654,9 +667,13 @@ __global__ void __launch_bounds__(128) silhouette_fast_kernel(TreeView t, const 
             }
         } while (sp > 0);
     }
+    if (seed.radius && best_edge < 0)
+        best = INFINITY;  // nothing within the seed radius: the fallback pass answers it
     out_dist[q] = best;
     if (out_edge)
         out_edge[q] = best_edge;
+    if (seed.fail_list)
+        append_failed(seed.fail_list, seed.fail_count, (uint32_t)q, best_edge < 0);
     if (kStats)
     {
         stats[3 * q] = n_int;
@@ -724,7 +741,7 @@ __global__ void __launch_bounds__(128) ray_kernel(TreeView t, const float *__res
 {
     uint32_t n_int = 0, n_leaf = 0;
     const int64_t qi = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (qi >= n)
+    if (qi >= query_count(t, n))
         return;
     const int64_t q = query_index(t, qi);
     const f3 o = load_point(origins, q), dir = load_point(dirs, q);
@@ -891,7 +908,7 @@ __global__ void __launch_bounds__(128) sample_kernel(TreeView t, const float *__
 {
     uint32_t n_int = 0, n_leaf = 0;
     const int64_t qi = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (qi >= n)
+    if (qi >= query_count(t, n))
         return;
     const int64_t q = query_index(t, qi);
     const f3 c = load_point(centers, q);
@@ -1018,28 +1035,28 @@ inline unsigned grid_for(int64_t n, int b) { return (unsigned)((n + b - 1) / b);
 }  // namespace
 
 cudaError_t launch_nearest(const TreeView &t, const float *pts, int64_t n, uint32_t *idx, float *dist, cudaStream_t st,
-                           uint32_t *stats)
+                           uint32_t *stats, const SeedArgs &seed)
 {
     if (n <= 0)
         return cudaSuccess;
     if (stats)
-        nearest_fast_kernel<true><<<grid_for(n, 128), 128, 0, st>>>(t, pts, n, idx, dist, stats);
-    else if (t.near_first)
-        nearest_fast_kernel<false><<<grid_for(n, 128), 128, 0, st>>>(t, pts, n, idx, dist, nullptr);
+        nearest_fast_kernel<true><<<grid_for(n, 128), 128, 0, st>>>(t, pts, n, idx, dist, stats, seed);
+    else if (t.near_first || seed.radius)
+        nearest_fast_kernel<false><<<grid_for(n, 128), 128, 0, st>>>(t, pts, n, idx, dist, nullptr, seed);
     else
         nearest_kernel<<<grid_for(n, 128), 128, 0, st>>>(t, pts, n, idx, dist);
     note_launch();
     return cudaGetLastError();
 }
 cudaError_t launch_silhouette(const TreeView &t, const float *pts, const uint8_t *flip, int64_t n, float *dist,
-                              int32_t *edge, cudaStream_t st, uint32_t *stats)
+                              int32_t *edge, cudaStream_t st, uint32_t *stats, const SeedArgs &seed)
 {
     if (n <= 0)
         return cudaSuccess;
     if (stats)
-        silhouette_fast_kernel<true><<<grid_for(n, 128), 128, 0, st>>>(t, pts, flip, n, dist, edge, stats);
-    else if (t.near_first)
-        silhouette_fast_kernel<false><<<grid_for(n, 128), 128, 0, st>>>(t, pts, flip, n, dist, edge, nullptr);
+        silhouette_fast_kernel<true><<<grid_for(n, 128), 128, 0, st>>>(t, pts, flip, n, dist, edge, stats, seed);
+    else if (t.near_first || seed.radius)
+        silhouette_fast_kernel<false><<<grid_for(n, 128), 128, 0, st>>>(t, pts, flip, n, dist, edge, nullptr, seed);
     else
         silhouette_kernel<<<grid_for(n, 128), 128, 0, st>>>(t, pts, flip, n, dist, edge);
     note_launch();

@@ -40,13 +40,23 @@ def close(a, b, rtol=RTOL, atol=ATOL):
 def compare_all(snch, ref, s, q):
     import torch
     R = ref.RefQueries(s)
-    d = {k: torch.from_numpy(np.ascontiguousarray(v)).cuda() for k, v in q.items()}
+    d = {k: torch.from_numpy(np.ascontiguousarray(v)).cuda() for k, v in q.items() if not k.startswith("_")}
     ri, rd = R.nearest(d["near_pts"])
     mi, md = s.query_nearest(d["near_pts"])
     rd, md = rd.cpu().numpy(), md.cpu().numpy()
     assert close(rd, md).all()
-    same = ri.cpu().numpy() == mi.cpu().numpy()
-    assert same.mean() > 0.999, same.mean()
+    # indices: equal, or an exact tie that the two builds' rounding breaks differently
+    ri, mi = ri.cpu().numpy().view(np.uint32), mi.cpu().numpy().view(np.uint32)
+    diff = np.nonzero(ri != mi)[0]
+    assert len(diff) <= 0.02 * len(ri), len(diff)
+    if len(diff):
+        from oracle import oracle
+        v, f = q["_verts"], q["_tris"]
+        pts = q["near_pts"][diff]
+        for k in range(min(len(diff), 512)):
+            _, da = oracle.brute_nearest_f64(v, f[ri[diff[k]]][None], pts[k][None])
+            _, db = oracle.brute_nearest_f64(v, f[mi[diff[k]]][None], pts[k][None])
+            assert abs(da[0] - db[0]) <= max(RTOL * db[0], ATOL), (da[0], db[0])
     rs = R.silhouette(d["sil_pts"], d["sil_flip"]).cpu().numpy()
     ms = s.query_silhouette(d["sil_pts"], d["sil_flip"])[0].cpu().numpy()
     assert close(rs, ms).mean() > 0.999
@@ -69,7 +79,7 @@ def test_reference_cuda_runs_on_our_tree_golden(ref, name):
     s = built_scene(snch, g["verts"], g["tris"])
     q = {"near_pts": g["near_pts"], "sil_pts": g["sil_pts"], "sil_flip": g["sil_flip"], "ray_o": g["ray_o"],
          "ray_d": g["ray_d"], "ray_tmax": g["ray_tmax"], "smp_c": g["smp_c"], "smp_r": g["smp_r"],
-         "smp_u": g["smp_u"]}
+         "smp_u": g["smp_u"], "_verts": g["verts"], "_tris": g["tris"]}
     compare_all(snch, ref, s, q)
     # and the reference's GPU answers match its CPU answers (same algorithm, FMA aside)
     import torch
@@ -86,4 +96,5 @@ def test_reference_cuda_runs_on_our_tree_config1(ref):
     for k in ("near_pts", "sil_pts", "ray_o", "smp_c"):
         q[k] = (q[k] * 2.4 - 1.2).astype(np.float32)
     s = built_scene(snch, v, f)
+    q["_verts"], q["_tris"] = v, f
     compare_all(snch, ref, s, q)
