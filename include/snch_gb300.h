@@ -190,6 +190,36 @@ int snch_query_silhouette_seeded(snch_scene_t scene, const float *points_xyz, co
                                  const float *radius, int64_t n, float *out_distance, int32_t *out_edge,
                                  uint32_t *num_fallback, snch_stream_t stream);
 
+/* ------------------------------------------------------------------ learned search radius
+ * A small MLP (32-frequency Fourier features of the point -> 4 x 64 ReLU ->
+ * 2 outputs) predicts log(nearest distance) and log(silhouette distance);
+ * its layers run on the 5th-generation tensor cores (tcgen05, BF16 x BF16 ->
+ * FP32 in tensor memory). radius = exp(prediction) * margin + floor feeds
+ * snch_query_*_seeded, whose fallback keeps results exact whatever the
+ * prediction. No reference counterpart. */
+typedef struct snch_mlp_s *snch_mlp_t;
+int64_t snch_mlp_num_params(void);
+/* points are normalised by the box [lo, hi]; seed fixes the initial weights */
+int snch_mlp_create(const float *box_lo, const float *box_hi, uint64_t seed, snch_mlp_t *out);
+int snch_mlp_destroy(snch_mlp_t mlp);
+/* fp32 parameter block (W1 64x192, b1, W2, b2, W3, b3, W4, b4, W5 2x64, b5) to / from HOST memory */
+int snch_mlp_get_params(snch_mlp_t mlp, float *host_params, int64_t count);
+int snch_mlp_set_params(snch_mlp_t mlp, const float *host_params, int64_t count);
+/* pinball-loss gradient (quantile tau) of n samples without an update: DEVICE points (n x 3),
+ * DEVICE targets (n x 2 log distances, NaN = no target); HOST gradient and loss (synchronous) */
+int snch_mlp_gradient(snch_mlp_t mlp, const float *points, const float *targets, int64_t n, float tau,
+                      float *host_grad, float *host_loss, snch_stream_t stream);
+/* Adam over `epochs` passes of n samples in batches; *host_loss = mean loss of the last epoch (synchronous) */
+int snch_mlp_train(snch_mlp_t mlp, const float *points, const float *targets, int64_t n, int epochs, int64_t batch,
+                   float lr, float tau, float *host_loss, snch_stream_t stream);
+/* fused tensor-core inference: DEVICE radius_near / radius_sil (either may be NULL) */
+int snch_mlp_predict_radius(snch_mlp_t mlp, const float *points, int64_t n, float margin, float floor,
+                            float *radius_near, float *radius_sil, snch_stream_t stream);
+/* building block: C[M x N] (+)= A[M x K] * B[N x K]^T, bf16 row-major A and B, fp32 C, on
+ * tcgen05; M % 128 == 0, K % 64 == 0, N in {64, 128, 192, 256}; all DEVICE buffers */
+int snch_gemm_bf16(const void *A, const void *B, float *C, int64_t M, int64_t N, int64_t K, int accumulate,
+                   uint32_t *device_status, snch_stream_t stream);
+
 /* Host-buffer forms of the four queries: copy in, run, copy out in pipelined
  * chunks on the scene's own streams; return when results are in host memory.
  * This is the call shape of the reference's benchmark loop (benchmark.cu:395-409). */

@@ -37,7 +37,7 @@ def _header_signatures():
     text = open(os.path.join(_build.INCLUDE, "snch_gb300.h")).read()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
     sigs = {}
-    for m in re.finditer(r"\b(int|size_t|uint64_t|const char \*)\s*(snch_\w+)\s*\(([^)]*)\)\s*;", text):
+    for m in re.finditer(r"\b(int|size_t|uint64_t|int64_t|const char \*)\s*(snch_\w+)\s*\(([^)]*)\)\s*;", text):
         ret, name, args = m.group(1), m.group(2), m.group(3)
         sigs[name] = (ret, [a.strip() for a in args.split(",") if a.strip() and a.strip() != "void"])
     return sigs
@@ -49,7 +49,7 @@ def _ctype(arg: str):
         return P
     t = a.split()[0]
     return {"int64_t": I64, "int": I, "size_t": C.c_size_t, "snch_scene_t": P, "snch_stream_t": P,
-            "uint32_t": C.c_uint32}[t]
+            "uint32_t": C.c_uint32, "uint64_t": C.c_uint64, "float": C.c_float, "snch_mlp_t": P}[t]
 
 
 _lib = None
@@ -69,7 +69,8 @@ def lib():
         L = C.CDLL(path)
         for name, (ret, args) in _header_signatures().items():
             f = getattr(L, name)  # AttributeError = header declares a symbol the library lacks
-            f.restype = {"int": I, "size_t": C.c_size_t, "uint64_t": C.c_uint64, "const char *": C.c_char_p}[ret]
+            f.restype = {"int": I, "size_t": C.c_size_t, "uint64_t": C.c_uint64, "int64_t": I64,
+                         "const char *": C.c_char_p}[ret]
             f.argtypes = [_ctype(a) for a in args]
         _lib = L
     return _lib

@@ -30,8 +30,9 @@ UNITS = [
     ("queries.cu", ["-fmad=false"]),
     ("abi.cu", []),
     ("noalloc_sort.cu", []),
+    ("mlp.cu", []),
 ]
-HEADERS = ["common.cuh", "internal.h"]
+HEADERS = ["common.cuh", "internal.h", "tcgen05.cuh"]
 
 
 def nvcc() -> str:

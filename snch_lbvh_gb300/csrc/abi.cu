@@ -4,6 +4,8 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <vector>
+#include <cmath>
 
 #include <atomic>
 
@@ -333,6 +335,75 @@ int run_seeded(snch_scene_s *s, const float *pts, const float *radius, int64_t n
     cudaFreeAsync(scratch, st);
     SNCH_CUDA(e);
     return SNCH_OK;
+}
+
+// ---- learned search radius
+struct MlpState
+{
+    float *params = nullptr, *grad = nullptr, *m = nullptr, *v = nullptr, *loss = nullptr;
+    uint32_t *status = nullptr;
+    float center[3], inv_half[3];
+    int step = 0;
+};
+
+uint64_t splitmix64(uint64_t &x)
+{
+    uint64_t z = (x += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+// He-uniform weights for the ReLU layers, a small head, zero biases, head bias log(0.05)
+std::vector<float> mlp_init_params(uint64_t seed)
+{
+    const int in[5] = {192, 64, 64, 64, 64}, out[5] = {64, 64, 64, 64, 2};
+    std::vector<float> p;
+    uint64_t st = seed;
+    for (int l = 0; l < 5; ++l)
+    {
+        const float bound = l < 4 ? std::sqrt(6.0f / in[l]) : 0.1f * std::sqrt(3.0f / in[l]);
+        for (int i = 0; i < in[l] * out[l]; ++i)
+        {
+            const double u = (double)(splitmix64(st) >> 11) * (1.0 / 9007199254740992.0);
+            p.push_back((float)((2.0 * u - 1.0) * bound));
+        }
+        for (int i = 0; i < out[l]; ++i)
+            p.push_back(l < 4 ? 0.0f : std::log(0.05f));
+    }
+    return p;
+}
+
+size_t mlp_workspace_bytes(int64_t rows)
+{
+    const size_t r = (size_t)rows;
+    return r * 192 * 2 + 8 * r * 64 * 2 + 256 * r * 2 + 64 * r * 2 + 64 * 64 * 2 + (64 * 192 + 3 * 4096) * 2 +
+           2 * r * 64 * 4 + 64 * 256 * 64 * 4 + 16 * 256;
+}
+
+MlpWorkspace mlp_workspace(char *base, int64_t rows)
+{
+    MlpWorkspace w;
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        char *p = base + off;
+        off += (bytes + 255) & ~size_t(255);
+        return p;
+    };
+    const size_t r = (size_t)rows;
+    w.X = take(r * 192 * 2);
+    for (int l = 0; l < 4; ++l)
+        w.H[l] = take(r * 64 * 2);
+    for (int l = 0; l < 4; ++l)
+        w.dZ[l] = take(r * 64 * 2);
+    w.T = take(256 * r * 2);
+    w.T2 = take(64 * r * 2);
+    w.Wt = take(64 * 64 * 2);
+    w.Wb = take((64 * 192 + 3 * 4096) * 2);
+    w.Z = reinterpret_cast<float *>(take(r * 64 * 4));
+    w.dH = reinterpret_cast<float *>(take(r * 64 * 4));
+    w.C = reinterpret_cast<float *>(take(64 * 256 * 64 * 4));  // up to 64 split-K slices
+    return w;
 }
 
 // ---- host-form pipeline: chunk i runs on pipe[i % 2]: H2D inputs, kernel, D2H outputs
@@ -864,6 +935,176 @@ int snch_sort_pairs(uint32_t *keys, uint32_t *vals, uint32_t *keys_tmp, uint32_t
         return fail(SNCH_ERR_INVALID_ARGUMENT, "NULL buffer");
     SNCH_CUDA(radix_sort_pairs(keys, vals, keys_tmp, vals_tmp, (uint32_t)n, key_bits, nullptr, scratch, device_status,
                                S(stream)));
+    return SNCH_OK;
+}
+
+// ------------------------------------------------------------------ learned search radius
+struct snch_mlp_s
+{
+    MlpState st;
+};
+
+int64_t snch_mlp_num_params(void) { return (int64_t)mlp_num_params(); }
+
+int snch_mlp_create(const float *lo, const float *hi, uint64_t seed, snch_mlp_t *out)
+{
+    if (!lo || !hi || !out)
+        return fail(SNCH_ERR_INVALID_ARGUMENT, "NULL argument");
+    *out = nullptr;
+    float scales[32];
+    for (int k = 0; k < 32; ++k)
+        scales[k] = (float)std::exp2(0.25 * k);
+    SNCH_CUDA(set_mlp_scales(scales));
+    auto *m = new snch_mlp_s();
+    for (int c = 0; c < 3; ++c)
+    {
+        if (!(hi[c] > lo[c]))
+        {
+            delete m;
+            return fail(SNCH_ERR_INVALID_ARGUMENT, "empty box");
+        }
+        m->st.center[c] = 0.5f * (lo[c] + hi[c]);
+        m->st.inv_half[c] = 2.0f / (hi[c] - lo[c]);
+    }
+    const size_t np = mlp_num_params();
+    const std::vector<float> p = mlp_init_params(seed);
+    cudaError_t e = cudaMalloc(&m->st.params, 4 * np);
+    if (e == cudaSuccess)
+        e = cudaMalloc(&m->st.grad, 4 * np);
+    if (e == cudaSuccess)
+        e = cudaMalloc(&m->st.m, 4 * np);
+    if (e == cudaSuccess)
+        e = cudaMalloc(&m->st.v, 4 * np);
+    if (e == cudaSuccess)
+        e = cudaMalloc(&m->st.loss, 256);
+    if (e == cudaSuccess)
+        e = cudaMalloc(&m->st.status, 256);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(m->st.params, p.data(), 4 * np, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = cudaMemset(m->st.m, 0, 4 * np);
+    if (e == cudaSuccess)
+        e = cudaMemset(m->st.v, 0, 4 * np);
+    if (e == cudaSuccess)
+        e = cudaMemset(m->st.status, 0, 4);
+    if (e != cudaSuccess)
+    {
+        snch_mlp_destroy(m);
+        return fail(SNCH_ERR_CUDA, std::string("snch_mlp_create: ") + cudaGetErrorString(e));
+    }
+    *out = m;
+    return SNCH_OK;
+}
+
+int snch_mlp_destroy(snch_mlp_t m)
+{
+    if (!m)
+        return fail(SNCH_ERR_INVALID_ARGUMENT, "mlp is NULL");
+    for (void *p : {(void *)m->st.params, (void *)m->st.grad, (void *)m->st.m, (void *)m->st.v, (void *)m->st.loss,
+                    (void *)m->st.status})
+        if (p)
+            cudaFree(p);
+    delete m;
+    return SNCH_OK;
+}
+
+int snch_mlp_get_params(snch_mlp_t m, float *host, int64_t count)
+{
+    if (!m || !host || count != (int64_t)mlp_num_params())
+        return fail(SNCH_ERR_INVALID_ARGUMENT, "need snch_mlp_num_params() floats");
+    SNCH_CUDA(cudaMemcpy(host, m->st.params, 4 * (size_t)count, cudaMemcpyDeviceToHost));
+    return SNCH_OK;
+}
+
+int snch_mlp_set_params(snch_mlp_t m, const float *host, int64_t count)
+{
+    if (!m || !host || count != (int64_t)mlp_num_params())
+        return fail(SNCH_ERR_INVALID_ARGUMENT, "need snch_mlp_num_params() floats");
+    SNCH_CUDA(cudaMemcpy(m->st.params, host, 4 * (size_t)count, cudaMemcpyHostToDevice));
+    return SNCH_OK;
+}
+
+int snch_mlp_gradient(snch_mlp_t m, const float *pts, const float *targets, int64_t n, float tau, float *host_grad,
+                      float *host_loss, snch_stream_t stream)
+{
+    if (!m || !pts || !targets || n <= 0 || n > (int64_t(1) << 24))
+        return fail(SNCH_ERR_INVALID_ARGUMENT, "bad arguments");
+    cudaStream_t st = S(stream);
+    const int64_t rows = (n + 127) / 128 * 128;
+    char *ws = nullptr;
+    SNCH_CUDA(cudaMallocAsync(reinterpret_cast<void **>(&ws), mlp_workspace_bytes(rows), st));
+    cudaError_t e = mlp_forward_backward(m->st.params, m->st.grad, pts, targets, n, rows, m->st.center,
+                                         m->st.inv_half, tau, mlp_workspace(ws, rows), m->st.loss, m->st.status, st);
+    if (e == cudaSuccess && host_grad)
+        e = cudaMemcpyAsync(host_grad, m->st.grad, 4 * mlp_num_params(), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess && host_loss)
+        e = cudaMemcpyAsync(host_loss, m->st.loss, 4, cudaMemcpyDeviceToHost, st);
+    cudaFreeAsync(ws, st);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(st);
+    SNCH_CUDA(e);
+    return SNCH_OK;
+}
+
+int snch_mlp_train(snch_mlp_t m, const float *pts, const float *targets, int64_t n, int epochs, int64_t batch,
+                   float lr, float tau, float *host_loss, snch_stream_t stream)
+{
+    if (!m || !pts || !targets || n <= 0 || epochs < 0 || batch < 128 || batch > (int64_t(1) << 20))
+        return fail(SNCH_ERR_INVALID_ARGUMENT, "bad arguments");
+    cudaStream_t st = S(stream);
+    const int64_t rows_max = (batch + 127) / 128 * 128;
+    char *ws = nullptr;
+    const int64_t steps = (n + batch - 1) / batch;
+    float *losses = nullptr;
+    SNCH_CUDA(cudaMallocAsync(reinterpret_cast<void **>(&ws), mlp_workspace_bytes(rows_max), st));
+    cudaError_t e = cudaMallocAsync(reinterpret_cast<void **>(&losses), 4 * (size_t)steps, st);
+    const MlpWorkspace w = mlp_workspace(ws, rows_max);
+    for (int ep = 0; ep < epochs && e == cudaSuccess; ++ep)
+        for (int64_t s = 0; s < steps && e == cudaSuccess; ++s)
+        {
+            const int64_t b0 = s * batch, cnt = std::min<int64_t>(batch, n - b0), rows = (cnt + 127) / 128 * 128;
+            e = mlp_forward_backward(m->st.params, m->st.grad, pts + 3 * b0, targets + 2 * b0, cnt, rows,
+                                     m->st.center, m->st.inv_half, tau, w, m->st.loss, m->st.status, st);
+            if (e == cudaSuccess)
+                e = mlp_adam(m->st.params, m->st.grad, m->st.m, m->st.v, lr, ++m->st.step, st);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(losses + s, m->st.loss, 4, cudaMemcpyDeviceToDevice, st);
+        }
+    std::vector<float> h((size_t)steps, 0.0f);
+    if (e == cudaSuccess && host_loss && epochs > 0)
+        e = cudaMemcpyAsync(h.data(), losses, 4 * (size_t)steps, cudaMemcpyDeviceToHost, st);
+    cudaFreeAsync(losses, st);
+    cudaFreeAsync(ws, st);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(st);
+    SNCH_CUDA(e);
+    if (host_loss)
+    {
+        double acc = 0;
+        for (float x : h)
+            acc += x;
+        *host_loss = steps ? (float)(acc / steps) : 0.0f;
+    }
+    return SNCH_OK;
+}
+
+int snch_mlp_predict_radius(snch_mlp_t m, const float *pts, int64_t n, float margin, float floor_, float *r_near,
+                            float *r_sil, snch_stream_t stream)
+{
+    if (!m || n < 0 || (n > 0 && (!pts || (!r_near && !r_sil))))
+        return fail(SNCH_ERR_INVALID_ARGUMENT, "bad arguments");
+    SNCH_CUDA(launch_mlp_radius(m->st.params, pts, n, m->st.center, m->st.inv_half, margin, floor_, r_near, r_sil,
+                                m->st.status, S(stream)));
+    return SNCH_OK;
+}
+
+int snch_gemm_bf16(const void *A, const void *B, float *C, int64_t M, int64_t N, int64_t K, int accumulate,
+                   uint32_t *device_status, snch_stream_t stream)
+{
+    if (!A || !B || !C || !device_status || M <= 0 || M % 128 || K <= 0 || K % 64 ||
+        (N != 64 && N != 128 && N != 192 && N != 256) || M > (int64_t(1) << 31) || K > (int64_t(1) << 30))
+        return fail(SNCH_ERR_INVALID_ARGUMENT, "need M % 128 == 0, K % 64 == 0, N in {64, 128, 192, 256}");
+    SNCH_CUDA(launch_gemm_bf16(A, B, C, M, N, K, accumulate, device_status, S(stream)));
     return SNCH_OK;
 }
 

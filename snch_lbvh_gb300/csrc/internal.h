@@ -68,6 +68,32 @@ cudaError_t launch_query_order(const TreeView &t, const float *pts, int64_t n, v
 cudaError_t launch_sample_point(const float *verts, const int32_t *tris, const int32_t *idx, const float *u,
                                 const float *v, int64_t n, float *out, cudaStream_t st);
 
+// ---- mlp.cu (learned search radius)
+struct MlpWorkspace
+{
+    void *X;      // rows x 192 bf16 features
+    void *H[4];   // rows x 64 bf16 activations
+    void *dZ[4];  // rows x 64 bf16 pre-activation gradients
+    void *T;      // 256 x rows bf16 (transposed activations, zero padded)
+    void *T2;     // 64 x rows bf16 (transposed gradients)
+    void *Wt;     // 64 x 64 bf16 (transposed weight)
+    void *Wb;     // bf16 copies of W1..W4
+    float *Z, *dH;  // rows x 64 fp32
+    float *C;       // 256 x 64 fp32 (weight-gradient GEMM result)
+};
+size_t mlp_num_params();
+cudaError_t set_mlp_scales(const float *scales);
+// splits > 1: split K, C holds one M x N slice per split (the caller reduces them)
+cudaError_t launch_gemm_bf16(const void *A, const void *B, float *C, int64_t M, int64_t N, int64_t K, int accumulate,
+                             uint32_t *status, cudaStream_t st, int splits = 1);
+cudaError_t launch_mlp_radius(const float *params, const float *pts, int64_t n, const float center[3],
+                              const float inv_half[3], float margin, float floor_, float *r_near, float *r_sil,
+                              uint32_t *status, cudaStream_t st);
+cudaError_t mlp_forward_backward(float *params, float *grad, const float *pts, const float *target, int64_t n,
+                                 int64_t rows, const float center[3], const float inv_half[3], float tau,
+                                 const MlpWorkspace &ws, float *loss, uint32_t *status, cudaStream_t st);
+cudaError_t mlp_adam(float *params, const float *grad, float *m, float *v, float lr, int step, cudaStream_t st);
+
 // ---- scan_sort.cu
 // Exclusive scan of 0/1 flags (totals below 2^30), one pass, decoupled look-back.
 size_t scan_flags_scratch_bytes(uint64_t n);

@@ -1,0 +1,165 @@
+"""Learned search radius on the tcgen05 tensor cores.
+
+1. The BF16 GEMM building block equals a float64 product of the same BF16
+   operands (fp32 accumulation only reorders sums).
+2. The training gradient equals the FP64 restatement (oracle/mlp_oracle.py)
+   with the same BF16 roundings: cosine >= 0.9999, relative L2 error <= 1e-2.
+3. The fused inference kernel's radius equals the restatement's to 2e-2
+   relative (BF16 activations that round the other way, __expf).
+4. Training lowers the pinball loss on exact distances of a mesh.
+5. Seeded queries with the learned radius return exactly the plain results.
+"""
+import numpy as np
+import pytest
+
+from oracle import mlp_oracle as mo
+from test_gpu_parity import bits, built_scene
+
+pytestmark = pytest.mark.gpu
+
+
+def bf16_tensor(rng, shape, scale=1.0):
+    import torch
+    return torch.from_numpy((rng.standard_normal(shape) * scale).astype(np.float32)).to(torch.bfloat16).cuda()
+
+
+@pytest.mark.parametrize("N", [64, 128, 192, 256])
+@pytest.mark.parametrize("M,K", [(128, 64), (384, 192), (256, 1024)])
+def test_gemm_bf16_matches_fp64(M, N, K):
+    import torch
+    from snch_lbvh_gb300.learned import gemm_bf16
+    rng = np.random.default_rng(M * 7 + N + K)
+    A, B = bf16_tensor(rng, (M, K)), bf16_tensor(rng, (N, K))
+    Ad, Bd = A.double().cpu().numpy(), B.double().cpu().numpy()
+    C, st = gemm_bf16(A, B)
+    ref = Ad @ Bd.T
+    bound = np.abs(Ad) @ np.abs(Bd).T * 1e-5 + 1e-6
+    got = C.cpu().numpy()
+    assert int(st.item()) == 0
+    assert np.all(np.abs(got - ref) <= bound), np.abs(got - ref).max()
+    C2, st = gemm_bf16(A, B, C_out=C.clone(), accumulate=True)  # C + A B^T
+    assert np.all(np.abs(C2.cpu().numpy() - 2 * ref) <= 2 * bound)
+    torch.cuda.synchronize()
+
+
+def test_gemm_bf16_rejects_bad_shapes():
+    import torch
+    import snch_lbvh_gb300 as snch
+    from snch_lbvh_gb300.learned import gemm_bf16
+    A = torch.zeros(100, 64, dtype=torch.bfloat16, device="cuda")
+    B = torch.zeros(64, 64, dtype=torch.bfloat16, device="cuda")
+    with pytest.raises(snch.SnchError):
+        gemm_bf16(A, B)
+    with pytest.raises(snch.SnchError):
+        gemm_bf16(torch.zeros(128, 64, dtype=torch.bfloat16, device="cuda"),
+                  torch.zeros(96, 64, dtype=torch.bfloat16, device="cuda"))
+
+
+def model_and_data(n=3000, seed=5):
+    from snch_lbvh_gb300.learned import LearnedRadius
+    rng = np.random.default_rng(seed)
+    lo, hi = np.array([-1.0, -0.5, 0.0], np.float32), np.array([1.0, 1.5, 0.5], np.float32)
+    m = LearnedRadius(lo, hi, seed=seed)
+    pts = (lo + (hi - lo) * rng.random((n, 3))).astype(np.float32)
+    return m, lo, hi, pts, rng
+
+
+def test_initial_params_deterministic():
+    from snch_lbvh_gb300.learned import LearnedRadius
+    a = LearnedRadius(np.zeros(3), np.ones(3), seed=11).params
+    b = LearnedRadius(np.zeros(3), np.ones(3), seed=11).params
+    c = LearnedRadius(np.zeros(3), np.ones(3), seed=12).params
+    np.testing.assert_array_equal(a, b)
+    assert not np.array_equal(a, c)
+    assert a.shape == (24962,) and np.all(np.isfinite(a))
+    assert np.allclose(a[-2:], np.log(np.float32(0.05)))
+
+
+@pytest.mark.parametrize("n", [3000, 20000])  # 20000: split-K weight gradients (9 slices)
+def test_gradient_matches_fp64_restatement(n):
+    m, lo, hi, pts, rng = model_and_data(n=n)
+    p = m.params
+    o, _ = mo.forward(p, pts, lo, hi)
+    targets = (o + rng.normal(0, 1.0, o.shape)).astype(np.float32)
+    targets[::5, 1] = np.nan
+    tau = 0.15
+    g_gpu, loss_gpu = m.gradient(pts, targets, tau)
+    loss_ref, g_ref = mo.loss_and_grad(p, pts, targets, lo, hi, tau)
+    assert abs(loss_gpu - loss_ref) <= 1e-3 * abs(loss_ref)
+    cos = g_gpu @ g_ref / (np.linalg.norm(g_gpu) * np.linalg.norm(g_ref))
+    rel = np.linalg.norm(g_gpu - g_ref) / np.linalg.norm(g_ref)
+    assert cos >= 0.9999 and rel <= 1e-2, (cos, rel)
+    # per layer, so that a wrong block (e.g. a transposed weight gradient) cannot hide
+    off = 0
+    for s in mo.SIZES:
+        k = int(np.prod(s))
+        gg, gr = g_gpu[off:off + k], g_ref[off:off + k]
+        if np.linalg.norm(gr) > 0:
+            assert np.linalg.norm(gg - gr) <= 2e-2 * np.linalg.norm(gr), (s, off)
+        off += k
+    assert m.params.tobytes() == p.tobytes()  # gradient() does not update
+
+
+@pytest.mark.parametrize("n", [0, 1, 1000, 128 * 700 + 3])
+def test_fused_inference_matches_fp64_restatement(n):
+    import torch
+    m, lo, hi, pts, rng = model_and_data(n=max(n, 1), seed=9)
+    pts = pts[:n]
+    # non-trivial weights: a few Adam steps on random targets
+    if n:
+        m.train(pts, (rng.normal(-3, 1, (n, 2))).astype(np.float32), epochs=2, batch=4096, lr=1e-2)
+    rn, rs = m.predict(pts, margin=1.5, floor=1e-4)
+    torch.cuda.synchronize()
+    if n == 0:
+        assert rn.numel() == 0
+        return
+    ref = mo.radius(m.params, pts, lo, hi, 1.5, 1e-4)
+    got = np.stack([rn.cpu().numpy(), rs.cpu().numpy()], 1)
+    rel = np.abs(got - ref) / ref
+    assert np.mean(rel <= 2e-2) >= 0.999 and rel.max() <= 0.1, rel.max()
+    rn2, _ = m.predict(pts, margin=1.5, floor=1e-4, which="near")
+    np.testing.assert_array_equal(rn2.cpu().numpy(), rn.cpu().numpy())
+
+
+@pytest.fixture(scope="module")
+def trained():
+    import torch
+    import snch_lbvh_gb300 as snch
+    from snch_lbvh_gb300 import meshes
+    from snch_lbvh_gb300.learned import LearnedRadius, targets_from_scene
+    sc = meshes.wost_scene(seed=2, n_meshes=8, torus_nu=60, torus_nv=30, ico_level=4)
+    s = built_scene(snch, sc.verts, sc.faces)
+    rng = np.random.default_rng(21)
+    train_pts = torch.from_numpy(rng.random((400_000, 3), dtype=np.float32)).cuda()
+    tgt = targets_from_scene(s, train_pts)
+    m = LearnedRadius(np.zeros(3), np.ones(3), seed=1)
+    _, loss0 = m.gradient(train_pts, tgt, tau=0.1)
+    loss = m.train(train_pts, tgt, epochs=12, batch=16384, lr=2e-3, tau=0.1)
+    return s, m, loss0, loss
+
+
+def test_training_lowers_loss(trained):
+    s, m, loss0, loss = trained
+    assert np.isfinite(loss) and loss < 0.5 * loss0, (loss0, loss)
+
+
+def test_learned_radius_queries_identical(trained):
+    import torch
+    s, m, _, _ = trained
+    rng = np.random.default_rng(77)
+    pts = torch.from_numpy(rng.random((300_000, 3), dtype=np.float32)).cuda()
+    flip = torch.from_numpy((rng.random(300_000) < 0.5).astype(np.uint8)).cuda()
+    rn, rs = m.predict(pts, margin=1.25)
+    i0, d0 = s.query_nearest(pts)
+    nf = torch.zeros(1, dtype=torch.int32, device="cuda")
+    i1, d1 = s.query_nearest_seeded(pts, rn, num_fallback=nf)
+    np.testing.assert_array_equal(i1.cpu().numpy(), i0.cpu().numpy())
+    np.testing.assert_array_equal(bits(d1.cpu().numpy()), bits(d0.cpu().numpy()))
+    frac_near = int(nf.item()) / len(pts)
+    sd0, se0 = s.query_silhouette(pts, flip)
+    sd1, se1 = s.query_silhouette_seeded(pts, rs, flip, num_fallback=nf)
+    np.testing.assert_array_equal(bits(sd1.cpu().numpy()), bits(sd0.cpu().numpy()))
+    np.testing.assert_array_equal(se1.cpu().numpy(), se0.cpu().numpy())
+    frac_sil = int(nf.item()) / len(pts)
+    assert frac_near < 0.5 and frac_sil < 0.5, (frac_near, frac_sil)
+    assert s.device_status() == 0
