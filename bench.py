@@ -55,6 +55,7 @@ def parse():
     ap.add_argument("--scale", type=float, default=1.0, help="fraction of the query batches (1.0 = full workload)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned-radius leg")
     return ap.parse_args()
 
 
@@ -191,6 +192,121 @@ def cpu_threads():
         return len(os.sched_getaffinity(0))
     except AttributeError:
         return os.cpu_count() or 1
+
+
+# --------------------------------------------------------------------- learned radius
+LEARNED_TRAIN = {"uniform": 4_000_000, "surface": 4_000_000, "band": 0.05, "epochs": 6, "batch": 65536,
+                 "lr": 2e-3, "tau": 0.9}
+MLP_FLOP_PER_QUERY = 2 * (192 * 64 + 3 * 64 * 64) + 2 * 2 * 64  # tensor-core layers + head
+
+
+def learned_leg(scene, sc, dev, counts, out, steps, scale):
+    """Nearest and silhouette queries seeded by the learned radius vs plain, on the
+    same batches: per-type q/s including the MLP inference, fallback fractions,
+    and a bit-for-bit comparison with the plain results. Training runs first and
+    is reported separately (a model is trained once per scene)."""
+    import torch
+    from snch_lbvh_gb300.learned import LearnedRadius, targets_from_scene, training_points
+    cfg = dict(LEARNED_TRAIN)
+    nu, ns = max(4096, int(cfg["uniform"] * scale)), max(4096, int(cfg["surface"] * scale))
+    pts = torch.from_numpy(training_points(sc.verts, sc.faces, nu, ns, cfg["band"], seed=77)).cuda()
+    tgt = targets_from_scene(scene, pts)
+    model = LearnedRadius(np.zeros(3), np.ones(3), seed=3)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    loss = model.train(pts, tgt, epochs=cfg["epochs"], batch=cfg["batch"], lr=cfg["lr"], tau=cfg["tau"])
+    torch.cuda.synchronize()
+    train_s = time.perf_counter() - t0
+    stream = torch.cuda.current_stream()
+    nn, ns_ = counts["near"], counts["sil"]
+    rn = torch.empty(nn, device="cuda")
+    rs = torch.empty(ns_, device="cuda")
+    o_near = (torch.empty(nn, dtype=torch.int32, device="cuda"), torch.empty(nn, device="cuda"))
+    o_sil = (torch.empty(ns_, device="cuda"), torch.empty(ns_, dtype=torch.int32, device="cuda"))
+    nf = torch.zeros(2, dtype=torch.int32, device="cuda")
+    res = {"training": {**cfg, "uniform": nu, "surface": ns, "final_loss": loss, "train_s": train_s},
+           "margins": {}}
+    best = None
+    for margin in (1.1, 1.25, 1.5):
+        ev = [[torch.cuda.Event(enable_timing=True) for _ in range(5)] for _ in range(steps + 1)]
+        for k in range(steps + 1):  # the first round is a warm-up
+            e = ev[k]
+            e[0].record(stream)
+            model.predict(dev["near_pts"], margin=margin, floor=1e-4, out=(rn, None), which="near")
+            e[1].record(stream)
+            scene.query_nearest_seeded(dev["near_pts"], rn, out=o_near, num_fallback=nf[0:1])
+            e[2].record(stream)
+            model.predict(dev["sil_pts"], margin=margin, floor=1e-4, out=(None, rs), which="sil")
+            e[3].record(stream)
+            scene.query_silhouette_seeded(dev["sil_pts"], rs, dev["sil_flip"], out=o_sil, num_fallback=nf[1:2])
+            e[4].record(stream)
+        torch.cuda.synchronize()
+        ms = np.array([[e[i].elapsed_time(e[i + 1]) for i in range(4)] for e in ev[1:]]).mean(0)
+        same = (torch.equal(o_near[0], out["near"][0]) and torch.equal(o_near[1].view(torch.int32),
+                                                                          out["near"][1].view(torch.int32))
+                and torch.equal(o_sil[0].view(torch.int32), out["sil"][0].view(torch.int32))
+                and torch.equal(o_sil[1], out["sil"][1]))
+        fb = nf.cpu().numpy()
+        r = {"near_qps": nn / ((ms[0] + ms[1]) / 1e3), "sil_qps": ns_ / ((ms[2] + ms[3]) / 1e3),
+             "mlp_ms": {"near": float(ms[0]), "sil": float(ms[2])},
+             "seeded_ms": {"near": float(ms[1]), "sil": float(ms[3])},
+             "fallback_frac": {"near": float(fb[0]) / nn, "sil": float(fb[1]) / ns_},
+             "identical_to_plain": bool(same),
+             "mlp_tflops": MLP_FLOP_PER_QUERY * nn / (ms[0] / 1e3) / 1e12}
+        res["margins"][str(margin)] = r
+        if best is None or r["near_qps"] + r["sil_qps"] > best[1]["near_qps"] + best[1]["sil_qps"]:
+            best = (margin, r)
+    res["best_margin"] = best[0]
+    res["near_qps"], res["sil_qps"] = best[1]["near_qps"], best[1]["sil_qps"]
+    res["identical_to_plain"] = all(r["identical_to_plain"] for r in res["margins"].values())
+    res["reference_order"] = learned_on_reference_order(scene, model, dev, best[0], best[1]["mlp_ms"], counts)
+    model.close()
+    return res
+
+
+def learned_on_reference_order(scene, model, dev, margin, mlp_ms, counts, sub=2_000_000):
+    """The same learned radius applied to the reference's own traversal order
+    (TRAVERSAL_REFERENCE_ORDER): plain vs seeded on the first `sub` queries of
+    each batch, one timed run each; the MLP time is the full batch's, scaled."""
+    import torch
+    import snch_lbvh_gb300 as snch
+    stream = torch.cuda.current_stream()
+    out = {"queries": {}}
+    scene.set_traversal(snch.TRAVERSAL_REFERENCE_ORDER)
+    try:
+        for kind, key in (("near", "near_pts"), ("sil", "sil_pts")):
+            m = min(counts[kind], sub)
+            pts = dev[key][:m]
+            rn, rs = model.predict(pts, margin=margin, floor=1e-4, which=kind)
+            r = rn if kind == "near" else rs
+            nf = torch.zeros(1, dtype=torch.int32, device="cuda")
+            e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+            if kind == "near":
+                e[0].record(stream)
+                a = scene.query_nearest(pts)
+                e[1].record(stream)
+                b = scene.query_nearest_seeded(pts, r, num_fallback=nf)
+                e[2].record(stream)
+            else:
+                flip = dev["sil_flip"][:m]
+                e[0].record(stream)
+                a = scene.query_silhouette(pts, flip)
+                e[1].record(stream)
+                b = scene.query_silhouette_seeded(pts, r, flip, num_fallback=nf)
+                e[2].record(stream)
+            torch.cuda.synchronize()
+            same = all(torch.equal(x.view(torch.int32), y.view(torch.int32)) for x, y in zip(a, b))
+            plain_ms, seeded_ms = e[0].elapsed_time(e[1]), e[1].elapsed_time(e[2])
+            mlp = mlp_ms[kind] * m / counts[kind]
+            out["queries"][kind] = m
+            out[f"{kind}_plain_qps"] = m / (plain_ms / 1e3)
+            out[f"{kind}_learned_qps"] = m / ((seeded_ms + mlp) / 1e3)
+            out[f"{kind}_speedup"] = plain_ms / (seeded_ms + mlp)
+            out[f"{kind}_fallback_frac"] = float(nf.item()) / m
+            out[f"{kind}_identical"] = bool(same)
+    finally:
+        scene.set_traversal(snch.TRAVERSAL_NEAR_FIRST)
+    return out
 
 
 # --------------------------------------------------------------------- reference arm
@@ -373,6 +489,15 @@ def run_ours(args):
                                   dev["smp_u"][:m["smp"]]).mean(0),
     }
 
+    # ---- learned radius vs plain on the same batches (outside the timed step)
+    learned = None
+    if not args.no_learned:
+        learned = learned_leg(scene, sc, dev, counts, out, max(1, min(args.steps, 3)), args.scale)
+        learned["plain_qps"] = {"near": float(per_type["near"]), "sil": float(per_type["sil"])}
+        learned["speedup"] = {"near": learned["near_qps"] / per_type["near"],
+                              "sil": learned["sil_qps"] / per_type["sil"]}
+        learned["status"] = int(scene.device_status())
+
     # ---- e2e through the host-buffer C ABI
     e2e = None
     if not args.no_e2e:
@@ -466,6 +591,7 @@ def run_ours(args):
         "clocks": clk,
         "roofline": roof,
         "e2e": e2e,
+        "learned": learned,
     }
     if cpu is not None:
         smp = cpu["sample"]

@@ -136,6 +136,10 @@ int snch_set_traversal(snch_scene_t scene, int mode);
 #define SNCH_OPT_TRAVERSAL 1
 #define SNCH_OPT_QUERY_ORDER 2
 #define SNCH_OPT_ORDER_MIN_BATCH 3
+/*   SNCH_OPT_PERSISTENT       1 (default): near-first nearest/silhouette batches run as
+ *                             persistent kernels whose lanes take the next query when
+ *                             their own is done; 0: one thread per query. Same results. */
+#define SNCH_OPT_PERSISTENT 4
 int snch_set_option(snch_scene_t scene, int option, int64_t value);
 
 /* Position of each sorted leaf in the reference's depth-first visit order,

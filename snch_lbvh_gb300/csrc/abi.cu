@@ -85,6 +85,7 @@ struct snch_scene_s
     int traversal = SNCH_TRAVERSAL_NEAR_FIRST;
     int query_order = 1;             // Morton-sort batches of at least order_min queries
     int64_t order_min = 65536;
+    int persistent = 1;              // lane-refill nearest/silhouette kernels
     cudaStream_t pipe[2] = {nullptr, nullptr};
     HostStage stage;
 
@@ -100,6 +101,7 @@ struct snch_scene_s
         t.edges = edges;
         t.status = small + kWStatus;
         t.near_first = traversal == SNCH_TRAVERSAL_NEAR_FIRST ? 1 : 0;
+        t.persistent = persistent;
         return t;
     }
 };
@@ -584,6 +586,11 @@ int snch_set_option(snch_scene_t s, int option, int64_t value)
         if (value < 0)
             return fail(SNCH_ERR_INVALID_ARGUMENT, "SNCH_OPT_ORDER_MIN_BATCH must be >= 0");
         s->order_min = value;
+        return SNCH_OK;
+    case SNCH_OPT_PERSISTENT:
+        if (value != 0 && value != 1)
+            return fail(SNCH_ERR_INVALID_ARGUMENT, "SNCH_OPT_PERSISTENT takes 0 or 1");
+        s->persistent = (int)value;
         return SNCH_OK;
     default:
         return fail(SNCH_ERR_INVALID_ARGUMENT, "unknown option " + std::to_string(option));

@@ -80,8 +80,13 @@ SNCH_DEV float leaf_distance2(const TreeView &t, uint32_t pos, f3 p, uint32_t &o
     return d;
 }
 
+// seed.radius: the search starts with best = r^2 (query.cuh:255 with a bound);
+// nodes holding a primitive at the final distance d* <= r are never pruned and
+// the traversal order does not depend on best, so the same leaf wins; when
+// nothing lies within r the query is listed for the unbounded fallback pass.
 __global__ void __launch_bounds__(128) nearest_kernel(TreeView t, const float *__restrict__ pts, int64_t n,
-                                                      uint32_t *__restrict__ out_idx, float *__restrict__ out_dist)
+                                                      uint32_t *__restrict__ out_idx, float *__restrict__ out_dist,
+                                                      SeedArgs seed)
 {
     const int64_t qi = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (qi >= query_count(t, n))
@@ -90,12 +95,21 @@ __global__ void __launch_bounds__(128) nearest_kernel(TreeView t, const float *_
     const f3 p = load_point(pts, q);
     uint32_t nearest = kInvalid;
     float best = INFINITY;
+    if (seed.radius)
+    {
+        const float r = __ldg(seed.radius + q);
+        best = r * r;
+    }
     const uint32_t ni = t.num_tris - 1;
     if (t.num_tris == 1)
     {
         uint32_t orig;
-        best = leaf_distance2(t, 0, p, orig);
-        nearest = orig;
+        const float d = leaf_distance2(t, 0, p, orig);
+        if (!seed.radius || d <= best)
+        {
+            best = d;
+            nearest = orig;
+        }
     }
     else if (t.num_tris > 1)
     {
@@ -163,8 +177,12 @@ __global__ void __launch_bounds__(128) nearest_kernel(TreeView t, const float *_
             }
         } while (sp > 0);
     }
+    if (seed.radius && nearest == kInvalid)
+        best = INFINITY;  // nothing within the seed radius: the fallback pass answers it
     out_idx[q] = nearest;
     out_dist[q] = sqrtf(best);
+    if (seed.fail_list)
+        append_failed(seed.fail_list, seed.fail_count, (uint32_t)q, nearest == kInvalid);
 }
 
 // ------------------------------------------------------------------ silhouette
@@ -293,9 +311,12 @@ SNCH_DEV bool leaf_silhouette(const TreeView &t, uint32_t pos, f3 o, float max_r
     return ret;
 }
 
+// seed.radius: the search starts with best = r (same argument as nearest_kernel:
+// the cone tests do not depend on best and the visit order is fixed)
 __global__ void __launch_bounds__(128) silhouette_kernel(TreeView t, const float *__restrict__ pts,
                                                          const uint8_t *__restrict__ flips, int64_t n,
-                                                         float *__restrict__ out_dist, int32_t *__restrict__ out_edge)
+                                                         float *__restrict__ out_dist, int32_t *__restrict__ out_edge,
+                                                         SeedArgs seed)
 {
     const int64_t qi = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (qi >= query_count(t, n))
@@ -303,7 +324,7 @@ __global__ void __launch_bounds__(128) silhouette_kernel(TreeView t, const float
     const int64_t q = query_index(t, qi);
     const f3 p = load_point(pts, q);
     const bool flip = flips ? __ldg(flips + q) != 0 : false;
-    float best = INFINITY;
+    float best = seed.radius ? __ldg(seed.radius + q) : INFINITY;
     int32_t best_edge = -1;
     const uint32_t ni = t.num_tris - 1;
     if (t.num_tris == 1)
@@ -390,9 +411,13 @@ __global__ void __launch_bounds__(128) silhouette_kernel(TreeView t, const float
             }
         } while (sp > 0);
     }
+    if (seed.radius && best_edge < 0)
+        best = INFINITY;  // nothing within the seed radius: the fallback pass answers it
     out_dist[q] = best;
     if (out_edge)
         out_edge[q] = best_edge;
+    if (seed.fail_list)
+        append_failed(seed.fail_list, seed.fail_count, (uint32_t)q, best_edge < 0);
 }
 
 // ------------------------------------------------------------------ near-first forms
@@ -679,6 +704,270 @@ __global__ void __launch_bounds__(128) silhouette_fast_kernel(TreeView t, const 
         stats[3 * q] = n_int;
         stats[3 * q + 1] = n_leaf;
         stats[3 * q + 2] = n_edge;
+    }
+}
+
+// ------------------------------------------------------------------ persistent forms
+// The per-query traversals above run one query per thread; a warp then runs
+// until its slowest query is done, and the per-query work of the nearest and
+// silhouette searches has a long tail (a point far from every silhouette edge
+// expands hundreds of nodes), so most lanes idle. The persistent forms below
+// run the SAME per-query traversal (same visits, same results) but refill a
+// lane with the next query of the batch as soon as its own query finishes:
+// each warp takes chunks of 32 consecutive queries (spatially coherent when
+// the batch is Morton-ordered) from a global counter, and lanes take queries
+// from the warp's chunk in lane order.
+
+struct WarpQueue
+{
+    unsigned long long next = 0, end = 0;
+    bool exhausted = false;
+};
+
+// lanes with `need` set receive a query index (qi >= 0) while the batch lasts;
+// called by all 32 lanes of the warp
+SNCH_DEV int64_t take_query(WarpQueue &wq, unsigned long long total, unsigned long long *counter, bool need)
+{
+    const unsigned full = 0xFFFFFFFFu;
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
+    int64_t qi = -1;
+    unsigned mask = __ballot_sync(full, need);
+    while (mask && !wq.exhausted)
+    {
+        if (wq.next >= wq.end)
+        {
+            unsigned long long base = 0;
+            if (lane == 0)
+                base = atomicAdd(counter, 32ull);
+            base = __shfl_sync(full, base, 0);
+            if (base >= total)
+            {
+                wq.exhausted = true;
+                break;
+            }
+            wq.next = base;
+            wq.end = base + 32ull < total ? base + 32ull : total;
+        }
+        const unsigned avail = (unsigned)(wq.end - wq.next);
+        const unsigned r = __popc(mask & lt);
+        const bool mine = ((mask >> lane) & 1u) && r < avail;
+        if (mine)
+            qi = (int64_t)(wq.next + r);
+        const unsigned taken = __ballot_sync(full, mine);
+        wq.next += __popc(taken);
+        mask &= ~taken;
+    }
+    return qi;
+}
+
+struct SilState
+{
+    int64_t q;
+    f3 p;
+    bool flip;
+    float best;
+    uint32_t best_key;
+    int32_t best_edge;
+    int sp;
+};
+
+template <bool kSeed>
+__global__ void __launch_bounds__(128) silhouette_persistent_kernel(TreeView t, const float *__restrict__ pts,
+                                                                    const uint8_t *__restrict__ flips, int64_t n,
+                                                                    float *__restrict__ out_dist,
+                                                                    int32_t *__restrict__ out_edge, SeedArgs seed,
+                                                                    unsigned long long *counter)
+{
+    const unsigned long long total = (unsigned long long)query_count(t, n);
+    const uint32_t ni = t.num_tris - 1;
+    uint32_t sn[kStackDepth];
+    float sd[kStackDepth];
+    SilState s;
+    s.q = -1;
+    s.sp = 0;
+    bool active = false;
+    WarpQueue wq;
+    uint32_t dummy = 0;
+    for (;;)
+    {
+        const int64_t qi = take_query(wq, total, counter, !active);
+        if (qi >= 0)
+        {
+            s.q = query_index(t, qi);
+            s.p = load_point(pts, s.q);
+            s.flip = flips ? __ldg(flips + s.q) != 0 : false;
+            s.best = kSeed ? __ldg(seed.radius + s.q) : INFINITY;
+            s.best_key = 0;
+            s.best_edge = -1;
+            sn[0] = 0;
+            sd[0] = mindist(load_root_box(t.aabbs), s.p);
+            s.sp = 1;
+            active = true;
+        }
+        if (!__any_sync(0xFFFFFFFFu, active))
+            break;
+        if (!active)
+            continue;
+        bool done = false;
+        --s.sp;
+        const uint32_t node = sn[s.sp];
+        if (!(sd[s.sp] > s.best * s.best))
+        {
+            if (s.sp > kStackDepth - 2)
+            {
+                atomicOr(t.status, kStatusStackOverflow);
+                s.best = NAN;
+                s.best_edge = -1;
+                done = true;
+            }
+            else
+            {
+                Box lb, rb;
+                uint32_t L, R;
+                unpack_inner(load_inner(t.inner + node), lb, rb, L, R);
+                const float4 *cr = reinterpret_cast<const float4 *>(t.inner_cones + node);
+                InnerConeRec icr;
+                icr.a = __ldg(cr);
+                icr.b = __ldg(cr + 1);
+                icr.c = __ldg(cr + 2);
+                Cone lc, rc;
+                unpack_cones(icr, lc, rc);
+                const f3 p = s.p;
+                const float Lmd = mindist(lb, p), Rmd = mindist(rb, p);
+                const float b2 = s.best * s.best;
+                const bool hitL = Lmd <= b2 && lc.half_angle >= 0.0f && cone_overlap(lc, p, lb, Lmd);
+                const bool hitR = Rmd <= b2 && rc.half_angle >= 0.0f && cone_overlap(rc, p, rb, Rmd);
+                if (hitL && L >= ni)
+                    leaf_silhouette_fast(t, L - ni, p, s.flip, s.best, s.best_key, s.best_edge, dummy);
+                if (hitR && R >= ni)
+                    leaf_silhouette_fast(t, R - ni, p, s.flip, s.best, s.best_key, s.best_edge, dummy);
+                const float b2n = s.best * s.best;
+                const bool pL = hitL && L < ni && Lmd <= b2n, pR = hitR && R < ni && Rmd <= b2n;
+                if (pL && pR)
+                {
+                    const bool l_first = Lmd <= Rmd;
+                    sn[s.sp] = l_first ? R : L;
+                    sd[s.sp] = l_first ? Rmd : Lmd;
+                    sn[s.sp + 1] = l_first ? L : R;
+                    sd[s.sp + 1] = l_first ? Lmd : Rmd;
+                    s.sp += 2;
+                }
+                else if (pL || pR)
+                {
+                    sn[s.sp] = pL ? L : R;
+                    sd[s.sp] = pL ? Lmd : Rmd;
+                    ++s.sp;
+                }
+            }
+        }
+        if (done || s.sp == 0)
+        {
+            if (kSeed && s.best_edge < 0)
+                s.best = INFINITY;  // nothing within the seed radius: the fallback pass answers it
+            out_dist[s.q] = s.best;
+            if (out_edge)
+                out_edge[s.q] = s.best_edge;
+            if (kSeed && seed.fail_list)
+                append_failed(seed.fail_list, seed.fail_count, (uint32_t)s.q, s.best_edge < 0);
+            active = false;
+        }
+    }
+}
+
+template <bool kSeed>
+__global__ void __launch_bounds__(128) nearest_persistent_kernel(TreeView t, const float *__restrict__ pts, int64_t n,
+                                                                 uint32_t *__restrict__ out_idx,
+                                                                 float *__restrict__ out_dist, SeedArgs seed,
+                                                                 unsigned long long *counter)
+{
+    const unsigned long long total = (unsigned long long)query_count(t, n);
+    const uint32_t ni = t.num_tris - 1;
+    uint32_t sn[kStackDepth];
+    float sd[kStackDepth];
+    int64_t q = -1;
+    f3 p = mk(0.f, 0.f, 0.f);
+    uint32_t nearest = kInvalid, best_rank = 0;
+    float best = INFINITY;
+    int sp = 0;
+    bool active = false;
+    WarpQueue wq;
+    for (;;)
+    {
+        const int64_t qi = take_query(wq, total, counter, !active);
+        if (qi >= 0)
+        {
+            q = query_index(t, qi);
+            p = load_point(pts, q);
+            nearest = kInvalid;
+            best_rank = 0;
+            best = INFINITY;
+            if (kSeed)
+            {
+                const float r = __ldg(seed.radius + q);
+                best = r * r;
+            }
+            sn[0] = 0;
+            sd[0] = mindist(load_root_box(t.aabbs), p);
+            sp = 1;
+            active = true;
+        }
+        if (!__any_sync(0xFFFFFFFFu, active))
+            break;
+        if (!active)
+            continue;
+        bool done = false;
+        --sp;
+        const uint32_t node = sn[sp];
+        if (!(sd[sp] > best))
+        {
+            if (sp > kStackDepth - 2)
+            {
+                atomicOr(t.status, kStatusStackOverflow);
+                nearest = kInvalid;
+                best = NAN;
+                done = true;
+            }
+            else
+            {
+                Box lb, rb;
+                uint32_t L, R;
+                unpack_inner(load_inner(t.inner + node), lb, rb, L, R);
+                const float Lmd = mindist(lb, p), Rmd = mindist(rb, p);
+                const float Lmm = minmaxdist(lb, p), Rmm = minmaxdist(rb, p);
+                const bool aL = Lmd <= Rmm, aR = Rmd <= Lmm;  // query.cuh:279, 297
+                if (aL && L >= ni && Lmd <= best)
+                    leaf_nearest_fast(t, L - ni, p, best, best_rank, nearest);
+                if (aR && R >= ni && Rmd <= best)
+                    leaf_nearest_fast(t, R - ni, p, best, best_rank, nearest);
+                const bool pL = aL && L < ni && Lmd <= best, pR = aR && R < ni && Rmd <= best;
+                if (pL && pR)
+                {
+                    const bool l_first = Lmd <= Rmd;
+                    sn[sp] = l_first ? R : L;
+                    sd[sp] = l_first ? Rmd : Lmd;
+                    sn[sp + 1] = l_first ? L : R;
+                    sd[sp + 1] = l_first ? Lmd : Rmd;
+                    sp += 2;
+                }
+                else if (pL || pR)
+                {
+                    sn[sp] = pL ? L : R;
+                    sd[sp] = pL ? Lmd : Rmd;
+                    ++sp;
+                }
+            }
+        }
+        if (done || sp == 0)
+        {
+            if (kSeed && nearest == kInvalid)
+                best = INFINITY;  // nothing within the seed radius: the fallback pass answers it
+            out_idx[q] = nearest;
+            out_dist[q] = sqrtf(best);
+            if (kSeed && seed.fail_list)
+                append_failed(seed.fail_list, seed.fail_count, (uint32_t)q, nearest == kInvalid);
+            active = false;
+        }
     }
 }
 
@@ -1032,6 +1321,35 @@ __global__ void query_keys_kernel(const float *__restrict__ pts, int64_t n, cons
 namespace
 {
 inline unsigned grid_for(int64_t n, int b) { return (unsigned)((n + b - 1) / b); }
+// persistent launch: as many 128-thread blocks as the GPU holds at once (fewer for
+// small batches), and a zeroed 64-bit work counter of its own (stream-ordered
+// allocation, so concurrent calls on other streams do not share it)
+template <typename... KArgs, typename... Args>
+cudaError_t launch_persistent(void (*kernel)(KArgs...), int64_t n, cudaStream_t st, Args... args)
+{
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess)
+        e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 128, 0);
+    if (e != cudaSuccess)
+        return e;
+    const int64_t need = (n + 127) / 128;
+    const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>(need, (int64_t)sms * std::max(per_sm, 1)));
+    unsigned long long *counter = nullptr;
+    if ((e = cudaMallocAsync(reinterpret_cast<void **>(&counter), sizeof(unsigned long long), st)) != cudaSuccess)
+        return e;
+    e = cudaMemsetAsync(counter, 0, sizeof(unsigned long long), st);
+    if (e == cudaSuccess)
+    {
+        kernel<<<grid, 128, 0, st>>>(args..., counter);
+        note_launch();
+        e = cudaGetLastError();
+    }
+    const cudaError_t f = cudaFreeAsync(counter, st);
+    return e != cudaSuccess ? e : f;
+}
 }  // namespace
 
 cudaError_t launch_nearest(const TreeView &t, const float *pts, int64_t n, uint32_t *idx, float *dist, cudaStream_t st,
@@ -1041,10 +1359,15 @@ cudaError_t launch_nearest(const TreeView &t, const float *pts, int64_t n, uint3
         return cudaSuccess;
     if (stats)
         nearest_fast_kernel<true><<<grid_for(n, 128), 128, 0, st>>>(t, pts, n, idx, dist, stats, seed);
-    else if (t.near_first || seed.radius)
+    else if (t.near_first && t.num_tris > 1 && t.persistent)
+    {
+        return seed.radius ? launch_persistent(nearest_persistent_kernel<true>, n, st, t, pts, n, idx, dist, seed)
+                           : launch_persistent(nearest_persistent_kernel<false>, n, st, t, pts, n, idx, dist, seed);
+    }
+    else if (t.near_first)
         nearest_fast_kernel<false><<<grid_for(n, 128), 128, 0, st>>>(t, pts, n, idx, dist, nullptr, seed);
     else
-        nearest_kernel<<<grid_for(n, 128), 128, 0, st>>>(t, pts, n, idx, dist);
+        nearest_kernel<<<grid_for(n, 128), 128, 0, st>>>(t, pts, n, idx, dist, seed);
     note_launch();
     return cudaGetLastError();
 }
@@ -1055,10 +1378,16 @@ cudaError_t launch_silhouette(const TreeView &t, const float *pts, const uint8_t
         return cudaSuccess;
     if (stats)
         silhouette_fast_kernel<true><<<grid_for(n, 128), 128, 0, st>>>(t, pts, flip, n, dist, edge, stats, seed);
-    else if (t.near_first || seed.radius)
+    else if (t.near_first && t.num_tris > 1 && t.persistent)
+    {
+        return seed.radius
+                   ? launch_persistent(silhouette_persistent_kernel<true>, n, st, t, pts, flip, n, dist, edge, seed)
+                   : launch_persistent(silhouette_persistent_kernel<false>, n, st, t, pts, flip, n, dist, edge, seed);
+    }
+    else if (t.near_first)
         silhouette_fast_kernel<false><<<grid_for(n, 128), 128, 0, st>>>(t, pts, flip, n, dist, edge, nullptr, seed);
     else
-        silhouette_kernel<<<grid_for(n, 128), 128, 0, st>>>(t, pts, flip, n, dist, edge);
+        silhouette_kernel<<<grid_for(n, 128), 128, 0, st>>>(t, pts, flip, n, dist, edge, seed);
     note_launch();
     return cudaGetLastError();
 }

@@ -22,7 +22,7 @@ import numpy as np
 from . import _dev, _ptr, _stream, _torch
 from ._ffi import check, lib
 
-__all__ = ["LearnedRadius", "targets_from_scene", "gemm_bf16", "NUM_FREQ", "feature_scales"]
+__all__ = ["LearnedRadius", "targets_from_scene", "training_points", "gemm_bf16", "NUM_FREQ", "feature_scales"]
 
 NUM_FREQ = 32
 
@@ -70,8 +70,12 @@ class LearnedRadius:
         p = np.ascontiguousarray(value, np.float32).reshape(-1)
         check(lib().snch_mlp_set_params(self._h, p.ctypes.data_as(C.c_void_p), len(p)))
 
-    def gradient(self, points, targets, tau: float = 0.1, stream=None):
-        """(gradient, loss) of the mean pinball loss at quantile tau; no update."""
+    def gradient(self, points, targets, tau: float = 0.9, stream=None):
+        """(gradient, loss) of the mean pinball loss at quantile tau; no update.
+
+        The loss is minimised by the tau-quantile of the target: tau = 0.9 makes
+        the predicted radius exceed the true distance for about 90 % of the
+        points (the rest fall back to the unbounded search)."""
         torch = _torch()
         p, t = _dev(points, torch.float32, 3), _dev(targets, torch.float32, 2)
         g = np.empty(self.num_params(), np.float32)
@@ -80,7 +84,7 @@ class LearnedRadius:
                                       g.ctypes.data_as(C.c_void_p), C.byref(loss), _stream(stream)))
         return g, float(loss.value)
 
-    def train(self, points, targets, epochs: int = 1, batch: int = 65536, lr: float = 2e-3, tau: float = 0.1,
+    def train(self, points, targets, epochs: int = 1, batch: int = 65536, lr: float = 2e-3, tau: float = 0.9,
               stream=None) -> float:
         """Adam over `epochs` passes; returns the mean loss of the last epoch."""
         torch = _torch()
@@ -103,6 +107,25 @@ class LearnedRadius:
         check(lib().snch_mlp_predict_radius(self._h, _ptr(p), n, C.c_float(margin), C.c_float(floor), _ptr(rn),
                                             _ptr(rs), _stream(stream)))
         return rn, rs
+
+
+def training_points(verts, faces, n_uniform: int, n_surface: int, band: float = 0.05, lo=(0, 0, 0), hi=(1, 1, 1),
+                    seed: int = 0):
+    """Sample points for training: n_uniform U(box) and n_surface near the mesh (a
+    uniform point of a random triangle moved along its normal by N(0, (band/3)^2)),
+    clipped to the box. float32 [n_uniform + n_surface, 3]."""
+    rng = np.random.default_rng(seed)
+    lo, hi = np.asarray(lo, np.float32), np.asarray(hi, np.float32)
+    u = lo + (hi - lo) * rng.random((n_uniform, 3), dtype=np.float32)
+    t = rng.integers(0, len(faces), n_surface)
+    a, b, c = (np.asarray(verts, np.float32)[np.asarray(faces)[t, i]] for i in range(3))
+    r1, r2 = rng.random(n_surface, dtype=np.float32), rng.random(n_surface, dtype=np.float32)
+    s1 = np.sqrt(r1)
+    p = a * (1 - s1)[:, None] + b * (s1 * (1 - r2))[:, None] + c * (s1 * r2)[:, None]
+    nrm = np.cross(b - a, c - a)
+    nrm /= np.maximum(np.linalg.norm(nrm, axis=1, keepdims=True), 1e-30)
+    p = p + nrm * rng.normal(0.0, band / 3.0, (n_surface, 1)).astype(np.float32)
+    return np.clip(np.concatenate([u, p.astype(np.float32)]), lo, hi).astype(np.float32)
 
 
 def targets_from_scene(scene, points, flip=None, stream=None):

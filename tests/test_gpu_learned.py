@@ -133,8 +133,8 @@ def trained():
     train_pts = torch.from_numpy(rng.random((400_000, 3), dtype=np.float32)).cuda()
     tgt = targets_from_scene(s, train_pts)
     m = LearnedRadius(np.zeros(3), np.ones(3), seed=1)
-    _, loss0 = m.gradient(train_pts, tgt, tau=0.1)
-    loss = m.train(train_pts, tgt, epochs=12, batch=16384, lr=2e-3, tau=0.1)
+    _, loss0 = m.gradient(train_pts, tgt, tau=0.9)
+    loss = m.train(train_pts, tgt, epochs=12, batch=16384, lr=2e-3, tau=0.9)
     return s, m, loss0, loss
 
 

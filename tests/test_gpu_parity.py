@@ -263,3 +263,38 @@ def test_query_order_does_not_change_results(snch):
     for x, y in zip(a, b):
         np.testing.assert_array_equal(x.view(np.uint8), y.view(np.uint8))
     assert s.device_status() == 0
+
+
+@pytest.mark.parametrize("n", [1, 31, 33, 1000, 300_000])
+def test_persistent_equals_one_thread_per_query(snch, n):
+    """Lane-refill persistent kernels (default) equal one-thread-per-query kernels,
+    plain and seeded, at batch sizes below, at and above one warp and one chunk."""
+    from snch_lbvh_gb300 import meshes
+    v, f = meshes.noisy_icosphere(5, 1.0, 0.01, seed=0)
+    rng = np.random.default_rng(n)
+    pts = meshes.box_queries(v, n, 1.2, seed=n + 3)
+    if n >= 1000:  # exact-tie probes: vertices and edge midpoints
+        e = np.concatenate([f[:, [0, 1]], f[:, [1, 2]]])[: n // 4]
+        mids = (0.5 * (v[e[:, 0]].astype(np.float64) + v[e[:, 1]])).astype(np.float32)
+        pts[: len(mids)] = mids
+        pts[len(mids): len(mids) + min(len(v), n // 4)] = v[: n // 4]
+    flip = (rng.random(n) < 0.5).astype(np.uint8)
+    s = built_scene(snch, v, f)
+
+    def run():
+        i, d = s.query_nearest(pts)
+        sd, se = s.query_silhouette(pts, flip)
+        r = np.where(rng.random(n) < 0.5, 0.01, 1.0).astype(np.float32)
+        i2, d2 = s.query_nearest_seeded(pts, r)
+        sd2, se2 = s.query_silhouette_seeded(pts, r, flip)
+        return [x.cpu().numpy() for x in (i, d, sd, se, i2, d2, sd2, se2)]
+
+    state = rng.bit_generator.state
+    s.set_option(snch.OPT_PERSISTENT, 0)
+    a = run()
+    rng.bit_generator.state = state
+    s.set_option(snch.OPT_PERSISTENT, 1)
+    b = run()
+    for x, y in zip(a, b):
+        np.testing.assert_array_equal(x.view(np.uint8), y.view(np.uint8))
+    assert s.device_status() == 0

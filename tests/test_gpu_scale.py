@@ -102,3 +102,25 @@ def test_near_first_equals_reference_order_full_scene(big):
     for x, y in zip(a, b):
         np.testing.assert_array_equal(x, y)
     assert s.device_status() == 0
+
+
+def test_persistent_equals_one_thread_per_query_full_scene(big):
+    """On the 2M-triangle scene: 2M nearest + 1M silhouette queries, lane-refill
+    persistent kernels vs one thread per query."""
+    import snch_lbvh_gb300 as snch
+    from snch_lbvh_gb300 import meshes
+    sc, s, _ = big
+    q = meshes.wost_queries(2_000_000, 1_000_000, 1, 1, seed=23)
+
+    def run():
+        i, d = s.query_nearest(q["near_pts"])
+        sd, se = s.query_silhouette(q["sil_pts"], q["sil_flip"])
+        return [x.cpu().numpy() for x in (i, d, sd, se)]
+
+    s.set_option(snch.OPT_PERSISTENT, 0)
+    a = run()
+    s.set_option(snch.OPT_PERSISTENT, 1)
+    b = run()
+    for x, y in zip(a, b):
+        np.testing.assert_array_equal(x.view(np.uint8), y.view(np.uint8))
+    assert s.device_status() == 0

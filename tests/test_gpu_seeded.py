@@ -53,3 +53,37 @@ def test_seeded_equals_unseeded(mesh):
     np.testing.assert_array_equal(bits(sd1.cpu().numpy()), bits(sd0n))
     np.testing.assert_array_equal(se1.cpu().numpy(), se0.cpu().numpy())
     assert s.device_status() == 0
+
+
+def test_seeded_reference_order_equals_unseeded():
+    """The reference's own traversal order with a starting bound (the learned
+    radius applied to the reference's algorithm) returns the unseeded
+    reference-order results, including exact ties (vertex and edge-midpoint probes)."""
+    import torch
+    import snch_lbvh_gb300 as snch
+    from snch_lbvh_gb300 import meshes
+    rng = np.random.default_rng(8)
+    v, f = meshes.noisy_icosphere(4, 1.0, 0.01, seed=0)
+    e = np.concatenate([f[:, [0, 1]], f[:, [1, 2]]])
+    mids = (0.5 * (v[e[:, 0]].astype(np.float64) + v[e[:, 1]])).astype(np.float32)
+    pts = np.concatenate([meshes.box_queries(v, 60_000, 1.2, seed=5), v, mids]).astype(np.float32)
+    flip = (rng.random(len(pts)) < 0.5).astype(np.uint8)
+    s = built_scene(snch, v, f)
+    s.set_traversal(snch.TRAVERSAL_REFERENCE_ORDER)
+    i0, d0 = s.query_nearest(pts)
+    sd0, se0 = s.query_silhouette(pts, flip)
+    d0n, sd0n = d0.cpu().numpy(), sd0.cpu().numpy()
+    nf = torch.zeros(1, dtype=torch.int32, device="cuda")
+    r, _ = radii_mix(d0n, rng)
+    i1, d1 = s.query_nearest_seeded(pts, r, num_fallback=nf)
+    np.testing.assert_array_equal(i1.cpu().numpy(), i0.cpu().numpy())
+    np.testing.assert_array_equal(bits(d1.cpu().numpy()), bits(d0n))
+    assert int(nf.item()) == int(((r * r) < (d0n * d0n)).sum())
+    rs, _ = radii_mix(sd0n, rng)
+    sd1, se1 = s.query_silhouette_seeded(pts, rs, flip, num_fallback=nf)
+    np.testing.assert_array_equal(bits(sd1.cpu().numpy()), bits(sd0n))
+    np.testing.assert_array_equal(se1.cpu().numpy(), se0.cpu().numpy())
+    s.set_traversal(snch.TRAVERSAL_NEAR_FIRST)
+    i2, d2 = s.query_nearest(pts)
+    np.testing.assert_array_equal(i2.cpu().numpy(), i0.cpu().numpy())
+    assert s.device_status() == 0
