@@ -136,9 +136,11 @@ int snch_set_traversal(snch_scene_t scene, int mode);
 #define SNCH_OPT_TRAVERSAL 1
 #define SNCH_OPT_QUERY_ORDER 2
 #define SNCH_OPT_ORDER_MIN_BATCH 3
-/*   SNCH_OPT_PERSISTENT       1 (default): near-first nearest/silhouette batches run as
- *                             persistent kernels whose lanes take the next query when
- *                             their own is done; 0: one thread per query. Same results. */
+/*   SNCH_OPT_PERSISTENT       1: near-first nearest/silhouette batches run as persistent
+ *                             kernels whose lanes take the next query when their own is
+ *                             done; 0 (default): one thread per query. Same results; on
+ *                             the 2M-triangle scene with Morton-ordered batches the
+ *                             refilled lanes lose their warp's coherence and run slower. */
 #define SNCH_OPT_PERSISTENT 4
 int snch_set_option(snch_scene_t scene, int option, int64_t value);
 
@@ -219,6 +221,13 @@ int snch_mlp_train(snch_mlp_t mlp, const float *points, const float *targets, in
 /* fused tensor-core inference: DEVICE radius_near / radius_sil (either may be NULL) */
 int snch_mlp_predict_radius(snch_mlp_t mlp, const float *points, int64_t n, float margin, float floor,
                             float *radius_near, float *radius_sil, snch_stream_t stream);
+/* Self-check of the silhouette traversal's fast normal-cone test against the
+ * exact one (no reference counterpart): n random box / cone / point cases, half
+ * of them within 1e-3 rad of the decision boundary; adds to DEVICE
+ * device_counts[3] = {decided and equal, decided and different, left to the
+ * exact test}. device_counts[1] must stay 0. */
+int snch_selfcheck_cone_filter(int64_t n, uint64_t seed, uint64_t *device_counts, snch_stream_t stream);
+
 /* building block: C[M x N] (+)= A[M x K] * B[N x K]^T, bf16 row-major A and B, fp32 C, on
  * tcgen05; M % 128 == 0, K % 64 == 0, N in {64, 128, 192, 256}; all DEVICE buffers */
 int snch_gemm_bf16(const void *A, const void *B, float *C, int64_t M, int64_t N, int64_t K, int accumulate,

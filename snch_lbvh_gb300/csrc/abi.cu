@@ -85,7 +85,7 @@ struct snch_scene_s
     int traversal = SNCH_TRAVERSAL_NEAR_FIRST;
     int query_order = 1;             // Morton-sort batches of at least order_min queries
     int64_t order_min = 65536;
-    int persistent = 1;              // lane-refill nearest/silhouette kernels
+    int persistent = 0;              // lane-refill nearest/silhouette kernels (measured slower: off)
     cudaStream_t pipe[2] = {nullptr, nullptr};
     HostStage stage;
 
@@ -1102,6 +1102,14 @@ int snch_mlp_predict_radius(snch_mlp_t m, const float *pts, int64_t n, float mar
         return fail(SNCH_ERR_INVALID_ARGUMENT, "bad arguments");
     SNCH_CUDA(launch_mlp_radius(m->st.params, pts, n, m->st.center, m->st.inv_half, margin, floor_, r_near, r_sil,
                                 m->st.status, S(stream)));
+    return SNCH_OK;
+}
+
+int snch_selfcheck_cone_filter(int64_t n, uint64_t seed, uint64_t *device_counts, snch_stream_t stream)
+{
+    if (n < 0 || (n > 0 && !device_counts))
+        return fail(SNCH_ERR_INVALID_ARGUMENT, "bad arguments");
+    SNCH_CUDA(launch_cone_filter_check(n, seed, reinterpret_cast<unsigned long long *>(device_counts), S(stream)));
     return SNCH_OK;
 }
 

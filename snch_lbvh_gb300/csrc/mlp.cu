@@ -51,6 +51,46 @@ constexpr int kNumParams = kB5 + kOut;
 // whose range reduction is exact
 __constant__ float c_scale[kFreq];
 
+// The 24 features of octave j (frequencies k = 4j .. 4j+3, columns 24j .. 24j+23):
+// f[6 kk + 2 a] = sin, f[6 kk + 2 a + 1] = cos of pi s_{4j+kk} u_a. Octave 0 comes
+// from sincospif; every further octave doubles the angles (s_{k+4} = 2 s_k exactly):
+// sin 2x = 2 sin x cos x, cos 2x = (cos x - sin x)(cos x + sin x). Seven doublings
+// grow the absolute error to about 2^7 float ulps (~1e-5), far below the BF16
+// spacing the features are stored with.
+struct Octaves
+{
+    float s[12], c[12];  // [kk * 3 + a]
+    __device__ __forceinline__ void init(const float u[3])
+    {
+#pragma unroll
+        for (int kk = 0; kk < 4; ++kk)
+#pragma unroll
+            for (int a = 0; a < 3; ++a)
+                sincospif(c_scale[kk] * u[a], &s[kk * 3 + a], &c[kk * 3 + a]);
+    }
+    __device__ __forceinline__ void emit(float (&f)[24]) const
+    {
+#pragma unroll
+        for (int kk = 0; kk < 4; ++kk)
+#pragma unroll
+            for (int a = 0; a < 3; ++a)
+            {
+                f[6 * kk + 2 * a] = s[kk * 3 + a];
+                f[6 * kk + 2 * a + 1] = c[kk * 3 + a];
+            }
+    }
+    __device__ __forceinline__ void next()
+    {
+#pragma unroll
+        for (int i = 0; i < 12; ++i)
+        {
+            const float sn = 2.0f * s[i] * c[i];
+            c[i] = (c[i] - s[i]) * (c[i] + s[i]);
+            s[i] = sn;
+        }
+    }
+};
+
 // ------------------------------------------------------------------ generic GEMM
 // C[M x N] (+)= A[M x K] * B[N x K]^T; A, B bf16 row-major (K contiguous), C fp32
 // row-major. M % 128 == 0, K % 64 == 0, N in {64, 128, 192, 256}.
@@ -169,9 +209,11 @@ __device__ __forceinline__ void store_bf16x8(uint8_t *dst, const float *v)
     *reinterpret_cast<uint4 *>(dst) = *reinterpret_cast<const uint4 *>(h);
 }
 
-// shared memory: W1 (64x192) | W2, W3, W4 (64x64 each) | A features (128x192) | H (128x64), bf16
+// shared memory: W1 (64x192) | W2, W3, W4 (64x64 each) | X features (128x192), bf16.
+// H (128x64, the hidden layer feeding the next MMA) reuses X's space: X is dead
+// once the first layer's MMAs have completed. 96 KB: two CTAs per SM.
 constexpr uint32_t kSmW1 = 0, kSmW2 = kSmW1 + 64 * 192 * 2, kSmW3 = kSmW2 + 64 * 64 * 2, kSmW4 = kSmW3 + 64 * 64 * 2;
-constexpr uint32_t kSmX = kSmW4 + 64 * 64 * 2, kSmH = kSmX + 128 * 192 * 2, kSmBytes = kSmH + 128 * 64 * 2;
+constexpr uint32_t kSmX = kSmW4 + 64 * 64 * 2, kSmH = kSmX, kSmBytes = kSmX + 128 * 192 * 2;
 constexpr uint32_t kSbo192 = (192 / 8) * 128, kSbo64 = (64 / 8) * 128;
 
 __global__ void __launch_bounds__(128) mlp_radius_kernel(RadiusArgs a)
@@ -239,19 +281,14 @@ __global__ void __launch_bounds__(128) mlp_radius_kernel(RadiusArgs a)
         if (valid)
             for (int c = 0; c < 3; ++c)
                 u[c] = (__ldg(a.pts + 3 * q + c) - a.center[c]) * a.inv_half[c];
+        Octaves oct;
+        oct.init(u);
 #pragma unroll 1
-        for (int k = 0; k < kFreq; k += 4)  // 24 features = 3 core-matrix columns per step
+        for (int k = 0; k < kFreq; k += 4)  // one octave: 24 features = 3 core-matrix columns
         {
             float f[24];
-#pragma unroll
-            for (int kk = 0; kk < 4; ++kk)
-                for (int c = 0; c < 3; ++c)
-                {
-                    float s, co;
-                    sincospif(c_scale[k + kk] * u[c], &s, &co);
-                    f[6 * kk + 2 * c] = s;
-                    f[6 * kk + 2 * c + 1] = co;
-                }
+            oct.emit(f);
+            oct.next();
 #pragma unroll
             for (int j = 0; j < 3; ++j)
                 store_bf16x8(smem + kSmX + tc::core_offset(tid, 6 * k + 8 * j, 128, kSbo192), f + 8 * j);
@@ -359,14 +396,16 @@ __global__ void features_kernel(const float *__restrict__ pts, int64_t n, int64_
         u[1] = (pts[3 * i + 1] - center.y) * inv_half.y;
         u[2] = (pts[3 * i + 2] - center.z) * inv_half.z;
     }
-    for (int k = 0; k < kFreq; ++k)
-        for (int c = 0; c < 3; ++c)
-        {
-            float s, co;
-            sincospif(c_scale[k] * u[c], &s, &co);
-            X[i * kIn + 6 * k + 2 * c] = __float2bfloat16_rn(i < n ? s : 0.f);
-            X[i * kIn + 6 * k + 2 * c + 1] = __float2bfloat16_rn(i < n ? co : 0.f);
-        }
+    Octaves oct;
+    oct.init(u);
+    for (int k = 0; k < kFreq; k += 4)
+    {
+        float f[24];
+        oct.emit(f);
+        oct.next();
+        for (int j = 0; j < 24; ++j)
+            X[i * kIn + 6 * k + j] = __float2bfloat16_rn(i < n ? f[j] : 0.f);
+    }
 }
 
 // H = relu(Z + b) (bf16) for a [B x 64] pre-activation

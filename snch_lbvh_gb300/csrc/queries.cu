@@ -233,6 +233,134 @@ SNCH_DEV bool cone_overlap(const Cone &bc, f3 o, const Box &b, float dist_to_box
     return hs >= kPi2 ? true : inrange(kPi2, mn, mx);
 }
 
+// ---- fast, decision-identical form of cone_overlap
+// cone_overlap's answer (for a query outside the box) is "the angle between the
+// cone axis and the direction to the box centroid is within hs = half_angle +
+// vch of 90 degrees", with vch = asin(radius / l) when the query is outside the
+// cone's bounding sphere (l > radius), or "hs >= 90 degrees". In angle space:
+// dev = |pi/2 - dax| = asin(|x|), x = axis . v / l; the test is dev <= hs. The
+// reference evaluates it with acosf/asinf/atan2f and IEEE divisions; here dev
+// and vch come from Abramowitz & Stegun 4.4.45 (arccos x = sqrt(1 - x) (a0 + a1 x
+// + a2 x^2 + a3 x^3), |error| <= 6.8e-5 on [0, 1], also in float32), and the
+// answer is taken only when the margin |dev - hs| exceeds kConeTol, which bounds
+// the error of both evaluations: 2 x 6.8e-5 for the polynomials, and the
+// propagated rounding of x (a few 1e-7 absolute, amplified by 1/sqrt(1 - x^2)
+// <= 22.4 for |x| <= 0.999, the same for radius / l), plus the reference's own
+// acosf/asinf error of a few ulps. Otherwise (ill-conditioned |x| or radius / l
+// above 0.999, a query inside the bounding sphere, a margin below kConeTol) the
+// exact cone_overlap decides. A decided answer therefore equals the one the
+// reference's float arithmetic gives.
+constexpr float kConeTol = 4.0e-4f;
+constexpr float kIllCond = 0.999f;
+
+SNCH_DEV float acos_as(float x)  // 0 <= x <= 1
+{
+    const float a0 = 1.5707288f, a1 = -0.2121144f, a2 = 0.0742610f, a3 = -0.0187293f;
+    return sqrtf(1.0f - x) * (a0 + x * (a1 + x * (a2 + x * a3)));
+}
+
+// 1: overlap, 0: no overlap, -1: undecided (take cone_overlap)
+SNCH_DEV int cone_overlap_fast(const Cone &bc, f3 o, const Box &b, float dist_to_box)
+{
+    if (bc.half_angle >= kPi2 || dist_to_box < kEps)
+        return 1;  // the same first test as cone_overlap
+    const f3 c = centroid(b);
+    const f3 v = mk(c.x - o.x, c.y - o.y, c.z - o.z);
+    const float l = len3(v);  // bit-identical to cone_overlap's l (the l > radius branch)
+    if (!(l > 0.0f))
+        return -1;
+    const float ax = fabsf(dot3(bc.axis, v)) * __frcp_rn(l);
+    if (!(ax <= kIllCond))
+        return -1;
+    const float dev = kPi2 - acos_as(ax);
+    const float ha = bc.half_angle;
+    if (dev <= ha - kConeTol)
+        return 1;
+    if (!(l > bc.radius))
+        return -1;
+    const float y = __fdividef(bc.radius, l);
+    if (!(y <= kIllCond))
+        return -1;
+    const float hs = ha + (kPi2 - acos_as(fmaxf(y, 0.0f)));
+    if (hs >= kPi2 + kConeTol || dev <= hs - kConeTol)
+        return 1;
+    if (hs <= kPi2 - kConeTol && dev >= hs + kConeTol)
+        return 0;
+    return -1;
+}
+
+SNCH_DEV bool cone_test(const Cone &bc, f3 o, const Box &b, float dist_to_box)
+{
+    const int f = cone_overlap_fast(bc, o, b, dist_to_box);
+    return f >= 0 ? f == 1 : cone_overlap(bc, o, b, dist_to_box);
+}
+
+// Self-check: counts where the fast form decides and agrees / disagrees with
+// cone_overlap, and where it leaves the decision to cone_overlap, on random
+// boxes, cones and points, half of them placed within 1e-3 rad of the decision
+// boundary. counts[0] agree, counts[1] disagree, counts[2] undecided.
+SNCH_DEV uint64_t mix64(uint64_t z)
+{
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+SNCH_DEV float unit_rand(uint64_t &st)
+{
+    st += 0x9E3779B97F4A7C15ull;
+    return (float)(mix64(st) >> 40) * (1.0f / 16777216.0f);
+}
+
+__global__ void cone_filter_check_kernel(int64_t n, uint64_t seed, unsigned long long *counts)
+{
+    __shared__ unsigned long long s_c[3];
+    if (threadIdx.x < 3)
+        s_c[threadIdx.x] = 0;
+    __syncthreads();
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n)
+    {
+        uint64_t st = mix64(seed ^ (0x632BE59BD9B4E019ull * (uint64_t)(i + 1)));
+        Box b;
+        const f3 c = mk(2.f * unit_rand(st) - 1.f, 2.f * unit_rand(st) - 1.f, 2.f * unit_rand(st) - 1.f);
+        const f3 h = mk(exp2f(-12.f + 11.f * unit_rand(st)), exp2f(-12.f + 11.f * unit_rand(st)),
+                        exp2f(-12.f + 11.f * unit_rand(st)));
+        b.lower = mk(c.x - h.x, c.y - h.y, c.z - h.z);
+        b.upper = mk(c.x + h.x, c.y + h.y, c.z + h.z);
+        Cone k;
+        const float z = 2.f * unit_rand(st) - 1.f, ph = 6.2831853f * unit_rand(st), rr = sqrtf(fmaxf(0.f, 1.f - z * z));
+        k.axis = mk(rr * cosf(ph), rr * sinf(ph), z);
+        k.half_angle = unit_rand(st) < 0.5f ? 0.3f * unit_rand(st) : kPi2 * unit_rand(st);
+        k.radius = len3(h) * (0.5f + unit_rand(st));
+        const float l = k.radius * exp2f(-1.f + 6.f * unit_rand(st));
+        // direction at a chosen angle to the axis: random, or near the decision boundary
+        float theta;
+        if (unit_rand(st) < 0.5f)
+            theta = 3.14159265f * unit_rand(st);
+        else
+        {
+            const float vch = l > k.radius ? asinf(k.radius / l) : 0.f;
+            const float hs = k.half_angle + vch;
+            const float side = unit_rand(st) < 0.5f ? -1.f : 1.f;
+            theta = kPi2 + side * hs + 1e-3f * (2.f * unit_rand(st) - 1.f);
+        }
+        // perpendicular to the axis
+        f3 pp = fabsf(k.axis.x) < 0.9f ? mk(0.f, -k.axis.z, k.axis.y) : mk(-k.axis.z, 0.f, k.axis.x);
+        const float pl = len3(pp);
+        pp = mk(pp.x / pl, pp.y / pl, pp.z / pl);
+        const f3 dir = mk(cosf(theta) * k.axis.x + sinf(theta) * pp.x, cosf(theta) * k.axis.y + sinf(theta) * pp.y,
+                          cosf(theta) * k.axis.z + sinf(theta) * pp.z);
+        const f3 o = mk(c.x - l * dir.x, c.y - l * dir.y, c.z - l * dir.z);
+        const float md = mindist(b, o);
+        const int f = cone_overlap_fast(k, o, b, md);
+        const int slot = f < 0 ? 2 : ((f == 1) == cone_overlap(k, o, b, md) ? 0 : 1);
+        atomicAdd(&s_c[slot], 1ull);
+    }
+    __syncthreads();
+    if (threadIdx.x < 3 && s_c[threadIdx.x])
+        atomicAdd(counts + threadIdx.x, s_c[threadIdx.x]);
+}
+
 // find_closest_point_line_segment(float3) scene.cuh:230-255
 SNCH_DEV float closest_point_segment(f3 pa, f3 pb, f3 x, f3 &pt)
 {
@@ -452,8 +580,11 @@ SNCH_DEV void leaf_nearest_fast(const TreeView &t, uint32_t pos, f3 p, float &be
     }
 }
 
+// (128, 10): at most 48 registers, ten blocks per SM. The traversals wait on
+// dependent L2 loads; the extra resident warps hide more of that latency
+// (measured on the 2M-triangle scene: silhouette -6 %, nearest -2 %).
 template <bool kStats>
-__global__ void __launch_bounds__(128) nearest_fast_kernel(TreeView t, const float *__restrict__ pts, int64_t n,
+__global__ void __launch_bounds__(128, 10) nearest_fast_kernel(TreeView t, const float *__restrict__ pts, int64_t n,
                                                            uint32_t *__restrict__ out_idx, float *__restrict__ out_dist,
                                                            uint32_t *__restrict__ stats, SeedArgs seed)
 {
@@ -483,24 +614,16 @@ __global__ void __launch_bounds__(128) nearest_fast_kernel(TreeView t, const flo
     }
     else if (t.num_tris > 1)
     {
+        // The nearer passing child is expanded next without a trip through the
+        // stack (it would be popped at once, and its bound re-check cannot fail);
+        // only the farther one is pushed. Same expansions in the same order.
         uint32_t sn[kStackDepth];
         float sd[kStackDepth];
-        int sp = 1;
-        sn[0] = 0;
-        sd[0] = mindist(load_root_box(t.aabbs), p);
-        do
+        int sp = 0;
+        uint32_t node = 0;
+        bool live = !(mindist(load_root_box(t.aabbs), p) > best);
+        while (live)
         {
-            --sp;
-            const uint32_t node = sn[sp];
-            if (sd[sp] > best)
-                continue;
-            if (sp > kStackDepth - 2)
-            {
-                atomicOr(t.status, kStatusStackOverflow);
-                nearest = kInvalid;
-                best = NAN;
-                break;
-            }
             Box lb, rb;
             uint32_t L, R;
             unpack_inner(load_inner(t.inner + node), lb, rb, L, R);
@@ -524,26 +647,37 @@ __global__ void __launch_bounds__(128) nearest_fast_kernel(TreeView t, const flo
             const bool pL = aL && L < ni && Lmd <= best, pR = aR && R < ni && Rmd <= best;
             if (pL && pR)
             {
+                if (sp > kStackDepth - 2)
+                {
+                    atomicOr(t.status, kStatusStackOverflow);
+                    nearest = kInvalid;
+                    best = NAN;
+                    break;
+                }
                 const bool l_first = Lmd <= Rmd;
                 sn[sp] = l_first ? R : L;
                 sd[sp] = l_first ? Rmd : Lmd;
-                sn[sp + 1] = l_first ? L : R;
-                sd[sp + 1] = l_first ? Lmd : Rmd;
-                sp += 2;
-            }
-            else if (pL)
-            {
-                sn[sp] = L;
-                sd[sp] = Lmd;
                 ++sp;
+                node = l_first ? L : R;
+                continue;
             }
-            else if (pR)
+            if (pL || pR)
             {
-                sn[sp] = R;
-                sd[sp] = Rmd;
-                ++sp;
+                node = pL ? L : R;
+                continue;
             }
-        } while (sp > 0);
+            live = false;
+            while (sp > 0)
+            {
+                --sp;
+                if (!(sd[sp] > best))
+                {
+                    node = sn[sp];
+                    live = true;
+                    break;
+                }
+            }
+        }
     }
     if (kStats)
     {
@@ -598,7 +732,7 @@ SNCH_DEV void leaf_silhouette_fast(const TreeView &t, uint32_t pos, f3 o, bool f
 }
 
 template <bool kStats>
-__global__ void __launch_bounds__(128) silhouette_fast_kernel(TreeView t, const float *__restrict__ pts,
+__global__ void __launch_bounds__(128, 10) silhouette_fast_kernel(TreeView t, const float *__restrict__ pts,
                                                               const uint8_t *__restrict__ flips, int64_t n,
                                                               float *__restrict__ out_dist,
                                                               int32_t *__restrict__ out_edge,
@@ -621,24 +755,14 @@ __global__ void __launch_bounds__(128) silhouette_fast_kernel(TreeView t, const 
     }
     else if (t.num_tris > 1)
     {
+        // nearer passing child next, farther one on the stack (as nearest_fast_kernel)
         uint32_t sn[kStackDepth];
         float sd[kStackDepth];
-        int sp = 1;
-        sn[0] = 0;
-        sd[0] = mindist(load_root_box(t.aabbs), p);
-        do
+        int sp = 0;
+        uint32_t node = 0;
+        bool live = !(mindist(load_root_box(t.aabbs), p) > best * best);
+        while (live)
         {
-            --sp;
-            const uint32_t node = sn[sp];
-            if (sd[sp] > best * best)
-                continue;
-            if (sp > kStackDepth - 2)
-            {
-                atomicOr(t.status, kStatusStackOverflow);
-                best = NAN;
-                best_edge = -1;
-                break;
-            }
             Box lb, rb;
             uint32_t L, R;
             unpack_inner(load_inner(t.inner + node), lb, rb, L, R);
@@ -651,8 +775,8 @@ __global__ void __launch_bounds__(128) silhouette_fast_kernel(TreeView t, const 
             unpack_cones(icr, lc, rc);
             const float Lmd = mindist(lb, p), Rmd = mindist(rb, p);
             const float b2 = best * best;
-            const bool hitL = Lmd <= b2 && lc.half_angle >= 0.0f && cone_overlap(lc, p, lb, Lmd);
-            const bool hitR = Rmd <= b2 && rc.half_angle >= 0.0f && cone_overlap(rc, p, rb, Rmd);
+            const bool hitL = Lmd <= b2 && lc.half_angle >= 0.0f && cone_test(lc, p, lb, Lmd);
+            const bool hitR = Rmd <= b2 && rc.half_angle >= 0.0f && cone_test(rc, p, rb, Rmd);
             if (kStats)
                 ++n_int;
             if (hitL && L >= ni)
@@ -671,26 +795,37 @@ __global__ void __launch_bounds__(128) silhouette_fast_kernel(TreeView t, const 
             const bool pL = hitL && L < ni && Lmd <= b2n, pR = hitR && R < ni && Rmd <= b2n;
             if (pL && pR)
             {
+                if (sp > kStackDepth - 2)
+                {
+                    atomicOr(t.status, kStatusStackOverflow);
+                    best = NAN;
+                    best_edge = -1;
+                    break;
+                }
                 const bool l_first = Lmd <= Rmd;
                 sn[sp] = l_first ? R : L;
                 sd[sp] = l_first ? Rmd : Lmd;
-                sn[sp + 1] = l_first ? L : R;
-                sd[sp + 1] = l_first ? Lmd : Rmd;
-                sp += 2;
-            }
-            else if (pL)
-            {
-                sn[sp] = L;
-                sd[sp] = Lmd;
                 ++sp;
+                node = l_first ? L : R;
+                continue;
             }
-            else if (pR)
+            if (pL || pR)
             {
-                sn[sp] = R;
-                sd[sp] = Rmd;
-                ++sp;
+                node = pL ? L : R;
+                continue;
             }
-        } while (sp > 0);
+            live = false;
+            while (sp > 0)
+            {
+                --sp;
+                if (!(sd[sp] > best * best))
+                {
+                    node = sn[sp];
+                    live = true;
+                    break;
+                }
+            }
+        }
     }
     if (seed.radius && best_edge < 0)
         best = INFINITY;  // nothing within the seed radius: the fallback pass answers it
@@ -836,8 +971,8 @@ __global__ void __launch_bounds__(128) silhouette_persistent_kernel(TreeView t, 
                 const f3 p = s.p;
                 const float Lmd = mindist(lb, p), Rmd = mindist(rb, p);
                 const float b2 = s.best * s.best;
-                const bool hitL = Lmd <= b2 && lc.half_angle >= 0.0f && cone_overlap(lc, p, lb, Lmd);
-                const bool hitR = Rmd <= b2 && rc.half_angle >= 0.0f && cone_overlap(rc, p, rb, Rmd);
+                const bool hitL = Lmd <= b2 && lc.half_angle >= 0.0f && cone_test(lc, p, lb, Lmd);
+                const bool hitR = Rmd <= b2 && rc.half_angle >= 0.0f && cone_test(rc, p, rb, Rmd);
                 if (hitL && L >= ni)
                     leaf_silhouette_fast(t, L - ni, p, s.flip, s.best, s.best_key, s.best_edge, dummy);
                 if (hitR && R >= ni)
@@ -1388,6 +1523,14 @@ cudaError_t launch_silhouette(const TreeView &t, const float *pts, const uint8_t
         silhouette_fast_kernel<false><<<grid_for(n, 128), 128, 0, st>>>(t, pts, flip, n, dist, edge, nullptr, seed);
     else
         silhouette_kernel<<<grid_for(n, 128), 128, 0, st>>>(t, pts, flip, n, dist, edge, seed);
+    note_launch();
+    return cudaGetLastError();
+}
+cudaError_t launch_cone_filter_check(int64_t n, uint64_t seed, unsigned long long *counts, cudaStream_t st)
+{
+    if (n <= 0)
+        return cudaSuccess;
+    cone_filter_check_kernel<<<grid_for(n, 256), 256, 0, st>>>(n, seed, counts);
     note_launch();
     return cudaGetLastError();
 }

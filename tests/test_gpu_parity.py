@@ -10,6 +10,7 @@ Bars:
     boundary flips; such queries must still agree within SIL_RTOL relative and
     be rarer than SIL_MAX_FLIP_FRACTION.
 """
+import ctypes as C
 import numpy as np
 import pytest
 
@@ -298,3 +299,18 @@ def test_persistent_equals_one_thread_per_query(snch, n):
     for x, y in zip(a, b):
         np.testing.assert_array_equal(x.view(np.uint8), y.view(np.uint8))
     assert s.device_status() == 0
+
+
+def test_fast_cone_test_agrees_with_exact(snch):
+    """The silhouette traversal's fast normal-cone test decides only where its
+    error bound allows and then agrees with the reference-arithmetic test: 4M
+    random cases, half of them within 1e-3 rad of the decision boundary."""
+    import torch
+    counts = torch.zeros(3, dtype=torch.int64, device="cuda")
+    for seed in (1, 2):
+        snch.check(snch.lib().snch_selfcheck_cone_filter(2_000_000, seed, C.c_void_p(counts.data_ptr()),
+                                                         C.c_void_p(torch.cuda.current_stream().cuda_stream)))
+    agree, disagree, undecided = (int(x) for x in counts.cpu())
+    assert agree + disagree + undecided == 4_000_000
+    assert disagree == 0
+    assert agree >= 0.5 * 4_000_000, (agree, undecided)
