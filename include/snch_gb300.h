@@ -196,6 +196,68 @@ int snch_query_silhouette_seeded(snch_scene_t scene, const float *points_xyz, co
                                  const float *radius, int64_t n, float *out_distance, int32_t *out_edge,
                                  uint32_t *num_fallback, snch_stream_t stream);
 
+/* ------------------------------------------------------------------ batched scenes
+ * Many independent meshes in one scene: one topology pass, one LBVH build and
+ * one query launch for all of them (no reference counterpart; a reference user
+ * builds one lbvh::scene<3> per mesh). Vertices and triangles are concatenated
+ * mesh after mesh; triangle vertex indices are PER MESH (0 = the mesh's first
+ * vertex). mesh_vert_start / mesh_tri_start are HOST arrays of num_meshes + 1
+ * entries (0 ... nv, 0 ... nt). device != 0: v and t are DEVICE buffers.
+ * snch_compute_silhouettes / snch_build_bvh / snch_destroy work as for a scene;
+ * each mesh's subtree is exactly the tree a scene of that mesh alone gets. */
+int snch_batch_create(const float *v, int64_t nv, const int32_t *t, int64_t nt, const int64_t *mesh_vert_start,
+                      const int64_t *mesh_tri_start, int32_t num_meshes, int device, snch_scene_t *out,
+                      snch_stream_t stream);
+/* number of meshes of a batched scene (0 for a plain scene) */
+int snch_batch_num_meshes(snch_scene_t scene, int32_t *out);
+/* per-query mesh (DEVICE int32); results as snch_query_nearest / _silhouette on a
+ * scene of that mesh alone: triangle index and edge id within the mesh */
+int snch_batch_query_nearest(snch_scene_t scene, const int32_t *mesh, const float *points, int64_t n,
+                             int32_t *index, float *distance, snch_stream_t stream);
+int snch_batch_query_silhouette(snch_scene_t scene, const int32_t *mesh, const float *points,
+                                const uint8_t *flip_or_null, int64_t n, float *distance, int32_t *edge_or_null,
+                                snch_stream_t stream);
+
+typedef struct snch_mlp_s *snch_mlp_t;
+
+/* ------------------------------------------------------------------ walk-on-stars driver
+ * Wavefront walk-on-stars (Sawhney et al. 2023) on a Dirichlet scene (its nearest
+ * query gives the distance to the Dirichlet boundary) and a Neumann scene
+ * (silhouette distance, rays, SampleTriangleInSphere), for the test problem
+ * u(x) = x_0: g = x_0 on Dirichlet faces, h = outward normal . e_0 on Neumann
+ * faces. Each step issues, for every live walker, one nearest, one silhouette,
+ * one ray and one sphere-sample query (the library's own batched calls);
+ * finished walkers are compacted away. With an MLP the nearest and silhouette
+ * queries are seeded with its radii (output 0: Dirichlet distance, output 1:
+ * Neumann silhouette distance); the walks are the same either way. The
+ * reference has no walk driver (its consumer, elaina, is an external project). */
+#define SNCH_WOST_MAX_STEPS 128
+typedef struct
+{
+    int64_t walkers;
+    int32_t max_steps; /* 1 .. SNCH_WOST_MAX_STEPS */
+    float epsilon;     /* Dirichlet shell: a walk ends at distance < epsilon */
+    float center[3];   /* walkers start uniform in this ball (inside the domain) */
+    float radius;
+    uint64_t seed;
+    float margin, floor_; /* learned radius = exp(prediction) * margin + floor_ */
+} snch_wost_params;
+typedef struct
+{
+    int32_t steps;                          /* steps run */
+    int64_t terminated;                     /* walks that reached the Dirichlet shell */
+    int64_t live[SNCH_WOST_MAX_STEPS];      /* walkers at the start of each step */
+    int64_t queries[SNCH_WOST_MAX_STEPS];   /* queries of each step, all four types */
+    float step_ms[SNCH_WOST_MAX_STEPS];     /* device time of each step */
+    float query_ms[SNCH_WOST_MAX_STEPS];    /* of which in the query batches and the radius model */
+    uint32_t fallback[SNCH_WOST_MAX_STEPS]; /* seeded queries that needed the unbounded pass */
+} snch_wost_stats;
+/* estimates: DEVICE float[walkers] (by walker); start_points: DEVICE float[3 walkers] or NULL;
+ * stats: HOST. Synchronous. */
+int snch_wost_trace(snch_scene_t dirichlet, snch_scene_t neumann, snch_mlp_t mlp_or_null,
+                    const snch_wost_params *params, float *estimates, float *start_points, snch_wost_stats *stats,
+                    snch_stream_t stream);
+
 /* ------------------------------------------------------------------ learned search radius
  * A small MLP (32-frequency Fourier features of the point -> 4 x 64 ReLU ->
  * 2 outputs) predicts log(nearest distance) and log(silhouette distance);
@@ -203,7 +265,6 @@ int snch_query_silhouette_seeded(snch_scene_t scene, const float *points_xyz, co
  * FP32 in tensor memory). radius = exp(prediction) * margin + floor feeds
  * snch_query_*_seeded, whose fallback keeps results exact whatever the
  * prediction. No reference counterpart. */
-typedef struct snch_mlp_s *snch_mlp_t;
 int64_t snch_mlp_num_params(void);
 /* points are normalised by the box [lo, hi]; seed fixes the initial weights */
 int snch_mlp_create(const float *box_lo, const float *box_hi, uint64_t seed, snch_mlp_t *out);

@@ -19,7 +19,7 @@ import numpy as np
 
 from ._ffi import BvhView, SnchError, check, lib  # noqa: F401
 
-__all__ = ["Scene", "SnchError", "BvhView", "lib"]
+__all__ = ["Scene", "BatchedScene", "SnchError", "BvhView", "lib"]
 
 INVALID = 0xFFFFFFFF
 TRAVERSAL_NEAR_FIRST = 0
@@ -299,3 +299,68 @@ class Scene:
         vp = lambda a: a.ctypes.data_as(C.c_void_p)  # noqa: E731
         check(lib().snch_sample_in_sphere_host(self._h, vp(c), vp(r), vp(uu), n, vp(idx), vp(pdf)))
         return idx, pdf
+
+
+class BatchedScene(Scene):
+    """Many independent meshes in one scene: one silhouette pass, one LBVH build
+    and one query launch for all of them (snch_batch_* in the C ABI). Each mesh's
+    subtree is the tree a ``Scene`` of that mesh alone gets, and the batched
+    queries return what that scene's queries return (per-mesh triangle index and
+    edge id)."""
+
+    def __init__(self, meshes, stream=None):
+        """meshes: sequence of (vertices [nv, 3], triangles [nt, 3]) with per-mesh
+        vertex indices; NumPy arrays, or CUDA tensors (all of them)."""
+        self._h = C.c_void_p()
+        torch = _torch()
+        device = len(meshes) > 0 and isinstance(meshes[0][0], torch.Tensor) and meshes[0][0].is_cuda
+        vs = np.zeros(len(meshes) + 1, np.int64)
+        ts = np.zeros(len(meshes) + 1, np.int64)
+        for m, (v, t) in enumerate(meshes):
+            vs[m + 1] = vs[m] + len(v)
+            ts[m + 1] = ts[m] + len(t)
+        self.vert_start, self.tri_start = vs, ts
+        L = lib()
+        if device:
+            v = torch.cat([x.to(torch.float32).reshape(-1, 3) for x, _ in meshes]).contiguous()
+            t = torch.cat([y.to(device=v.device, dtype=torch.int32).reshape(-1, 3) for _, y in meshes]).contiguous()
+            vp, tp = _ptr(v), _ptr(t)
+        else:
+            v = np.ascontiguousarray(np.concatenate([np.zeros((0, 3), np.float32)] +
+                                                    [_host(x, np.float32, 3) for x, _ in meshes]), np.float32)
+            t = np.ascontiguousarray(np.concatenate([np.zeros((0, 3), np.int32)] +
+                                                    [_host(y, np.int32, 3) for _, y in meshes]), np.int32)
+            vp, tp = v.ctypes.data_as(C.c_void_p), t.ctypes.data_as(C.c_void_p)
+        check(L.snch_batch_create(vp, int(vs[-1]), tp, int(ts[-1]), vs.ctypes.data_as(C.c_void_p),
+                                  ts.ctypes.data_as(C.c_void_p), len(meshes), int(device), C.byref(self._h),
+                                  _stream(stream)))
+
+    @property
+    def num_meshes(self) -> int:
+        m = C.c_int32()
+        check(lib().snch_batch_num_meshes(self._h, C.byref(m)))
+        return int(m.value)
+
+    def query_nearest_batch(self, mesh, points, stream=None, out=None):
+        """(index within the mesh, int32 [-1 = none], distance) for each (mesh, point)."""
+        torch = _torch()
+        p = _dev(points, torch.float32, 3)
+        m = _dev(mesh, torch.int32)
+        n = p.shape[0]
+        idx, dist = out if out is not None else (torch.empty(n, dtype=torch.int32, device="cuda"),
+                                                 torch.empty(n, dtype=torch.float32, device="cuda"))
+        check(lib().snch_batch_query_nearest(self._h, _ptr(m), _ptr(p), n, _ptr(idx), _ptr(dist), _stream(stream)))
+        return idx, dist
+
+    def query_silhouette_batch(self, mesh, points, flip=None, stream=None, out=None):
+        """(distance, edge id within the mesh or -1) for each (mesh, point)."""
+        torch = _torch()
+        p = _dev(points, torch.float32, 3)
+        m = _dev(mesh, torch.int32)
+        n = p.shape[0]
+        f = None if flip is None else _dev(flip, torch.uint8)
+        dist, edge = out if out is not None else (torch.empty(n, dtype=torch.float32, device="cuda"),
+                                                  torch.empty(n, dtype=torch.int32, device="cuda"))
+        check(lib().snch_batch_query_silhouette(self._h, _ptr(m), _ptr(p), _ptr(f), n, _ptr(dist), _ptr(edge),
+                                                _stream(stream)))
+        return dist, edge

@@ -31,6 +31,7 @@ UNITS = [
     ("abi.cu", []),
     ("noalloc_sort.cu", []),
     ("mlp.cu", []),
+    ("wost.cu", []),
 ]
 HEADERS = ["common.cuh", "internal.h", "tcgen05.cuh"]
 

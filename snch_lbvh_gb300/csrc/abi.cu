@@ -86,6 +86,11 @@ struct snch_scene_s
     int query_order = 1;             // Morton-sort batches of at least order_min queries
     int64_t order_min = 65536;
     int persistent = 0;              // lane-refill nearest/silhouette kernels (measured slower: off)
+    // batched scene (num_meshes > 0): independent meshes, one build, per-mesh queries
+    uint32_t num_meshes = 0;
+    uint32_t *tri_mesh = nullptr, *mesh_tri_start = nullptr, *mesh_box = nullptr, *sorted_mesh = nullptr,
+             *mesh_root = nullptr, *perm = nullptr, *perm_tmp = nullptr, *mkey_tmp = nullptr;
+    int32_t *mesh_edge_start = nullptr;
     cudaStream_t pipe[2] = {nullptr, nullptr};
     HostStage stage;
 
@@ -122,7 +127,9 @@ void free_scene(snch_scene_s *s)
     void *ptrs[] = {s->verts, s->tris, s->tri_edges, s->tri_owned, s->edge_verts, s->nodes, s->aabbs, s->cones,
                     s->inner, s->inner_cones, s->leaves, s->edges, s->keys, s->vals, s->keys_tmp, s->vals_tmp,
                     s->flags, s->sizes, s->centroids, s->small, s->scratch, s->ref_objects, s->ref_edges,
-                    s->stage.in[0], s->stage.in[1], s->stage.out[0], s->stage.out[1]};
+                    s->stage.in[0], s->stage.in[1], s->stage.out[0], s->stage.out[1],
+                    s->tri_mesh, s->mesh_tri_start, s->mesh_box, s->sorted_mesh, s->mesh_root, s->perm,
+                    s->perm_tmp, s->mkey_tmp, s->mesh_edge_start};
     for (void *p : ptrs)
         if (p)
             cudaFree(p);
@@ -160,6 +167,21 @@ int allocate(snch_scene_s *s)
     const size_t scratch = std::max(topology_scratch_bytes((uint32_t)n), sort_scratch_bytes((uint32_t)n, 30));
     SNCH_CUDA(cudaMalloc(&s->scratch, scratch));
     SNCH_CUDA(cudaMemset(s->small, 0, kSmallWords * 4));
+    return SNCH_OK;
+}
+
+int allocate_batch(snch_scene_s *s)
+{
+    const size_t n = s->num_tris, m = s->num_meshes;
+    SNCH_CUDA(dalloc(&s->tri_mesh, n));
+    SNCH_CUDA(dalloc(&s->mesh_tri_start, m + 1));
+    SNCH_CUDA(dalloc(&s->mesh_box, 6 * m));
+    SNCH_CUDA(dalloc(&s->sorted_mesh, n));
+    SNCH_CUDA(dalloc(&s->mesh_root, m));
+    SNCH_CUDA(dalloc(&s->perm, n));
+    SNCH_CUDA(dalloc(&s->perm_tmp, n));
+    SNCH_CUDA(dalloc(&s->mkey_tmp, n));
+    SNCH_CUDA(dalloc(&s->mesh_edge_start, m));
     return SNCH_OK;
 }
 
@@ -252,6 +274,17 @@ BuildArgs build_args(snch_scene_s *s)
     a.leaves = s->leaves;
     a.edges = s->edges;
     a.status = s->small + kWStatus;
+    a.num_meshes = s->num_meshes;
+    a.tri_mesh = s->tri_mesh;
+    a.mesh_tri_start = s->mesh_tri_start;
+    a.mesh_box = s->mesh_box;
+    a.sorted_mesh = s->sorted_mesh;
+    a.mesh_root = s->mesh_root;
+    a.perm = s->perm;
+    a.perm_tmp = s->perm_tmp;
+    a.mkey_tmp = s->mkey_tmp;
+    a.tri_edges = s->tri_edges;
+    a.mesh_edge_start = s->mesh_edge_start;
     return a;
 }
 
@@ -288,10 +321,22 @@ struct BatchView
             cudaFreeAsync(scratch, st);
     }
 };
-cudaError_t batch_view(const snch_scene_s *s, const float *keys_from, int64_t n, cudaStream_t st, BatchView &b)
+cudaError_t batch_view(const snch_scene_s *s, const float *keys_from, int64_t n, cudaStream_t st, BatchView &b,
+                       const uint32_t *query_mesh = nullptr)
 {
     b.t = s->view();
     b.st = st;
+    if (query_mesh)
+    {
+        // batched queries: per-mesh subtrees, near-first one-thread-per-query kernels
+        b.t.query_mesh = query_mesh;
+        b.t.mesh_root = s->mesh_root;
+        b.t.mesh_tri_start = s->mesh_tri_start;
+        b.t.mesh_edge_start = s->mesh_edge_start;
+        b.t.num_meshes = s->num_meshes;
+        b.t.near_first = 1;
+        b.t.persistent = 0;
+    }
     if (!s->query_order || n < s->order_min || n >= (int64_t(1) << 30) || s->num_tris < 2)
         return cudaSuccess;
     cudaError_t e = cudaMallocAsync(&b.scratch, query_order_scratch_bytes(n), st);
@@ -551,6 +596,7 @@ int snch_build_bvh(snch_scene_t s, snch_stream_t stream)
         SNCH_CUDA(launch_build_front(a, st));
         SNCH_CUDA(radix_sort_pairs(s->keys, s->vals, s->keys_tmp, s->vals_tmp, s->num_tris, 30, s->small + kWHist,
                                    s->scratch, s->small + kWStatus, st));
+        SNCH_CUDA(launch_mesh_pass(a, s->scratch, st));  // batched scenes only
         SNCH_CUDA(launch_build_back(a, st));
         SNCH_CUDA(launch_ref_objects(s->verts, s->tris, s->tri_owned, s->edge_verts, s->num_tris, s->ref_objects,
                                      s->ref_edges, st));
@@ -779,7 +825,7 @@ int snch_sample_on_object(snch_scene_t s, const int32_t *idx, const float *u, co
     SNCH_CUDA(cudaStreamSynchronize(S(stream)));
     if (bad)
         return fail(SNCH_ERR_INVALID_ARGUMENT, std::to_string(bad) + " object indices out of range");
-    SNCH_CUDA(launch_sample_point(s->verts, s->tris, idx, u, v, n, pts, S(stream)));
+    SNCH_CUDA(launch_sample_point(s->verts, s->tris, s->num_tris, idx, u, v, n, pts, S(stream)));
     return SNCH_OK;
 }
 
@@ -1105,6 +1151,120 @@ int snch_mlp_predict_radius(snch_mlp_t m, const float *pts, int64_t n, float mar
     return SNCH_OK;
 }
 
+// ------------------------------------------------------------------ batched scenes
+int snch_batch_create(const float *v, int64_t nv, const int32_t *t, int64_t nt, const int64_t *mesh_vert_start,
+                      const int64_t *mesh_tri_start, int32_t num_meshes, int device, snch_scene_t *out,
+                      snch_stream_t stream)
+{
+    if (!out)
+        return fail(SNCH_ERR_INVALID_ARGUMENT, "out_scene is NULL");
+    *out = nullptr;
+    if (num_meshes < 1 || num_meshes > 65536 || !mesh_vert_start || !mesh_tri_start)
+        return fail(SNCH_ERR_INVALID_ARGUMENT, "need 1..65536 meshes and their vertex / triangle starts");
+    if (mesh_vert_start[0] != 0 || mesh_tri_start[0] != 0 || mesh_vert_start[num_meshes] != nv ||
+        mesh_tri_start[num_meshes] != nt)
+        return fail(SNCH_ERR_INVALID_ARGUMENT, "mesh starts must run from 0 to the vertex / triangle counts");
+    for (int32_t m = 0; m < num_meshes; ++m)
+        if (mesh_vert_start[m + 1] < mesh_vert_start[m] || mesh_tri_start[m + 1] < mesh_tri_start[m])
+            return fail(SNCH_ERR_INVALID_ARGUMENT, "mesh starts must not decrease (mesh " + std::to_string(m) + ")");
+    cudaStream_t st = S(stream);
+    if (nv < 0 || nt < 0 || (nv > 0 && !v) || (nt > 0 && !t))
+        return fail(SNCH_ERR_INVALID_ARGUMENT, "bad vertex or triangle buffer");
+    if (nt >= (int64_t(1) << 30) || nv >= (int64_t(1) << 31))
+        return fail(SNCH_ERR_TOO_LARGE, "at most 2^30 - 1 triangles and 2^31 - 1 vertices are supported");
+    snch_scene_s *s = new snch_scene_s();
+    s->num_verts = (uint32_t)nv;
+    s->num_tris = (uint32_t)nt;
+    s->num_meshes = (uint32_t)num_meshes;
+    int rc = allocate(s);
+    if (rc == SNCH_OK)
+        rc = allocate_batch(s);
+    if (rc != SNCH_OK)
+    {
+        free_scene(s);
+        return rc;
+    }
+    std::vector<uint32_t> ts(num_meshes + 1);
+    for (int32_t m = 0; m <= num_meshes; ++m)
+        ts[m] = (uint32_t)mesh_tri_start[m];
+    int64_t *vs_dev = nullptr;
+    cudaError_t e = cudaSuccess;
+    if (nv)
+        e = cudaMemcpyAsync(s->verts, v, 12 * (size_t)nv, device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                            st);
+    if (e == cudaSuccess)
+        e = cudaMallocAsync(reinterpret_cast<void **>(&vs_dev), 8 * (size_t)(num_meshes + 1), st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(vs_dev, mesh_vert_start, 8 * (size_t)(num_meshes + 1), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(s->mesh_tri_start, ts.data(), 4 * (size_t)(num_meshes + 1), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && nt)
+        e = cudaMemcpyAsync(s->tris, t, 12 * (size_t)nt, device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                            st);
+    if (e == cudaSuccess)
+        e = launch_mesh_setup(s->mesh_tri_start, vs_dev, (uint32_t)num_meshes, (uint32_t)nt, s->tri_mesh, s->tris,
+                              s->small + kWBad, st);
+    uint32_t bad = 0;
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(&bad, s->small + kWBad, 4, cudaMemcpyDeviceToHost, st);
+    if (vs_dev)
+        cudaFreeAsync(vs_dev, st);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess)
+    {
+        free_scene(s);
+        return fail(SNCH_ERR_CUDA, std::string("batch upload: ") + cudaGetErrorString(e));
+    }
+    if (bad)
+    {
+        free_scene(s);
+        return fail(SNCH_ERR_INVALID_ARGUMENT, std::to_string(bad) + " triangle vertex indices outside their mesh");
+    }
+    *out = s;
+    return SNCH_OK;
+}
+
+int snch_batch_num_meshes(snch_scene_t s, int32_t *out)
+{
+    if (!s || !out)
+        return fail(SNCH_ERR_INVALID_ARGUMENT, "NULL argument");
+    *out = (int32_t)s->num_meshes;
+    return SNCH_OK;
+}
+
+int snch_batch_query_nearest(snch_scene_t s, const int32_t *mesh, const float *pts, int64_t n, int32_t *idx,
+                             float *dist, snch_stream_t stream)
+{
+    int rc = check_built(s);
+    if (rc == SNCH_OK && !s->num_meshes)
+        rc = fail(SNCH_ERR_INVALID_ARGUMENT, "not a batched scene");
+    if (rc == SNCH_OK)
+        rc = check_n(n, {mesh, pts, idx, dist});
+    if (rc != SNCH_OK || n == 0)
+        return rc;
+    BatchView b;
+    SNCH_CUDA(batch_view(s, pts, n, S(stream), b, reinterpret_cast<const uint32_t *>(mesh)));
+    SNCH_CUDA(launch_nearest(b.t, pts, n, reinterpret_cast<uint32_t *>(idx), dist, S(stream)));
+    return SNCH_OK;
+}
+
+int snch_batch_query_silhouette(snch_scene_t s, const int32_t *mesh, const float *pts, const uint8_t *flip,
+                                int64_t n, float *dist, int32_t *edge, snch_stream_t stream)
+{
+    int rc = check_built(s);
+    if (rc == SNCH_OK && !s->num_meshes)
+        rc = fail(SNCH_ERR_INVALID_ARGUMENT, "not a batched scene");
+    if (rc == SNCH_OK)
+        rc = check_n(n, {mesh, pts, dist});
+    if (rc != SNCH_OK || n == 0)
+        return rc;
+    BatchView b;
+    SNCH_CUDA(batch_view(s, pts, n, S(stream), b, reinterpret_cast<const uint32_t *>(mesh)));
+    SNCH_CUDA(launch_silhouette(b.t, pts, flip, n, dist, edge, S(stream)));
+    return SNCH_OK;
+}
+
 int snch_selfcheck_cone_filter(int64_t n, uint64_t seed, uint64_t *device_counts, snch_stream_t stream)
 {
     if (n < 0 || (n > 0 && !device_counts))
@@ -1121,6 +1281,154 @@ int snch_gemm_bf16(const void *A, const void *B, float *C, int64_t M, int64_t N,
         return fail(SNCH_ERR_INVALID_ARGUMENT, "need M % 128 == 0, K % 64 == 0, N in {64, 128, 192, 256}");
     SNCH_CUDA(launch_gemm_bf16(A, B, C, M, N, K, accumulate, device_status, S(stream)));
     return SNCH_OK;
+}
+
+
+// ------------------------------------------------------------------ walk-on-stars driver
+int snch_wost_trace(snch_scene_t dir, snch_scene_t neu, snch_mlp_t mlp, const snch_wost_params *p, float *estimates,
+                    float *start_points, snch_wost_stats *stats, snch_stream_t stream)
+{
+    int rc = check_built(dir);
+    if (rc == SNCH_OK)
+        rc = check_built(neu);
+    if (rc != SNCH_OK)
+        return rc;
+    if (!p || !estimates || !stats || p->walkers <= 0 || p->walkers >= (int64_t(1) << 31) || p->max_steps < 1 ||
+        p->max_steps > SNCH_WOST_MAX_STEPS || !(p->epsilon > 0.f) || !(p->radius >= 0.f))
+        return fail(SNCH_ERR_INVALID_ARGUMENT, "bad walk-on-stars parameters");
+    if (dir->num_tris == 0)
+        return fail(SNCH_ERR_INVALID_ARGUMENT, "the Dirichlet scene is empty: walks would never end");
+    if (dir->num_meshes || neu->num_meshes)
+        return fail(SNCH_ERR_INVALID_ARGUMENT, "walk-on-stars takes plain scenes");
+    std::memset(stats, 0, sizeof(*stats));
+    cudaStream_t st = S(stream);
+    const size_t n = (size_t)p->walkers;
+    const bool has_neu = neu->num_tris > 0;
+    // one block: two walker states, the step batches, query outputs, counters
+    const size_t per = 2 * (12 + 12 + 1 + 4 + 4) + 4 + 4 + 4 + 4 + 4 + 4 + 12 + 4 + 4 + 4 + 4 + 1 + 4 + 8 + 4 + 4 + 4 +
+                       12 + 4 + 4;
+    char *blk = nullptr;
+    SNCH_CUDA(cudaMallocAsync(reinterpret_cast<void **>(&blk), per * n + 64 * 256, st));
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        char *q = blk + off;
+        off += (bytes + 255) & ~size_t(255);
+        return q;
+    };
+    WalkState A, B;
+    for (WalkState *w : {&A, &B})
+    {
+        w->x = reinterpret_cast<float *>(take(12 * n));
+        w->nb = reinterpret_cast<float *>(take(12 * n));
+        w->on_b = reinterpret_cast<uint8_t *>(take(n));
+        w->total = reinterpret_cast<float *>(take(4 * n));
+        w->id = reinterpret_cast<uint32_t *>(take(4 * n));
+    }
+    float *d_dir = reinterpret_cast<float *>(take(4 * n)), *d_sil = reinterpret_cast<float *>(take(4 * n));
+    float *r_near = reinterpret_cast<float *>(take(4 * n)), *r_sil = reinterpret_cast<float *>(take(4 * n));
+    uint32_t *near_idx = reinterpret_cast<uint32_t *>(take(4 * n));
+    int32_t *sil_edge = reinterpret_cast<int32_t *>(take(4 * n));
+    WalkStep ws{};
+    ws.dir = reinterpret_cast<float *>(take(12 * n));
+    ws.radius = reinterpret_cast<float *>(take(4 * n));
+    ws.u = reinterpret_cast<float *>(take(4 * n));
+    ws.su = reinterpret_cast<float *>(take(4 * n));
+    ws.sv = reinterpret_cast<float *>(take(4 * n));
+    ws.hit = reinterpret_cast<uint8_t *>(take(n));
+    ws.t = reinterpret_cast<float *>(take(4 * n));
+    ws.uv = reinterpret_cast<float *>(take(8 * n));
+    ws.hit_idx = reinterpret_cast<uint32_t *>(take(4 * n));
+    ws.smp_idx = reinterpret_cast<int32_t *>(take(4 * n));
+    ws.smp_pdf = reinterpret_cast<float *>(take(4 * n));
+    ws.smp_pt = reinterpret_cast<float *>(take(12 * n));
+    uint32_t *counts = reinterpret_cast<uint32_t *>(take(256));  // live, terminated, fallback x2
+    WalkStep run_step = ws;
+    if (!has_neu)
+    {
+        run_step.hit = nullptr;
+        run_step.smp_idx = nullptr;
+    }
+    cudaEvent_t ev[4];
+    for (auto &e : ev)
+        cudaEventCreate(&e);
+    auto finish = [&](int code) {
+        for (auto &e : ev)
+            cudaEventDestroy(e);
+        cudaFreeAsync(blk, st);
+        cudaStreamSynchronize(st);
+        return code;
+    };
+#define WOST_TRY(expr)                                                                                              \
+    do                                                                                                              \
+    {                                                                                                               \
+        cudaError_t e_ = (expr);                                                                                    \
+        if (e_ != cudaSuccess)                                                                                      \
+            return finish(fail(SNCH_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(e_)));                 \
+    } while (0)
+#define WOST_RC(expr)                                                                                               \
+    do                                                                                                              \
+    {                                                                                                               \
+        const int r_ = (expr);                                                                                      \
+        if (r_ != SNCH_OK)                                                                                          \
+            return finish(r_);                                                                                      \
+    } while (0)
+    WOST_TRY(launch_wost_init(A, (int64_t)n, p->center, p->radius, p->seed, start_points, st));
+    int64_t live = (int64_t)n;
+    for (int step = 0; step < p->max_steps && live > 0; ++step)
+    {
+        stats->live[step] = live;
+        WOST_TRY(cudaMemsetAsync(counts, 0, 16, st));
+        WOST_TRY(cudaEventRecord(ev[0], st));
+        // distances: to the Dirichlet boundary, to the Neumann silhouettes
+        if (mlp)
+        {
+            WOST_TRY(launch_mlp_radius(mlp->st.params, A.x, live, mlp->st.center, mlp->st.inv_half, p->margin,
+                                       p->floor_, r_near, has_neu ? r_sil : nullptr, mlp->st.status, st));
+            WOST_RC(snch_query_nearest_seeded(dir, A.x, r_near, live, near_idx, d_dir, counts + 2, stream));
+            if (has_neu)
+                WOST_RC(snch_query_silhouette_seeded(neu, A.x, nullptr, r_sil, live, d_sil, sil_edge, counts + 3,
+                                                     stream));
+        }
+        else
+        {
+            WOST_RC(snch_query_nearest(dir, A.x, live, near_idx, d_dir, stream));
+            if (has_neu)
+                WOST_RC(snch_query_silhouette(neu, A.x, nullptr, live, d_sil, sil_edge, stream));
+        }
+        WOST_TRY(cudaEventRecord(ev[1], st));
+        WOST_TRY(launch_wost_prepare(A, live, d_dir, has_neu ? d_sil : nullptr, B, ws, (uint32_t)step,
+                                     (uint32_t)(p->max_steps - 1), p->epsilon, p->seed, estimates, counts, st));
+        uint32_t h[4] = {0, 0, 0, 0};
+        WOST_TRY(cudaMemcpyAsync(h, counts, 16, cudaMemcpyDeviceToHost, st));
+        WOST_TRY(cudaStreamSynchronize(st));
+        const int64_t next = h[0];
+        stats->terminated += h[1];
+        stats->fallback[step] = h[2] + h[3];
+        WOST_TRY(cudaEventRecord(ev[2], st));
+        if (next > 0 && has_neu)
+        {
+            WOST_RC(snch_query_ray(neu, B.x, ws.dir, ws.radius, next, ws.hit, ws.t, ws.uv, ws.hit_idx, stream));
+            WOST_RC(snch_sample_in_sphere(neu, B.x, ws.radius, ws.u, next, ws.smp_idx, ws.smp_pdf, stream));
+            WOST_TRY(launch_sample_point(neu->verts, neu->tris, neu->num_tris, ws.smp_idx, ws.su, ws.sv, next,
+                                         ws.smp_pt, st));
+        }
+        WOST_TRY(cudaEventRecord(ev[3], st));
+        WOST_TRY(launch_wost_update(B, next, run_step, neu->verts, neu->tris, st));
+        WOST_TRY(cudaStreamSynchronize(st));
+        float a = 0.f, b = 0.f, c = 0.f;
+        cudaEventElapsedTime(&a, ev[0], ev[1]);
+        cudaEventElapsedTime(&b, ev[2], ev[3]);
+        cudaEventElapsedTime(&c, ev[0], ev[3]);
+        stats->query_ms[step] = a + b;
+        stats->step_ms[step] = c;
+        stats->queries[step] = live * (has_neu ? 2 : 1) + next * (has_neu ? 2 : 0);
+        stats->steps = step + 1;
+        std::swap(A, B);
+        live = next;
+    }
+#undef WOST_TRY
+#undef WOST_RC
+    return finish(SNCH_OK);
 }
 
 }  // extern "C"

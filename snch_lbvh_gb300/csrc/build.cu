@@ -92,6 +92,30 @@ __global__ void __launch_bounds__(256) leaf_bounds_kernel(BuildArgs a)
     }
     __shared__ float s[8][6];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    // batched scenes: a block whose triangles all belong to one mesh reduces into
+    // that mesh's box; a block straddling meshes adds each triangle on its own
+    uint32_t *box = a.scene_box;
+    if (a.num_meshes)
+    {
+        const uint32_t first = blockIdx.x * blockDim.x;
+        const uint32_t last = min(first + blockDim.x, a.num_tris) - 1;
+        const uint32_t m0 = __ldg(a.tri_mesh + first), m1 = __ldg(a.tri_mesh + last);
+        if (m0 != m1)
+        {
+            if (i < a.num_tris)
+            {
+                uint32_t *mb = a.mesh_box + 6 * (uint64_t)__ldg(a.tri_mesh + i);
+                const float w[6] = {b.upper.x, b.upper.y, b.upper.z, b.lower.x, b.lower.y, b.lower.z};
+                for (int c = 0; c < 6; ++c)
+                    if (c < 3)
+                        atomicMax(mb + c, float_to_ordered(w[c]));
+                    else
+                        atomicMin(mb + c, float_to_ordered(w[c]));
+            }
+            return;
+        }
+        box = a.mesh_box + 6 * (uint64_t)m0;
+    }
     if (lane == 0)
         for (int c = 0; c < 6; ++c)
             s[warp][c] = v[c];
@@ -103,10 +127,79 @@ __global__ void __launch_bounds__(256) leaf_bounds_kernel(BuildArgs a)
         for (int w = 1; w < (int)(blockDim.x >> 5); ++w)
             r = c < 3 ? fmaxf(r, s[w][c]) : fminf(r, s[w][c]);
         if (c < 3)
-            atomicMax(a.scene_box + c, float_to_ordered(r));
+            atomicMax(box + c, float_to_ordered(r));
         else
-            atomicMin(a.scene_box + c, float_to_ordered(r));
+            atomicMin(box + c, float_to_ordered(r));
     }
+}
+
+// batched scenes: empty per-mesh boxes, no mesh roots yet, no first edge yet
+__global__ void init_mesh_kernel(uint32_t *mesh_box, uint32_t *mesh_root, int32_t *mesh_edge_start,
+                                 uint32_t num_meshes)
+{
+    const uint32_t m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= num_meshes)
+        return;
+    for (int c = 0; c < 3; ++c)
+    {
+        mesh_box[6 * (uint64_t)m + c] = float_to_ordered(-INFINITY);
+        mesh_box[6 * (uint64_t)m + 3 + c] = float_to_ordered(INFINITY);
+    }
+    mesh_root[m] = kInvalid;
+    mesh_edge_start[m] = 0x7FFFFFFF;
+}
+
+// first silhouette edge id of each mesh: edge ids are handed out in triangle
+// order, so a mesh's edges are the ids from its smallest one on
+__global__ void mesh_edges_kernel(const int32_t *__restrict__ tri_edges, const uint32_t *__restrict__ tri_mesh,
+                                  uint32_t n, int32_t *mesh_edge_start)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    int32_t e = 0x7FFFFFFF;
+    for (int k = 0; k < 3; ++k)
+    {
+        const int32_t x = __ldg(tri_edges + 3 * (uint64_t)i + k);
+        if (x >= 0 && x < e)
+            e = x;
+    }
+    if (e != 0x7FFFFFFF)
+        atomicMin(mesh_edge_start + __ldg(tri_mesh + i), e);
+}
+
+// batched scene set-up: mesh of every triangle (binary search of the mesh
+// starts), and the triangles' per-mesh vertex indices made batch-wide; counts
+// indices outside their own mesh's vertex range
+__global__ void mesh_setup_kernel(const uint32_t *__restrict__ tri_start, const int64_t *__restrict__ vert_start,
+                                  uint32_t num_meshes, uint32_t n, uint32_t *__restrict__ tri_mesh,
+                                  int32_t *__restrict__ tris, uint32_t *bad)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    uint32_t lo = 0, hi = num_meshes;  // last m with tri_start[m] <= i
+    while (hi - lo > 1)
+    {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(tri_start + mid) <= i)
+            lo = mid;
+        else
+            hi = mid;
+    }
+    while (lo + 1 < num_meshes && __ldg(tri_start + lo + 1) <= i)  // empty meshes share a start
+        ++lo;
+    tri_mesh[i] = lo;
+    const int64_t v0 = vert_start[lo], nv = vert_start[lo + 1] - v0;
+    uint32_t b = 0;
+    for (int k = 0; k < 3; ++k)
+    {
+        const int32_t v = tris[3 * (uint64_t)i + k];
+        b += (v < 0 || v >= nv) ? 1u : 0u;
+        tris[3 * (uint64_t)i + k] = (int32_t)(v0 + v);
+    }
+    if (b)
+        atomicAdd(bad, b);
 }
 
 // default_morton_code_calculator<Real,3> bvh.cuh:281-304
@@ -116,13 +209,12 @@ __global__ void __launch_bounds__(256) morton_kernel(BuildArgs a)
     for (int i = threadIdx.x; i < 4 * 256; i += blockDim.x)
         (&s_hist[0][0])[i] = 0;
     __syncthreads();
-    const f3 upper = mk(ordered_to_float(a.scene_box[0]), ordered_to_float(a.scene_box[1]),
-                        ordered_to_float(a.scene_box[2]));
-    const f3 lower = mk(ordered_to_float(a.scene_box[3]), ordered_to_float(a.scene_box[4]),
-                        ordered_to_float(a.scene_box[5]));
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < a.num_tris)
     {
+        const uint32_t *box = a.num_meshes ? a.mesh_box + 6 * (uint64_t)__ldg(a.tri_mesh + i) : a.scene_box;
+        const f3 upper = mk(ordered_to_float(box[0]), ordered_to_float(box[1]), ordered_to_float(box[2]));
+        const f3 lower = mk(ordered_to_float(box[3]), ordered_to_float(box[4]), ordered_to_float(box[5]));
         const float4 c = a.centroids[i];
         f3 p = mk(c.x, c.y, c.z);
         p.x -= lower.x;
@@ -150,15 +242,32 @@ __global__ void __launch_bounds__(256) morton_kernel(BuildArgs a)
 // common_upper_bits on the 64-bit key (code << 32 | sorted object index):
 // equal to the reference's 32-bit path whenever the codes are unique
 // (bvh.cuh:505-515, morton_code.cuh:144-167)
-SNCH_DEV int delta(const uint32_t *__restrict__ k, const uint32_t *__restrict__ s, uint32_t a, uint32_t b)
+// Batched scenes compare (mesh id : 16 bits, code, index within the mesh): keys
+// of different meshes share fewer than 16 leading bits, keys of one mesh 16 +
+// their single-mesh value, so inside a mesh every comparison the build makes
+// comes out as in a build of that mesh alone, and a mesh boundary acts like
+// the end of the array.
+struct KeyView
 {
-    const uint32_t x = __ldg(k + a) ^ __ldg(k + b);
-    return x ? __clz(x) : 32 + __clz(__ldg(s + a) ^ __ldg(s + b));
+    const uint32_t *k;      // codes, sorted
+    const uint32_t *s;      // original triangle index of each sorted position
+    const uint32_t *m;      // mesh of each sorted position (nullptr: one mesh)
+    const uint32_t *start;  // first triangle of each mesh
+};
+SNCH_DEV int delta(const KeyView &v, uint32_t a, uint32_t b)
+{
+    const uint32_t x = __ldg(v.k + a) ^ __ldg(v.k + b);
+    if (!v.m)
+        return x ? __clz(x) : 32 + __clz(__ldg(v.s + a) ^ __ldg(v.s + b));
+    const uint32_t ma = __ldg(v.m + a), mb = __ldg(v.m + b);
+    if (ma != mb)
+        return __clz(ma ^ mb) - 16;
+    const uint32_t st = __ldg(v.start + ma);
+    return 16 + (x ? __clz(x) : 32 + __clz((__ldg(v.s + a) - st) ^ (__ldg(v.s + b) - st)));
 }
 
 // determine_range bvh.cuh:109-167 (unsigned index arithmetic as in the reference)
-SNCH_DEV void determine_range(const uint32_t *k, const uint32_t *s, uint32_t n, uint32_t idx, uint32_t &lo,
-                              uint32_t &hi)
+SNCH_DEV void determine_range(const KeyView &kv, uint32_t n, uint32_t idx, uint32_t &lo, uint32_t &hi)
 {
     if (idx == 0)
     {
@@ -166,22 +275,22 @@ SNCH_DEV void determine_range(const uint32_t *k, const uint32_t *s, uint32_t n, 
         hi = n - 1;
         return;
     }
-    const int L_delta = delta(k, s, idx, idx - 1);
-    const int R_delta = delta(k, s, idx, idx + 1);
+    const int L_delta = delta(kv, idx, idx - 1);
+    const int R_delta = delta(kv, idx, idx + 1);
     const int d = (R_delta > L_delta) ? 1 : -1;
     const int delta_min = L_delta < R_delta ? L_delta : R_delta;
     int l_max = 2;
     int dl = -1;
     int i_tmp = (int)(idx + (uint32_t)(d * l_max));
     if (0 <= i_tmp && (uint32_t)i_tmp < n)
-        dl = delta(k, s, idx, (uint32_t)i_tmp);
+        dl = delta(kv, idx, (uint32_t)i_tmp);
     while (dl > delta_min)
     {
         l_max <<= 1;
         i_tmp = (int)(idx + (uint32_t)(d * l_max));
         dl = -1;
         if (0 <= i_tmp && (uint32_t)i_tmp < n)
-            dl = delta(k, s, idx, (uint32_t)i_tmp);
+            dl = delta(kv, idx, (uint32_t)i_tmp);
     }
     int l = 0;
     int t = l_max >> 1;
@@ -190,7 +299,7 @@ SNCH_DEV void determine_range(const uint32_t *k, const uint32_t *s, uint32_t n, 
         i_tmp = (int)(idx + (uint32_t)((l + t) * d));
         dl = -1;
         if (0 <= i_tmp && (uint32_t)i_tmp < n)
-            dl = delta(k, s, idx, (uint32_t)i_tmp);
+            dl = delta(kv, idx, (uint32_t)i_tmp);
         if (dl > delta_min)
             l += t;
         t >>= 1;
@@ -207,11 +316,11 @@ SNCH_DEV void determine_range(const uint32_t *k, const uint32_t *s, uint32_t n, 
 }
 
 // find_split bvh.cuh:169-199
-SNCH_DEV uint32_t find_split(const uint32_t *k, const uint32_t *s, uint32_t first, uint32_t last)
+SNCH_DEV uint32_t find_split(const KeyView &kv, uint32_t first, uint32_t last)
 {
-    if (__ldg(k + first) == __ldg(k + last) && __ldg(s + first) == __ldg(s + last))
-        return (first + last) >> 1;
-    const int delta_node = delta(k, s, first, last);
+    if (first == last)
+        return first;
+    const int delta_node = delta(kv, first, last);
     int split = (int)first;
     int stride = (int)(last - first);
     do
@@ -220,7 +329,7 @@ SNCH_DEV uint32_t find_split(const uint32_t *k, const uint32_t *s, uint32_t firs
         const int middle = split + stride;
         if ((uint32_t)middle < last)
         {
-            if (delta(k, s, first, (uint32_t)middle) > delta_node)
+            if (delta(kv, first, (uint32_t)middle) > delta_node)
                 split = middle;
         }
     } while (stride > 1);
@@ -241,11 +350,27 @@ __global__ void __launch_bounds__(256) karras_kernel(BuildArgs a)
     nodes[ni + idx].object = a.vals[idx];
     if (idx == 0)
         nodes[0].parent = kInvalid;
+    if (a.num_meshes)
+    {
+        // a one-triangle mesh: its root is its leaf
+        const uint32_t m = __ldg(a.sorted_mesh + idx);
+        if ((idx == 0 || __ldg(a.sorted_mesh + idx - 1) != m) && (idx == n - 1 || __ldg(a.sorted_mesh + idx + 1) != m))
+            a.mesh_root[m] = ni + idx;
+    }
     if (idx >= ni)
         return;
     uint32_t lo, hi;
-    determine_range(a.keys, a.vals, n, idx, lo, hi);
-    const uint32_t gamma = find_split(a.keys, a.vals, lo, hi);
+    const KeyView kv{a.keys, a.vals, a.num_meshes ? a.sorted_mesh : nullptr, a.mesh_tri_start};
+    determine_range(kv, n, idx, lo, hi);
+    const uint32_t gamma = find_split(kv, lo, hi);
+    if (a.num_meshes)
+    {
+        // the internal node covering exactly one mesh is that mesh's root
+        const uint32_t m = __ldg(a.sorted_mesh + lo);
+        if (__ldg(a.sorted_mesh + hi) == m && (lo == 0 || __ldg(a.sorted_mesh + lo - 1) != m) &&
+            (hi == n - 1 || __ldg(a.sorted_mesh + hi + 1) != m))
+            a.mesh_root[m] = idx;
+    }
     uint32_t left = gamma, right = gamma + 1;
     if ((lo < hi ? lo : hi) == gamma)
         left += ni;
@@ -579,6 +704,14 @@ cudaError_t launch_build_front(const BuildArgs &a, cudaStream_t st)
     const uint32_t n = a.num_tris;
     init_build_kernel<<<1, 256, 0, st>>>(a.scene_box, a.hist);
     note_launch();
+    if (a.num_meshes)
+    {
+        init_mesh_kernel<<<(a.num_meshes + 255) / 256, 256, 0, st>>>(a.mesh_box, a.mesh_root, a.mesh_edge_start,
+                                                                     a.num_meshes);
+        note_launch();
+        mesh_edges_kernel<<<(n + 255) / 256, 256, 0, st>>>(a.tri_edges, a.tri_mesh, n, a.mesh_edge_start);
+        note_launch();
+    }
     const uint32_t g = (n + 255) / 256;
     leaf_bounds_kernel<<<g, 256, 0, st>>>(a);
     note_launch();
@@ -605,6 +738,79 @@ cudaError_t launch_build_back(const BuildArgs &a, cudaStream_t st)
     return cudaGetLastError();
 }
 
+// batched scenes, after the Morton sort: mesh id of each sorted position and
+// the identity permutation, then (after the stable sort by mesh id) the codes
+// and triangle indices gathered into (mesh, code, index) order
+__global__ void mesh_keys_kernel(const uint32_t *__restrict__ vals, const uint32_t *__restrict__ tri_mesh, uint32_t n,
+                                 uint32_t *__restrict__ mkey, uint32_t *__restrict__ perm)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n)
+    {
+        const uint32_t v = vals[i];
+        mkey[i] = v < n ? __ldg(tri_mesh + v) : 0u;
+        perm[i] = i;
+    }
+}
+__global__ void gather_pairs_kernel(const uint32_t *__restrict__ keys, const uint32_t *__restrict__ vals,
+                                    const uint32_t *__restrict__ perm, uint32_t n, uint32_t *__restrict__ keys_out,
+                                    uint32_t *__restrict__ vals_out)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n)
+    {
+        const uint32_t p = perm[i];
+        keys_out[i] = p < n ? keys[p] : 0u;
+        vals_out[i] = p < n ? vals[p] : kInvalid;
+    }
+}
+
+cudaError_t launch_mesh_setup(const uint32_t *tri_start, const int64_t *vert_start, uint32_t num_meshes, uint32_t n,
+                              uint32_t *tri_mesh, int32_t *tris, uint32_t *bad, cudaStream_t st)
+{
+    cudaError_t e = cudaMemsetAsync(bad, 0, 4, st);
+    if (e != cudaSuccess || n == 0)
+        return e;
+    mesh_setup_kernel<<<(n + 255) / 256, 256, 0, st>>>(tri_start, vert_start, num_meshes, n, tri_mesh, tris, bad);
+    note_launch();
+    return cudaGetLastError();
+}
+
+int mesh_key_bits(uint32_t num_meshes)
+{
+    int b = 1;
+    while (b < 16 && (1u << b) < num_meshes)
+        ++b;
+    return b;
+}
+
+size_t mesh_pass_scratch_bytes(uint32_t n, uint32_t num_meshes)
+{
+    return sort_scratch_bytes(n, mesh_key_bits(num_meshes));
+}
+
+// keys/vals hold the Morton-sorted (code, triangle); keys_tmp/vals_tmp are n words each
+cudaError_t launch_mesh_pass(const BuildArgs &a, void *scratch, cudaStream_t st)
+{
+    const uint32_t n = a.num_tris;
+    if (!a.num_meshes || n == 0)
+        return cudaSuccess;
+    mesh_keys_kernel<<<(n + 255) / 256, 256, 0, st>>>(a.vals, a.tri_mesh, n, a.sorted_mesh, a.perm);
+    note_launch();
+    cudaError_t e = radix_sort_pairs(a.sorted_mesh, a.perm, a.mkey_tmp, a.perm_tmp, n, mesh_key_bits(a.num_meshes),
+                                     nullptr, scratch, a.status, st);
+    if (e != cudaSuccess)
+        return e;
+    // gathered into the scratch pair, then back
+    gather_pairs_kernel<<<(n + 255) / 256, 256, 0, st>>>(a.keys, a.vals, a.perm, n, a.mkey_tmp, a.perm_tmp);
+    note_launch();
+    if ((e = cudaMemcpyAsync(a.keys, a.mkey_tmp, 4 * (size_t)n, cudaMemcpyDeviceToDevice, st)) != cudaSuccess)
+        return e;
+    if ((e = cudaMemcpyAsync(a.vals, a.perm_tmp, 4 * (size_t)n, cudaMemcpyDeviceToDevice, st)) != cudaSuccess)
+        return e;
+    return cudaGetLastError();
+}
+
 }  // namespace snch
 
 namespace snch
@@ -614,9 +820,11 @@ cudaError_t launch_ref_objects(const float *verts, const int32_t *tris, const in
                                snch_silhouette_edge *edges, cudaStream_t st)
 {
     if (num_tris)
+    {
         ref_objects_kernel<<<(num_tris + 255) / 256, 256, 0, st>>>(verts, tris, tri_owned, edge_verts, num_tris, objs,
                                                                   edges);
         note_launch();
+    }
     return cudaGetLastError();
 }
 

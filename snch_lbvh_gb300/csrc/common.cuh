@@ -96,7 +96,39 @@ struct TreeView
     const uint32_t *order = nullptr;  // optional: thread i answers query order[i] (Morton-sorted batches)
     const uint32_t *order_count = nullptr;  // optional: device count of valid entries of order
     int persistent = 0;  // 1: nearest/silhouette run as persistent lane-refill kernels (same results)
+    // batched queries over a batched scene: the mesh of each query (input position)
+    // selects the subtree it searches; results are reported per mesh
+    const uint32_t *query_mesh = nullptr;
+    const uint32_t *mesh_root = nullptr;       // subtree root per mesh (leaf id for one triangle)
+    const uint32_t *mesh_tri_start = nullptr;  // first (global) triangle per mesh
+    const int32_t *mesh_edge_start = nullptr;  // first (global) silhouette edge id per mesh
+    uint32_t num_meshes = 0;
 };
+
+// Where a query's search starts: the whole tree (node 0), or for a batched
+// query its mesh's subtree; kInvalid = nothing to search (no triangles, or an
+// unknown mesh). Offsets turn batch-wide triangle / edge ids into per-mesh ids.
+struct QueryRoot
+{
+    uint32_t node;
+    uint32_t tri_off;
+    int32_t edge_off;
+};
+SNCH_DEV QueryRoot query_root(const TreeView &t, int64_t q)
+{
+    QueryRoot r{t.num_tris ? 0u : 0xFFFFFFFFu, 0u, 0};
+    if (t.query_mesh)
+    {
+        const uint32_t m = __ldg(t.query_mesh + q);
+        r.node = m < t.num_meshes ? __ldg(t.mesh_root + m) : 0xFFFFFFFFu;
+        if (r.node != 0xFFFFFFFFu)
+        {
+            r.tri_off = __ldg(t.mesh_tri_start + m);
+            r.edge_off = __ldg(t.mesh_edge_start + m);
+        }
+    }
+    return r;
+}
 
 // Seeded search: per-query initial radius, and where queries that find
 // nothing inside it are listed for the unbounded fallback pass.

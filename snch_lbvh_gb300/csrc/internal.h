@@ -40,15 +40,59 @@ struct BuildArgs
     LeafRec *leaves;
     EdgeRec *edges;
     uint32_t *status;
+    // batched scenes (num_meshes > 0): many independent meshes in one build. The
+    // triangles are mesh-major; each mesh gets its own Morton box, the sort key
+    // is (mesh, code, local index) and the Karras split prefers mesh boundaries,
+    // so every mesh's subtree is exactly the tree a build of that mesh alone gives.
+    uint32_t num_meshes;
+    const uint32_t *tri_mesh;        // mesh of each (original) triangle
+    const uint32_t *mesh_tri_start;  // num_meshes + 1
+    uint32_t *mesh_box;              // 6 ordered uints per mesh
+    uint32_t *sorted_mesh;           // mesh of each sorted position
+    uint32_t *mesh_root;             // subtree root per mesh (a leaf id for one triangle, kInvalid for none)
+    uint32_t *perm, *perm_tmp, *mkey_tmp;  // mesh-pass sort scratch
+    const int32_t *tri_edges;        // edge id of each triangle side (topology)
+    int32_t *mesh_edge_start;        // first silhouette edge id per mesh
 };
 
 // ---- build.cu
 cudaError_t launch_build_front(const BuildArgs &a, cudaStream_t st);
 cudaError_t launch_build_back(const BuildArgs &a, cudaStream_t st);
+// batched scenes: after the Morton sort, the stable pass by mesh id
+cudaError_t launch_mesh_pass(const BuildArgs &a, void *scratch, cudaStream_t st);
+size_t mesh_pass_scratch_bytes(uint32_t n, uint32_t num_meshes);
+cudaError_t launch_mesh_setup(const uint32_t *tri_start, const int64_t *vert_start, uint32_t num_meshes, uint32_t n,
+                              uint32_t *tri_mesh, int32_t *tris, uint32_t *bad, cudaStream_t st);
 cudaError_t launch_ref_objects(const float *verts, const int32_t *tris, const int32_t *tri_owned,
                                const int32_t *edge_verts, uint32_t num_tris, snch_triangle *objs,
                                snch_silhouette_edge *edges, cudaStream_t st);
 cudaError_t launch_validate(const int32_t *tris, int64_t n, int64_t num_verts, uint32_t *bad, cudaStream_t st);
+
+// ---- wost.cu: wavefront walk-on-stars walker updates
+struct WalkState  // structure of arrays, one entry per live walker
+{
+    float *x;        // 3 per walker: current point
+    float *nb;       // 3 per walker: outward normal of the Neumann face it stands on
+    uint8_t *on_b;   // 1: on the Neumann boundary
+    float *total;    // accumulated Neumann source terms
+    uint32_t *id;    // walker index (estimates are written at it)
+};
+struct WalkStep  // per-step batch inputs and results of the ray and sphere-sample queries
+{
+    float *dir, *radius, *u, *su, *sv;
+    uint8_t *hit;
+    float *t, *uv;
+    uint32_t *hit_idx;
+    int32_t *smp_idx;
+    float *smp_pdf, *smp_pt;
+};
+cudaError_t launch_wost_init(const WalkState &s, int64_t n, const float center[3], float radius, uint64_t seed,
+                             float *start, cudaStream_t st);
+cudaError_t launch_wost_prepare(const WalkState &in, int64_t n, const float *d_dir, const float *d_sil,
+                                const WalkState &out, const WalkStep &step_in, uint32_t step, uint32_t last_step,
+                                float eps, uint64_t seed, float *estimates, uint32_t *counts, cudaStream_t st);
+cudaError_t launch_wost_update(const WalkState &s, int64_t n, const WalkStep &step, const float *nverts,
+                               const int32_t *ntris, cudaStream_t st);
 
 // ---- queries.cu (stats != nullptr: per-query work counters, 3 words per query)
 cudaError_t launch_nearest(const TreeView &t, const float *pts, int64_t n, uint32_t *idx, float *dist, cudaStream_t st,
@@ -66,8 +110,8 @@ cudaError_t launch_sample(const TreeView &t, const float *c, const float *r, con
 size_t query_order_scratch_bytes(int64_t n);
 cudaError_t launch_query_order(const TreeView &t, const float *pts, int64_t n, void *scratch, uint32_t **order,
                                cudaStream_t st);
-cudaError_t launch_sample_point(const float *verts, const int32_t *tris, const int32_t *idx, const float *u,
-                                const float *v, int64_t n, float *out, cudaStream_t st);
+cudaError_t launch_sample_point(const float *verts, const int32_t *tris, uint32_t num_tris, const int32_t *idx,
+                                const float *u, const float *v, int64_t n, float *out, cudaStream_t st);
 
 // ---- mlp.cu (learned search radius)
 struct MlpWorkspace

@@ -602,17 +602,13 @@ __global__ void __launch_bounds__(128, 10) nearest_fast_kernel(TreeView t, const
         best = r * r;
     }
     const uint32_t ni = t.num_tris - 1;
-    if (t.num_tris == 1)
+    const QueryRoot qr = query_root(t, q);
+    if (qr.node == kInvalid)
     {
-        uint32_t orig;
-        const float d = leaf_distance2(t, 0, p, orig);
-        if (d <= best)
-        {
-            best = d;
-            nearest = orig;
-        }
     }
-    else if (t.num_tris > 1)
+    else if (qr.node >= ni)  // a one-triangle tree or mesh
+        leaf_nearest_fast(t, qr.node - ni, p, best, best_rank, nearest);
+    else
     {
         // The nearer passing child is expanded next without a trip through the
         // stack (it would be popped at once, and its bound re-check cannot fail);
@@ -620,8 +616,8 @@ __global__ void __launch_bounds__(128, 10) nearest_fast_kernel(TreeView t, const
         uint32_t sn[kStackDepth];
         float sd[kStackDepth];
         int sp = 0;
-        uint32_t node = 0;
-        bool live = !(mindist(load_root_box(t.aabbs), p) > best);
+        uint32_t node = qr.node;
+        bool live = !(mindist(load_root_box(t.aabbs + qr.node), p) > best);
         while (live)
         {
             Box lb, rb;
@@ -687,7 +683,7 @@ __global__ void __launch_bounds__(128, 10) nearest_fast_kernel(TreeView t, const
     }
     if (seed.radius && nearest == kInvalid)
         best = INFINITY;  // nothing within the seed radius: the fallback pass answers it
-    out_idx[q] = nearest;
+    out_idx[q] = nearest == kInvalid ? kInvalid : nearest - qr.tri_off;
     out_dist[q] = sqrtf(best);
     if (seed.fail_list)
         append_failed(seed.fail_list, seed.fail_count, (uint32_t)q, nearest == kInvalid);
@@ -749,18 +745,20 @@ __global__ void __launch_bounds__(128, 10) silhouette_fast_kernel(TreeView t, co
     uint32_t best_key = 0;
     int32_t best_edge = -1;
     const uint32_t ni = t.num_tris - 1;
-    if (t.num_tris == 1)
+    const QueryRoot qr = query_root(t, q);
+    if (qr.node == kInvalid)
     {
-        leaf_silhouette_fast(t, 0, p, flip, best, best_key, best_edge, n_edge);
     }
-    else if (t.num_tris > 1)
+    else if (qr.node >= ni)  // a one-triangle tree or mesh
+        leaf_silhouette_fast(t, qr.node - ni, p, flip, best, best_key, best_edge, n_edge);
+    else
     {
         // nearer passing child next, farther one on the stack (as nearest_fast_kernel)
         uint32_t sn[kStackDepth];
         float sd[kStackDepth];
         int sp = 0;
-        uint32_t node = 0;
-        bool live = !(mindist(load_root_box(t.aabbs), p) > best * best);
+        uint32_t node = qr.node;
+        bool live = !(mindist(load_root_box(t.aabbs + qr.node), p) > best * best);
         while (live)
         {
             Box lb, rb;
@@ -831,7 +829,7 @@ __global__ void __launch_bounds__(128, 10) silhouette_fast_kernel(TreeView t, co
         best = INFINITY;  // nothing within the seed radius: the fallback pass answers it
     out_dist[q] = best;
     if (out_edge)
-        out_edge[q] = best_edge;
+        out_edge[q] = best_edge < 0 ? best_edge : best_edge - qr.edge_off;
     if (seed.fail_list)
         append_failed(seed.fail_list, seed.fail_count, (uint32_t)q, best_edge < 0);
     if (kStats)
@@ -1401,14 +1399,22 @@ __global__ void __launch_bounds__(128) sample_kernel(TreeView t, const float *__
 }
 
 // sample_triangle scene.cuh:14-27 on the triangle of ORIGINAL index idx
+// an index outside [0, num_tris) (a draw that found no triangle) gives a NaN point
 __global__ void sample_point_kernel(const float *__restrict__ verts, const int32_t *__restrict__ tris,
-                                    const int32_t *__restrict__ idx, const float *__restrict__ us,
-                                    const float *__restrict__ vs, int64_t n, float *__restrict__ out)
+                                    uint32_t num_tris, const int32_t *__restrict__ idx,
+                                    const float *__restrict__ us, const float *__restrict__ vs, int64_t n,
+                                    float *__restrict__ out)
 {
     const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (q >= n)
         return;
-    const int32_t *tr = tris + 3 * (int64_t)__ldg(idx + q);
+    const int32_t k = __ldg(idx + q);
+    if (k < 0 || (uint32_t)k >= num_tris)
+    {
+        out[3 * q] = out[3 * q + 1] = out[3 * q + 2] = NAN;
+        return;
+    }
+    const int32_t *tr = tris + 3 * (int64_t)k;
     const f3 pa = load_vert(verts, __ldg(tr)), pb = load_vert(verts, __ldg(tr + 1)), pc = load_vert(verts, __ldg(tr + 2));
     float u = __ldg(us + q), v = __ldg(vs + q);
     if (u + v > 1.0f)
@@ -1426,13 +1432,29 @@ __global__ void sample_point_kernel(const float *__restrict__ verts, const int32
 // 30-bit Morton code of each query point inside the root box (same encoding
 // as the leaves, morton_code.cuh:61-70); sorting a batch by it makes the 32
 // queries of a warp spatial neighbours. Results do not depend on the order.
+// Morton code of the query point in the tree's root box; for batched queries
+// (mesh of each query given) in its mesh's root box, below the mesh id:
+// key = mesh << (32 - mesh_bits) | the code's top (32 - mesh_bits) bits
 __global__ void query_keys_kernel(const float *__restrict__ pts, int64_t n, const Box *__restrict__ root,
-                                  uint32_t *__restrict__ keys, uint32_t *__restrict__ vals)
+                                  uint32_t *__restrict__ keys, uint32_t *__restrict__ vals, TreeView t,
+                                  int mesh_bits)
 {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n)
         return;
-    const Box b = load_root_box(root);
+    uint32_t m = 0, node = 0;
+    if (t.query_mesh)
+    {
+        m = __ldg(t.query_mesh + i);
+        node = m < t.num_meshes ? __ldg(t.mesh_root + m) : kInvalid;
+        if (node == kInvalid)
+        {
+            keys[i] = 0xFFFFFFFFu;
+            vals[i] = (uint32_t)i;
+            return;
+        }
+    }
+    const Box b = load_root_box(root + node);
     f3 p = load_point(pts, i);
     p.x = (p.x - b.lower.x) / (b.upper.x - b.lower.x);
     p.y = (p.y - b.lower.y) / (b.upper.y - b.lower.y);
@@ -1448,7 +1470,8 @@ __global__ void query_keys_kernel(const float *__restrict__ pts, int64_t n, cons
         v = (v | (v << 2)) & 0x49249249u;
         return v;
     };
-    keys[i] = expand(x) * 4 + expand(y) * 2 + expand(z);
+    const uint32_t code = expand(x) * 4 + expand(y) * 2 + expand(z);
+    keys[i] = t.query_mesh ? (m << (32 - mesh_bits)) | (code >> (mesh_bits - 2)) : code;
     vals[i] = (uint32_t)i;
 }
 
@@ -1564,22 +1587,27 @@ cudaError_t launch_query_order(const TreeView &t, const float *pts, int64_t n, v
     uint32_t *keys = static_cast<uint32_t *>(scratch);
     uint32_t *vals = keys + n, *keys_tmp = vals + n, *vals_tmp = keys_tmp + n;
     void *sort_scratch = vals_tmp + n;
-    query_keys_kernel<<<grid_for(n, 256), 256, 0, st>>>(pts, n, t.aabbs, keys, vals);
+    // batched: mesh ids take the top mesh_bits (>= 2) bits of the key
+    int mesh_bits = 2;
+    while (mesh_bits < 16 && (1u << mesh_bits) < t.num_meshes)
+        ++mesh_bits;
+    query_keys_kernel<<<grid_for(n, 256), 256, 0, st>>>(pts, n, t.aabbs, keys, vals, t, mesh_bits);
     note_launch();
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess)
-        e = radix_sort_pairs(keys, vals, keys_tmp, vals_tmp, (uint32_t)n, 30, nullptr, sort_scratch, t.status, st);
+        e = radix_sort_pairs(keys, vals, keys_tmp, vals_tmp, (uint32_t)n, t.query_mesh ? 32 : 30, nullptr,
+                             sort_scratch, t.status, st);
     *order = vals;
     return e;
 }
-size_t query_order_scratch_bytes(int64_t n) { return 16 * (size_t)n + sort_scratch_bytes((uint32_t)n, 30) + 256; }
+size_t query_order_scratch_bytes(int64_t n) { return 16 * (size_t)n + sort_scratch_bytes((uint32_t)n, 32) + 256; }
 
-cudaError_t launch_sample_point(const float *verts, const int32_t *tris, const int32_t *idx, const float *u,
-                                const float *v, int64_t n, float *out, cudaStream_t st)
+cudaError_t launch_sample_point(const float *verts, const int32_t *tris, uint32_t num_tris, const int32_t *idx,
+                                const float *u, const float *v, int64_t n, float *out, cudaStream_t st)
 {
     if (n <= 0)
         return cudaSuccess;
-    sample_point_kernel<<<grid_for(n, 256), 256, 0, st>>>(verts, tris, idx, u, v, n, out);
+    sample_point_kernel<<<grid_for(n, 256), 256, 0, st>>>(verts, tris, num_tris, idx, u, v, n, out);
     note_launch();
     return cudaGetLastError();
 }

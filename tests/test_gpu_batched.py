@@ -1,0 +1,123 @@
+"""Batched scenes: many meshes built and queried together give, mesh by mesh,
+exactly what a Scene of that mesh alone gives (per-mesh triangle indices and
+silhouette edge ids, distances bit for bit), in any mix and order of queries."""
+import numpy as np
+import pytest
+
+from conftest import golden_names, load_golden
+from test_gpu_parity import bits, built_scene
+
+pytestmark = pytest.mark.gpu
+
+
+def mixed_meshes(rng, count):
+    from snch_lbvh_gb300 import meshes
+    out = []
+    for k in range(count):
+        kind = k % 3
+        if kind == 0:
+            v, f = meshes.noisy_icosphere(int(rng.integers(0, 4)), float(rng.uniform(0.2, 1.0)), 0.01,
+                                          seed=int(rng.integers(1 << 30)))
+        elif kind == 1:
+            nu = int(rng.integers(6, 40))
+            v, f = meshes.noisy_torus(float(rng.uniform(0.2, 0.5)), 0.1, nu, max(3, nu // 2), 0.002,
+                                      seed=int(rng.integers(1 << 30)))
+        else:
+            g = load_golden(golden_names()[k // 3 % len(golden_names())])
+            v, f = g["verts"], g["tris"]
+        v = (v + rng.uniform(-2, 2, 3)).astype(np.float32)  # meshes overlap in space and in Morton boxes
+        out.append((v.astype(np.float32), f.astype(np.int32)))
+    return out
+
+
+def check_batch(snch, ms, rng, per_mesh=3000):
+    b = snch.BatchedScene(ms)
+    b.compute_silhouettes()
+    b.build_bvh()
+    assert b.num_meshes == len(ms)
+    mesh_ids, pts, flips, expect = [], [], [], []
+    for m, (v, f) in enumerate(ms):
+        if len(v) == 0:
+            p = rng.random((50, 3), dtype=np.float32)
+        else:
+            p = snch_box_queries(v, per_mesh, rng)
+        fl = (rng.random(len(p)) < 0.5).astype(np.uint8)
+        if len(f):
+            s = built_scene(snch, v, f)
+            i, d = s.query_nearest(p)
+            sd, se = s.query_silhouette(p, fl)
+            expect.append([x.cpu().numpy() for x in (i, d, sd, se)])
+        else:
+            n = len(p)
+            expect.append([np.full(n, -1, np.int32), np.full(n, np.inf, np.float32), np.full(n, np.inf, np.float32),
+                           np.full(n, -1, np.int32)])
+        mesh_ids.append(np.full(len(p), m, np.int32))
+        pts.append(p)
+        flips.append(fl)
+    mesh_ids, pts, flips = np.concatenate(mesh_ids), np.concatenate(pts), np.concatenate(flips)
+    exp = [np.concatenate([e[k] for e in expect]) for k in range(4)]
+    perm = rng.permutation(len(pts))  # queries of all meshes interleaved
+    i, d = b.query_nearest_batch(mesh_ids[perm], pts[perm])
+    sd, se = b.query_silhouette_batch(mesh_ids[perm], pts[perm], flips[perm])
+    got = [x.cpu().numpy() for x in (i, d, sd, se)]
+    for g, e in zip(got, exp):
+        np.testing.assert_array_equal(bits(g), bits(e[perm]))
+    assert b.device_status() == 0
+    return b
+
+
+def snch_box_queries(v, n, rng):
+    lo, hi = v.min(0), v.max(0)
+    c, h = (lo + hi) / 2, (hi - lo) / 2 * 1.2 + 1e-3
+    p = (c + h * (2 * rng.random((n, 3)) - 1)).astype(np.float32)
+    # exact-tie probes: vertices
+    k = min(len(v), n // 4)
+    p[:k] = v[:k]
+    return p
+
+
+def test_batched_equals_single_scenes_golden_and_mixed(snch_mod):
+    rng = np.random.default_rng(1)
+    ms = mixed_meshes(rng, 24)
+    ms.insert(5, (np.zeros((0, 3), np.float32), np.zeros((0, 3), np.int32)))  # an empty mesh
+    ms.insert(9, (np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], np.float32), np.array([[0, 1, 2]], np.int32)))
+    check_batch(snch_mod, ms, rng)
+
+
+def test_batched_many_meshes_ordered_batch(snch_mod):
+    """300 meshes (mesh ids need 9 bits), > 65536 queries (Morton-ordered by mesh)."""
+    rng = np.random.default_rng(2)
+    from snch_lbvh_gb300 import meshes
+    ms = []
+    for k in range(300):
+        v, f, _ = meshes.icosphere(int(rng.integers(0, 3)), float(rng.uniform(0.1, 1)))
+        ms.append(((v + rng.uniform(-1, 1, 3)).astype(np.float32), f.astype(np.int32)))
+    check_batch(snch_mod, ms, rng, per_mesh=400)
+
+
+def test_batched_rejects_bad_input(snch_mod):
+    snch = snch_mod
+    v = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], np.float32)
+    with pytest.raises(snch.SnchError):
+        snch.BatchedScene([(v, np.array([[0, 1, 3]], np.int32))])  # index 3 outside its mesh
+    with pytest.raises(snch.SnchError):
+        snch.BatchedScene([])
+    s = snch.Scene(v, np.array([[0, 1, 2]], np.int32))
+    s.compute_silhouettes()
+    s.build_bvh()
+    with pytest.raises(snch.SnchError):
+        s_b = snch.BatchedScene.__new__(snch.BatchedScene)
+        s_b._h = s._h
+        try:
+            s_b.query_nearest_batch(np.zeros(1, np.int32), np.zeros((1, 3), np.float32))
+        finally:
+            s_b._h = None
+
+
+@pytest.fixture(scope="module")
+def snch_mod():
+    import torch
+    assert torch.cuda.is_available()
+    import snch_lbvh_gb300
+    snch_lbvh_gb300.lib()
+    return snch_lbvh_gb300
