@@ -56,6 +56,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-radius leg")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched-meshes leg")
+    ap.add_argument("--no-wost", action="store_true", help="skip the walk-on-stars leg")
     return ap.parse_args()
 
 
@@ -309,6 +311,133 @@ def learned_on_reference_order(scene, model, dev, margin, mlp_ms, counts, sub=2_
     return out
 
 
+# --------------------------------------------------------------------- batched meshes
+def batched_leg(scale, per_tri=8):
+    """256 independent meshes (log-uniform 1k..500k triangles): one batched scene
+    (one topology pass, one build, one launch per query type) vs one scene per
+    mesh (a build and two query launches per mesh), same queries: per_tri x
+    triangles nearest and silhouette points per mesh, uniform in the mesh's box
+    scaled by 1.2. Device time with CUDA events; results compared bit for bit."""
+    import torch
+    import snch_lbvh_gb300 as snch
+    from snch_lbvh_gb300 import meshes
+    ms = meshes.batched_meshes(seed=5)
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(11)
+    counts = [max(1, int(per_tri * len(f) * scale)) for _, f in ms]
+    dev = [(torch.from_numpy(v).cuda(), torch.from_numpy(f).cuda()) for v, f in ms]
+    pts, mid = [], []
+    for m, (v, _) in enumerate(dev):
+        lo, hi = v.min(0).values, v.max(0).values
+        c, h = (lo + hi) / 2, (hi - lo) / 2 * 1.2
+        pts.append(c + h * (2 * torch.rand((counts[m], 3), device="cuda", generator=gen) - 1))
+        mid.append(torch.full((counts[m],), m, dtype=torch.int32, device="cuda"))
+    P, M = torch.cat(pts), torch.cat(mid)
+    n = len(P)
+    stream = torch.cuda.current_stream()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    b = snch.BatchedScene(dev)
+    torch.cuda.synchronize()
+    ev[0].record(stream)
+    b.compute_silhouettes()
+    b.build_bvh()
+    ev[1].record(stream)
+    bi, bd = b.query_nearest_batch(M, P)
+    ev[2].record(stream)
+    bs, be = b.query_silhouette_batch(M, P)
+    ev[3].record(stream)
+    torch.cuda.synchronize()
+    batched = [ev[0].elapsed_time(ev[1]), ev[1].elapsed_time(ev[2]), ev[2].elapsed_time(ev[3])]
+    # one scene per mesh, on the first eighth of each mesh's queries (x 1 triangles;
+    # the per-mesh silhouette launches of the full set take minutes), against the
+    # batched launches on the same subset
+    sub = [p_[: max(1, len(p_) // 8)] for p_ in pts]
+    Ps, Ms = torch.cat(sub), torch.cat([m_[: len(p_)] for m_, p_ in zip(mid, sub)])
+    ns = len(Ps)
+    e = [torch.cuda.Event(enable_timing=True) for _ in range(6)]
+    e[0].record(stream)
+    si, sd = b.query_nearest_batch(Ms, Ps)
+    e[1].record(stream)
+    ss, se = b.query_silhouette_batch(Ms, Ps)
+    e[2].record(stream)
+    scenes = [snch.Scene(v, f) for v, f in dev]
+    torch.cuda.synchronize()
+    e[3].record(stream)
+    for s_ in scenes:
+        s_.compute_silhouettes()
+        s_.build_bvh()
+    e[4].record(stream)
+    outs = [s_.query_nearest(p_) for s_, p_ in zip(scenes, sub)]
+    e5 = torch.cuda.Event(enable_timing=True)
+    e5.record(stream)
+    outs2 = [s_.query_silhouette(p_) for s_, p_ in zip(scenes, sub)]
+    e[5].record(stream)
+    torch.cuda.synchronize()
+    single = [e[3].elapsed_time(e[4]), e[4].elapsed_time(e5), e5.elapsed_time(e[5])]
+    bsub = [e[0].elapsed_time(e[1]), e[1].elapsed_time(e[2])]
+    same = (torch.equal(si, torch.cat([o[0] for o in outs]).view(torch.int32))
+            and torch.equal(sd.view(torch.int32), torch.cat([o[1] for o in outs]).view(torch.int32))
+            and torch.equal(ss.view(torch.int32), torch.cat([o[0] for o in outs2]).view(torch.int32))
+            and torch.equal(se, torch.cat([o[1] for o in outs2])))
+    status = b.device_status()
+    for s_ in scenes:
+        s_.close()
+    b.close()
+    return {"workload": f"{len(ms)} meshes, {sum(len(f) for _, f in ms):,} triangles, {n:,} nearest + {n:,} "
+                        f"silhouette queries ({per_tri * scale:g} x triangles per mesh, uniform in the mesh's box "
+                        f"x 1.2)",
+            "batched_ms": {"build": batched[0], "near": batched[1], "sil": batched[2]},
+            "batched_qps": {"near": n / (batched[1] / 1e3), "sil": n / (batched[2] / 1e3)},
+            "subset": f"{ns:,} queries per type (the first eighth of each mesh's)",
+            "per_mesh_ms": {"build": single[0], "near": single[1], "sil": single[2]},
+            "per_mesh_qps": {"near": ns / (single[1] / 1e3), "sil": ns / (single[2] / 1e3)},
+            "batched_subset_qps": {"near": ns / (bsub[0] / 1e3), "sil": ns / (bsub[1] / 1e3)},
+            "build_speedup": single[0] / batched[0],
+            "identical_to_per_mesh": bool(same), "device_status": int(status)}
+
+
+# --------------------------------------------------------------------- walk-on-stars
+def wost_leg(scale, walkers=1_000_000, max_steps=128):
+    """Wavefront walk-on-stars on the 20,480-triangle noisy icosphere with 50/50
+    Dirichlet/Neumann faces: 1M walkers from the ball of radius 0.95, up to 128
+    steps, one nearest + silhouette + ray + sphere-sample query per live walker
+    and step; plain vs learned radius (trained on the walk's own distances).
+    Per-step queries/s; estimates compared bit for bit."""
+    import torch
+    from snch_lbvh_gb300 import meshes, wost
+    from snch_lbvh_gb300.learned import LearnedRadius, training_points
+    v, f = meshes.noisy_icosphere(5, 1.0, 0.01, seed=0)
+    flags = (np.random.default_rng(1).random(len(f)) < 0.5).astype(np.uint8)
+    d, nsc = wost.split_boundary(v, f, flags)
+    n = max(1024, int(walkers * scale))
+    pts = torch.from_numpy(training_points(v, f, max(4096, int(4_000_000 * scale)), max(4096, int(4_000_000 * scale)),
+                                           0.05, lo=(-1.2, -1.2, -1.2), hi=(1.2, 1.2, 1.2), seed=9)).cuda()
+    _, dd = d.query_nearest(pts)
+    ds, _ = nsc.query_silhouette(pts)
+    t = torch.stack([dd, ds], 1)
+    t = torch.log(torch.where(torch.isfinite(t) & (t > 0), t, torch.full_like(t, float("nan"))))
+    model = LearnedRadius(np.full(3, -1.2), np.full(3, 1.2), seed=4)
+    t0 = time.perf_counter()
+    model.train(pts, t, epochs=6, batch=65536, lr=2e-3, tau=0.9)
+    train_s = time.perf_counter() - t0
+    wost.trace(d, nsc, min(n, 65536), max_steps=4, seed=1)  # warm-up
+    e0, x0, s0 = wost.trace(d, nsc, n, max_steps=max_steps, seed=3)
+    e1, _, s1 = wost.trace(d, nsc, n, max_steps=max_steps, seed=3, model=model, margin=1.5)
+    err = (e0 - x0[:, 0]).double()
+    q0, q1 = sum(s0["queries"]), sum(s1["queries"])
+    res = {"workload": f"{n:,} walkers, <= {max_steps} steps, 20,480-triangle icosphere, 50/50 Dirichlet/Neumann faces",
+           "steps": s0["steps"], "terminated_frac": s0["terminated"] / n, "queries": q0,
+           "plain": {"query_qps": q0 / (sum(s0["query_ms"]) / 1e3), "step_qps": q0 / (sum(s0["step_ms"]) / 1e3)},
+           "learned": {"query_qps": q1 / (sum(s1["query_ms"]) / 1e3), "step_qps": q1 / (sum(s1["step_ms"]) / 1e3),
+                       "fallback_frac": sum(s1["fallback"]) / max(1, 2 * sum(s1["live"])), "train_s": train_s},
+           "identical_estimates": bool(torch.equal(e0.view(torch.int32), e1.view(torch.int32))),
+           "estimate_error": {"mean": float(err.mean()), "std": float(err.std())},
+           "per_step_live": s0["live"][:8] + ["..."] + s0["live"][-3:],
+           "per_step_qps_plain": [round(q / (m / 1e3)) for q, m in zip(s0["queries"][:8], s0["step_ms"][:8])]}
+    model.close()
+    return res
+
+
 # --------------------------------------------------------------------- reference arm
 def run_reference(args):
     ws, rank, _ = dist_env()
@@ -498,6 +627,13 @@ def run_ours(args):
                               "sil": learned["sil_qps"] / per_type["sil"]}
         learned["status"] = int(scene.device_status())
 
+    # ---- batched meshes and walk-on-stars (single GPU only; outside the timed step)
+    batched = wost_res = None
+    if ws == 1 and not args.no_batched:
+        batched = batched_leg(args.scale)
+    if ws == 1 and not args.no_wost:
+        wost_res = wost_leg(args.scale)
+
     # ---- e2e through the host-buffer C ABI
     e2e = None
     if not args.no_e2e:
@@ -592,6 +728,8 @@ def run_ours(args):
         "roofline": roof,
         "e2e": e2e,
         "learned": learned,
+        "batched": batched,
+        "wost": wost_res,
     }
     if cpu is not None:
         smp = cpu["sample"]

@@ -182,3 +182,27 @@ def wost_queries(n_near: int, n_sil: int, n_ray: int, n_smp: int, seed: int = 1)
     q["smp_r"] = np.exp(rng.uniform(math.log(1e-3), math.log(0.5), n_smp)).astype(np.float32)
     q["smp_u"] = rng.random(n_smp, dtype=np.float32)
     return q
+
+
+def batched_meshes(seed: int = 5, count: int = 256, lo: float = 1e3, hi: float = 5e5):
+    """Independent meshes of the batched workload: alternating noisy icospheres
+    and tori, triangle counts log-uniform in [lo, hi] (icospheres: the nearest
+    subdivision level, 20 * 4^L faces; tori: nu x nv quads with nv = nu / 2),
+    noise sigma = 0.5 % of the mesh's size, each placed in the unit cube.
+    Returns a list of (float32 vertices, int32 faces)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(count):
+        target = float(np.exp(rng.uniform(np.log(lo), np.log(hi))))
+        major = rng.uniform(0.1, 0.5)
+        sub = int(rng.integers(0, 2**31 - 1))
+        if k % 2 == 0:
+            level = int(np.clip(np.rint(np.log(target / 20.0) / np.log(4.0)), 1, 7))
+            v, f = noisy_icosphere(level, major, 0.005 * 2.0 * major, sub)
+        else:
+            nu = max(6, int(round(np.sqrt(target))))
+            nv = max(3, int(round(target / (2.0 * nu))))
+            minor = 0.25 * major
+            v, f = noisy_torus(major, minor, nu, nv, 0.005 * 2.0 * (major + minor), sub)
+        out.append((place_in_unit_cube(v, rng).astype(np.float32), f.astype(np.int32)))
+    return out
