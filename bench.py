@@ -348,10 +348,10 @@ def batched_leg(scale, per_tri=8):
     ev[3].record(stream)
     torch.cuda.synchronize()
     batched = [ev[0].elapsed_time(ev[1]), ev[1].elapsed_time(ev[2]), ev[2].elapsed_time(ev[3])]
-    # one scene per mesh, on the first eighth of each mesh's queries (x 1 triangles;
-    # the per-mesh silhouette launches of the full set take minutes), against the
-    # batched launches on the same subset
-    sub = [p_[: max(1, len(p_) // 8)] for p_ in pts]
+    # one scene per mesh, on the first 1/32 of each mesh's queries (a quarter of its
+    # triangle count; the per-mesh silhouette launches of the full set take minutes),
+    # against the batched launches on the same subset
+    sub = [p_[: max(1, len(p_) // 32)] for p_ in pts]
     Ps, Ms = torch.cat(sub), torch.cat([m_[: len(p_)] for m_, p_ in zip(mid, sub)])
     ns = len(Ps)
     e = [torch.cuda.Event(enable_timing=True) for _ in range(6)]
@@ -388,7 +388,7 @@ def batched_leg(scale, per_tri=8):
                         f"x 1.2)",
             "batched_ms": {"build": batched[0], "near": batched[1], "sil": batched[2]},
             "batched_qps": {"near": n / (batched[1] / 1e3), "sil": n / (batched[2] / 1e3)},
-            "subset": f"{ns:,} queries per type (the first eighth of each mesh's)",
+            "subset": f"{ns:,} queries per type (the first 1/32 of each mesh's)",
             "per_mesh_ms": {"build": single[0], "near": single[1], "sil": single[2]},
             "per_mesh_qps": {"near": ns / (single[1] / 1e3), "sil": ns / (single[2] / 1e3)},
             "batched_subset_qps": {"near": ns / (bsub[0] / 1e3), "sil": ns / (bsub[1] / 1e3)},

@@ -24,7 +24,7 @@ __all__ = ["Scene", "BatchedScene", "SnchError", "BvhView", "lib"]
 INVALID = 0xFFFFFFFF
 TRAVERSAL_NEAR_FIRST = 0
 TRAVERSAL_REFERENCE_ORDER = 1
-OPT_TRAVERSAL, OPT_QUERY_ORDER, OPT_ORDER_MIN_BATCH, OPT_PERSISTENT = 1, 2, 3, 4
+OPT_TRAVERSAL, OPT_QUERY_ORDER, OPT_ORDER_MIN_BATCH, OPT_PERSISTENT, OPT_TAIL_CAP = 1, 2, 3, 4, 5
 
 
 def _torch():

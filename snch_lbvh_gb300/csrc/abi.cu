@@ -86,6 +86,7 @@ struct snch_scene_s
     int query_order = 1;             // Morton-sort batches of at least order_min queries
     int64_t order_min = 65536;
     int persistent = 0;              // lane-refill nearest/silhouette kernels (measured slower: off)
+    int64_t tail_cap = 0;            // near-first expansions before a query is deferred (0: off; measured slower)
     // batched scene (num_meshes > 0): independent meshes, one build, per-mesh queries
     uint32_t num_meshes = 0;
     uint32_t *tri_mesh = nullptr, *mesh_tri_start = nullptr, *mesh_box = nullptr, *sorted_mesh = nullptr,
@@ -348,37 +349,74 @@ cudaError_t batch_view(const snch_scene_s *s, const float *keys_from, int64_t n,
     return e;
 }
 
-// Seeded pass over the batch, then the unbounded pass over the queries that
-// found nothing inside their radius (listed by the seeded kernel itself).
+// One nearest / silhouette batch in up to three passes:
+//   1. the batch (Morton-ordered), seeded with `radius` if given, near-first
+//      searches capped at tail_cap expansions (the long ones are deferred with
+//      the best distance they had);
+//   2. the deferred queries, seeded with that distance (same results);
+//   3. with a user radius: the queries with nothing inside it, unbounded.
+// Every pass reads its query list and count on the device: no host sync.
 template <typename Launch>
-int run_seeded(snch_scene_s *s, const float *pts, const float *radius, int64_t n, uint32_t *num_fallback,
-               cudaStream_t st, Launch launch)
+int run_query(snch_scene_s *s, const float *pts, const float *radius, int64_t n, uint32_t *num_fallback,
+              cudaStream_t st, Launch launch, const uint32_t *query_mesh = nullptr)
 {
-    char *scratch = nullptr;
-    SNCH_CUDA(cudaMallocAsync(reinterpret_cast<void **>(&scratch), 4 * (size_t)n + 256, st));
-    uint32_t *count = reinterpret_cast<uint32_t *>(scratch);
-    uint32_t *list = reinterpret_cast<uint32_t *>(scratch + 256);
-    cudaError_t e = cudaMemsetAsync(count, 0, 4, st);
-    if (e == cudaSuccess)
+    const bool capped = s->tail_cap > 0 && s->traversal == SNCH_TRAVERSAL_NEAR_FIRST && !s->persistent;
+    BatchView b;
+    if (!capped && !radius)
     {
-        BatchView b;
-        e = batch_view(s, pts, n, st, b);
-        SeedArgs seed;
-        seed.radius = radius;
-        seed.fail_list = list;
-        seed.fail_count = count;
-        if (e == cudaSuccess)
-            e = launch(b.t, seed);
-        if (e == cudaSuccess)
-        {
-            TreeView fallback = s->view();
-            fallback.order = list;
-            fallback.order_count = count;
-            e = launch(fallback, SeedArgs());
-        }
-        if (e == cudaSuccess && num_fallback)
-            e = cudaMemcpyAsync(num_fallback, count, 4, cudaMemcpyDeviceToDevice, st);
+        SNCH_CUDA(batch_view(s, pts, n, st, b, query_mesh));
+        SNCH_CUDA(launch(b.t, SeedArgs()));
+        return SNCH_OK;
     }
+    char *scratch = nullptr;
+    const size_t lists = (radius ? 1 : 0) + (capped ? 3 : 0);
+    SNCH_CUDA(cudaMallocAsync(reinterpret_cast<void **>(&scratch), 256 + lists * (4 * (size_t)n + 256), st));
+    uint32_t *fail_count = reinterpret_cast<uint32_t *>(scratch), *defer_count = fail_count + 1;
+    char *next = scratch + 256;
+    auto take = [&]() {
+        char *q = next;
+        next += 4 * (size_t)n + 256;
+        return q;
+    };
+    uint32_t *fail_list = radius ? reinterpret_cast<uint32_t *>(take()) : nullptr;
+    uint32_t *defer_list = capped ? reinterpret_cast<uint32_t *>(take()) : nullptr;
+    float *defer_radius = capped ? reinterpret_cast<float *>(take()) : nullptr;
+    cudaError_t e = cudaMemsetAsync(scratch, 0, 256, st);
+    if (e == cudaSuccess)
+        e = batch_view(s, pts, n, st, b, query_mesh);
+    SeedArgs s1;
+    s1.radius = radius;
+    s1.fail_list = fail_list;
+    s1.fail_count = radius ? fail_count : nullptr;
+    if (capped)
+    {
+        s1.cap = (uint32_t)s->tail_cap;
+        s1.defer_list = defer_list;
+        s1.defer_count = defer_count;
+        s1.defer_radius = defer_radius;
+    }
+    if (e == cudaSuccess)
+        e = launch(b.t, s1);
+    if (e == cudaSuccess && capped)
+    {
+        TreeView t2 = b.t;
+        t2.order = defer_list;
+        t2.order_count = defer_count;
+        SeedArgs s2;
+        s2.radius = defer_radius;
+        s2.fail_list = fail_list;
+        s2.fail_count = radius ? fail_count : nullptr;
+        e = launch(t2, s2);
+    }
+    if (e == cudaSuccess && radius)
+    {
+        TreeView t3 = b.t;
+        t3.order = fail_list;
+        t3.order_count = fail_count;
+        e = launch(t3, SeedArgs());
+    }
+    if (e == cudaSuccess && num_fallback)
+        e = cudaMemcpyAsync(num_fallback, fail_count, 4, cudaMemcpyDeviceToDevice, st);
     cudaFreeAsync(scratch, st);
     SNCH_CUDA(e);
     return SNCH_OK;
@@ -633,6 +671,11 @@ int snch_set_option(snch_scene_t s, int option, int64_t value)
             return fail(SNCH_ERR_INVALID_ARGUMENT, "SNCH_OPT_ORDER_MIN_BATCH must be >= 0");
         s->order_min = value;
         return SNCH_OK;
+    case SNCH_OPT_TAIL_CAP:
+        if (value < 0 || value > (int64_t(1) << 30))
+            return fail(SNCH_ERR_INVALID_ARGUMENT, "SNCH_OPT_TAIL_CAP must be in [0, 2^30]");
+        s->tail_cap = value;
+        return SNCH_OK;
     case SNCH_OPT_PERSISTENT:
         if (value != 0 && value != 1)
             return fail(SNCH_ERR_INVALID_ARGUMENT, "SNCH_OPT_PERSISTENT takes 0 or 1");
@@ -761,10 +804,11 @@ int snch_query_nearest(snch_scene_t s, const float *pts, int64_t n, uint32_t *id
         rc = check_n(n, {pts, idx, dist});
     if (rc != SNCH_OK)
         return rc;
-    BatchView b;
-    SNCH_CUDA(batch_view(s, pts, n, S(stream), b));
-    SNCH_CUDA(launch_nearest(b.t, pts, n, idx, dist, S(stream)));
-    return SNCH_OK;
+    if (n == 0)
+        return SNCH_OK;
+    return run_query(s, pts, nullptr, n, nullptr, S(stream), [&](const TreeView &t, const SeedArgs &seed) {
+        return launch_nearest(t, pts, n, idx, dist, S(stream), nullptr, seed);
+    });
 }
 
 int snch_query_silhouette(snch_scene_t s, const float *pts, const uint8_t *flip, int64_t n, float *dist, int32_t *edge,
@@ -775,10 +819,11 @@ int snch_query_silhouette(snch_scene_t s, const float *pts, const uint8_t *flip,
         rc = check_n(n, {pts, dist});
     if (rc != SNCH_OK)
         return rc;
-    BatchView b;
-    SNCH_CUDA(batch_view(s, pts, n, S(stream), b));
-    SNCH_CUDA(launch_silhouette(b.t, pts, flip, n, dist, edge, S(stream)));
-    return SNCH_OK;
+    if (n == 0)
+        return SNCH_OK;
+    return run_query(s, pts, nullptr, n, nullptr, S(stream), [&](const TreeView &t, const SeedArgs &seed) {
+        return launch_silhouette(t, pts, flip, n, dist, edge, S(stream), nullptr, seed);
+    });
 }
 
 int snch_query_ray(snch_scene_t s, const float *o, const float *d, const float *tmax, int64_t n, uint8_t *hit, float *t,
@@ -910,7 +955,7 @@ int snch_query_nearest_seeded(snch_scene_t s, const float *pts, const float *rad
         rc = check_n(n, {pts, radius, idx, dist});
     if (rc != SNCH_OK || n == 0)
         return rc;
-    return run_seeded(s, pts, radius, n, num_fallback, S(stream), [&](const TreeView &t, const SeedArgs &seed) {
+    return run_query(s, pts, radius, n, num_fallback, S(stream), [&](const TreeView &t, const SeedArgs &seed) {
         return launch_nearest(t, pts, n, idx, dist, S(stream), nullptr, seed);
     });
 }
@@ -923,7 +968,7 @@ int snch_query_silhouette_seeded(snch_scene_t s, const float *pts, const uint8_t
         rc = check_n(n, {pts, radius, dist});
     if (rc != SNCH_OK || n == 0)
         return rc;
-    return run_seeded(s, pts, radius, n, num_fallback, S(stream), [&](const TreeView &t, const SeedArgs &seed) {
+    return run_query(s, pts, radius, n, num_fallback, S(stream), [&](const TreeView &t, const SeedArgs &seed) {
         return launch_silhouette(t, pts, flip, n, dist, edge, S(stream), nullptr, seed);
     });
 }
@@ -1243,10 +1288,12 @@ int snch_batch_query_nearest(snch_scene_t s, const int32_t *mesh, const float *p
         rc = check_n(n, {mesh, pts, idx, dist});
     if (rc != SNCH_OK || n == 0)
         return rc;
-    BatchView b;
-    SNCH_CUDA(batch_view(s, pts, n, S(stream), b, reinterpret_cast<const uint32_t *>(mesh)));
-    SNCH_CUDA(launch_nearest(b.t, pts, n, reinterpret_cast<uint32_t *>(idx), dist, S(stream)));
-    return SNCH_OK;
+    return run_query(
+        s, pts, nullptr, n, nullptr, S(stream),
+        [&](const TreeView &t, const SeedArgs &seed) {
+            return launch_nearest(t, pts, n, reinterpret_cast<uint32_t *>(idx), dist, S(stream), nullptr, seed);
+        },
+        reinterpret_cast<const uint32_t *>(mesh));
 }
 
 int snch_batch_query_silhouette(snch_scene_t s, const int32_t *mesh, const float *pts, const uint8_t *flip,
@@ -1259,10 +1306,12 @@ int snch_batch_query_silhouette(snch_scene_t s, const int32_t *mesh, const float
         rc = check_n(n, {mesh, pts, dist});
     if (rc != SNCH_OK || n == 0)
         return rc;
-    BatchView b;
-    SNCH_CUDA(batch_view(s, pts, n, S(stream), b, reinterpret_cast<const uint32_t *>(mesh)));
-    SNCH_CUDA(launch_silhouette(b.t, pts, flip, n, dist, edge, S(stream)));
-    return SNCH_OK;
+    return run_query(
+        s, pts, nullptr, n, nullptr, S(stream),
+        [&](const TreeView &t, const SeedArgs &seed) {
+            return launch_silhouette(t, pts, flip, n, dist, edge, S(stream), nullptr, seed);
+        },
+        reinterpret_cast<const uint32_t *>(mesh));
 }
 
 int snch_selfcheck_cone_filter(int64_t n, uint64_t seed, uint64_t *device_counts, snch_stream_t stream)

@@ -647,6 +647,14 @@ __global__ void __launch_bounds__(256) rank_kernel(BuildArgs a)
         node = p;
     }
     a.leaves[j].v2.w = __uint_as_float(r);
+    // the leaf's rank and owned-edge count in its parent's traversal record
+    const uint32_t p = n > 1 ? a.nodes[ni + j].parent : kInvalid;
+    if (p < ni)
+    {
+        const uint32_t info = (r & kLeafRankMask) | (__float_as_uint(a.leaves[j].v1.w) << 30);
+        float *d = reinterpret_cast<float *>(&a.inner[p].d);
+        d[a.nodes[p].left == ni + j ? 2 : 3] = __uint_as_float(info);
+    }
 }
 
 // Objects in the reference's device layout (scene.cuh:708-722 silhouette_edge,

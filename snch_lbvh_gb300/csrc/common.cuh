@@ -57,10 +57,14 @@ struct NodeRec
 // (four 16-B vector loads) instead of the reference's four scattered records.
 //   a = (L.upper.xyz, L.lower.x)  b = (L.lower.yz, R.upper.xy)
 //   c = (R.upper.z, R.lower.xyz)  d = (bits L, bits R, 0, 0)
+// d = (bits L, bits R, leaf info of L, leaf info of R); a leaf child's info is
+// its DFS rank | owned-edge count << 30 (written by the rank pass), so the
+// silhouette traversal reaches a leaf's edges without reading its LeafRec.
 struct alignas(64) InnerRec
 {
     float4 a, b, c, d;
 };
+constexpr uint32_t kLeafRankMask = (1u << 30) - 1u;
 // Child cones of an internal node (silhouette traversal), 48 B:
 //   a = (L.axis.xyz, L.half)  b = (L.radius, R.axis.xyz)  c = (R.half, R.radius, 0, 0)
 struct alignas(16) InnerConeRec
@@ -135,8 +139,18 @@ SNCH_DEV QueryRoot query_root(const TreeView &t, int64_t q)
 struct SeedArgs
 {
     const float *radius = nullptr;   // nullptr: unbounded
-    uint32_t *fail_list = nullptr;   // query indices with an empty seeded result
+    uint32_t *fail_list = nullptr;   // query indices with an empty seeded result (finite radius)
     uint32_t *fail_count = nullptr;
+    // Tail cap (near-first kernels): a query still searching after `cap` node
+    // expansions stops, writes the distance of the best candidate it has (an
+    // upper bound of its answer; +inf if none) to defer_radius[q] and is listed
+    // in defer_list; a second, seeded pass over the list finishes it with the
+    // same result. The warps of the first pass no longer wait for their slowest
+    // lane, and the second pass runs the long searches densely, tightly bounded.
+    uint32_t cap = 0;                // 0: no cap
+    uint32_t *defer_list = nullptr;
+    uint32_t *defer_count = nullptr;
+    float *defer_radius = nullptr;
 };
 
 // index of the query answered by global thread i
@@ -241,6 +255,11 @@ SNCH_DEV void unpack_inner(const InnerRec &r, Box &l, Box &rb, uint32_t &L, uint
     rb.lower = mk(r.c.y, r.c.z, r.c.w);
     L = __float_as_uint(r.d.x);
     R = __float_as_uint(r.d.y);
+}
+SNCH_DEV void unpack_leaf_info(const InnerRec &r, uint32_t &Linfo, uint32_t &Rinfo)
+{
+    Linfo = __float_as_uint(r.d.z);
+    Rinfo = __float_as_uint(r.d.w);
 }
 SNCH_DEV InnerRec pack_inner(const Box &l, const Box &r, uint32_t L, uint32_t R)
 {

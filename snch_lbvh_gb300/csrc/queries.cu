@@ -580,9 +580,15 @@ SNCH_DEV void leaf_nearest_fast(const TreeView &t, uint32_t pos, f3 p, float &be
     }
 }
 
-// (128, 10): at most 48 registers, ten blocks per SM. The traversals wait on
-// dependent L2 loads; the extra resident warps hide more of that latency
-// (measured on the 2M-triangle scene: silhouette -6 %, nearest -2 %).
+// Child records the traversal may expand next are requested into L1 before
+// the leaf work of this node runs, so their latency overlaps it.
+constexpr bool kPrefetchChildren = true;
+SNCH_DEV void prefetch_l1(const void *p) { asm volatile("prefetch.global.L1 [%0];" ::"l"(p)); }
+
+// (128, 10): at most 48 registers, ten blocks per SM (silhouette: (128, 9), 56
+// registers, nine blocks). The traversals wait on dependent L2 loads; the extra
+// resident warps hide more of that latency (measured on the 2M-triangle scene:
+// silhouette -12 %, nearest -2 % against 60 registers / eight blocks).
 template <bool kStats>
 __global__ void __launch_bounds__(128, 10) nearest_fast_kernel(TreeView t, const float *__restrict__ pts, int64_t n,
                                                            uint32_t *__restrict__ out_idx, float *__restrict__ out_dist,
@@ -595,12 +601,14 @@ __global__ void __launch_bounds__(128, 10) nearest_fast_kernel(TreeView t, const
     const int64_t q = query_index(t, qi);
     const f3 p = load_point(pts, q);
     uint32_t nearest = kInvalid, best_rank = 0;
-    float best = INFINITY;
+    float best = INFINITY, r0 = INFINITY;
     if (seed.radius)
     {
-        const float r = __ldg(seed.radius + q);
-        best = r * r;
+        r0 = __ldg(seed.radius + q);
+        best = r0 * r0;
     }
+    bool deferred = false;
+    uint32_t budget = seed.cap ? seed.cap : 0xFFFFFFFFu;
     const uint32_t ni = t.num_tris - 1;
     const QueryRoot qr = query_root(t, q);
     if (qr.node == kInvalid)
@@ -620,6 +628,11 @@ __global__ void __launch_bounds__(128, 10) nearest_fast_kernel(TreeView t, const
         bool live = !(mindist(load_root_box(t.aabbs + qr.node), p) > best);
         while (live)
         {
+            if (!kStats && budget-- == 0)
+            {
+                deferred = true;
+                break;
+            }
             Box lb, rb;
             uint32_t L, R;
             unpack_inner(load_inner(t.inner + node), lb, rb, L, R);
@@ -628,6 +641,13 @@ __global__ void __launch_bounds__(128, 10) nearest_fast_kernel(TreeView t, const
             const float Lmd = mindist(lb, p), Rmd = mindist(rb, p);
             const float Lmm = minmaxdist(lb, p), Rmm = minmaxdist(rb, p);
             const bool aL = Lmd <= Rmm, aR = Rmd <= Lmm;  // query.cuh:279, 297
+            if (kPrefetchChildren)
+            {
+                if (aL && L < ni && Lmd <= best)
+                    prefetch_l1(t.inner + L);
+                if (aR && R < ni && Rmd <= best)
+                    prefetch_l1(t.inner + R);
+            }
             if (aL && L >= ni && Lmd <= best)
             {
                 leaf_nearest_fast(t, L - ni, p, best, best_rank, nearest);
@@ -681,12 +701,20 @@ __global__ void __launch_bounds__(128, 10) nearest_fast_kernel(TreeView t, const
         stats[3 * q + 1] = n_leaf;
         stats[3 * q + 2] = 0;
     }
+    if (deferred)
+    {
+        // the bound handed to the second pass: a float whose square is >= best
+        seed.defer_radius[q] = best < INFINITY ? nextafterf(sqrtf(best), INFINITY) : INFINITY;
+        append_failed(seed.defer_list, seed.defer_count, (uint32_t)q, true);
+        return;
+    }
+    const bool failed = seed.radius && nearest == kInvalid && r0 < INFINITY;
     if (seed.radius && nearest == kInvalid)
         best = INFINITY;  // nothing within the seed radius: the fallback pass answers it
     out_idx[q] = nearest == kInvalid ? kInvalid : nearest - qr.tri_off;
     out_dist[q] = sqrtf(best);
     if (seed.fail_list)
-        append_failed(seed.fail_list, seed.fail_count, (uint32_t)q, nearest == kInvalid);
+        append_failed(seed.fail_list, seed.fail_count, (uint32_t)q, failed);
 }
 
 // one leaf of the silhouette query; key = rank * 4 + slot orders candidates
@@ -727,8 +755,45 @@ SNCH_DEV void leaf_silhouette_fast(const TreeView &t, uint32_t pos, f3 o, bool f
     }
 }
 
+// the same for a leaf reached through its parent: rank and owned-edge count
+// come from the parent's record (InnerRec.d), not from the LeafRec
+SNCH_DEV void leaf_silhouette_info(const TreeView &t, uint32_t pos, uint32_t info, f3 o, bool flip, float &best,
+                                   uint32_t &best_key, int32_t &best_edge, uint32_t &n_edge)
+{
+    const uint32_t n_owned = info >> 30;
+    const uint32_t rank = info & kLeafRankMask;
+    n_edge += n_owned;
+    for (uint32_t k = 0; k < n_owned; ++k)
+    {
+        const float4 *e = reinterpret_cast<const float4 *>(t.edges + 3 * (uint64_t)pos + k);
+        const float4 ea = __ldg(e), eb = __ldg(e + 1);
+        const f3 pa = mk(ea.x, ea.y, ea.z), pb = mk(eb.x, eb.y, eb.z);
+        f3 cp;
+        const float d = closest_point_segment(pa, pb, o, cp);
+        if (d > best)
+            continue;
+        const uint32_t flags = __float_as_uint(ea.w);
+        bool is_sil = (flags & 1u) == 0u || (flags & 2u) == 0u;
+        if (!is_sil)
+        {
+            const float4 ec = __ldg(e + 2), ed = __ldg(e + 3);
+            is_sil = is_silhouette_edge(pa, pb, mk(ec.x, ec.y, ec.z), mk(ed.x, ed.y, ed.z),
+                                        mk(o.x - cp.x, o.y - cp.y, o.z - cp.z), d, flip);
+        }
+        if (!is_sil)
+            continue;
+        const uint32_t key = rank * 4u + k;
+        if (d < best || best_edge < 0 || (d > 0.0f ? key > best_key : key < best_key))
+        {
+            best = d;
+            best_key = key;
+            best_edge = __float_as_int(eb.w);
+        }
+    }
+}
+
 template <bool kStats>
-__global__ void __launch_bounds__(128, 10) silhouette_fast_kernel(TreeView t, const float *__restrict__ pts,
+__global__ void __launch_bounds__(128, 9) silhouette_fast_kernel(TreeView t, const float *__restrict__ pts,
                                                               const uint8_t *__restrict__ flips, int64_t n,
                                                               float *__restrict__ out_dist,
                                                               int32_t *__restrict__ out_edge,
@@ -741,9 +806,12 @@ __global__ void __launch_bounds__(128, 10) silhouette_fast_kernel(TreeView t, co
     const int64_t q = query_index(t, qi);
     const f3 p = load_point(pts, q);
     const bool flip = flips ? __ldg(flips + q) != 0 : false;
-    float best = seed.radius ? __ldg(seed.radius + q) : INFINITY;
+    const float r0 = seed.radius ? __ldg(seed.radius + q) : INFINITY;
+    float best = r0;
     uint32_t best_key = 0;
     int32_t best_edge = -1;
+    bool deferred = false;
+    uint32_t budget = seed.cap ? seed.cap : 0xFFFFFFFFu;
     const uint32_t ni = t.num_tris - 1;
     const QueryRoot qr = query_root(t, q);
     if (qr.node == kInvalid)
@@ -761,9 +829,16 @@ __global__ void __launch_bounds__(128, 10) silhouette_fast_kernel(TreeView t, co
         bool live = !(mindist(load_root_box(t.aabbs + qr.node), p) > best * best);
         while (live)
         {
+            if (!kStats && budget-- == 0)
+            {
+                deferred = true;
+                break;
+            }
             Box lb, rb;
-            uint32_t L, R;
-            unpack_inner(load_inner(t.inner + node), lb, rb, L, R);
+            uint32_t L, R, Linfo, Rinfo;
+            const InnerRec rec = load_inner(t.inner + node);
+            unpack_inner(rec, lb, rb, L, R);
+            unpack_leaf_info(rec, Linfo, Rinfo);
             const float4 *cr = reinterpret_cast<const float4 *>(t.inner_cones + node);
             InnerConeRec icr;
             icr.a = __ldg(cr);
@@ -777,15 +852,28 @@ __global__ void __launch_bounds__(128, 10) silhouette_fast_kernel(TreeView t, co
             const bool hitR = Rmd <= b2 && rc.half_angle >= 0.0f && cone_test(rc, p, rb, Rmd);
             if (kStats)
                 ++n_int;
+            if (kPrefetchChildren)
+            {
+                if (hitL && L < ni)
+                {
+                    prefetch_l1(t.inner + L);
+                    prefetch_l1(t.inner_cones + L);
+                }
+                if (hitR && R < ni)
+                {
+                    prefetch_l1(t.inner + R);
+                    prefetch_l1(t.inner_cones + R);
+                }
+            }
             if (hitL && L >= ni)
             {
-                leaf_silhouette_fast(t, L - ni, p, flip, best, best_key, best_edge, n_edge);
+                leaf_silhouette_info(t, L - ni, Linfo, p, flip, best, best_key, best_edge, n_edge);
                 if (kStats)
                     ++n_leaf;
             }
             if (hitR && R >= ni)
             {
-                leaf_silhouette_fast(t, R - ni, p, flip, best, best_key, best_edge, n_edge);
+                leaf_silhouette_info(t, R - ni, Rinfo, p, flip, best, best_key, best_edge, n_edge);
                 if (kStats)
                     ++n_leaf;
             }
@@ -825,13 +913,20 @@ __global__ void __launch_bounds__(128, 10) silhouette_fast_kernel(TreeView t, co
             }
         }
     }
+    if (deferred)
+    {
+        seed.defer_radius[q] = best;  // best candidate so far, or the seed radius
+        append_failed(seed.defer_list, seed.defer_count, (uint32_t)q, true);
+        return;
+    }
+    const bool failed = seed.radius && best_edge < 0 && r0 < INFINITY;
     if (seed.radius && best_edge < 0)
         best = INFINITY;  // nothing within the seed radius: the fallback pass answers it
     out_dist[q] = best;
     if (out_edge)
         out_edge[q] = best_edge < 0 ? best_edge : best_edge - qr.edge_off;
     if (seed.fail_list)
-        append_failed(seed.fail_list, seed.fail_count, (uint32_t)q, best_edge < 0);
+        append_failed(seed.fail_list, seed.fail_count, (uint32_t)q, failed);
     if (kStats)
     {
         stats[3 * q] = n_int;
@@ -1175,18 +1270,18 @@ __global__ void __launch_bounds__(128) ray_kernel(TreeView t, const float *__res
     const uint32_t ni = t.num_tris - 1;
     if (t.num_tris > 0)
     {
+        // The closer hit child is processed next without a trip through the
+        // stack (the reference pushes it last and pops it at once, with the
+        // same bound check), so the visit order is the reference's.
         uint32_t sn[kStackDepth];
         float sd[kStackDepth];
-        int sp = 1;
-        sn[0] = 0;
-        sd[0] = INFINITY;
-        do
+        int sp = 0;
+        uint32_t node = 0;
+        float nd = INFINITY;
+        for (;;)
         {
-            --sp;
-            const uint32_t node = sn[sp];
-            if (sd[sp] > min_dist)
-                continue;
-            if (node >= ni)
+            bool next = !(nd > min_dist);
+            if (next && node >= ni)
             {
                 f3 pa, pb, pc;
                 uint32_t orig, n_owned;
@@ -1202,8 +1297,9 @@ __global__ void __launch_bounds__(128) ray_kernel(TreeView t, const float *__res
                     bv = vv;
                     nearest = orig;
                 }
+                next = false;
             }
-            else
+            else if (next)
             {
                 if (sp > kStackDepth - 2)
                 {
@@ -1235,24 +1331,25 @@ __global__ void __launch_bounds__(128) ray_kernel(TreeView t, const float *__res
                     sn[sp] = other;
                     sd[sp] = Rd;
                     ++sp;
-                    sn[sp] = closer;
-                    sd[sp] = Ld;
-                    ++sp;
+                    node = closer;
+                    nd = Ld;
+                    continue;
                 }
-                else if (Lh)
+                if (Lh || Rh)
                 {
-                    sn[sp] = L;
-                    sd[sp] = Ld;
-                    ++sp;
+                    node = Lh ? L : R;
+                    nd = Lh ? Ld : Rd;
+                    continue;
                 }
-                else if (Rh)
-                {
-                    sn[sp] = R;
-                    sd[sp] = Rd;
-                    ++sp;
-                }
+                next = false;
             }
-        } while (sp > 0);
+            // pop
+            if (sp == 0)
+                break;
+            --sp;
+            node = sn[sp];
+            nd = sd[sp];
+        }
     }
     out_hit[q] = found ? 1 : 0;
     out_t[q] = min_dist;

@@ -314,3 +314,33 @@ def test_fast_cone_test_agrees_with_exact(snch):
     assert agree + disagree + undecided == 4_000_000
     assert disagree == 0
     assert agree >= 0.5 * 4_000_000, (agree, undecided)
+
+
+@pytest.mark.parametrize("cap", [1, 7, 128])
+def test_tail_cap_does_not_change_results(snch, cap):
+    """Capped first pass + seeded second pass (SNCH_OPT_TAIL_CAP) equals the
+    uncapped searches, plain and seeded, on random points and exact-tie probes."""
+    from snch_lbvh_gb300 import meshes
+    v, f = meshes.noisy_icosphere(5, 1.0, 0.01, seed=0)
+    rng = np.random.default_rng(cap)
+    e = np.concatenate([f[:, [0, 1]], f[:, [1, 2]]])
+    mids = (0.5 * (v[e[:, 0]].astype(np.float64) + v[e[:, 1]])).astype(np.float32)
+    pts = np.concatenate([meshes.box_queries(v, 200_000, 1.2, seed=cap), v, mids]).astype(np.float32)
+    flip = (rng.random(len(pts)) < 0.5).astype(np.uint8)
+    radius = np.where(rng.random(len(pts)) < 0.5, 0.02, 0.5).astype(np.float32)
+    s = built_scene(snch, v, f)
+
+    def run():
+        i, d = s.query_nearest(pts)
+        sd, se = s.query_silhouette(pts, flip)
+        i2, d2 = s.query_nearest_seeded(pts, radius)
+        sd2, se2 = s.query_silhouette_seeded(pts, radius, flip)
+        return [x.cpu().numpy() for x in (i, d, sd, se, i2, d2, sd2, se2)]
+
+    s.set_option(snch.OPT_TAIL_CAP, 0)
+    a = run()
+    s.set_option(snch.OPT_TAIL_CAP, cap)
+    b = run()
+    for x, y in zip(a, b):
+        np.testing.assert_array_equal(x.view(np.uint8), y.view(np.uint8))
+    assert s.device_status() == 0

@@ -124,3 +124,26 @@ def test_persistent_equals_one_thread_per_query_full_scene(big):
     for x, y in zip(a, b):
         np.testing.assert_array_equal(x.view(np.uint8), y.view(np.uint8))
     assert s.device_status() == 0
+
+
+def test_tail_cap_full_scene(big):
+    """On the 2M-triangle scene: 2M nearest + 1M silhouette queries, uncapped vs
+    a cap of 32 expansions (most queries deferred) vs the default."""
+    import snch_lbvh_gb300 as snch
+    from snch_lbvh_gb300 import meshes
+    sc, s, _ = big
+    q = meshes.wost_queries(2_000_000, 1_000_000, 1, 1, seed=29)
+
+    def run():
+        i, d = s.query_nearest(q["near_pts"])
+        sd, se = s.query_silhouette(q["sil_pts"], q["sil_flip"])
+        return [x.cpu().numpy() for x in (i, d, sd, se)]
+
+    s.set_option(snch.OPT_TAIL_CAP, 0)
+    a = run()
+    for cap in (32, 128):
+        s.set_option(snch.OPT_TAIL_CAP, cap)
+        b = run()
+        for x, y in zip(a, b):
+            np.testing.assert_array_equal(x.view(np.uint8), y.view(np.uint8))
+    assert s.device_status() == 0
