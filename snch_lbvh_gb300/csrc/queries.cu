@@ -580,9 +580,11 @@ SNCH_DEV void leaf_nearest_fast(const TreeView &t, uint32_t pos, f3 p, float &be
     }
 }
 
-// Child records the traversal may expand next are requested into L1 before
-// the leaf work of this node runs, so their latency overlaps it.
-constexpr bool kPrefetchChildren = true;
+// Child records the traversal may expand next can be requested into L1 before
+// the leaf work of this node runs, to overlap their latency with it. Measured
+// 2 % slower on the 2M-triangle scene (the prefetched lines of the farther
+// child evict lines still in use), so off.
+constexpr bool kPrefetchChildren = false;
 SNCH_DEV void prefetch_l1(const void *p) { asm volatile("prefetch.global.L1 [%0];" ::"l"(p)); }
 
 // (128, 10): at most 48 registers, ten blocks per SM (silhouette: (128, 9), 56
