@@ -121,9 +121,24 @@ class scene3
         check(snch_sample_on_object(h_, index, u, v, n, points_xyz, stream));
     }
 
+    // seeded forms: same results as query_nearest / query_silhouette for any radii
+    void query_nearest_seeded(const float *points_xyz, const float *radius, int64_t n, uint32_t *index,
+                              float *distance, uint32_t *num_fallback = nullptr, snch_stream_t stream = nullptr) const
+    {
+        check(snch_query_nearest_seeded(h_, points_xyz, radius, n, index, distance, num_fallback, stream));
+    }
+    void query_silhouette_seeded(const float *points_xyz, const uint8_t *flip, const float *radius, int64_t n,
+                                 float *distance, int32_t *edge = nullptr, uint32_t *num_fallback = nullptr,
+                                 snch_stream_t stream = nullptr) const
+    {
+        check(snch_query_silhouette_seeded(h_, points_xyz, flip, radius, n, distance, edge, num_fallback, stream));
+    }
+    void set_option(int option, int64_t value) { check(snch_set_option(h_, option, value)); }
+
     snch_scene_t handle() const { return h_; }
 
-  private:
+  protected:
+    explicit scene3(snch_scene_t h) : h_(h) {}
     void reset()
     {
         if (h_)
@@ -132,6 +147,86 @@ class scene3
     }
     snch_scene_t h_ = nullptr;
     snch_bvh_view view_{};
+};
+
+// Many independent meshes in one scene (snch_batch_*): one build, one query
+// launch per type; results per mesh as a scene3 of that mesh alone gives.
+class batch3 : public scene3
+{
+  public:
+    // concatenated vertices / triangles (per-mesh vertex indices) and num_meshes + 1
+    // starts of each; device != 0: vertices and triangles are device buffers
+    batch3(const float *vertices_xyz, int64_t num_vertices, const int32_t *triangles, int64_t num_triangles,
+           const std::vector<int64_t> &mesh_vert_start, const std::vector<int64_t> &mesh_tri_start, int device = 0,
+           snch_stream_t stream = nullptr)
+        : scene3(create(vertices_xyz, num_vertices, triangles, num_triangles, mesh_vert_start, mesh_tri_start,
+                        device, stream))
+    {
+    }
+    int32_t num_meshes() const
+    {
+        int32_t m = 0;
+        check(snch_batch_num_meshes(h_, &m));
+        return m;
+    }
+    void query_nearest(const int32_t *mesh, const float *points_xyz, int64_t n, int32_t *index, float *distance,
+                       snch_stream_t stream = nullptr) const
+    {
+        check(snch_batch_query_nearest(h_, mesh, points_xyz, n, index, distance, stream));
+    }
+    void query_silhouette(const int32_t *mesh, const float *points_xyz, const uint8_t *flip, int64_t n,
+                          float *distance, int32_t *edge = nullptr, snch_stream_t stream = nullptr) const
+    {
+        check(snch_batch_query_silhouette(h_, mesh, points_xyz, flip, n, distance, edge, stream));
+    }
+
+  private:
+    static snch_scene_t create(const float *v, int64_t nv, const int32_t *t, int64_t nt,
+                               const std::vector<int64_t> &vs, const std::vector<int64_t> &ts, int device,
+                               snch_stream_t stream)
+    {
+        if (vs.size() != ts.size() || vs.size() < 2)
+            throw std::runtime_error("batch3: need num_meshes + 1 vertex and triangle starts");
+        snch_scene_t h = nullptr;
+        check(snch_batch_create(v, nv, t, nt, vs.data(), ts.data(), static_cast<int32_t>(vs.size() - 1), device, &h,
+                                stream));
+        return h;
+    }
+};
+
+// Learned search radius (snch_mlp_*): train on (point, log distance) pairs,
+// predict per-query radii for the seeded queries.
+class learned_radius
+{
+  public:
+    learned_radius(const float box_lo[3], const float box_hi[3], uint64_t seed = 0)
+    {
+        check(snch_mlp_create(box_lo, box_hi, seed, &h_));
+    }
+    learned_radius(const learned_radius &) = delete;
+    learned_radius &operator=(const learned_radius &) = delete;
+    ~learned_radius()
+    {
+        if (h_)
+            snch_mlp_destroy(h_);
+    }
+    // device points (n x 3) and targets (n x 2: log nearest, log silhouette distance; NaN = none)
+    float train(const float *points, const float *targets, int64_t n, int epochs = 1, int64_t batch = 65536,
+                float lr = 2e-3f, float tau = 0.9f, snch_stream_t stream = nullptr)
+    {
+        float loss = 0.f;
+        check(snch_mlp_train(h_, points, targets, n, epochs, batch, lr, tau, &loss, stream));
+        return loss;
+    }
+    void predict(const float *points, int64_t n, float *radius_near, float *radius_sil, float margin = 1.5f,
+                 float floor = 1e-4f, snch_stream_t stream = nullptr) const
+    {
+        check(snch_mlp_predict_radius(h_, points, n, margin, floor, radius_near, radius_sil, stream));
+    }
+    snch_mlp_t handle() const { return h_; }
+
+  private:
+    snch_mlp_t h_ = nullptr;
 };
 
 }  // namespace snch

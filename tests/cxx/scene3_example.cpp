@@ -60,8 +60,66 @@ int main(int argc, char **argv)
     // inradius of the icosahedron with unit circumradius
     const double r_in = std::sqrt((5.0 + 2.0 * std::sqrt(5.0)) / 15.0);
     std::printf("nearest idx=%u dist=%.7f expected=%.7f\n", idx, dist, r_in);
-    cudaFree(d_pts);
-    cudaFree(d_dist);
-    cudaFree(d_idx);
-    return (idx < 20 && std::fabs(dist - r_in) < 1e-5) ? 0 : 4;
+    if (!(idx < 20 && std::fabs(dist - r_in) < 1e-5))
+        return 4;
+
+    // two copies of the icosahedron in one batch: the second shifted by +3 in x;
+    // each query asks its own mesh and gets what the single scene gives
+    std::vector<float> bv;
+    std::vector<int32_t> bf;
+    for (int m = 0; m < 2; ++m)
+    {
+        for (auto &p : v)
+        {
+            bv.push_back(p.x + 3.0f * m);
+            bv.push_back(p.y);
+            bv.push_back(p.z);
+        }
+        for (auto &q : f)
+        {
+            bf.push_back(q.x);
+            bf.push_back(q.y);
+            bf.push_back(q.z);
+        }
+    }
+    snch::batch3 batch(bv.data(), 24, bf.data(), 40, {0, 12, 24}, {0, 20, 40});
+    batch.compute_silhouettes();
+    batch.build_bvh();
+    if (batch.num_meshes() != 2)
+        return 5;
+    const float h2[6] = {0.f, 0.f, 0.f, 3.f, 0.f, 0.f};
+    const int32_t hm[2] = {0, 1};
+    float *d2 = nullptr, *dd = nullptr;
+    int32_t *dm = nullptr, *di = nullptr;
+    cudaMalloc(&d2, sizeof h2);
+    cudaMalloc(&dd, 8);
+    cudaMalloc(&dm, 8);
+    cudaMalloc(&di, 8);
+    cudaMemcpy(d2, h2, sizeof h2, cudaMemcpyHostToDevice);
+    cudaMemcpy(dm, hm, sizeof hm, cudaMemcpyHostToDevice);
+    batch.query_nearest(dm, d2, 2, di, dd);
+    float bd[2];
+    int32_t bi[2];
+    cudaMemcpy(bd, dd, 8, cudaMemcpyDeviceToHost);
+    cudaMemcpy(bi, di, 8, cudaMemcpyDeviceToHost);
+    std::printf("batched: idx=%d,%d dist=%.7f,%.7f\n", bi[0], bi[1], bd[0], bd[1]);
+    if (bi[0] != (int32_t)idx || bi[1] != (int32_t)idx || bd[0] != dist || bd[1] != dist)
+        return 6;
+
+    // learned radius (untrained) seeding the nearest query: same answer
+    const float lo[3] = {-1.f, -1.f, -1.f}, hi[3] = {1.f, 1.f, 1.f};
+    snch::learned_radius model(lo, hi, 7);
+    float *dr = nullptr;
+    cudaMalloc(&dr, 4);
+    model.predict(d_pts, 1, dr, nullptr);
+    scene.query_nearest_seeded(d_pts, dr, 1, d_idx, d_dist);
+    float sdist = 0;
+    uint32_t sidx = 0;
+    cudaMemcpy(&sdist, d_dist, 4, cudaMemcpyDeviceToHost);
+    cudaMemcpy(&sidx, d_idx, 4, cudaMemcpyDeviceToHost);
+    std::printf("seeded: idx=%u dist=%.7f\n", sidx, sdist);
+    for (void *q : {(void *)d_pts, (void *)d_dist, (void *)d_idx, (void *)d2, (void *)dd, (void *)dm, (void *)di,
+                    (void *)dr})
+        cudaFree(q);
+    return (sidx == idx && sdist == dist) ? 0 : 7;
 }
