@@ -64,7 +64,9 @@ int main(int argc, char **argv)
         return 4;
 
     // two copies of the icosahedron in one batch: the second shifted by +3 in x;
-    // each query asks its own mesh and gets what the single scene gives
+    // each query asks its own mesh and gets what a single scene of that mesh
+    // gives. The centre is equidistant from all 20 faces and the shift rounds
+    // the coordinates, so the shifted copy is compared with its own scene.
     std::vector<float> bv;
     std::vector<int32_t> bf;
     for (int m = 0; m < 2; ++m)
@@ -102,8 +104,17 @@ int main(int argc, char **argv)
     int32_t bi[2];
     cudaMemcpy(bd, dd, 8, cudaMemcpyDeviceToHost);
     cudaMemcpy(bi, di, 8, cudaMemcpyDeviceToHost);
-    std::printf("batched: idx=%d,%d dist=%.7f,%.7f\n", bi[0], bi[1], bd[0], bd[1]);
-    if (bi[0] != (int32_t)idx || bi[1] != (int32_t)idx || bd[0] != dist || bd[1] != dist)
+    snch::scene3 shifted(bv.data() + 36, 12, bf.data() + 60, 20);
+    shifted.compute_silhouettes();
+    shifted.build_bvh();
+    shifted.query_nearest(d2 + 3, 1, d_idx, d_dist);
+    float sh_dist = 0;
+    uint32_t sh_idx = 0;
+    cudaMemcpy(&sh_dist, d_dist, 4, cudaMemcpyDeviceToHost);
+    cudaMemcpy(&sh_idx, d_idx, 4, cudaMemcpyDeviceToHost);
+    std::printf("batched: idx=%d,%d dist=%.7f,%.7f single: idx=%u,%u dist=%.7f,%.7f\n", bi[0], bi[1], bd[0], bd[1],
+                idx, sh_idx, dist, sh_dist);
+    if (bi[0] != (int32_t)idx || bi[1] != (int32_t)sh_idx || bd[0] != dist || bd[1] != sh_dist)
         return 6;
 
     // learned radius (untrained) seeding the nearest query: same answer
