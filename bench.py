@@ -348,10 +348,10 @@ def batched_leg(scale, per_tri=8):
     ev[3].record(stream)
     torch.cuda.synchronize()
     batched = [ev[0].elapsed_time(ev[1]), ev[1].elapsed_time(ev[2]), ev[2].elapsed_time(ev[3])]
-    # one scene per mesh, on the first 1/32 of each mesh's queries (a quarter of its
+    # one scene per mesh, on the first 1/128 of each mesh's queries (1/16 of its
     # triangle count; the per-mesh silhouette launches of the full set take minutes),
     # against the batched launches on the same subset
-    sub = [p_[: max(1, len(p_) // 32)] for p_ in pts]
+    sub = [p_[: max(1, len(p_) // 128)] for p_ in pts]
     Ps, Ms = torch.cat(sub), torch.cat([m_[: len(p_)] for m_, p_ in zip(mid, sub)])
     ns = len(Ps)
     e = [torch.cuda.Event(enable_timing=True) for _ in range(6)]
@@ -379,21 +379,51 @@ def batched_leg(scale, per_tri=8):
             and torch.equal(sd.view(torch.int32), torch.cat([o[1] for o in outs]).view(torch.int32))
             and torch.equal(ss.view(torch.int32), torch.cat([o[0] for o in outs2]).view(torch.int32))
             and torch.equal(se, torch.cat([o[1] for o in outs2])))
-    status = b.device_status()
     for s_ in scenes:
         s_.close()
+    # autotuned (node width, threads per block) on a 1/256 sample of each mesh's queries
+    tsub = [p_[: max(1, len(p_) // 256)] for p_ in pts]
+    Pt, Mt = torch.cat(tsub), torch.cat([m_[: len(p_)] for m_, p_ in zip(mid, tsub)])
+    tuned = b.autotune(Pt, Pt, None, near_mesh=Mt, sil_mesh=Mt)
+    chosen = {"near": "w%d_b%d" % b.search_config("nearest"), "sil": "w%d_b%d" % b.search_config("silhouette")}
+    # the whole step (topology + build of all meshes + both query batches) as one
+    # captured CUDA graph, launched once to warm up and once timed
+    gst = torch.cuda.Stream()
+    go = ((torch.empty(n, dtype=torch.int32, device="cuda"), torch.empty(n, dtype=torch.float32, device="cuda")),
+          (torch.empty(n, dtype=torch.float32, device="cuda"), torch.empty(n, dtype=torch.int32, device="cuda")))
+    torch.cuda.synchronize()
+    g = b.capture(True, P, go[0], P, None, go[1], near_mesh=M, sil_mesh=M, stream=gst)
+    g.launch(gst)
+    ge = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    ge[0].record(gst)
+    g.launch(gst)
+    ge[1].record(gst)
+    gst.synchronize()
+    graph_ms = ge[0].elapsed_time(ge[1])
+    graph_same = (torch.equal(go[0][0], bi) and torch.equal(go[0][1].view(torch.int32), bd.view(torch.int32))
+                  and torch.equal(go[1][0].view(torch.int32), bs.view(torch.int32)) and torch.equal(go[1][1], be))
+    g.close()
+    status = b.device_status()
     b.close()
     return {"workload": f"{len(ms)} meshes, {sum(len(f) for _, f in ms):,} triangles, {n:,} nearest + {n:,} "
                         f"silhouette queries ({per_tri * scale:g} x triangles per mesh, uniform in the mesh's box "
                         f"x 1.2)",
             "batched_ms": {"build": batched[0], "near": batched[1], "sil": batched[2]},
             "batched_qps": {"near": n / (batched[1] / 1e3), "sil": n / (batched[2] / 1e3)},
-            "subset": f"{ns:,} queries per type (the first 1/32 of each mesh's)",
+            "subset": f"{ns:,} queries per type (the first 1/128 of each mesh's)",
             "per_mesh_ms": {"build": single[0], "near": single[1], "sil": single[2]},
             "per_mesh_qps": {"near": ns / (single[1] / 1e3), "sil": ns / (single[2] / 1e3)},
             "batched_subset_qps": {"near": ns / (bsub[0] / 1e3), "sil": ns / (bsub[1] / 1e3)},
             "build_speedup": single[0] / batched[0],
-            "identical_to_per_mesh": bool(same), "device_status": int(status)}
+            "identical_to_per_mesh": bool(same),
+            "autotune_ms": {"sample": f"{len(Pt):,} queries per type",
+                            "near": {f"w{w}_b{bk}": t for (w, bk), t in tuned["nearest"].items()},
+                            "sil": {f"w{w}_b{bk}": t for (w, bk), t in tuned["silhouette"].items()},
+                            "chosen": chosen},
+            "graph": {"step_ms": graph_ms, "qps": 2 * n / (graph_ms / 1e3),
+                      "what": "one CUDA-graph launch: topology + build of all meshes + both query batches",
+                      "identical": bool(graph_same)},
+            "device_status": int(status)}
 
 
 # --------------------------------------------------------------------- walk-on-stars

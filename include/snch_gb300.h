@@ -42,9 +42,10 @@ typedef enum
 } snch_status;
 
 /* bits of the device status word (snch_get_device_status) */
-#define SNCH_DEVICE_STACK_OVERFLOW 1u   /* a traversal needed more than 64 stack entries       */
+#define SNCH_DEVICE_STACK_OVERFLOW 1u   /* a traversal needed more stack entries than it holds */
 #define SNCH_DEVICE_LOOKBACK_TIMEOUT 2u /* a bounded cross-block wait gave up (results invalid) */
 #define SNCH_DEVICE_HASH_FULL 4u        /* the edge hash table overflowed (results invalid)    */
+#define SNCH_DEVICE_TREE_DEPTH 16u      /* a wide-record pass met a tree deeper than its bound  */
 
 /* Reference-layout records, byte-compatible with the reference's device view
  * (bvh.cuh:27-33 node, aabb.cuh:12-16 aabb<float,3>, cone.cuh:11-16 cone<float,3>,
@@ -101,6 +102,11 @@ int snch_scene_destroy(snch_scene_t scene);
 
 /* Sizes (synchronises the scene's build stream for num_edges). */
 int snch_scene_info(snch_scene_t scene, int64_t *num_vertices, int64_t *num_triangles, int64_t *num_edges);
+/* The scene's DEVICE vertex buffer (3 floats per vertex, the scene's own copy;
+ * no reference counterpart): a caller that moves the vertices writes them here
+ * (stream-ordered before the next snch_build_bvh) instead of re-creating the
+ * scene. The triangles, and so the silhouette topology, stay as created. */
+int snch_scene_vertices(snch_scene_t scene, float **out_device_xyz);
 
 /* Device status word of the scene (OR of SNCH_DEVICE_* bits set by its
  * kernels since the last reset); synchronises the given stream. */
@@ -148,6 +154,26 @@ int snch_set_traversal(snch_scene_t scene, int mode);
  *                             they had reached. Same results; on the 2M-triangle scene
  *                             every cap from 48 to 256 ran 3-27 % slower than none. */
 #define SNCH_OPT_TAIL_CAP 5
+/*   SNCH_OPT_NODE_WIDTH       2 (default), 4 or 8: the near-first nearest and
+ *                             silhouette searches read binary nodes, or 4- / 8-way
+ *                             nodes collapsed from the same tree. Same results at
+ *                             every width. Setting 4 or 8 allocates that width's
+ *                             records (3N/4 + 1 records of 256 / 512 B) and, on a
+ *                             built scene, fills them on the legacy default stream
+ *                             (synchronous); every later snch_build_bvh fills them
+ *                             on its own stream with no host synchronisation.
+ *   SNCH_OPT_NODE_WIDTH_NEAREST / _SILHOUETTE  the same for one query type. */
+#define SNCH_OPT_NODE_WIDTH 6
+#define SNCH_OPT_NODE_WIDTH_NEAREST 7
+#define SNCH_OPT_NODE_WIDTH_SILHOUETTE 8
+/*   SNCH_OPT_BLOCK            64, 128 (default) or 256 threads per block of the binary
+ *                             near-first nearest and silhouette searches (the same
+ *                             threads per SM in smaller or larger blocks; a block's
+ *                             slot is freed only when its slowest query is done).
+ *   SNCH_OPT_BLOCK_NEAREST / _SILHOUETTE  the same for one query type. */
+#define SNCH_OPT_BLOCK 9
+#define SNCH_OPT_BLOCK_NEAREST 10
+#define SNCH_OPT_BLOCK_SILHOUETTE 11
 int snch_set_option(snch_scene_t scene, int option, int64_t value);
 
 /* Position of each sorted leaf in the reference's depth-first visit order,
@@ -223,6 +249,41 @@ int snch_batch_query_nearest(snch_scene_t scene, const int32_t *mesh, const floa
 int snch_batch_query_silhouette(snch_scene_t scene, const int32_t *mesh, const float *points,
                                 const uint8_t *flip_or_null, int64_t n, float *distance, int32_t *edge_or_null,
                                 snch_stream_t stream);
+
+/* Autotuner (no reference counterpart): times this scene's nearest and
+ * silhouette searches in SNCH_AUTOTUNE_CONFIGS configurations -- (node width,
+ * threads per block) = (2, 128), (4, 128), (8, 128), (2, 64), (2, 256) -- on
+ * caller sample batches (DEVICE buffers; for a batched scene near_mesh /
+ * sil_mesh give each query's mesh, else NULL; a count of 0 skips that query
+ * type), keeps the fastest configuration per query type (SNCH_OPT_NODE_WIDTH_*,
+ * SNCH_OPT_BLOCK_*) and releases the wide records no type keeps. out_ms (HOST,
+ * may be NULL): 2 x SNCH_AUTOTUNE_CONFIGS floats, milliseconds per batch in that
+ * order for nearest, then silhouette. Synchronous. Results are the same in
+ * every configuration; only their speed differs. */
+#define SNCH_AUTOTUNE_CONFIGS 5
+int snch_autotune(snch_scene_t scene, const int32_t *near_mesh, const float *near_points, int64_t n_near,
+                  const int32_t *sil_mesh, const float *sil_points, const uint8_t *sil_flip_or_null, int64_t n_sil,
+                  float *out_ms, snch_stream_t stream);
+/* node width and threads per block of the nearest (which = 0) or silhouette (1)
+ * search; either output may be NULL */
+int snch_get_search_config(snch_scene_t scene, int which, int32_t *out_width, int32_t *out_block);
+
+/* CUDA-graph capture (no reference counterpart): one graph holds a rebuild of
+ * the scene (rebuild != 0: silhouette topology + LBVH + wide records) and one
+ * nearest and one silhouette batch (a count of 0 leaves that batch out; for a
+ * batched scene near_mesh / sil_mesh give each query's mesh), so that a solver
+ * step is one snch_graph_launch. The graph keeps the buffer ADDRESSES given
+ * here: refill the same device buffers (vertex positions through
+ * snch_scene_vertices, queries) between launches. The scene must have been
+ * built once before the capture and must outlive the graph; its tree holds what
+ * the last launch built. `stream` must be a created stream. */
+typedef struct snch_graph_s *snch_graph_t;
+int snch_graph_create(snch_scene_t scene, int rebuild, const int32_t *near_mesh, const float *near_points,
+                      int64_t n_near, int32_t *near_index, float *near_distance, const int32_t *sil_mesh,
+                      const float *sil_points, const uint8_t *sil_flip_or_null, int64_t n_sil, float *sil_distance,
+                      int32_t *sil_edge_or_null, snch_graph_t *out_graph, snch_stream_t stream);
+int snch_graph_launch(snch_graph_t graph, snch_stream_t stream);
+int snch_graph_destroy(snch_graph_t graph);
 
 typedef struct snch_mlp_s *snch_mlp_t;
 

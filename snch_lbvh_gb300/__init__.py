@@ -19,12 +19,14 @@ import numpy as np
 
 from ._ffi import BvhView, SnchError, check, lib  # noqa: F401
 
-__all__ = ["Scene", "BatchedScene", "SnchError", "BvhView", "lib"]
+__all__ = ["Scene", "BatchedScene", "Graph", "SnchError", "BvhView", "lib"]
 
 INVALID = 0xFFFFFFFF
 TRAVERSAL_NEAR_FIRST = 0
 TRAVERSAL_REFERENCE_ORDER = 1
 OPT_TRAVERSAL, OPT_QUERY_ORDER, OPT_ORDER_MIN_BATCH, OPT_PERSISTENT, OPT_TAIL_CAP = 1, 2, 3, 4, 5
+OPT_NODE_WIDTH, OPT_NODE_WIDTH_NEAREST, OPT_NODE_WIDTH_SILHOUETTE = 6, 7, 8
+OPT_BLOCK, OPT_BLOCK_NEAREST, OPT_BLOCK_SILHOUETTE = 9, 10, 11
 
 
 def _torch():
@@ -114,7 +116,8 @@ class Scene:
         check(lib().snch_set_traversal(self._h, int(mode)))
 
     def set_option(self, option: int, value: int):
-        """OPT_TRAVERSAL, OPT_QUERY_ORDER (Morton-sorted batches), OPT_ORDER_MIN_BATCH."""
+        """OPT_TRAVERSAL, OPT_QUERY_ORDER (Morton-sorted batches), OPT_ORDER_MIN_BATCH,
+        OPT_PERSISTENT, OPT_TAIL_CAP, OPT_NODE_WIDTH[_NEAREST|_SILHOUETTE] (2, 4 or 8)."""
         check(lib().snch_set_option(self._h, int(option), int(value)))
 
     def leaf_ranks(self):
@@ -178,6 +181,55 @@ class Scene:
         check(lib().snch_query_visits(self._h, k, _ptr(ins[0]), _ptr(ins[1]), _ptr(ins[2]), _ptr(f), n, _ptr(out),
                                       _stream(stream)))
         return out.cpu().numpy().view(np.uint32)
+
+    def vertices(self):
+        """The scene's device vertex buffer as a (V, 3) float32 CUDA tensor view
+        (write moved vertices here before the next build_bvh)."""
+        torch = _torch()
+        ptr = C.c_void_p()
+        check(lib().snch_scene_vertices(self._h, C.byref(ptr)))
+        nv, _, _ = self.info()
+        if nv == 0:
+            return torch.zeros((0, 3), dtype=torch.float32, device="cuda")
+        return _wrap_device(ptr.value, (nv, 3))
+
+    def capture(self, rebuild=True, near_points=None, near_out=None, sil_points=None, sil_flip=None, sil_out=None,
+                near_mesh=None, sil_mesh=None, stream=None):
+        """Captures [rebuild +] one nearest and one silhouette batch into a CUDA graph
+        (Graph.launch() replays it on the same buffers, which the caller refills)."""
+        return Graph(self, rebuild, near_points, near_out, sil_points, sil_flip, sil_out, near_mesh, sil_mesh,
+                     stream)
+
+    def search_config(self, which: str = "nearest"):
+        """(node width, threads per block) of the nearest or silhouette search."""
+        w, b = C.c_int32(), C.c_int32()
+        check(lib().snch_get_search_config(self._h, {"nearest": 0, "silhouette": 1}[which], C.byref(w), C.byref(b)))
+        return int(w.value), int(b.value)
+
+    def node_width(self, which: str = "nearest") -> int:
+        return self.search_config(which)[0]
+
+    AUTOTUNE_CONFIGS = ((2, 128), (4, 128), (8, 128), (2, 64), (2, 256))
+
+    def autotune(self, near_points=None, sil_points=None, sil_flip=None, near_mesh=None, sil_mesh=None,
+                 stream=None):
+        """Times the nearest / silhouette searches in each (node width, threads per
+        block) of AUTOTUNE_CONFIGS on these sample batches and keeps the fastest per
+        type (same results in every configuration). Returns
+        {"nearest": {(width, block): ms, ...}, "silhouette": {...}}."""
+        torch = _torch()
+        pn = None if near_points is None else _dev(near_points, torch.float32, 3)
+        ps = None if sil_points is None else _dev(sil_points, torch.float32, 3)
+        f = None if sil_flip is None else _dev(sil_flip, torch.uint8)
+        mn = None if near_mesh is None else _dev(near_mesh, torch.int32)
+        ms_ = None if sil_mesh is None else _dev(sil_mesh, torch.int32)
+        k = len(self.AUTOTUNE_CONFIGS)
+        out = (C.c_float * (2 * k))()
+        check(lib().snch_autotune(self._h, _ptr(mn), _ptr(pn), 0 if pn is None else pn.shape[0], _ptr(ms_), _ptr(ps),
+                                  _ptr(f), 0 if ps is None else ps.shape[0], C.cast(out, C.c_void_p),
+                                  _stream(stream)))
+        return {"nearest": dict(zip(self.AUTOTUNE_CONFIGS, out[0:k])),
+                "silhouette": dict(zip(self.AUTOTUNE_CONFIGS, out[k:2 * k]))}
 
     # ------------------------------------------------------------ device-buffer queries
     def query_nearest(self, points, stream=None, out=None):
@@ -299,6 +351,56 @@ class Scene:
         vp = lambda a: a.ctypes.data_as(C.c_void_p)  # noqa: E731
         check(lib().snch_sample_in_sphere_host(self._h, vp(c), vp(r), vp(uu), n, vp(idx), vp(pdf)))
         return idx, pdf
+
+
+def _wrap_device(addr, shape):
+    """A float32 CUDA tensor viewing library-owned device memory (no copy)."""
+    torch = _torch()
+    n = int(np.prod(shape))
+
+    class _Mem:
+        __cuda_array_interface__ = {"shape": (n,), "typestr": "<f4", "data": (int(addr), False), "version": 3}
+
+    return torch.as_tensor(_Mem(), device="cuda").view(*shape)
+
+
+class Graph:
+    """A captured solver step (snch_graph_create): the tensors given at capture are
+    the graph's inputs and outputs; refill them in place between launches."""
+
+    def __init__(self, scene, rebuild, near_points, near_out, sil_points, sil_flip, sil_out, near_mesh, sil_mesh,
+                 stream):
+        torch = _torch()
+        self._h = C.c_void_p()
+        self._keep = [scene, near_points, near_out, sil_points, sil_flip, sil_out, near_mesh, sil_mesh]
+        for x in (near_points, sil_points, sil_flip, near_mesh, sil_mesh):
+            assert x is None or (torch.is_tensor(x) and x.is_cuda and x.is_contiguous()), \
+                "graph inputs must be contiguous CUDA tensors (their addresses are captured)"
+        nn = 0 if near_points is None else near_points.shape[0]
+        ns = 0 if sil_points is None else sil_points.shape[0]
+        ni, nd = near_out if near_out is not None else (None, None)
+        sd, se = sil_out if sil_out is not None else (None, None)
+        st = stream if stream is not None else torch.cuda.current_stream()
+        if st.cuda_stream == 0:
+            raise SnchError(-1, "capture needs a created stream (torch.cuda.Stream()), not the default stream")
+        check(lib().snch_graph_create(scene._h, int(bool(rebuild)), _ptr(near_mesh), _ptr(near_points), nn,
+                                      _ptr(ni), _ptr(nd), _ptr(sil_mesh), _ptr(sil_points), _ptr(sil_flip), ns,
+                                      _ptr(sd), _ptr(se), C.byref(self._h), C.c_void_p(st.cuda_stream)))
+
+    def launch(self, stream=None):
+        check(lib().snch_graph_launch(self._h, _stream(stream)))
+
+    def close(self):
+        if self._h:
+            lib().snch_graph_destroy(self._h)
+            self._h = None
+            self._keep = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class BatchedScene(Scene):

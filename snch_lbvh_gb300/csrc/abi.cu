@@ -94,6 +94,14 @@ struct snch_scene_s
     int32_t *mesh_edge_start = nullptr;
     cudaStream_t pipe[2] = {nullptr, nullptr};
     HostStage stage;
+    // node width of the near-first nearest / silhouette searches (2, 4 or 8)
+    // and the wide records of the built tree: [0] 4-way, [1] 8-way
+    int width_near = 2, width_sil = 2;
+    int block_near = 128, block_sil = 128;  // threads per block of the binary searches
+    float4 *wide[2] = {nullptr, nullptr};
+    uint32_t *wide_idx[2] = {nullptr, nullptr};  // wide index of each wide-root binary node
+    size_t wide_cap[2] = {0, 0};  // records allocated
+    bool wide_ready[2] = {false, false};
 
     TreeView view() const
     {
@@ -108,6 +116,20 @@ struct snch_scene_s
         t.status = small + kWStatus;
         t.near_first = traversal == SNCH_TRAVERSAL_NEAR_FIRST ? 1 : 0;
         t.persistent = persistent;
+        t.width_near = width_near;
+        t.width_sil = width_sil;
+        t.block_near = block_near;
+        t.block_sil = block_sil;
+        if (wide_ready[0])
+        {
+            t.wide4 = wide[0];
+            t.wide4_of = wide_idx[0];
+        }
+        if (wide_ready[1])
+        {
+            t.wide8 = wide[1];
+            t.wide8_of = wide_idx[1];
+        }
         return t;
     }
 };
@@ -130,7 +152,8 @@ void free_scene(snch_scene_s *s)
                     s->flags, s->sizes, s->centroids, s->small, s->scratch, s->ref_objects, s->ref_edges,
                     s->stage.in[0], s->stage.in[1], s->stage.out[0], s->stage.out[1],
                     s->tri_mesh, s->mesh_tri_start, s->mesh_box, s->sorted_mesh, s->mesh_root, s->perm,
-                    s->perm_tmp, s->mkey_tmp, s->mesh_edge_start};
+                    s->perm_tmp, s->mkey_tmp, s->mesh_edge_start, s->wide[0], s->wide[1], s->wide_idx[0],
+                    s->wide_idx[1]};
     for (void *p : ptrs)
         if (p)
             cudaFree(p);
@@ -287,6 +310,78 @@ BuildArgs build_args(snch_scene_s *s)
     a.tri_edges = s->tri_edges;
     a.mesh_edge_start = s->mesh_edge_start;
     return a;
+}
+
+// Wide records of width W. A tree of n >= 2 leaves has fewer than 3n/4 wide
+// nodes (a wide node has at least three children unless both its binary
+// children are leaves; such nodes hold two leaves each, so with a of them and
+// b others, 2a + 3b <= (a + b - 1) + n and a <= n/2), so the records are
+// allocated once per scene at that bound, when a width first needs them, and
+// every later build fills them without a host synchronisation.
+size_t wide_capacity(uint32_t num_tris) { return (size_t)num_tris * 3 / 4 + 1; }
+
+int alloc_wide(snch_scene_s *s, int W)
+{
+    const int k = W == 4 ? 0 : 1;
+    if (s->wide[k] || s->num_tris < 2)
+        return SNCH_OK;
+    const size_t rec = sizeof(float4) * (W == 4 ? WideLayout<4>::kRecF4 : WideLayout<8>::kRecF4);
+    SNCH_CUDA(dalloc(&s->wide_idx[k], s->num_tris - 1));
+    SNCH_CUDA(cudaMalloc(reinterpret_cast<void **>(&s->wide[k]), wide_capacity(s->num_tris) * rec));
+    s->wide_cap[k] = wide_capacity(s->num_tris);
+    return SNCH_OK;
+}
+
+// Fills the wide records of width W for the built tree (stream-ordered).
+int ensure_wide(snch_scene_s *s, int W, cudaStream_t st)
+{
+    const int k = W == 4 ? 0 : 1;
+    if (s->wide_ready[k])
+        return SNCH_OK;
+    if (s->num_tris < 2)
+    {
+        s->wide_ready[k] = true;  // a one-triangle tree is searched as its leaf
+        return SNCH_OK;
+    }
+    if (!s->wide[k])
+        return fail(SNCH_ERR_INVALID_ARGUMENT, "wide records are allocated by snch_set_option (node width)");
+    WideArgs a{};
+    a.width = W;
+    a.num_tris = s->num_tris;
+    a.nodes = s->nodes;
+    a.aabbs = s->aabbs;
+    a.cones = s->cones;
+    a.leaves = s->leaves;
+    a.num_meshes = s->num_meshes;
+    a.mesh_root = s->mesh_root;
+    a.flags = s->flags;
+    a.wide_of = s->wide_idx[k];
+    a.capacity = (uint32_t)s->wide_cap[k];
+    a.out = s->wide[k];
+    a.status = s->small + kWStatus;
+    char *scratch = nullptr;
+    SNCH_CUDA(cudaMallocAsync(reinterpret_cast<void **>(&scratch), wide_scratch_bytes(s->num_tris) + 256, st));
+    a.count = reinterpret_cast<uint32_t *>(scratch);
+    a.scratch = scratch + 256;
+    cudaError_t e = launch_wide_count(a, st);
+    if (e == cudaSuccess)
+        e = launch_wide_fill(a, st);
+    cudaFreeAsync(scratch, st);
+    SNCH_CUDA(e);
+    s->wide_ready[k] = true;
+    return SNCH_OK;
+}
+
+int ensure_widths(snch_scene_s *s, cudaStream_t st)
+{
+    for (int W : {4, 8})
+        if (s->width_near == W || s->width_sil == W)
+        {
+            int rc = ensure_wide(s, W, st);
+            if (rc != SNCH_OK)
+                return rc;
+        }
+    return SNCH_OK;
 }
 
 int check_built(snch_scene_t s)
@@ -639,8 +734,9 @@ int snch_build_bvh(snch_scene_t s, snch_stream_t stream)
         SNCH_CUDA(launch_ref_objects(s->verts, s->tris, s->tri_owned, s->edge_verts, s->num_tris, s->ref_objects,
                                      s->ref_edges, st));
     }
+    s->wide_ready[0] = s->wide_ready[1] = false;
     s->built = true;
-    return SNCH_OK;
+    return ensure_widths(s, st);
 }
 
 int snch_set_traversal(snch_scene_t s, int mode)
@@ -681,6 +777,39 @@ int snch_set_option(snch_scene_t s, int option, int64_t value)
             return fail(SNCH_ERR_INVALID_ARGUMENT, "SNCH_OPT_PERSISTENT takes 0 or 1");
         s->persistent = (int)value;
         return SNCH_OK;
+    case SNCH_OPT_BLOCK:
+    case SNCH_OPT_BLOCK_NEAREST:
+    case SNCH_OPT_BLOCK_SILHOUETTE:
+        if (value != 64 && value != 128 && value != 256)
+            return fail(SNCH_ERR_INVALID_ARGUMENT, "block size must be 64, 128 or 256");
+        if (option != SNCH_OPT_BLOCK_SILHOUETTE)
+            s->block_near = (int)value;
+        if (option != SNCH_OPT_BLOCK_NEAREST)
+            s->block_sil = (int)value;
+        return SNCH_OK;
+    case SNCH_OPT_NODE_WIDTH:
+    case SNCH_OPT_NODE_WIDTH_NEAREST:
+    case SNCH_OPT_NODE_WIDTH_SILHOUETTE:
+    {
+        if (value != 2 && value != 4 && value != 8)
+            return fail(SNCH_ERR_INVALID_ARGUMENT, "node width must be 2, 4 or 8");
+        if (option != SNCH_OPT_NODE_WIDTH_SILHOUETTE)
+            s->width_near = (int)value;
+        if (option != SNCH_OPT_NODE_WIDTH_NEAREST)
+            s->width_sil = (int)value;
+        if (value > 2)
+        {
+            int rc = alloc_wide(s, (int)value);
+            if (rc != SNCH_OK)
+                return rc;
+        }
+        if (!s->built)
+            return SNCH_OK;
+        int rc = ensure_widths(s, nullptr);
+        if (rc == SNCH_OK)
+            SNCH_CUDA(cudaStreamSynchronize(nullptr));
+        return rc;
+    }
     default:
         return fail(SNCH_ERR_INVALID_ARGUMENT, "unknown option " + std::to_string(option));
     }
@@ -1312,6 +1441,229 @@ int snch_batch_query_silhouette(snch_scene_t s, const int32_t *mesh, const float
             return launch_silhouette(t, pts, flip, n, dist, edge, S(stream), nullptr, seed);
         },
         reinterpret_cast<const uint32_t *>(mesh));
+}
+
+int snch_autotune(snch_scene_t s, const int32_t *near_mesh, const float *near_pts, int64_t n_near,
+                  const int32_t *sil_mesh, const float *sil_pts, const uint8_t *sil_flip, int64_t n_sil, float *out_ms,
+                  snch_stream_t stream)
+{
+    int rc = check_built(s);
+    if (rc == SNCH_OK)
+        rc = check_n(n_near, {near_pts});
+    if (rc == SNCH_OK)
+        rc = check_n(n_sil, {sil_pts});
+    if (rc == SNCH_OK && s->num_meshes && ((n_near && !near_mesh) || (n_sil && !sil_mesh)))
+        rc = fail(SNCH_ERR_INVALID_ARGUMENT, "a batched scene needs the mesh of every sample query");
+    if (rc != SNCH_OK)
+        return rc;
+    cudaStream_t st = S(stream);
+    // candidates (node width, threads per block); the block size applies to the binary searches
+    constexpr int kConfigs = SNCH_AUTOTUNE_CONFIGS;
+    const int cw[kConfigs] = {2, 4, 8, 2, 2}, cb[kConfigs] = {128, 128, 128, 64, 256};
+    float ms[2][kConfigs] = {};
+    char *out = nullptr;
+    const int64_t nmax = std::max<int64_t>(1, std::max(n_near, n_sil));
+    SNCH_CUDA(cudaMallocAsync(reinterpret_cast<void **>(&out), 8 * (size_t)nmax, st));
+    uint32_t *o_idx = reinterpret_cast<uint32_t *>(out);
+    float *o_dist = reinterpret_cast<float *>(out + 4 * (size_t)nmax);
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    cudaError_t e = cudaEventCreate(&ev[0]);
+    if (e == cudaSuccess)
+        e = cudaEventCreate(&ev[1]);
+    const int saved[4] = {s->width_near, s->width_sil, s->block_near, s->block_sil};
+    auto run = [&](int kind) -> int {
+        if (kind == 0)
+            return s->num_meshes
+                       ? snch_batch_query_nearest(s, near_mesh, near_pts, n_near, reinterpret_cast<int32_t *>(o_idx),
+                                                  o_dist, stream)
+                       : snch_query_nearest(s, near_pts, n_near, o_idx, o_dist, stream);
+        return s->num_meshes ? snch_batch_query_silhouette(s, sil_mesh, sil_pts, sil_flip, n_sil, o_dist,
+                                                           reinterpret_cast<int32_t *>(o_idx), stream)
+                             : snch_query_silhouette(s, sil_pts, sil_flip, n_sil, o_dist,
+                                                     reinterpret_cast<int32_t *>(o_idx), stream);
+    };
+    for (int c = 0; c < kConfigs && e == cudaSuccess && rc == SNCH_OK; ++c)
+    {
+        const int w = cw[c];
+        if (w > 2)
+            rc = alloc_wide(s, w);
+        s->width_near = s->width_sil = w;
+        s->block_near = s->block_sil = cb[c];
+        if (rc == SNCH_OK)
+            rc = ensure_widths(s, st);
+        for (int kind = 0; kind < 2 && rc == SNCH_OK && e == cudaSuccess; ++kind)
+        {
+            if ((kind == 0 ? n_near : n_sil) == 0)
+                continue;
+            rc = run(kind);  // warm-up
+            if (rc == SNCH_OK)
+                e = cudaEventRecord(ev[0], st);
+            constexpr int kReps = 3;
+            for (int r = 0; r < kReps && rc == SNCH_OK && e == cudaSuccess; ++r)
+                rc = run(kind);
+            if (rc == SNCH_OK && e == cudaSuccess)
+                e = cudaEventRecord(ev[1], st);
+            if (rc == SNCH_OK && e == cudaSuccess)
+                e = cudaEventSynchronize(ev[1]);
+            float t = 0.0f;
+            if (rc == SNCH_OK && e == cudaSuccess)
+                e = cudaEventElapsedTime(&t, ev[0], ev[1]);
+            ms[kind][c] = t / kReps;
+        }
+    }
+    for (cudaEvent_t x : ev)
+        if (x)
+            cudaEventDestroy(x);
+    cudaFreeAsync(out, st);
+    if (rc != SNCH_OK || e != cudaSuccess)
+    {
+        s->width_near = saved[0];
+        s->width_sil = saved[1];
+        s->block_near = saved[2];
+        s->block_sil = saved[3];
+        if (rc != SNCH_OK)
+            return rc;
+        SNCH_CUDA(e);
+    }
+    int best[2] = {-1, -1};
+    for (int kind = 0; kind < 2; ++kind)
+    {
+        if ((kind == 0 ? n_near : n_sil) == 0)
+            continue;
+        best[kind] = 0;
+        for (int c = 1; c < kConfigs; ++c)
+            if (ms[kind][c] < ms[kind][best[kind]])
+                best[kind] = c;
+    }
+    s->width_near = best[0] < 0 ? saved[0] : cw[best[0]];
+    s->block_near = best[0] < 0 ? saved[2] : cb[best[0]];
+    s->width_sil = best[1] < 0 ? saved[1] : cw[best[1]];
+    s->block_sil = best[1] < 0 ? saved[3] : cb[best[1]];
+    // records of a width no query type keeps are released
+    SNCH_CUDA(cudaStreamSynchronize(st));
+    for (int k = 0; k < 2; ++k)
+    {
+        const int w = k == 0 ? 4 : 8;
+        if (s->width_near != w && s->width_sil != w && s->wide[k])
+        {
+            cudaFree(s->wide[k]);
+            cudaFree(s->wide_idx[k]);
+            s->wide[k] = nullptr;
+            s->wide_idx[k] = nullptr;
+            s->wide_cap[k] = 0;
+            s->wide_ready[k] = false;
+        }
+    }
+    if (out_ms)
+        for (int kind = 0; kind < 2; ++kind)
+            for (int c = 0; c < kConfigs; ++c)
+                out_ms[kConfigs * kind + c] = ms[kind][c];
+    return SNCH_OK;
+}
+
+struct snch_graph_s
+{
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    uint64_t kernels = 0;  // kernels per launch of the graph
+};
+
+int snch_graph_create(snch_scene_t s, int rebuild, const int32_t *near_mesh, const float *near_pts, int64_t n_near,
+                      int32_t *near_idx, float *near_dist, const int32_t *sil_mesh, const float *sil_pts,
+                      const uint8_t *sil_flip, int64_t n_sil, float *sil_dist, int32_t *sil_edge, snch_graph_t *out,
+                      snch_stream_t stream)
+{
+    if (!out)
+        return fail(SNCH_ERR_INVALID_ARGUMENT, "out_graph is NULL");
+    *out = nullptr;
+    int rc = check_built(s);
+    if (rc != SNCH_OK)
+        return rc == SNCH_ERR_NOT_BUILT ? fail(rc, "build the scene once before capturing it") : rc;
+    if (!stream)
+        return fail(SNCH_ERR_INVALID_ARGUMENT, "graph capture needs a created stream (not the legacy default stream)");
+    if ((rc = check_n(n_near, {near_pts, near_idx, near_dist})) != SNCH_OK ||
+        (rc = check_n(n_sil, {sil_pts, sil_dist})) != SNCH_OK)
+        return rc;
+    if (s->num_meshes && ((n_near && !near_mesh) || (n_sil && !sil_mesh)))
+        return fail(SNCH_ERR_INVALID_ARGUMENT, "a batched scene needs the mesh of every query");
+    cudaStream_t st = S(stream);
+    const uint64_t k0 = g_kernel_launches.load(std::memory_order_relaxed);
+    SNCH_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    if (rebuild)
+    {
+        rc = snch_compute_silhouettes(s, stream);
+        if (rc == SNCH_OK)
+            rc = snch_build_bvh(s, stream);
+    }
+    if (rc == SNCH_OK && n_near)
+        rc = s->num_meshes ? snch_batch_query_nearest(s, near_mesh, near_pts, n_near, near_idx, near_dist, stream)
+                           : snch_query_nearest(s, near_pts, n_near, reinterpret_cast<uint32_t *>(near_idx), near_dist,
+                                                stream);
+    if (rc == SNCH_OK && n_sil)
+        rc = s->num_meshes
+                 ? snch_batch_query_silhouette(s, sil_mesh, sil_pts, sil_flip, n_sil, sil_dist, sil_edge, stream)
+                 : snch_query_silhouette(s, sil_pts, sil_flip, n_sil, sil_dist, sil_edge, stream);
+    cudaGraph_t graph = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(st, &graph);
+    const uint64_t kernels = g_kernel_launches.load(std::memory_order_relaxed) - k0;
+    g_kernel_launches.fetch_sub(kernels, std::memory_order_relaxed);  // recorded, not launched
+    if (rc != SNCH_OK || e != cudaSuccess)
+    {
+        if (graph)
+            cudaGraphDestroy(graph);
+        if (rc != SNCH_OK)
+            return rc;
+        SNCH_CUDA(e);
+    }
+    cudaGraphExec_t exec = nullptr;
+    const cudaError_t ei = cudaGraphInstantiate(&exec, graph, 0);
+    if (ei != cudaSuccess)
+    {
+        cudaGraphDestroy(graph);
+        SNCH_CUDA(ei);
+    }
+    *out = new snch_graph_s{graph, exec, kernels};
+    return SNCH_OK;
+}
+
+int snch_graph_launch(snch_graph_t g, snch_stream_t stream)
+{
+    if (!g)
+        return fail(SNCH_ERR_INVALID_ARGUMENT, "graph is NULL");
+    SNCH_CUDA(cudaGraphLaunch(g->exec, S(stream)));
+    note_launch((unsigned)g->kernels);
+    return SNCH_OK;
+}
+
+int snch_graph_destroy(snch_graph_t g)
+{
+    if (!g)
+        return fail(SNCH_ERR_INVALID_ARGUMENT, "graph is NULL");
+    if (g->exec)
+        cudaGraphExecDestroy(g->exec);
+    if (g->graph)
+        cudaGraphDestroy(g->graph);
+    delete g;
+    return SNCH_OK;
+}
+
+int snch_scene_vertices(snch_scene_t s, float **out)
+{
+    if (!s || !out)
+        return fail(SNCH_ERR_INVALID_ARGUMENT, "scene and out are required");
+    *out = s->verts;
+    return SNCH_OK;
+}
+
+int snch_get_search_config(snch_scene_t s, int which, int32_t *out_width, int32_t *out_block)
+{
+    if (!s || (which != 0 && which != 1))
+        return fail(SNCH_ERR_INVALID_ARGUMENT, "scene and which (0 or 1) are required");
+    if (out_width)
+        *out_width = which == 0 ? s->width_near : s->width_sil;
+    if (out_block)
+        *out_block = which == 0 ? s->block_near : s->block_sil;
+    return SNCH_OK;
 }
 
 int snch_selfcheck_cone_filter(int64_t n, uint64_t seed, uint64_t *device_counts, snch_stream_t stream)

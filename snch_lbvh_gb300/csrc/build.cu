@@ -706,6 +706,210 @@ __global__ void validate_kernel(const int32_t *tris, int64_t n, int64_t num_vert
         atomicAdd(bad, c);
 }
 
+// ------------------------------------------------------------------ wide records
+// Mesh roots of a batched scene: a wide node's depth is counted from its mesh's
+// root, and the nodes that join meshes (above every mesh root) are never searched.
+__global__ void wide_mark_kernel(const uint32_t *__restrict__ mesh_root, uint32_t num_meshes, uint32_t ni,
+                                 uint8_t *__restrict__ stop)
+{
+    const uint32_t m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m < num_meshes)
+    {
+        const uint32_t r = mesh_root[m];
+        if (r < ni)
+            stop[r] = 1;
+    }
+}
+
+// flags[i] = 1 when binary internal node i roots a wide record: its depth below
+// the tree root (or its mesh root, stop != nullptr) is a multiple of k
+__global__ void __launch_bounds__(256) wide_flag_kernel(const NodeRec *__restrict__ nodes, uint32_t ni, int k,
+                                                        const uint8_t *__restrict__ stop, uint32_t *__restrict__ flags,
+                                                        uint32_t *status)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ni)
+        return;
+    uint32_t node = i, d = 0;
+    bool found = false, joins_meshes = false;
+    for (int level = 0; level < 256; ++level)
+    {
+        if (stop && stop[node])
+        {
+            found = true;
+            break;
+        }
+        const uint32_t p = nodes[node].parent;
+        if (p >= ni)
+        {
+            found = true;
+            joins_meshes = stop != nullptr;
+            break;
+        }
+        node = p;
+        ++d;
+    }
+    if (!found)
+        atomicOr(status, kStatusTreeDepth);
+    flags[i] = (found && !joins_meshes && d % (uint32_t)k == 0u) ? 1u : 0u;
+}
+
+// One wide record per flagged node: the slot tree of its binary descendants
+// kLevels down (node / pass / empty positions, see WideLayout).
+template <int W>
+__global__ void __launch_bounds__(128) wide_fill_kernel(const NodeRec *__restrict__ nodes, const Box *__restrict__ aabbs,
+                                                        const Cone *__restrict__ cones,
+                                                        const LeafRec *__restrict__ leaves, uint32_t ni,
+                                                        const uint32_t *__restrict__ flags,
+                                                        const uint32_t *__restrict__ wide_of, float4 *__restrict__ out,
+                                                        uint32_t capacity, uint32_t *status)
+{
+    using Lay = WideLayout<W>;
+    constexpr int P = Lay::P, F = Lay::F;
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ni || !flags[i])
+        return;
+    if (wide_of[i] >= capacity)
+    {
+        atomicOr(status, kStatusTreeDepth);
+        return;
+    }
+    enum : uint8_t
+    {
+        kEmpty = 0,
+        kNode = 1,
+        kPass = 2
+    };
+    uint32_t at[F];
+    uint8_t kind[F];
+    at[0] = nodes[i].left;
+    at[1] = nodes[i].right;
+    kind[0] = kind[1] = kNode;
+#pragma unroll
+    for (int f = 2; f < F; ++f)
+    {
+        const int pf = ((f + 2) >> 1) - 2;
+        const bool left = (f & 1) == 0;
+        at[f] = kInvalid;
+        kind[f] = kEmpty;
+        if (kind[pf] == kNode && at[pf] < ni)
+        {
+            at[f] = left ? nodes[at[pf]].left : nodes[at[pf]].right;
+            kind[f] = kNode;
+        }
+        else if (kind[pf] != kEmpty && left)  // a leaf above: forwarded to the leftmost position
+        {
+            at[f] = at[pf];
+            kind[f] = kPass;
+        }
+    }
+    float *rec = reinterpret_cast<float *>(out + (size_t)wide_of[i] * Lay::kRecF4);
+    uint32_t *u = reinterpret_cast<uint32_t *>(rec);
+    float *cn = rec + Lay::kCone;
+#pragma unroll
+    for (int f = 0; f < P; ++f)
+    {
+        Box b;
+        Cone c;
+        const uint8_t k = f < F ? kind[f] : (uint8_t)kEmpty;
+        if (k == kNode)
+        {
+            b = aabbs[at[f]];
+            c = cones[at[f]];
+        }
+        else
+        {
+            // a pass position carries its leaf's box (its sibling is empty, so
+            // the sibling test passes; the distance tests stay those of the leaf)
+            // and a cone that passes every test
+            b.lower = mk(INFINITY, INFINITY, INFINITY);
+            b.upper = mk(-INFINITY, -INFINITY, -INFINITY);
+            if (k == kPass)
+                b = aabbs[at[f]];
+            c.axis = mk(0.0f, 0.0f, 0.0f);
+            c.half_angle = k == kPass ? kPi : -1.0f;
+            c.radius = 0.0f;
+        }
+        rec[0 * P + f] = b.lower.x;
+        rec[1 * P + f] = b.lower.y;
+        rec[2 * P + f] = b.lower.z;
+        rec[3 * P + f] = b.upper.x;
+        rec[4 * P + f] = b.upper.y;
+        rec[5 * P + f] = b.upper.z;
+        cn[0 * P + f] = c.axis.x;
+        cn[1 * P + f] = c.axis.y;
+        cn[2 * P + f] = c.axis.z;
+        cn[3 * P + f] = c.half_angle;
+        cn[4 * P + f] = c.radius;
+    }
+#pragma unroll
+    for (int sl = 0; sl < W; ++sl)
+    {
+        const int f = Lay::S0 + sl;
+        uint32_t child = kInvalid, info = 0;
+        if (kind[f] != kEmpty)
+        {
+            const uint32_t g = at[f];
+            if (g < ni)
+            {
+                if (!flags[g])
+                    atomicOr(status, kStatusTreeDepth);
+                child = wide_of[g];
+            }
+            else
+            {
+                const uint32_t pos = g - ni;
+                child = kWideLeaf | pos;
+                const uint32_t rank = __float_as_uint(leaves[pos].v2.w);
+                info = (rank & kLeafRankMask) | (__float_as_uint(leaves[pos].v1.w) << 30);
+            }
+        }
+        u[Lay::kChild + sl] = child;
+        u[Lay::kInfo + sl] = info;
+    }
+}
+
+size_t wide_scratch_bytes(uint32_t num_tris)
+{
+    const uint32_t ni = num_tris > 1 ? num_tris - 1 : 1;
+    return 256 + ((ni + 255) & ~255u) + scan_flags_scratch_bytes(ni) + 256;
+}
+
+cudaError_t launch_wide_count(const WideArgs &a, cudaStream_t st)
+{
+    const uint32_t ni = a.num_tris - 1;
+    char *sc = static_cast<char *>(a.scratch);
+    uint8_t *stop = nullptr;
+    cudaError_t e = cudaSuccess;
+    if (a.num_meshes)
+    {
+        stop = reinterpret_cast<uint8_t *>(sc + 256);
+        if ((e = cudaMemsetAsync(stop, 0, ni, st)) != cudaSuccess)
+            return e;
+        wide_mark_kernel<<<(a.num_meshes + 255) / 256, 256, 0, st>>>(a.mesh_root, a.num_meshes, ni, stop);
+        note_launch();
+    }
+    wide_flag_kernel<<<(ni + 255) / 256, 256, 0, st>>>(a.nodes, ni, a.width == 4 ? 2 : 3, stop, a.flags, a.status);
+    note_launch();
+    if ((e = cudaGetLastError()) != cudaSuccess)
+        return e;
+    void *scan_scratch = sc + 256 + ((ni + 255) & ~255u);
+    return scan_flags(a.flags, a.wide_of, ni, a.count, scan_scratch, a.status, st);
+}
+
+cudaError_t launch_wide_fill(const WideArgs &a, cudaStream_t st)
+{
+    const uint32_t ni = a.num_tris - 1;
+    if (a.width == 4)
+        wide_fill_kernel<4><<<(ni + 127) / 128, 128, 0, st>>>(a.nodes, a.aabbs, a.cones, a.leaves, ni, a.flags,
+                                                              a.wide_of, a.out, a.capacity, a.status);
+    else
+        wide_fill_kernel<8><<<(ni + 127) / 128, 128, 0, st>>>(a.nodes, a.aabbs, a.cones, a.leaves, ni, a.flags,
+                                                              a.wide_of, a.out, a.capacity, a.status);
+    note_launch();
+    return cudaGetLastError();
+}
+
 // ------------------------------------------------------------------ launchers
 cudaError_t launch_build_front(const BuildArgs &a, cudaStream_t st)
 {

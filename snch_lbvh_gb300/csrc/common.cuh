@@ -28,6 +28,7 @@ enum : uint32_t
     kStatusLookbackTimeout = 2u,   // a decoupled look-back wait gave up
     kStatusHashFull = 4u,          // the edge hash table had no free slot
     kStatusRefitTimeout = 8u,      // reserved
+    kStatusTreeDepth = 16u,        // a wide-record pass met a tree deeper than its bound
 };
 
 struct f3
@@ -85,6 +86,41 @@ struct alignas(64) EdgeRec
     float4 a, b, c, d;
 };
 
+// Wide traversal records (4- or 8-way nodes collapsed from the binary tree).
+// The binary internal nodes whose depth below the (mesh) root is a multiple
+// of k (k = 2 for W = 4, k = 3 for W = 8) become wide nodes. A record holds
+// the k binary levels below its node as a slot tree: level l (1..k) has 2^l
+// positions, flat index f = 2^l - 2 + j, parent ((f + 2) >> 1) - 2, so a
+// search applies at every collapsed level exactly the tests the binary search
+// applies there (which makes the set of leaves it reaches the binary one).
+// A leaf met above the last level is forwarded to the leftmost position below
+// it through "pass" positions (the leaf's box with an empty sibling, so the
+// sibling test passes, and a cone of half-angle pi, so the cone test passes);
+// positions under nothing are empty (empty box, cone half-angle -1).
+// The last level's W positions are the children. Floats, structure of arrays
+// over P = 2 W positions (F = 2 W - 2 used):
+//   [0, 6 P)            lower.x, lower.y, lower.z, upper.x, upper.y, upper.z
+//   [6 P, 6 P + W)      child: wide node index, kWideLeaf | sorted leaf position, or kInvalid
+//   [6 P + W, 6 P + 2 W) leaf info of a leaf child: DFS rank | owned-edge count << 30
+//   [6 P + 2 W, 11 P + 2 W) cone axis.x, axis.y, axis.z, half_angle, radius
+// = 384 B (W = 4) / 768 B (W = 8); the nearest search reads the first
+// 224 / 448 B of a record, the silhouette search all of it.
+constexpr uint32_t kWideLeaf = 0x80000000u;
+template <int W>
+struct WideLayout
+{
+    static_assert(W == 4 || W == 8, "wide nodes are 4- or 8-way");
+    static constexpr int P = 2 * W;                 // slot-tree positions (padded)
+    static constexpr int F = 2 * W - 2;             // positions used
+    static constexpr int S0 = W - 2;                // position of the first child slot
+    static constexpr int kLevels = W == 4 ? 2 : 3;  // binary levels per record
+    static constexpr int kChild = 6 * P;            // float offsets
+    static constexpr int kInfo = 6 * P + W;
+    static constexpr int kCone = 6 * P + 2 * W;
+    static constexpr int kRecF4 = (11 * P + 2 * W) / 4;  // record size in float4
+    static constexpr int kStack = W == 4 ? 96 : 128;     // traversal stack entries
+};
+
 // Everything a query kernel reads, passed by value.
 struct TreeView
 {
@@ -107,6 +143,13 @@ struct TreeView
     const uint32_t *mesh_tri_start = nullptr;  // first (global) triangle per mesh
     const int32_t *mesh_edge_start = nullptr;  // first (global) silhouette edge id per mesh
     uint32_t num_meshes = 0;
+    // node width of the near-first nearest / silhouette searches: 2 (binary
+    // records above) or 4 / 8 (wide records); same results at every width
+    int width_near = 2, width_sil = 2;
+    // threads per block of the binary near-first nearest / silhouette searches (64, 128, 256)
+    int block_near = 128, block_sil = 128;
+    const float4 *wide4 = nullptr, *wide8 = nullptr;        // wide records
+    const uint32_t *wide4_of = nullptr, *wide8_of = nullptr;  // wide index of each binary wide-root node
 };
 
 // Where a query's search starts: the whole tree (node 0), or for a batched

@@ -55,6 +55,32 @@ struct BuildArgs
     int32_t *mesh_edge_start;        // first silhouette edge id per mesh
 };
 
+// Wide (4- or 8-way) traversal records of a built tree (build.cu): a count
+// pass (flags + exclusive scan -> wide_of, *count on the device), then a fill
+// pass into `out` (capacity records of WideLayout<W>::kRecF4 float4; a record
+// index at or beyond it is not written and sets kStatusTreeDepth).
+struct WideArgs
+{
+    int width;  // 4 or 8
+    uint32_t num_tris;  // >= 2
+    const NodeRec *nodes;
+    const Box *aabbs;
+    const Cone *cones;
+    const LeafRec *leaves;
+    uint32_t num_meshes;  // batched scenes: depth counted from each mesh root
+    const uint32_t *mesh_root;
+    uint32_t *flags;    // N-1 words (the refit's arrival counters, free after a build)
+    uint32_t *wide_of;  // N-1 words: wide index of each wide-root node
+    uint32_t *count;    // device word: number of wide records
+    void *scratch;      // wide_scratch_bytes(num_tris)
+    float4 *out;
+    uint32_t capacity;  // records of out
+    uint32_t *status;
+};
+size_t wide_scratch_bytes(uint32_t num_tris);
+cudaError_t launch_wide_count(const WideArgs &a, cudaStream_t st);
+cudaError_t launch_wide_fill(const WideArgs &a, cudaStream_t st);
+
 // ---- build.cu
 cudaError_t launch_build_front(const BuildArgs &a, cudaStream_t st);
 cudaError_t launch_build_back(const BuildArgs &a, cudaStream_t st);

@@ -591,8 +591,12 @@ SNCH_DEV void prefetch_l1(const void *p) { asm volatile("prefetch.global.L1 [%0]
 // registers, nine blocks). The traversals wait on dependent L2 loads; the extra
 // resident warps hide more of that latency (measured on the 2M-triangle scene:
 // silhouette -12 %, nearest -2 % against 60 registers / eight blocks).
-template <bool kStats>
-__global__ void __launch_bounds__(128, 10) nearest_fast_kernel(TreeView t, const float *__restrict__ pts, int64_t n,
+// Block size kBlock (64, 128 or 256; TreeView::block_near / block_sil): the same threads per SM
+// (1280 nearest, 1152 silhouette) in smaller or larger blocks. A block's slot
+// on the SM is freed only when its slowest query is done, so smaller blocks
+// lose less to the long tail of per-query work.
+template <bool kStats, int kBlock = 128>
+__global__ void __launch_bounds__(kBlock, 1280 / kBlock) nearest_fast_kernel(TreeView t, const float *__restrict__ pts, int64_t n,
                                                            uint32_t *__restrict__ out_idx, float *__restrict__ out_dist,
                                                            uint32_t *__restrict__ stats, SeedArgs seed)
 {
@@ -794,8 +798,8 @@ SNCH_DEV void leaf_silhouette_info(const TreeView &t, uint32_t pos, uint32_t inf
     }
 }
 
-template <bool kStats>
-__global__ void __launch_bounds__(128, 9) silhouette_fast_kernel(TreeView t, const float *__restrict__ pts,
+template <bool kStats, int kBlock = 128>
+__global__ void __launch_bounds__(kBlock, 1152 / kBlock) silhouette_fast_kernel(TreeView t, const float *__restrict__ pts,
                                                               const uint8_t *__restrict__ flips, int64_t n,
                                                               float *__restrict__ out_dist,
                                                               int32_t *__restrict__ out_edge,
@@ -920,6 +924,417 @@ __global__ void __launch_bounds__(128, 9) silhouette_fast_kernel(TreeView t, con
         seed.defer_radius[q] = best;  // best candidate so far, or the seed radius
         append_failed(seed.defer_list, seed.defer_count, (uint32_t)q, true);
         return;
+    }
+    const bool failed = seed.radius && best_edge < 0 && r0 < INFINITY;
+    if (seed.radius && best_edge < 0)
+        best = INFINITY;  // nothing within the seed radius: the fallback pass answers it
+    out_dist[q] = best;
+    if (out_edge)
+        out_edge[q] = best_edge < 0 ? best_edge : best_edge - qr.edge_off;
+    if (seed.fail_list)
+        append_failed(seed.fail_list, seed.fail_count, (uint32_t)q, failed);
+    if (kStats)
+    {
+        stats[3 * q] = n_int;
+        stats[3 * q + 1] = n_leaf;
+        stats[3 * q + 2] = n_edge;
+    }
+}
+
+// ------------------------------------------------------------------ wide nodes
+// Near-first searches over 4- or 8-way records (WideLayout): one expansion
+// reads a record of k = 2 or 3 binary levels as consecutive 16-B loads. At
+// every collapsed level the search applies the test the binary search applies
+// there -- nearest: a child is kept iff its mindist <= its sibling's
+// minmaxdist (query.cuh:279, 297); silhouette: iff its cone is valid, its
+// mindist <= best^2 and the cone test passes (query.cuh:356-381) -- so it
+// reaches the leaves the binary search reaches, and the answer (the minimum
+// over them, exact ties broken by the leaf's rank in the reference's order)
+// is the binary search's. Pruning by the running best (mindist > best, strict)
+// is applied where it is cheap; it never removes a leaf that attains the
+// minimum, so where it is applied does not change the answer.
+
+// resident blocks per SM of the wide kernels (measured on the 2M-triangle
+// scene: 10 beats 8 and 12 for both widths)
+#ifndef SNCH_WIDE_MIN_BLOCKS
+#define SNCH_WIDE_MIN_BLOCKS 10
+#endif
+
+// ascending compare-exchange on (key, value) pairs held in registers
+SNCH_DEV void cas_pair(float &ka, uint32_t &va, float &kb, uint32_t &vb)
+{
+    if (kb < ka)
+    {
+        const float tk = ka;
+        ka = kb;
+        kb = tk;
+        const uint32_t tv = va;
+        va = vb;
+        vb = tv;
+    }
+}
+// sorting networks: 5 comparators for 4 keys, Batcher's 19 for 8
+template <int W>
+SNCH_DEV void sort_children(float (&k)[W], uint32_t (&v)[W])
+{
+    if constexpr (W == 4)
+    {
+        cas_pair(k[0], v[0], k[1], v[1]);
+        cas_pair(k[2], v[2], k[3], v[3]);
+        cas_pair(k[0], v[0], k[2], v[2]);
+        cas_pair(k[1], v[1], k[3], v[3]);
+        cas_pair(k[1], v[1], k[2], v[2]);
+    }
+    else
+    {
+        constexpr int net[19][2] = {{0, 1}, {2, 3}, {4, 5}, {6, 7}, {0, 2}, {1, 3}, {4, 6}, {5, 7}, {1, 2}, {5, 6},
+                                    {0, 4}, {1, 5}, {2, 6}, {3, 7}, {2, 4}, {3, 5}, {1, 2}, {3, 4}, {5, 6}};
+#pragma unroll
+        for (int c = 0; c < 19; ++c)
+            cas_pair(k[net[c][0]], v[net[c][0]], k[net[c][1]], v[net[c][1]]);
+    }
+}
+
+// box / cone of slot-tree position f (scalar loads; the record's lines are in L1)
+template <int W>
+SNCH_DEV Box wide_box(const float4 *__restrict__ rec, int f)
+{
+    constexpr int P = WideLayout<W>::P;
+    const float *x = reinterpret_cast<const float *>(rec) + f;
+    Box b;
+    b.lower = mk(__ldg(x), __ldg(x + P), __ldg(x + 2 * P));
+    b.upper = mk(__ldg(x + 3 * P), __ldg(x + 4 * P), __ldg(x + 5 * P));
+    return b;
+}
+template <int W>
+SNCH_DEV Cone wide_cone(const float4 *__restrict__ rec, int f)
+{
+    constexpr int P = WideLayout<W>::P;
+    const float *x = reinterpret_cast<const float *>(rec) + WideLayout<W>::kCone + f;
+    Cone c;
+    c.axis = mk(__ldg(x), __ldg(x + P), __ldg(x + 2 * P));
+    c.half_angle = __ldg(x + 3 * P);
+    c.radius = __ldg(x + 4 * P);
+    return c;
+}
+
+template <int W>
+SNCH_DEV void wide_child_ids(const float4 *__restrict__ rec, uint32_t (&ch)[W], uint32_t (&info)[W])
+{
+    using Lay = WideLayout<W>;
+    const uint4 *c4 = reinterpret_cast<const uint4 *>(reinterpret_cast<const float *>(rec) + Lay::kChild);
+    const uint4 *i4 = reinterpret_cast<const uint4 *>(reinterpret_cast<const float *>(rec) + Lay::kInfo);
+#pragma unroll
+    for (int q4 = 0; q4 < W / 4; ++q4)
+    {
+        const uint4 c = __ldg(c4 + q4), i = __ldg(i4 + q4);
+        ch[4 * q4 + 0] = c.x;
+        ch[4 * q4 + 1] = c.y;
+        ch[4 * q4 + 2] = c.z;
+        ch[4 * q4 + 3] = c.w;
+        info[4 * q4 + 0] = i.x;
+        info[4 * q4 + 1] = i.y;
+        info[4 * q4 + 2] = i.z;
+        info[4 * q4 + 3] = i.w;
+    }
+}
+
+// Nearest: the sibling tests of every slot-tree position, four positions per
+// group of 16-B loads (siblings never straddle a group). Returns the accepted
+// positions as a bit mask and the children's squared mindist in md.
+template <int W>
+SNCH_DEV uint32_t wide_nearest_tests(const float4 *__restrict__ rec, f3 p, float (&md)[W])
+{
+    using Lay = WideLayout<W>;
+    constexpr int Q = Lay::P / 4;
+    uint32_t acc = 0;
+#pragma unroll
+    for (int g = 0; g < Q; ++g)
+    {
+        if (4 * g >= Lay::F)
+            break;
+        const float4 lx = __ldg(rec + 0 * Q + g), ly = __ldg(rec + 1 * Q + g), lz = __ldg(rec + 2 * Q + g);
+        const float4 hx = __ldg(rec + 3 * Q + g), hy = __ldg(rec + 4 * Q + g), hz = __ldg(rec + 5 * Q + g);
+        const float lxa[4] = {lx.x, lx.y, lx.z, lx.w}, lya[4] = {ly.x, ly.y, ly.z, ly.w},
+                    lza[4] = {lz.x, lz.y, lz.z, lz.w};
+        const float hxa[4] = {hx.x, hx.y, hx.z, hx.w}, hya[4] = {hy.x, hy.y, hy.z, hy.w},
+                    hza[4] = {hz.x, hz.y, hz.z, hz.w};
+        float gmd[4], gmm[4];
+#pragma unroll
+        for (int c = 0; c < 4; ++c)
+        {
+            Box b;
+            b.lower = mk(lxa[c], lya[c], lza[c]);
+            b.upper = mk(hxa[c], hya[c], hza[c]);
+            gmd[c] = mindist(b, p);
+            gmm[c] = minmaxdist(b, p);
+        }
+#pragma unroll
+        for (int c = 0; c < 4; c += 2)
+        {
+            const int f = 4 * g + c;
+            if (f >= Lay::F)
+                break;
+            const bool pok = f < 2 || ((acc >> (((f + 2) >> 1) - 2)) & 1u);
+            acc |= (uint32_t)(pok && gmd[c] <= gmm[c + 1]) << f;
+            acc |= (uint32_t)(pok && gmd[c + 1] <= gmm[c]) << (f + 1);
+        }
+#pragma unroll
+        for (int c = 0; c < 4; ++c)
+        {
+            const int f = 4 * g + c;
+            if (f >= Lay::S0 && f < Lay::S0 + W)
+                md[f - Lay::S0] = gmd[c];
+        }
+    }
+    return acc >> Lay::S0;
+}
+
+// After the leaves of a record: continue with the nearest accepted internal
+// child, push the others (farthest deepest). key[i] = mindist of an accepted
+// internal child, val[i] = its wide index, kInvalid for the rest. Returns false
+// when the stack is full.
+template <int W, int S>
+SNCH_DEV bool wide_descend(float (&key)[W], uint32_t (&val)[W], uint32_t (&sn)[S], float (&sd)[S], int &sp,
+                           uint32_t &next)
+{
+    sort_children<W>(key, val);
+    next = kInvalid;
+#pragma unroll
+    for (int i = 0; i < W; ++i)
+        if (next == kInvalid && val[i] != kInvalid)
+            next = val[i];
+#pragma unroll
+    for (int i = W - 1; i >= 0; --i)
+    {
+        if (val[i] != kInvalid && val[i] != next)
+        {
+            if (sp >= S)
+                return false;
+            sn[sp] = val[i];
+            sd[sp] = key[i];
+            ++sp;
+        }
+    }
+    return true;
+}
+
+template <int W, bool kStats>
+__global__ void __launch_bounds__(128, SNCH_WIDE_MIN_BLOCKS)
+    nearest_wide_kernel(TreeView t, const float *__restrict__ pts, int64_t n, uint32_t *__restrict__ out_idx,
+                        float *__restrict__ out_dist, uint32_t *__restrict__ stats, SeedArgs seed)
+{
+    using Lay = WideLayout<W>;
+    uint32_t n_int = 0, n_leaf = 0;
+    const int64_t qi = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (qi >= query_count(t, n))
+        return;
+    const int64_t q = query_index(t, qi);
+    const f3 p = load_point(pts, q);
+    uint32_t nearest = kInvalid, best_rank = 0;
+    float best = INFINITY, r0 = INFINITY;
+    if (seed.radius)
+    {
+        r0 = __ldg(seed.radius + q);
+        best = r0 * r0;
+    }
+    const uint32_t ni = t.num_tris - 1;
+    const float4 *__restrict__ recs = W == 4 ? t.wide4 : t.wide8;
+    const QueryRoot qr = query_root(t, q);
+    if (qr.node == kInvalid)
+    {
+    }
+    else if (qr.node >= ni)  // a one-triangle tree or mesh
+        leaf_nearest_fast(t, qr.node - ni, p, best, best_rank, nearest);
+    else
+    {
+        uint32_t sn[Lay::kStack];
+        float sd[Lay::kStack];
+        int sp = 0;
+        uint32_t node = __ldg((W == 4 ? t.wide4_of : t.wide8_of) + qr.node);
+        bool live = !(mindist(load_root_box(t.aabbs + qr.node), p) > best);
+        while (live)
+        {
+            const float4 *rec = recs + (size_t)node * Lay::kRecF4;
+            float md[W];
+            const uint32_t acc = wide_nearest_tests<W>(rec, p, md);
+            uint32_t ch[W], info[W];
+            wide_child_ids<W>(rec, ch, info);
+            if (kStats)
+                ++n_int;
+#pragma unroll
+            for (int i = 0; i < W; ++i)
+            {
+                if (((acc >> i) & 1u) && ch[i] != kInvalid && (ch[i] & kWideLeaf) && md[i] <= best)
+                {
+                    leaf_nearest_fast(t, ch[i] & ~kWideLeaf, p, best, best_rank, nearest);
+                    if (kStats)
+                        ++n_leaf;
+                }
+            }
+            float key[W];
+            uint32_t val[W];
+#pragma unroll
+            for (int i = 0; i < W; ++i)
+            {
+                const bool ok = ((acc >> i) & 1u) && ch[i] != kInvalid && !(ch[i] & kWideLeaf) && md[i] <= best;
+                key[i] = ok ? md[i] : INFINITY;
+                val[i] = ok ? ch[i] : kInvalid;
+            }
+            uint32_t next;
+            if (!wide_descend<W, Lay::kStack>(key, val, sn, sd, sp, next))
+            {
+                atomicOr(t.status, kStatusStackOverflow);
+                nearest = kInvalid;
+                best = NAN;
+                break;
+            }
+            if (next != kInvalid)
+            {
+                node = next;
+                continue;
+            }
+            live = false;
+            while (sp > 0)
+            {
+                --sp;
+                if (!(sd[sp] > best))
+                {
+                    node = sn[sp];
+                    live = true;
+                    break;
+                }
+            }
+        }
+    }
+    if (kStats)
+    {
+        stats[3 * q] = n_int;
+        stats[3 * q + 1] = n_leaf;
+        stats[3 * q + 2] = 0;
+    }
+    const bool failed = seed.radius && nearest == kInvalid && r0 < INFINITY;
+    if (seed.radius && nearest == kInvalid)
+        best = INFINITY;  // nothing within the seed radius: the fallback pass answers it
+    out_idx[q] = nearest == kInvalid ? kInvalid : nearest - qr.tri_off;
+    out_dist[q] = sqrtf(best);
+    if (seed.fail_list)
+        append_failed(seed.fail_list, seed.fail_count, (uint32_t)q, failed);
+}
+
+template <int W, bool kStats>
+__global__ void __launch_bounds__(128, SNCH_WIDE_MIN_BLOCKS)
+    silhouette_wide_kernel(TreeView t, const float *__restrict__ pts, const uint8_t *__restrict__ flips, int64_t n,
+                           float *__restrict__ out_dist, int32_t *__restrict__ out_edge, uint32_t *__restrict__ stats,
+                           SeedArgs seed)
+{
+    using Lay = WideLayout<W>;
+    uint32_t n_int = 0, n_leaf = 0, n_edge = 0;
+    const int64_t qi = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (qi >= query_count(t, n))
+        return;
+    const int64_t q = query_index(t, qi);
+    const f3 p = load_point(pts, q);
+    const bool flip = flips ? __ldg(flips + q) != 0 : false;
+    const float r0 = seed.radius ? __ldg(seed.radius + q) : INFINITY;
+    float best = r0;
+    uint32_t best_key = 0;
+    int32_t best_edge = -1;
+    const uint32_t ni = t.num_tris - 1;
+    const float4 *__restrict__ recs = W == 4 ? t.wide4 : t.wide8;
+    const QueryRoot qr = query_root(t, q);
+    if (qr.node == kInvalid)
+    {
+    }
+    else if (qr.node >= ni)  // a one-triangle tree or mesh
+        leaf_silhouette_fast(t, qr.node - ni, p, flip, best, best_key, best_edge, n_edge);
+    else
+    {
+        uint32_t sn[Lay::kStack];
+        float sd[Lay::kStack];
+        int sp = 0;
+        uint32_t node = __ldg((W == 4 ? t.wide4_of : t.wide8_of) + qr.node);
+        bool live = !(mindist(load_root_box(t.aabbs + qr.node), p) > best * best);
+        while (live)
+        {
+            const float4 *rec = recs + (size_t)node * Lay::kRecF4;
+            const float b2 = best * best;
+            // slot-tree positions in level order (a rolled loop: one inlined cone
+            // test); a position is tested only if its parent position passed;
+            // empty positions fail through their invalid cone, pass positions pass
+            uint32_t acc = 0;
+#pragma unroll 1
+            for (int f = 0; f < Lay::F; ++f)
+            {
+                if (f >= 2 && !((acc >> (((f + 2) >> 1) - 2)) & 1u))
+                    continue;
+                const Box b = wide_box<W>(rec, f);
+                const float m = mindist(b, p);
+                if (m <= b2)
+                {
+                    const Cone cn = wide_cone<W>(rec, f);
+                    if (cn.half_angle >= 0.0f && cone_test(cn, p, b, m))
+                        acc |= 1u << f;
+                }
+            }
+            const uint32_t hits = acc >> Lay::S0;
+            uint32_t ch[W], info[W];
+            wide_child_ids<W>(rec, ch, info);
+            if (kStats)
+                ++n_int;
+#pragma unroll
+            for (int i = 0; i < W; ++i)
+            {
+                if (((hits >> i) & 1u) && (ch[i] & kWideLeaf))
+                {
+                    leaf_silhouette_info(t, ch[i] & ~kWideLeaf, info[i], p, flip, best, best_key, best_edge, n_edge);
+                    if (kStats)
+                        ++n_leaf;
+                }
+            }
+            const float b2n = best * best;
+            float key[W];
+            uint32_t val[W];
+#pragma unroll
+            for (int i = 0; i < W; ++i)
+            {
+                key[i] = INFINITY;
+                val[i] = kInvalid;
+                if (((hits >> i) & 1u) && !(ch[i] & kWideLeaf))
+                {
+                    const float m = mindist(wide_box<W>(rec, Lay::S0 + i), p);
+                    if (m <= b2n)
+                    {
+                        key[i] = m;
+                        val[i] = ch[i];
+                    }
+                }
+            }
+            uint32_t next;
+            if (!wide_descend<W, Lay::kStack>(key, val, sn, sd, sp, next))
+            {
+                atomicOr(t.status, kStatusStackOverflow);
+                best = NAN;
+                best_edge = -1;
+                break;
+            }
+            if (next != kInvalid)
+            {
+                node = next;
+                continue;
+            }
+            live = false;
+            while (sp > 0)
+            {
+                --sp;
+                if (!(sd[sp] > best * best))
+                {
+                    node = sn[sp];
+                    live = true;
+                    break;
+                }
+            }
+        }
     }
     const bool failed = seed.radius && best_edge < 0 && r0 < INFINITY;
     if (seed.radius && best_edge < 0)
@@ -1578,6 +1993,14 @@ __global__ void query_keys_kernel(const float *__restrict__ pts, int64_t n, cons
 namespace
 {
 inline unsigned grid_for(int64_t n, int b) { return (unsigned)((n + b - 1) / b); }
+// the wide searches serve near-first, one-thread-per-query, uncapped launches
+// over a tree whose wide records of that width exist
+inline bool wide_ok(const TreeView &t, int width, const SeedArgs &seed)
+{
+    if (!t.near_first || t.persistent || seed.cap || t.num_tris < 2)
+        return false;
+    return (width == 4 && t.wide4 && t.wide4_of) || (width == 8 && t.wide8 && t.wide8_of);
+}
 // persistent launch: as many 128-thread blocks as the GPU holds at once (fewer for
 // small batches), and a zeroed 64-bit work counter of its own (stream-ordered
 // allocation, so concurrent calls on other streams do not share it)
@@ -1614,13 +2037,27 @@ cudaError_t launch_nearest(const TreeView &t, const float *pts, int64_t n, uint3
 {
     if (n <= 0)
         return cudaSuccess;
-    if (stats)
+    if (wide_ok(t, t.width_near, seed))
+    {
+        const unsigned g = grid_for(n, 128);
+        if (t.width_near == 4)
+            stats ? nearest_wide_kernel<4, true><<<g, 128, 0, st>>>(t, pts, n, idx, dist, stats, seed)
+                  : nearest_wide_kernel<4, false><<<g, 128, 0, st>>>(t, pts, n, idx, dist, nullptr, seed);
+        else
+            stats ? nearest_wide_kernel<8, true><<<g, 128, 0, st>>>(t, pts, n, idx, dist, stats, seed)
+                  : nearest_wide_kernel<8, false><<<g, 128, 0, st>>>(t, pts, n, idx, dist, nullptr, seed);
+    }
+    else if (stats)
         nearest_fast_kernel<true><<<grid_for(n, 128), 128, 0, st>>>(t, pts, n, idx, dist, stats, seed);
     else if (t.near_first && t.num_tris > 1 && t.persistent)
     {
         return seed.radius ? launch_persistent(nearest_persistent_kernel<true>, n, st, t, pts, n, idx, dist, seed)
                            : launch_persistent(nearest_persistent_kernel<false>, n, st, t, pts, n, idx, dist, seed);
     }
+    else if (t.near_first && t.block_near == 64)
+        nearest_fast_kernel<false, 64><<<grid_for(n, 64), 64, 0, st>>>(t, pts, n, idx, dist, nullptr, seed);
+    else if (t.near_first && t.block_near == 256)
+        nearest_fast_kernel<false, 256><<<grid_for(n, 256), 256, 0, st>>>(t, pts, n, idx, dist, nullptr, seed);
     else if (t.near_first)
         nearest_fast_kernel<false><<<grid_for(n, 128), 128, 0, st>>>(t, pts, n, idx, dist, nullptr, seed);
     else
@@ -1633,7 +2070,17 @@ cudaError_t launch_silhouette(const TreeView &t, const float *pts, const uint8_t
 {
     if (n <= 0)
         return cudaSuccess;
-    if (stats)
+    if (wide_ok(t, t.width_sil, seed))
+    {
+        const unsigned g = grid_for(n, 128);
+        if (t.width_sil == 4)
+            stats ? silhouette_wide_kernel<4, true><<<g, 128, 0, st>>>(t, pts, flip, n, dist, edge, stats, seed)
+                  : silhouette_wide_kernel<4, false><<<g, 128, 0, st>>>(t, pts, flip, n, dist, edge, nullptr, seed);
+        else
+            stats ? silhouette_wide_kernel<8, true><<<g, 128, 0, st>>>(t, pts, flip, n, dist, edge, stats, seed)
+                  : silhouette_wide_kernel<8, false><<<g, 128, 0, st>>>(t, pts, flip, n, dist, edge, nullptr, seed);
+    }
+    else if (stats)
         silhouette_fast_kernel<true><<<grid_for(n, 128), 128, 0, st>>>(t, pts, flip, n, dist, edge, stats, seed);
     else if (t.near_first && t.num_tris > 1 && t.persistent)
     {
@@ -1641,6 +2088,11 @@ cudaError_t launch_silhouette(const TreeView &t, const float *pts, const uint8_t
                    ? launch_persistent(silhouette_persistent_kernel<true>, n, st, t, pts, flip, n, dist, edge, seed)
                    : launch_persistent(silhouette_persistent_kernel<false>, n, st, t, pts, flip, n, dist, edge, seed);
     }
+    else if (t.near_first && t.block_sil == 64)
+        silhouette_fast_kernel<false, 64><<<grid_for(n, 64), 64, 0, st>>>(t, pts, flip, n, dist, edge, nullptr, seed);
+    else if (t.near_first && t.block_sil == 256)
+        silhouette_fast_kernel<false, 256>
+            <<<grid_for(n, 256), 256, 0, st>>>(t, pts, flip, n, dist, edge, nullptr, seed);
     else if (t.near_first)
         silhouette_fast_kernel<false><<<grid_for(n, 128), 128, 0, st>>>(t, pts, flip, n, dist, edge, nullptr, seed);
     else
