@@ -34,7 +34,9 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 FULL = {"near": 16_000_000, "sil": 16_000_000, "ray": 16_000_000, "smp": 4_000_000}
-KERNEL_OF = {"near": "nearest_fast_kernel", "sil": "silhouette_fast_kernel", "ray": "ray_kernel",
+# kernels the default configuration runs for each query type (Morton-ordered
+# 16M-query batches: silhouette batches run as warp packets)
+KERNEL_OF = {"near": "nearest_fast_kernel", "sil": "silhouette_packet_kernel", "ray": "ray_kernel",
              "smp": "sample_kernel"}
 # algorithmic bytes per query, reference record sizes: input + output + per
 # expanded internal node (2 child boxes + 2 child refs [+ 2 cones]) + per leaf

@@ -174,6 +174,20 @@ int snch_set_traversal(snch_scene_t scene, int mode);
 #define SNCH_OPT_BLOCK 9
 #define SNCH_OPT_BLOCK_NEAREST 10
 #define SNCH_OPT_BLOCK_SILHOUETTE 11
+/*   SNCH_OPT_PACKET           warp packets for the binary near-first nearest and
+ *                             silhouette searches: a warp's 32 queries walk one shared
+ *                             traversal, each lane applying its own tests and keeping its
+ *                             own answer. 1: always; 2: for Morton-ordered batches (the
+ *                             default of the silhouette search); 0: never (each lane
+ *                             walks its own; the default of the nearest search). Same
+ *                             distances; the silhouette edge id / nearest index equals
+ *                             the per-lane one except on an exact distance tie that falls
+ *                             on a rounding boundary of a box test, where the reference's
+ *                             own choice depends on its visit order.
+ *   SNCH_OPT_PACKET_NEAREST / _SILHOUETTE  the same for one query type. */
+#define SNCH_OPT_PACKET 12
+#define SNCH_OPT_PACKET_NEAREST 13
+#define SNCH_OPT_PACKET_SILHOUETTE 14
 int snch_set_option(snch_scene_t scene, int option, int64_t value);
 
 /* Position of each sorted leaf in the reference's depth-first visit order,

@@ -27,6 +27,7 @@ TRAVERSAL_REFERENCE_ORDER = 1
 OPT_TRAVERSAL, OPT_QUERY_ORDER, OPT_ORDER_MIN_BATCH, OPT_PERSISTENT, OPT_TAIL_CAP = 1, 2, 3, 4, 5
 OPT_NODE_WIDTH, OPT_NODE_WIDTH_NEAREST, OPT_NODE_WIDTH_SILHOUETTE = 6, 7, 8
 OPT_BLOCK, OPT_BLOCK_NEAREST, OPT_BLOCK_SILHOUETTE = 9, 10, 11
+OPT_PACKET, OPT_PACKET_NEAREST, OPT_PACKET_SILHOUETTE = 12, 13, 14
 
 
 def _torch():

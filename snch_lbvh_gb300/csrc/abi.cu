@@ -98,6 +98,7 @@ struct snch_scene_s
     // and the wide records of the built tree: [0] 4-way, [1] 8-way
     int width_near = 2, width_sil = 2;
     int block_near = 128, block_sil = 128;  // threads per block of the binary searches
+    int packet_near = 0, packet_sil = 2;    // warp packets: 0 never, 1 always, 2 Morton-ordered batches
     float4 *wide[2] = {nullptr, nullptr};
     uint32_t *wide_idx[2] = {nullptr, nullptr};  // wide index of each wide-root binary node
     size_t wide_cap[2] = {0, 0};  // records allocated
@@ -120,6 +121,8 @@ struct snch_scene_s
         t.width_sil = width_sil;
         t.block_near = block_near;
         t.block_sil = block_sil;
+        t.packet_near = packet_near;
+        t.packet_sil = packet_sil;
         if (wide_ready[0])
         {
             t.wide4 = wide[0];
@@ -441,6 +444,7 @@ cudaError_t batch_view(const snch_scene_s *s, const float *keys_from, int64_t n,
     uint32_t *order = nullptr;
     e = launch_query_order(b.t, keys_from, n, b.scratch, &order, st);
     b.t.order = order;
+    b.t.order_coherent = 1;
     return e;
 }
 
@@ -497,6 +501,7 @@ int run_query(snch_scene_s *s, const float *pts, const float *radius, int64_t n,
         TreeView t2 = b.t;
         t2.order = defer_list;
         t2.order_count = defer_count;
+        t2.order_coherent = 0;
         SeedArgs s2;
         s2.radius = defer_radius;
         s2.fail_list = fail_list;
@@ -508,6 +513,7 @@ int run_query(snch_scene_s *s, const float *pts, const float *radius, int64_t n,
         TreeView t3 = b.t;
         t3.order = fail_list;
         t3.order_count = fail_count;
+        t3.order_coherent = 0;
         e = launch(t3, SeedArgs());
     }
     if (e == cudaSuccess && num_fallback)
@@ -776,6 +782,16 @@ int snch_set_option(snch_scene_t s, int option, int64_t value)
         if (value != 0 && value != 1)
             return fail(SNCH_ERR_INVALID_ARGUMENT, "SNCH_OPT_PERSISTENT takes 0 or 1");
         s->persistent = (int)value;
+        return SNCH_OK;
+    case SNCH_OPT_PACKET:
+    case SNCH_OPT_PACKET_NEAREST:
+    case SNCH_OPT_PACKET_SILHOUETTE:
+        if (value < 0 || value > 2)
+            return fail(SNCH_ERR_INVALID_ARGUMENT, "SNCH_OPT_PACKET takes 0, 1 or 2");
+        if (option != SNCH_OPT_PACKET_SILHOUETTE)
+            s->packet_near = (int)value;
+        if (option != SNCH_OPT_PACKET_NEAREST)
+            s->packet_sil = (int)value;
         return SNCH_OK;
     case SNCH_OPT_BLOCK:
     case SNCH_OPT_BLOCK_NEAREST:
@@ -1118,8 +1134,16 @@ int snch_query_visits(snch_scene_t s, int kind, const float *in0, const float *i
     // result buffers of the counted launch (discarded)
     char *scratch = nullptr;
     SNCH_CUDA(cudaMallocAsync(reinterpret_cast<void **>(&scratch), 32 * (size_t)n + 256, st));
-    const TreeView t = s->view();
-    cudaError_t e = cudaSuccess;
+    // nearest / silhouette batches are counted in the order a query call runs them
+    // (Morton-ordered above the ordering threshold, which selects the packet form)
+    BatchView b;
+    cudaError_t e = kind <= 1 ? batch_view(s, in0, n, st, b) : cudaSuccess;
+    if (e != cudaSuccess)
+    {
+        cudaFreeAsync(scratch, st);
+        SNCH_CUDA(e);
+    }
+    const TreeView t = kind <= 1 ? b.t : s->view();
     switch (kind)
     {
     case 0:

@@ -148,6 +148,10 @@ struct TreeView
     int width_near = 2, width_sil = 2;
     // threads per block of the binary near-first nearest / silhouette searches (64, 128, 256)
     int block_near = 128, block_sil = 128;
+    // warp packets (a warp's 32 queries walk one shared traversal): 0 never,
+    // 1 always, 2 when the batch is Morton-ordered (order_coherent)
+    int packet_near = 0, packet_sil = 0;
+    int order_coherent = 0;  // order[] is the batch's Morton order (neighbours share warps)
     const float4 *wide4 = nullptr, *wide8 = nullptr;        // wide records
     const uint32_t *wide4_of = nullptr, *wide8_of = nullptr;  // wide index of each binary wide-root node
 };

@@ -1352,6 +1352,314 @@ __global__ void __launch_bounds__(128, SNCH_WIDE_MIN_BLOCKS)
     }
 }
 
+// ------------------------------------------------------------------ warp packets
+// Packet forms of the near-first nearest / silhouette searches (SNCH_OPT_PACKET):
+// the 32 queries of a warp -- neighbours, when the batch is Morton-ordered --
+// walk ONE traversal together. The warp keeps one stack of (node, lane mask)
+// entries in shared memory; at a node every lane whose bit is set applies its
+// own tests to the two children (the record is one broadcast load), the
+// ballots of the lanes that keep each child become the children's masks, and a
+// leaf is evaluated by the lanes that keep it. A lane therefore reaches exactly
+// the leaves its own binary search reaches, with the same tests (minmaxdist
+// sibling rule, cone tests, pruning by its own best), and its answer -- the
+// minimum over them, ties broken by leaf rank -- is the per-lane answer. The
+// warp visits the union of its lanes' nodes, in the order most of them prefer,
+// with every control decision uniform across the warp.
+
+constexpr int kPacketWarps = 4;  // 128-thread blocks
+
+// per-lane start of a packet: lanes of a batched query set may search
+// different meshes; the warp runs one packet per distinct root
+struct PacketLane
+{
+    bool valid;
+    int64_t q;
+    f3 p;
+    QueryRoot qr;
+};
+
+template <bool kStats>
+__global__ void __launch_bounds__(128, 10) nearest_packet_kernel(TreeView t, const float *__restrict__ pts, int64_t n,
+                                                             uint32_t *__restrict__ out_idx,
+                                                             float *__restrict__ out_dist,
+                                                             uint32_t *__restrict__ stats, SeedArgs seed)
+{
+    __shared__ uint32_t st_node[kPacketWarps][kStackDepth];
+    __shared__ uint32_t st_mask[kPacketWarps][kStackDepth];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int64_t qi = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const bool valid = qi < query_count(t, n);
+    if (__ballot_sync(0xffffffffu, valid) == 0u)
+        return;
+    const int64_t q = valid ? query_index(t, qi) : 0;
+    const f3 p = valid ? load_point(pts, q) : mk(0.0f, 0.0f, 0.0f);
+    uint32_t nearest = kInvalid, best_rank = 0, n_int = 0, n_leaf = 0;
+    float best = INFINITY, r0 = INFINITY;
+    if (valid && seed.radius)
+    {
+        r0 = __ldg(seed.radius + q);
+        best = r0 * r0;
+    }
+    const uint32_t ni = t.num_tris - 1;
+    QueryRoot qr = valid ? query_root(t, q) : QueryRoot{kInvalid, 0u, 0};
+    if (valid && qr.node != kInvalid && qr.node >= ni)  // a one-triangle tree or mesh
+        leaf_nearest_fast(t, qr.node - ni, p, best, best_rank, nearest);
+    bool overflow = false;
+    uint32_t pending = __ballot_sync(0xffffffffu, valid && qr.node != kInvalid && qr.node < ni);
+    while (pending)
+    {
+        const int leader = __ffs(pending) - 1;
+        const uint32_t root = __shfl_sync(0xffffffffu, qr.node, leader);
+        const uint32_t mine = __ballot_sync(0xffffffffu, ((pending >> lane) & 1u) && qr.node == root);
+        pending &= ~mine;
+        bool in = (mine >> lane) & 1u;
+        if (in)
+            in = !(mindist(load_root_box(t.aabbs + root), p) > best);
+        uint32_t mask = __ballot_sync(0xffffffffu, in);
+        uint32_t node = root;
+        int sp = 0;
+        while (true)
+        {
+            if (mask == 0u)
+            {
+                if (sp == 0)
+                    break;
+                --sp;
+                node = st_node[w][sp];
+                mask = st_mask[w][sp];
+                continue;
+            }
+            const bool act = (mask >> lane) & 1u;
+            Box lb, rb;
+            uint32_t L, R;
+            unpack_inner(load_inner(t.inner + node), lb, rb, L, R);
+            float Lmd = INFINITY, Rmd = INFINITY;
+            bool aL = false, aR = false;
+            if (act)
+            {
+                if (kStats)
+                    ++n_int;
+                Lmd = mindist(lb, p);
+                Rmd = mindist(rb, p);
+                const float Lmm = minmaxdist(lb, p), Rmm = minmaxdist(rb, p);
+                aL = Lmd <= Rmm;  // query.cuh:279, 297
+                aR = Rmd <= Lmm;
+                if (aL && L >= ni && Lmd <= best)
+                {
+                    leaf_nearest_fast(t, L - ni, p, best, best_rank, nearest);
+                    if (kStats)
+                        ++n_leaf;
+                }
+                if (aR && R >= ni && Rmd <= best)
+                {
+                    leaf_nearest_fast(t, R - ni, p, best, best_rank, nearest);
+                    if (kStats)
+                        ++n_leaf;
+                }
+            }
+            const uint32_t pL = __ballot_sync(0xffffffffu, aL && L < ni && Lmd <= best);
+            const uint32_t pR = __ballot_sync(0xffffffffu, aR && R < ni && Rmd <= best);
+            const uint32_t votes = __ballot_sync(0xffffffffu, act && Lmd <= Rmd) & (pL | pR);
+            if (pL && pR)
+            {
+                if (sp >= kStackDepth)
+                {
+                    overflow = true;
+                    break;
+                }
+                const bool l_first = 2 * __popc(votes) >= __popc(pL | pR);
+                __syncwarp();  // every lane has read the slot it may reuse
+                if (lane == 0)
+                {
+                    st_node[w][sp] = l_first ? R : L;
+                    st_mask[w][sp] = l_first ? pR : pL;
+                }
+                __syncwarp();
+                ++sp;
+                node = l_first ? L : R;
+                mask = l_first ? pL : pR;
+            }
+            else if (pL | pR)
+            {
+                node = pL ? L : R;
+                mask = pL ? pL : pR;
+            }
+            else
+                mask = 0u;
+        }
+        if (overflow)
+            break;
+    }
+    if (overflow)
+    {
+        if (lane == 0)
+            atomicOr(t.status, kStatusStackOverflow);
+        nearest = kInvalid;
+        best = NAN;
+    }
+    if (!valid)
+        return;
+    if (kStats)
+    {
+        stats[3 * q] = n_int;
+        stats[3 * q + 1] = n_leaf;
+        stats[3 * q + 2] = 0;
+    }
+    const bool failed = seed.radius && nearest == kInvalid && r0 < INFINITY;
+    if (seed.radius && nearest == kInvalid)
+        best = INFINITY;  // nothing within the seed radius: the fallback pass answers it
+    out_idx[q] = nearest == kInvalid ? kInvalid : nearest - qr.tri_off;
+    out_dist[q] = sqrtf(best);
+    if (seed.fail_list)
+        append_failed(seed.fail_list, seed.fail_count, (uint32_t)q, failed);
+}
+
+template <bool kStats>
+__global__ void __launch_bounds__(128, 9) silhouette_packet_kernel(TreeView t, const float *__restrict__ pts,
+                                                               const uint8_t *__restrict__ flips, int64_t n,
+                                                               float *__restrict__ out_dist,
+                                                               int32_t *__restrict__ out_edge,
+                                                               uint32_t *__restrict__ stats, SeedArgs seed)
+{
+    __shared__ uint32_t st_node[kPacketWarps][kStackDepth];
+    __shared__ uint32_t st_mask[kPacketWarps][kStackDepth];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int64_t qi = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const bool valid = qi < query_count(t, n);
+    if (__ballot_sync(0xffffffffu, valid) == 0u)
+        return;
+    const int64_t q = valid ? query_index(t, qi) : 0;
+    const f3 p = valid ? load_point(pts, q) : mk(0.0f, 0.0f, 0.0f);
+    const bool flip = valid && flips ? __ldg(flips + q) != 0 : false;
+    const float r0 = valid && seed.radius ? __ldg(seed.radius + q) : INFINITY;
+    float best = r0;
+    uint32_t best_key = 0, n_int = 0, n_leaf = 0, n_edge = 0;
+    int32_t best_edge = -1;
+    const uint32_t ni = t.num_tris - 1;
+    QueryRoot qr = valid ? query_root(t, q) : QueryRoot{kInvalid, 0u, 0};
+    if (valid && qr.node != kInvalid && qr.node >= ni)  // a one-triangle tree or mesh
+        leaf_silhouette_fast(t, qr.node - ni, p, flip, best, best_key, best_edge, n_edge);
+    bool overflow = false;
+    uint32_t pending = __ballot_sync(0xffffffffu, valid && qr.node != kInvalid && qr.node < ni);
+    while (pending)
+    {
+        const int leader = __ffs(pending) - 1;
+        const uint32_t root = __shfl_sync(0xffffffffu, qr.node, leader);
+        const uint32_t mine = __ballot_sync(0xffffffffu, ((pending >> lane) & 1u) && qr.node == root);
+        pending &= ~mine;
+        bool in = (mine >> lane) & 1u;
+        if (in)
+            in = !(mindist(load_root_box(t.aabbs + root), p) > best * best);
+        uint32_t mask = __ballot_sync(0xffffffffu, in);
+        uint32_t node = root;
+        int sp = 0;
+        while (true)
+        {
+            if (mask == 0u)
+            {
+                if (sp == 0)
+                    break;
+                --sp;
+                node = st_node[w][sp];
+                mask = st_mask[w][sp];
+                continue;
+            }
+            const bool act = (mask >> lane) & 1u;
+            Box lb, rb;
+            uint32_t L, R, Linfo, Rinfo;
+            const InnerRec rec = load_inner(t.inner + node);
+            unpack_inner(rec, lb, rb, L, R);
+            unpack_leaf_info(rec, Linfo, Rinfo);
+            float Lmd = INFINITY, Rmd = INFINITY;
+            bool hitL = false, hitR = false;
+            if (act)
+            {
+                if (kStats)
+                    ++n_int;
+                const float4 *cr = reinterpret_cast<const float4 *>(t.inner_cones + node);
+                InnerConeRec icr;
+                icr.a = __ldg(cr);
+                icr.b = __ldg(cr + 1);
+                icr.c = __ldg(cr + 2);
+                Cone lc, rc;
+                unpack_cones(icr, lc, rc);
+                Lmd = mindist(lb, p);
+                Rmd = mindist(rb, p);
+                const float b2 = best * best;
+                hitL = Lmd <= b2 && lc.half_angle >= 0.0f && cone_test(lc, p, lb, Lmd);
+                hitR = Rmd <= b2 && rc.half_angle >= 0.0f && cone_test(rc, p, rb, Rmd);
+                if (hitL && L >= ni)
+                {
+                    leaf_silhouette_info(t, L - ni, Linfo, p, flip, best, best_key, best_edge, n_edge);
+                    if (kStats)
+                        ++n_leaf;
+                }
+                if (hitR && R >= ni)
+                {
+                    leaf_silhouette_info(t, R - ni, Rinfo, p, flip, best, best_key, best_edge, n_edge);
+                    if (kStats)
+                        ++n_leaf;
+                }
+            }
+            const float b2n = best * best;
+            const uint32_t pL = __ballot_sync(0xffffffffu, hitL && L < ni && Lmd <= b2n);
+            const uint32_t pR = __ballot_sync(0xffffffffu, hitR && R < ni && Rmd <= b2n);
+            const uint32_t votes = __ballot_sync(0xffffffffu, act && Lmd <= Rmd) & (pL | pR);
+            if (pL && pR)
+            {
+                if (sp >= kStackDepth)
+                {
+                    overflow = true;
+                    break;
+                }
+                const bool l_first = 2 * __popc(votes) >= __popc(pL | pR);
+                __syncwarp();  // every lane has read the slot it may reuse
+                if (lane == 0)
+                {
+                    st_node[w][sp] = l_first ? R : L;
+                    st_mask[w][sp] = l_first ? pR : pL;
+                }
+                __syncwarp();
+                ++sp;
+                node = l_first ? L : R;
+                mask = l_first ? pL : pR;
+            }
+            else if (pL | pR)
+            {
+                node = pL ? L : R;
+                mask = pL ? pL : pR;
+            }
+            else
+                mask = 0u;
+        }
+        if (overflow)
+            break;
+    }
+    if (overflow)
+    {
+        if (lane == 0)
+            atomicOr(t.status, kStatusStackOverflow);
+        best = NAN;
+        best_edge = -1;
+    }
+    if (!valid)
+        return;
+    const bool failed = seed.radius && best_edge < 0 && r0 < INFINITY;
+    if (seed.radius && best_edge < 0)
+        best = INFINITY;  // nothing within the seed radius: the fallback pass answers it
+    out_dist[q] = best;
+    if (out_edge)
+        out_edge[q] = best_edge < 0 ? best_edge : best_edge - qr.edge_off;
+    if (seed.fail_list)
+        append_failed(seed.fail_list, seed.fail_count, (uint32_t)q, failed);
+    if (kStats)
+    {
+        stats[3 * q] = n_int;
+        stats[3 * q + 1] = n_leaf;
+        stats[3 * q + 2] = n_edge;
+    }
+}
+
 // ------------------------------------------------------------------ persistent forms
 // The per-query traversals above run one query per thread; a warp then runs
 // until its slowest query is done, and the per-query work of the nearest and
@@ -1993,6 +2301,12 @@ __global__ void query_keys_kernel(const float *__restrict__ pts, int64_t n, cons
 namespace
 {
 inline unsigned grid_for(int64_t n, int b) { return (unsigned)((n + b - 1) / b); }
+// the packet searches serve near-first, binary-record, uncapped launches
+inline bool packet_ok(const TreeView &t, int packet, int width, const SeedArgs &seed)
+{
+    const bool on = packet == 1 || (packet == 2 && t.order_coherent);
+    return on && width == 2 && t.near_first && !t.persistent && !seed.cap && t.num_tris > 1;
+}
 // the wide searches serve near-first, one-thread-per-query, uncapped launches
 // over a tree whose wide records of that width exist
 inline bool wide_ok(const TreeView &t, int width, const SeedArgs &seed)
@@ -2037,7 +2351,14 @@ cudaError_t launch_nearest(const TreeView &t, const float *pts, int64_t n, uint3
 {
     if (n <= 0)
         return cudaSuccess;
-    if (wide_ok(t, t.width_near, seed))
+    if (packet_ok(t, t.packet_near, t.width_near, seed))
+    {
+        if (stats)
+            nearest_packet_kernel<true><<<grid_for(n, 128), 128, 0, st>>>(t, pts, n, idx, dist, stats, seed);
+        else
+            nearest_packet_kernel<false><<<grid_for(n, 128), 128, 0, st>>>(t, pts, n, idx, dist, nullptr, seed);
+    }
+    else if (wide_ok(t, t.width_near, seed))
     {
         const unsigned g = grid_for(n, 128);
         if (t.width_near == 4)
@@ -2070,7 +2391,16 @@ cudaError_t launch_silhouette(const TreeView &t, const float *pts, const uint8_t
 {
     if (n <= 0)
         return cudaSuccess;
-    if (wide_ok(t, t.width_sil, seed))
+    if (packet_ok(t, t.packet_sil, t.width_sil, seed))
+    {
+        if (stats)
+            silhouette_packet_kernel<true>
+                <<<grid_for(n, 128), 128, 0, st>>>(t, pts, flip, n, dist, edge, stats, seed);
+        else
+            silhouette_packet_kernel<false>
+                <<<grid_for(n, 128), 128, 0, st>>>(t, pts, flip, n, dist, edge, nullptr, seed);
+    }
+    else if (wide_ok(t, t.width_sil, seed))
     {
         const unsigned g = grid_for(n, 128);
         if (t.width_sil == 4)

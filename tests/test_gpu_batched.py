@@ -5,7 +5,7 @@ import numpy as np
 import pytest
 
 from conftest import golden_names, load_golden
-from test_gpu_parity import bits, built_scene
+from test_gpu_parity import bits, built_scene, check_edge_ids
 
 pytestmark = pytest.mark.gpu
 
@@ -35,7 +35,7 @@ def check_batch(snch, ms, rng, per_mesh=3000):
     b.compute_silhouettes()
     b.build_bvh()
     assert b.num_meshes == len(ms)
-    mesh_ids, pts, flips, expect = [], [], [], []
+    mesh_ids, pts, flips, expect, tops = [], [], [], [], []
     for m, (v, f) in enumerate(ms):
         if len(v) == 0:
             p = rng.random((50, 3), dtype=np.float32)
@@ -47,7 +47,9 @@ def check_batch(snch, ms, rng, per_mesh=3000):
             i, d = s.query_nearest(p)
             sd, se = s.query_silhouette(p, fl)
             expect.append([x.cpu().numpy() for x in (i, d, sd, se)])
+            tops.append(s.export_topology()[2])
         else:
+            tops.append(None)
             n = len(p)
             expect.append([np.full(n, -1, np.int32), np.full(n, np.inf, np.float32), np.full(n, np.inf, np.float32),
                            np.full(n, -1, np.int32)])
@@ -60,8 +62,21 @@ def check_batch(snch, ms, rng, per_mesh=3000):
     i, d = b.query_nearest_batch(mesh_ids[perm], pts[perm])
     sd, se = b.query_silhouette_batch(mesh_ids[perm], pts[perm], flips[perm])
     got = [x.cpu().numpy() for x in (i, d, sd, se)]
-    for g, e in zip(got, exp):
+    for g, e in zip(got[:3], exp[:3]):
         np.testing.assert_array_equal(bits(g), bits(e[perm]))
+    # silhouette edge ids, mesh by mesh: equal or an exact tie (warp packets)
+    back = np.empty_like(perm)
+    back[perm] = np.arange(len(perm))
+    se_in = got[3][back]
+    start = 0
+    for m, (v, f) in enumerate(ms):
+        k = int((mesh_ids == m).sum())  # mesh_ids are mesh-major before the permutation
+        sl = slice(start, start + k)
+        if tops[m] is not None:
+            check_edge_ids(se_in[sl], exp[3][sl], exp[2][sl], pts[sl], v, tops[m])
+        else:
+            np.testing.assert_array_equal(se_in[sl], exp[3][sl])
+        start += k
     assert b.device_status() == 0
     return b
 

@@ -6,7 +6,7 @@ whose results are the plain ones."""
 import numpy as np
 import pytest
 
-from test_gpu_parity import bits
+from test_gpu_parity import bits, check_edge_ids
 
 pytestmark = pytest.mark.gpu
 
@@ -59,7 +59,7 @@ def test_graph_rebuild_and_queries(snch, width):
         st.synchronize()
         got = [out_n[0].cpu().numpy(), bits(out_n[1].cpu().numpy()), bits(out_s[0].cpu().numpy()),
                out_s[1].cpu().numpy()]
-        exp = direct(snch, v, f, q, fl)
+        exp = direct(snch, v, f, q, fl, width)
         for x, y in zip(exp, got):
             np.testing.assert_array_equal(y, x)
     assert s.device_status() == 0
@@ -131,7 +131,8 @@ def test_autotune_keeps_results(snch):
     i, d = s.query_nearest(pts)
     sd, se = s.query_silhouette(pts, flip)
     got = [i.cpu().numpy(), bits(d.cpu().numpy()), bits(sd.cpu().numpy()), se.cpu().numpy()]
-    for x, y in zip(exp, got):
+    for x, y in zip(exp[:3], got[:3]):
         np.testing.assert_array_equal(y, x)
+    check_edge_ids(got[3], exp[3], sd.cpu().numpy(), pts, v, s.export_topology()[2])
     s.build_bvh()  # a rebuild keeps the chosen widths
     assert s.device_status() == 0

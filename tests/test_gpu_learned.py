@@ -13,7 +13,7 @@ import numpy as np
 import pytest
 
 from oracle import mlp_oracle as mo
-from test_gpu_parity import bits, built_scene
+from test_gpu_parity import bits, check_edge_ids, built_scene
 
 pytestmark = pytest.mark.gpu
 
@@ -159,7 +159,8 @@ def test_learned_radius_queries_identical(trained):
     sd0, se0 = s.query_silhouette(pts, flip)
     sd1, se1 = s.query_silhouette_seeded(pts, rs, flip, num_fallback=nf)
     np.testing.assert_array_equal(bits(sd1.cpu().numpy()), bits(sd0.cpu().numpy()))
-    np.testing.assert_array_equal(se1.cpu().numpy(), se0.cpu().numpy())
+    check_edge_ids(se1.cpu().numpy(), se0.cpu().numpy(), sd0.cpu().numpy(), pts.cpu().numpy(),
+                   s.vertices().cpu().numpy(), s.export_topology()[2])
     frac_sil = int(nf.item()) / len(pts)
     assert frac_near < 0.5 and frac_sil < 0.5, (frac_near, frac_sil)
     assert s.device_status() == 0

@@ -37,6 +37,33 @@ def snch():
     return snch_lbvh_gb300
 
 
+def seg_dist64(p, a, b):
+    """FP64 distance from points p (n, 3) to segments a-b (n, 3)."""
+    p, a, b = (np.asarray(x, np.float64) for x in (p, a, b))
+    u, v = b - a, p - a
+    t = np.clip(np.einsum("ij,ij->i", u, v) / np.maximum(np.einsum("ij,ij->i", u, u), 1e-300), 0.0, 1.0)
+    return np.linalg.norm(p - (a + u * t[:, None]), axis=1)
+
+
+def check_edge_ids(got, exp, dist, pts, verts, edge_verts, max_frac=1e-4):
+    """Silhouette edge ids of two searches with bit-identical distances: equal, or
+    both edges at the returned distance (an exact tie that falls on a rounding
+    boundary of a box test, where the reference's own choice depends on its visit
+    order), in at most max_frac of the queries (and at most 3 below 30,000)."""
+    got, exp = np.asarray(got), np.asarray(exp)
+    bad = np.nonzero(got != exp)[0]
+    assert len(bad) <= max(3, max_frac * len(got)), f"{len(bad)} edge ids differ"
+    if len(bad) == 0:
+        return 0
+    assert np.all(got[bad] >= 0) and np.all(exp[bad] >= 0), "only one search found a silhouette edge"
+    d = np.asarray(dist, np.float64)[bad]
+    for e in (got[bad], exp[bad]):
+        ev = np.asarray(edge_verts)[e]
+        de = seg_dist64(np.asarray(pts)[bad], verts[ev[:, 1]], verts[ev[:, 2]])
+        assert np.all(np.abs(de - d) <= 1e-6 * np.maximum(d, 1e-3)), "differing edge ids are not a distance tie"
+    return len(bad)
+
+
 def built_scene(snch, verts, tris):
     s = snch.Scene(verts, tris)
     s.compute_silhouettes()
@@ -236,8 +263,9 @@ def test_near_first_equals_reference_order_config1(snch):
     s = built_scene(snch, v, f)
     a = run_all(s, q, snch.TRAVERSAL_REFERENCE_ORDER)
     b = run_all(s, q, snch.TRAVERSAL_NEAR_FIRST)
-    for x, y in zip(a, b):
+    for x, y in zip(a[:3], b[:3]):
         np.testing.assert_array_equal(x, y)
+    check_edge_ids(b[3], a[3], a[2].view(np.float32), pts, v, s.export_topology()[2])
     assert s.device_status() == 0
 
 
@@ -261,8 +289,10 @@ def test_query_order_does_not_change_results(snch):
     a = everything()
     s.set_option(snch.OPT_QUERY_ORDER, 1)
     b = everything()
-    for x, y in zip(a, b):
-        np.testing.assert_array_equal(x.view(np.uint8), y.view(np.uint8))
+    for k, (x, y) in enumerate(zip(a, b)):
+        if k != 3:  # silhouette edge ids: ordered batches run as warp packets
+            np.testing.assert_array_equal(x.view(np.uint8), y.view(np.uint8))
+    check_edge_ids(b[3], a[3], a[2], q["sil_pts"], v, s.export_topology()[2])
     assert s.device_status() == 0
 
 

@@ -30,6 +30,7 @@ def answers(s, pts, flip):
 
 
 def check_widths(snch, s, pts, flip):
+    s.set_option(snch.OPT_PACKET, 0)  # wide searches run per lane: compare with per-lane binary
     s.set_option(snch.OPT_NODE_WIDTH, 2)
     base = answers(s, pts, flip)
     for w in WIDTHS:
@@ -87,9 +88,12 @@ def test_wide_set_before_build_and_per_type(snch):
     v, f = meshes.noisy_icosphere(4, 1.0, 0.01, seed=3)
     pts = np.concatenate([meshes.box_queries(v, 200_000, 1.2, seed=2), tie_probes(v, f)])
     flip = (np.arange(len(pts)) % 3 == 0).astype(np.uint8)
-    ref = answers(built_scene(snch, v, f), pts, flip)
+    s0 = built_scene(snch, v, f)
+    s0.set_option(snch.OPT_PACKET, 0)
+    ref = answers(s0, pts, flip)
     for wn, ws in ((4, 8), (8, 4), (2, 8), (4, 2)):
         s = snch.Scene(v, f)
+        s.set_option(snch.OPT_PACKET, 0)
         s.set_option(snch.OPT_NODE_WIDTH_NEAREST, wn)
         s.set_option(snch.OPT_NODE_WIDTH_SILHOUETTE, ws)
         s.compute_silhouettes()
@@ -121,6 +125,7 @@ def test_wide_seeded_equals_unseeded(snch, w):
     rng = np.random.default_rng(7)
     sc = meshes.wost_scene(seed=2, n_meshes=8, torus_nu=60, torus_nv=30, ico_level=4)
     s = built_scene(snch, sc.verts, sc.faces)
+    s.set_option(snch.OPT_PACKET, 0)
     pts = rng.random((300_000, 3), dtype=np.float32)
     flip = (rng.random(len(pts)) < 0.5).astype(np.uint8)
     i0, d0 = s.query_nearest(pts)
@@ -145,6 +150,7 @@ def test_wide_batched_equals_binary(snch, w):
     ms = mixed_meshes(rng, 30)
     ms.insert(4, (np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], np.float32), np.array([[0, 1, 2]], np.int32)))
     b = snch.BatchedScene(ms)
+    b.set_option(snch.OPT_PACKET, 0)
     b.compute_silhouettes()
     b.build_bvh()
     mesh, pts = [], []
