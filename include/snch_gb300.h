@@ -97,6 +97,25 @@ int snch_build_bvh(snch_scene_t scene, snch_stream_t stream);
  * reference's device layout (device pointers owned by the scene). */
 int snch_get_bvh_view(snch_scene_t scene, snch_bvh_view *out_view);
 
+/* scene_loader<3>(filename) scene_loader.cuh:86-152, a host-side reader: "v x y z"
+ * vertices and "f a b c" triangles (1-based in the file, 0-based out; the first
+ * three indices of a longer face; every other line ignored), into caller HOST
+ * buffers of vert_capacity vertices (3 floats each) and tri_capacity triangles;
+ * *num_verts / *num_tris receive the counts in the file whatever the capacities,
+ * so a call with capacities 0 sizes the buffers. A face token "7/1/3" or "7//3"
+ * gives vertex 7 (the reference's loader cannot read such files). Missing
+ * numbers read as 0. Error "Could not open .obj file." as the reference's. */
+int snch_obj_read(const char *path, float *verts, int64_t vert_capacity, int32_t *tris, int64_t tri_capacity,
+                  int64_t *num_verts, int64_t *num_tris);
+
+/* A built plain scene to / from a flat binary file (no reference counterpart;
+ * the reference rebuilds every time): the mesh, the silhouette topology and
+ * every tree array, so that snch_scene_load gives a built scene with the same
+ * tree and the same query results without rebuilding. Host-endian, for this
+ * library's version; save synchronises `stream`, load is synchronous. */
+int snch_scene_save(snch_scene_t scene, const char *path, snch_stream_t stream);
+int snch_scene_load(const char *path, snch_scene_t *out_scene, snch_stream_t stream);
+
 /* ~scene: frees every device buffer of the scene. */
 int snch_scene_destroy(snch_scene_t scene);
 
@@ -209,6 +228,24 @@ int snch_query_nearest(snch_scene_t scene, const float *points_xyz, int64_t n, u
 int snch_query_silhouette(snch_scene_t scene, const float *points_xyz, const uint8_t *flip, int64_t n,
                           float *out_distance, int32_t *out_edge, snch_stream_t stream);
 
+/* query_device(bvh, overlaps(box), out, max) query.cuh:177-231: for each query
+ * box (6 floats: lower xyz, upper xyz) the ORIGINAL indices of the triangles whose
+ * leaf box (FLT_EPSILON-inflated, scene.cuh:870-885) overlaps it, in the
+ * reference's visit order; the first max_per_query of them go to
+ * out_index[q * max_per_query + k], out_count[q] = how many overlap in all (the
+ * reference's return value; may exceed max_per_query). Plain scenes only. */
+int snch_query_overlap(snch_scene_t scene, const float *boxes, int64_t n, uint32_t max_per_query,
+                       uint32_t *out_index, uint32_t *out_count, snch_stream_t stream);
+/* query_device(bvh, line_intersect(line), element_test, out, max) query.cuh:15-77
+ * with the scene's triangles as elements: for each line (origin xyz, direction
+ * xyz; infinite both ways, the slab test of aabb.cuh:329-348) the triangles it
+ * crosses, each with the line parameter t of the crossing, in the reference's
+ * visit order. The element test (the caller's functor in the reference, which
+ * ships none for triangles) is intersect_test's arithmetic (scene.cuh:1005-1052)
+ * for a line: any t. Layout as snch_query_overlap; out_t beside out_index. */
+int snch_query_line(snch_scene_t scene, const float *origins, const float *dirs, int64_t n, uint32_t max_per_query,
+                    uint32_t *out_index, float *out_t, uint32_t *out_count, snch_stream_t stream);
+
 /* query_device(bvh, ray_intersect(ray(o, d), tmax), intersect_test()) query.cuh:82-169
  * -> (hit, t, uv (2 floats), object index); t = +inf, uv = 0, index 0xFFFFFFFF on a miss. */
 int snch_query_ray(snch_scene_t scene, const float *origins_xyz, const float *dirs_xyz, const float *tmax,
@@ -290,7 +327,9 @@ int snch_get_search_config(snch_scene_t scene, int which, int32_t *out_width, in
  * here: refill the same device buffers (vertex positions through
  * snch_scene_vertices, queries) between launches. The scene must have been
  * built once before the capture and must outlive the graph; its tree holds what
- * the last launch built. `stream` must be a created stream. */
+ * the last launch built. `stream` must be a created stream. A launch rewrites the
+ * scene's tree: order it after every other call still using the scene (an event
+ * or a synchronisation when they run on other streams), as for snch_build_bvh. */
 typedef struct snch_graph_s *snch_graph_t;
 int snch_graph_create(snch_scene_t scene, int rebuild, const int32_t *near_mesh, const float *near_points,
                       int64_t n_near, int32_t *near_index, float *near_distance, const int32_t *sil_mesh,

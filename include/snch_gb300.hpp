@@ -135,6 +135,34 @@ class scene3
     }
     void set_option(int option, int64_t value) { check(snch_set_option(h_, option, value)); }
 
+    // query_device(overlaps(box)) / query_device(line_intersect(line)): the first
+    // max_per_query results per query at [q * max_per_query ...], totals in count
+    void query_overlap(const float *boxes_lo_hi, int64_t n, uint32_t max_per_query, uint32_t *index,
+                       uint32_t *count, snch_stream_t stream = nullptr) const
+    {
+        check(snch_query_overlap(h_, boxes_lo_hi, n, max_per_query, index, count, stream));
+    }
+    void query_line(const float *origins_xyz, const float *dirs_xyz, int64_t n, uint32_t max_per_query,
+                    uint32_t *index, float *t, uint32_t *count, snch_stream_t stream = nullptr) const
+    {
+        check(snch_query_line(h_, origins_xyz, dirs_xyz, n, max_per_query, index, t, count, stream));
+    }
+
+    // a built scene to / from a file (no rebuild on load)
+    void save(const std::string &path, snch_stream_t stream = nullptr) const
+    {
+        check(snch_scene_save(h_, path.c_str(), stream));
+    }
+    static scene3 load(const std::string &path, snch_stream_t stream = nullptr)
+    {
+        snch_scene_t h = nullptr;
+        check(snch_scene_load(path.c_str(), &h, stream));
+        scene3 s(h);
+        s.view_ = {};
+        check(snch_get_bvh_view(h, &s.view_));
+        return s;
+    }
+
     snch_scene_t handle() const { return h_; }
 
   protected:
@@ -147,6 +175,35 @@ class scene3
     }
     snch_scene_t h_ = nullptr;
     snch_bvh_view view_{};
+};
+
+// scene_loader<3>(filename) scene_loader.cuh:86-152: vertices (float3-like) and
+// 0-based triangles (int3-like) of an OBJ file, throwing std::runtime_error as
+// the reference does ("Could not open .obj file.")
+template <typename Float3, typename Int3>
+class scene_loader3
+{
+  public:
+    explicit scene_loader3(const std::string &filename)
+    {
+        int64_t nv = 0, nt = 0;
+        check(snch_obj_read(filename.c_str(), nullptr, 0, nullptr, 0, &nv, &nt));
+        std::vector<float> v(static_cast<size_t>(3 * nv));
+        std::vector<int32_t> t(static_cast<size_t>(3 * nt));
+        check(snch_obj_read(filename.c_str(), v.data(), nv, t.data(), nt, &nv, &nt));
+        for (int64_t i = 0; i < nv; ++i)
+            vertices_.push_back(Float3{v[3 * i], v[3 * i + 1], v[3 * i + 2]});
+        for (int64_t i = 0; i < nt; ++i)
+            indices_.push_back(Int3{t[3 * i], t[3 * i + 1], t[3 * i + 2]});
+    }
+    const std::vector<Float3> &get_vertices() const { return vertices_; }
+    const std::vector<Int3> &get_indices() const { return indices_; }
+    std::size_t vertices_size() const { return vertices_.size(); }
+    std::size_t primitives_size() const { return indices_.size(); }
+
+  private:
+    std::vector<Float3> vertices_;
+    std::vector<Int3> indices_;
 };
 
 // Many independent meshes in one scene (snch_batch_*): one build, one query

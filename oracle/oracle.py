@@ -64,6 +64,8 @@ def _declare(L):
     L.orc_max_depth.argtypes = [P, I64]
     L.orc_max_depth.restype = I
     L.orc_leaf_ranks.argtypes = [P, I64, P]
+    L.orc_query_overlap.argtypes = [P, P, I64, I64, P, P, I]
+    L.orc_query_line.argtypes = [P, P, P, I64, I64, P, P, P, I]
 
 
 def _p(a: np.ndarray | None):
@@ -156,6 +158,25 @@ class Tree:
         lib().orc_sample_in_sphere(C.byref(self._s), _p(c), _p(r), _p(uu), n, _p(idx), _p(pdf), _p(st),
                                    nthreads or nthreads_default())
         return (idx, pdf, st) if stats else (idx, pdf)
+
+    def overlap(self, boxes, max_out, nthreads=None):
+        b = _c(boxes, np.float32).reshape(-1, 6)
+        n = len(b)
+        idx = np.full((n, max_out), 0xFFFFFFFF, np.uint32)
+        cnt = np.empty(n, np.uint32)
+        lib().orc_query_overlap(C.byref(self._s), _p(b), n, max_out, _p(idx), _p(cnt), nthreads or nthreads_default())
+        return idx, cnt
+
+    def line(self, origins, dirs, max_out, nthreads=None):
+        o = _c(origins, np.float32).reshape(-1, 3)
+        d = _c(dirs, np.float32).reshape(-1, 3)
+        n = len(o)
+        idx = np.full((n, max_out), 0xFFFFFFFF, np.uint32)
+        t = np.full((n, max_out), np.nan, np.float32)
+        cnt = np.empty(n, np.uint32)
+        lib().orc_query_line(C.byref(self._s), _p(o), _p(d), n, max_out, _p(idx), _p(t), _p(cnt),
+                             nthreads or nthreads_default())
+        return idx, t, cnt
 
     def sample_on_object(self, idx, u, v):
         i, uu, vv = _c(idx, np.int32), _c(u, np.float32), _c(v, np.float32)

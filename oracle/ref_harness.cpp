@@ -22,6 +22,7 @@
 #include <cstdio>
 #include <iostream>
 #include <unordered_map>
+#include <string>
 #include <vector>
 using std::max;
 using std::min;
@@ -41,6 +42,7 @@ static inline void __threadfence() {}
 
 #include "snch_lbvh/lbvh.cuh"
 #include "snch_lbvh/scene.cuh"
+#include "snch_lbvh/scene_loader.cuh"
 
 namespace
 {
@@ -58,8 +60,34 @@ namespace
     }
 } // namespace
 
+// --obj in.obj out.bin: the reference's own OBJ reader (scene_loader.cuh:86-152):
+// int64 nv, nt, then nv x float3 and nt x int3
+static int read_obj_mode(const char *obj, const char *out_path)
+{
+    lbvh::scene_loader<3> ld(obj);
+    FILE *out = std::fopen(out_path, "wb");
+    if (!out)
+        return 6;
+    const int64_t n[2] = {static_cast<int64_t>(ld.vertices_size()), static_cast<int64_t>(ld.primitives_size())};
+    write_n(out, n, 2);
+    for (const float3 &v : ld.get_vertices())
+    {
+        const float q[3] = {v.x, v.y, v.z};
+        write_n(out, q, 3);
+    }
+    for (const int3 &t : ld.get_indices())
+    {
+        const int32_t q[3] = {t.x, t.y, t.z};
+        write_n(out, q, 3);
+    }
+    std::fclose(out);
+    return 0;
+}
+
 int main(int argc, char **argv)
 {
+    if (argc == 4 && std::string(argv[1]) == "--obj")
+        return read_obj_mode(argv[2], argv[3]);
     if (argc != 3)
     {
         std::fprintf(stderr, "usage: %s in.bin out.bin\n", argv[0]);
@@ -68,19 +96,21 @@ int main(int argc, char **argv)
     FILE *in = std::fopen(argv[1], "rb");
     if (!in)
         return 3;
-    int64_t hdr[7];
-    if (std::fread(hdr, sizeof(int64_t), 7, in) != 7)
+    int64_t hdr[10];
+    if (std::fread(hdr, sizeof(int64_t), 10, in) != 10)
         return 4;
     const int64_t nv = hdr[0], nt = hdr[1], n_near = hdr[2], n_sil = hdr[3], n_ray = hdr[4], n_smp = hdr[5],
-                  n_obj = hdr[6];
-    std::vector<float> verts, near_pts, sil_pts, ray_o, ray_d, ray_tmax, smp_c, smp_r, smp_u, obj_u, obj_v;
+                  n_obj = hdr[6], n_box = hdr[7], n_line = hdr[8], max_out = hdr[9];
+    std::vector<float> verts, near_pts, sil_pts, ray_o, ray_d, ray_tmax, smp_c, smp_r, smp_u, obj_u, obj_v, boxes,
+        line_o, line_d;
     std::vector<int32_t> tris, obj_idx;
     std::vector<uint8_t> sil_flip;
     bool ok = read_n(in, verts, nv * 3) && read_n(in, tris, nt * 3) && read_n(in, near_pts, n_near * 3) &&
               read_n(in, sil_pts, n_sil * 3) && read_n(in, sil_flip, n_sil) && read_n(in, ray_o, n_ray * 3) &&
               read_n(in, ray_d, n_ray * 3) && read_n(in, ray_tmax, n_ray) && read_n(in, smp_c, n_smp * 3) &&
               read_n(in, smp_r, n_smp) && read_n(in, smp_u, n_smp) && read_n(in, obj_idx, n_obj) &&
-              read_n(in, obj_u, n_obj) && read_n(in, obj_v, n_obj);
+              read_n(in, obj_u, n_obj) && read_n(in, obj_v, n_obj) && read_n(in, boxes, n_box * 6) &&
+              read_n(in, line_o, n_line * 3) && read_n(in, line_d, n_line * 3);
     std::fclose(in);
     if (!ok)
         return 5;
@@ -211,6 +241,64 @@ int main(int argc, char **argv)
         const float3 p = lbvh::sample_on_object(bvh, obj_idx[q], lbvh::scene<3>::sample_on_object(), obj_u[q], obj_v[q]);
         float xyz[3] = {p.x, p.y, p.z};
         write_n(out, xyz, 3);
+    }
+    // AABB-overlap enumeration (query.cuh:177-231) and line enumeration
+    // (query.cuh:15-77): up to max_out results in the reference's output order
+    // and the total count it returns. Query boxes are given lower xyz, upper xyz.
+    // The line query's element test is the caller's functor (the 3D scene ships
+    // none): here the Moller-Trumbore arithmetic of scene<3>::intersect_test
+    // (scene.cuh:1005-1052) without its t >= 0 condition -- a line, not a ray --
+    // returning the line parameter t.
+    if (tree_ok)
+    {
+        std::vector<uint32_t> found(static_cast<size_t>(max_out));
+        for (int64_t q = 0; q < n_box; ++q)
+        {
+            lbvh::aabb<float, 3> b;
+            b.lower = make_float3(boxes[6 * q], boxes[6 * q + 1], boxes[6 * q + 2]);
+            b.upper = make_float3(boxes[6 * q + 3], boxes[6 * q + 4], boxes[6 * q + 5]);
+            const uint32_t cnt =
+                lbvh::query_device(bvh, lbvh::overlaps(b), found.data(), static_cast<unsigned int>(max_out));
+            write_n(out, &cnt, 1);
+            write_n(out, found.data(), std::min<int64_t>(cnt, max_out));
+        }
+        auto line_test = [](const lbvh::line<float, 3> &r, const lbvh::scene<3>::triangle &object) {
+            const float3 v0 = object.vertices[object.vertex_indices.x];
+            const float3 v1 = object.vertices[object.vertex_indices.y];
+            const float3 v2 = object.vertices[object.vertex_indices.z];
+            const float3 edge1 = {v1.x - v0.x, v1.y - v0.y, v1.z - v0.z};
+            const float3 edge2 = {v2.x - v0.x, v2.y - v0.y, v2.z - v0.z};
+            const float3 h = {r.dir.y * edge2.z - r.dir.z * edge2.y, r.dir.z * edge2.x - r.dir.x * edge2.z,
+                              r.dir.x * edge2.y - r.dir.y * edge2.x};
+            const float det = edge1.x * h.x + edge1.y * h.y + edge1.z * h.z;
+            if (std::fabs(det) < lbvh::epsilon<float>())
+                return thrust::make_pair(false, 0.0f);
+            const float inv_det = 1.0f / det;
+            const float3 sv = {r.origin.x - v0.x, r.origin.y - v0.y, r.origin.z - v0.z};
+            const float u = (sv.x * h.x + sv.y * h.y + sv.z * h.z) * inv_det;
+            if (u < 0.0f || u > 1.0f)
+                return thrust::make_pair(false, 0.0f);
+            const float3 qv = {sv.y * edge1.z - sv.z * edge1.y, sv.z * edge1.x - sv.x * edge1.z,
+                               sv.x * edge1.y - sv.y * edge1.x};
+            const float v = (r.dir.x * qv.x + r.dir.y * qv.y + r.dir.z * qv.z) * inv_det;
+            if (v < 0.0f || u + v > 1.0f)
+                return thrust::make_pair(false, 0.0f);
+            return thrust::make_pair(true, (edge2.x * qv.x + edge2.y * qv.y + edge2.z * qv.z) * inv_det);
+        };
+        std::vector<thrust::pair<unsigned int, float>> hits(static_cast<size_t>(max_out));
+        for (int64_t q = 0; q < n_line; ++q)
+        {
+            const float3 o = make_float3(line_o[3 * q], line_o[3 * q + 1], line_o[3 * q + 2]);
+            const float3 d = make_float3(line_d[3 * q], line_d[3 * q + 1], line_d[3 * q + 2]);
+            const uint32_t cnt = lbvh::query_device(bvh, lbvh::line_intersect(lbvh::line<float, 3>(o, d)), line_test,
+                                                    hits.data(), static_cast<unsigned int>(max_out));
+            write_n(out, &cnt, 1);
+            for (int64_t k = 0; k < std::min<int64_t>(cnt, max_out); ++k)
+            {
+                write_n(out, &hits[k].first, 1);
+                write_n(out, &hits[k].second, 1);
+            }
+        }
     }
     std::fclose(out);
     return 0;

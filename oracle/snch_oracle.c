@@ -1165,3 +1165,111 @@ void orc_brute_ray_f64(const float *verts, const int32_t *tris, int64_t nt, cons
     brute_ctx c = {verts, tris, nt, origins, NULL, dirs, tmax, idx, t, hit};
     orc_parallel(n, nthreads, brute_ray_body, &c);
 }
+
+
+/* ---------------------------------------------------------------- enumeration queries
+ * query_device(overlaps(box)) query.cuh:177-231 and query_device(line_intersect(line),
+ * element_test) query.cuh:15-77: the traversal pushes L then R and pops the top, leaf
+ * children are reported when their parent is expanded (L before R); results beyond
+ * max_out are counted, not written. counts[q] = the total. A one-leaf tree (where the
+ * reference reads past its node array) tests its only leaf. */
+
+/* intersects(aabb, aabb) aabb.cuh:66-81 */
+static inline int box_overlap(box3 a, box3 b) {
+    if (a.upper.x < b.lower.x || b.upper.x < a.lower.x) return 0;
+    if (a.upper.y < b.lower.y || b.upper.y < a.lower.y) return 0;
+    if (a.upper.z < b.lower.z || b.upper.z < a.lower.z) return 0;
+    return 1;
+}
+/* intersects(line<float,3>, aabb) aabb.cuh:329-348 (fmin / fmax drop NaN) */
+static inline int line_box(f3 o, f3 inv, box3 b) {
+    float t1 = (b.lower.x - o.x) * inv.x, t2 = (b.upper.x - o.x) * inv.x;
+    float tmin = fminf(t1, t2), tmax = fmaxf(t1, t2);
+    t1 = (b.lower.y - o.y) * inv.y; t2 = (b.upper.y - o.y) * inv.y;
+    tmin = fmaxf(tmin, fminf(t1, t2)); tmax = fminf(tmax, fmaxf(t1, t2));
+    t1 = (b.lower.z - o.z) * inv.z; t2 = (b.upper.z - o.z) * inv.z;
+    tmin = fmaxf(tmin, fminf(t1, t2)); tmax = fminf(tmax, fmaxf(t1, t2));
+    return tmax >= tmin;
+}
+/* the line's element test: scene<3>::intersect_test's Moller-Trumbore arithmetic
+ * (scene.cuh:1005-1052) for a line (any t) */
+static int line_triangle(f3 o, f3 dir, f3 v0, f3 v1, f3 v2, float *t) {
+    f3 e1 = sub(v1, v0), e2 = sub(v2, v0);
+    f3 h = mk(dir.y * e2.z - dir.z * e2.y, dir.z * e2.x - dir.x * e2.z, dir.x * e2.y - dir.y * e2.x);
+    float det = e1.x * h.x + e1.y * h.y + e1.z * h.z;
+    if (fabsf(det) < ORC_EPS) return 0;
+    float inv_det = 1.0f / det;
+    f3 sv = sub(o, v0);
+    float u = (sv.x * h.x + sv.y * h.y + sv.z * h.z) * inv_det;
+    if (u < 0.0f || u > 1.0f) return 0;
+    f3 qv = mk(sv.y * e1.z - sv.z * e1.y, sv.z * e1.x - sv.x * e1.z, sv.x * e1.y - sv.y * e1.x);
+    float v = (dir.x * qv.x + dir.y * qv.y + dir.z * qv.z) * inv_det;
+    if (v < 0.0f || u + v > 1.0f) return 0;
+    *t = (e2.x * qv.x + e2.y * qv.y + e2.z * qv.z) * inv_det;
+    return 1;
+}
+
+typedef struct {
+    const orc_scene *s; const float *q0; const float *q1; int64_t max_out;
+    uint32_t *idx; float *t; uint32_t *count; int line;
+} enum_ctx;
+static void enum_leaf(enum_ctx *c, uint32_t obj, f3 o, f3 dir, int64_t q, uint32_t *found) {
+    float t = 0.0f;
+    if (c->line) {
+        const int32_t *tr = c->s->tris + 3 * (int64_t)obj;
+        if (!line_triangle(o, dir, vload(c->s->verts, tr[0]), vload(c->s->verts, tr[1]), vload(c->s->verts, tr[2]), &t))
+            return;
+    }
+    if (*found < c->max_out) {
+        c->idx[q * c->max_out + *found] = obj;
+        if (c->line) c->t[q * c->max_out + *found] = t;
+    }
+    ++*found;
+}
+static void enum_body(void *vc, int64_t b, int64_t e) {
+    enum_ctx *c = (enum_ctx *)vc;
+    const orc_scene *s = c->s;
+    const uint32_t N = (uint32_t)s->num_tris;
+    uint32_t stk[ORC_STACK];
+    for (int64_t q = b; q < e; ++q) {
+        box3 qb = {{0, 0, 0}, {0, 0, 0}};
+        f3 o = mk(0, 0, 0), dir = mk(0, 0, 0), inv = mk(0, 0, 0);
+        if (c->line) {
+            o = vload(c->q0, (int32_t)q); dir = vload(c->q1, (int32_t)q);
+            inv = mk(1.0f / dir.x, 1.0f / dir.y, 1.0f / dir.z);
+        } else {
+            const float *x = c->q0 + 6 * q;
+            qb.lower = mk(x[0], x[1], x[2]); qb.upper = mk(x[3], x[4], x[5]);
+        }
+        uint32_t found = 0;
+        if (N == 1) {
+            box3 lb = node_box(s, 0);
+            if (c->line ? line_box(o, inv, lb) : box_overlap(qb, lb)) enum_leaf(c, s->nodes[3], o, dir, q, &found);
+        } else if (N > 1) {
+            int sp = 0;
+            stk[sp++] = 0;
+            do {
+                uint32_t node = stk[--sp];
+                uint32_t ch[2] = {s->nodes[4 * (int64_t)node + 1], s->nodes[4 * (int64_t)node + 2]};
+                for (int k = 0; k < 2; ++k) {
+                    box3 cb = node_box(s, ch[k]);
+                    if (!(c->line ? line_box(o, inv, cb) : box_overlap(qb, cb))) continue;
+                    uint32_t obj = s->nodes[4 * (int64_t)ch[k] + 3];
+                    if (obj != 0xFFFFFFFFu) enum_leaf(c, obj, o, dir, q, &found);
+                    else if (sp < ORC_STACK) stk[sp++] = ch[k];
+                }
+            } while (sp > 0);
+        }
+        c->count[q] = found;
+    }
+}
+void orc_query_overlap(const orc_scene *s, const float *boxes, int64_t n, int64_t max_out, uint32_t *idx,
+                       uint32_t *count, int nthreads) {
+    enum_ctx c = {s, boxes, NULL, max_out, idx, NULL, count, 0};
+    orc_parallel(n, nthreads, enum_body, &c);
+}
+void orc_query_line(const orc_scene *s, const float *origins, const float *dirs, int64_t n, int64_t max_out,
+                    uint32_t *idx, float *t, uint32_t *count, int nthreads) {
+    enum_ctx c = {s, origins, dirs, max_out, idx, t, count, 1};
+    orc_parallel(n, nthreads, enum_body, &c);
+}

@@ -100,6 +100,14 @@ void orc_brute_ray_f64(const float *verts, const int32_t *tris, int64_t nt, cons
                        const float *dirs, const float *tmax, int64_t n, uint8_t *hit, double *t,
                        uint32_t *idx, int nthreads);
 
+/* query_device(overlaps(box)) query.cuh:177-231 / query_device(line_intersect(line))
+ * query.cuh:15-77 (element test: intersect_test's arithmetic for a line, any t):
+ * boxes n x {lower.xyz, upper.xyz}; the first max_out results per query in the
+ * reference's order at idx[q * max_out ...] (and t), the total in count[q]. */
+void orc_query_overlap(const orc_scene *s, const float *boxes, int64_t n, int64_t max_out, uint32_t *idx,
+                       uint32_t *count, int nthreads);
+void orc_query_line(const orc_scene *s, const float *origins, const float *dirs, int64_t n, int64_t max_out,
+                    uint32_t *idx, float *t, uint32_t *count, int nthreads);
 int orc_max_depth(const uint32_t *nodes, int64_t nt);
 
 /* Position of every sorted leaf in the reference's full depth-first order

@@ -14,12 +14,13 @@ return NumPy arrays (copies pipelined inside the library).
 from __future__ import annotations
 
 import ctypes as C
+import os
 
 import numpy as np
 
 from ._ffi import BvhView, SnchError, check, lib  # noqa: F401
 
-__all__ = ["Scene", "BatchedScene", "Graph", "SnchError", "BvhView", "lib"]
+__all__ = ["Scene", "BatchedScene", "Graph", "SnchError", "BvhView", "lib", "read_obj"]
 
 INVALID = 0xFFFFFFFF
 TRAVERSAL_NEAR_FIRST = 0
@@ -61,6 +62,20 @@ def _host(x, dtype, cols=None):
     return a.reshape(-1, cols) if cols else a.reshape(-1)
 
 
+def read_obj(path):
+    """scene_loader<3>(path) scene_loader.cuh:86-152: (vertices float32 [V, 3],
+    triangles int32 [T, 3], 0-based) of a Wavefront OBJ file."""
+    L = lib()
+    p = C.cast(C.c_char_p(os.fsencode(path)), C.c_void_p)
+    nv, nt = C.c_int64(), C.c_int64()
+    check(L.snch_obj_read(p, None, 0, None, 0, C.byref(nv), C.byref(nt)))
+    v = np.empty((nv.value, 3), np.float32)
+    t = np.empty((nt.value, 3), np.int32)
+    check(L.snch_obj_read(p, v.ctypes.data_as(C.c_void_p), nv.value, t.ctypes.data_as(C.c_void_p), nt.value,
+                          C.byref(nv), C.byref(nt)))
+    return v, t
+
+
 class Scene:
     """lbvh::scene<3>: a triangle mesh, its silhouette edges and its SNCH-LBVH."""
 
@@ -78,6 +93,19 @@ class Scene:
             t = _host(triangles, np.int32, 3)
             check(L.snch_scene_create(v.ctypes.data_as(C.c_void_p), len(v), t.ctypes.data_as(C.c_void_p), len(t),
                                       C.byref(self._h)))
+
+    def save(self, path, stream=None):
+        """Writes the built scene to a flat binary file (snch_scene_save)."""
+        check(lib().snch_scene_save(self._h, C.cast(C.c_char_p(os.fsencode(path)), C.c_void_p), _stream(stream)))
+
+    @classmethod
+    def load(cls, path, stream=None):
+        """A built Scene read from a file written by save() (no rebuild)."""
+        s = cls.__new__(cls)
+        s._h = C.c_void_p()
+        check(lib().snch_scene_load(C.cast(C.c_char_p(os.fsencode(path)), C.c_void_p), C.byref(s._h),
+                                    _stream(stream)))
+        return s
 
     # ------------------------------------------------------------ lifetime
     def close(self):
@@ -278,6 +306,30 @@ class Scene:
                                                   torch.empty(n, dtype=torch.int32, device="cuda"))
         check(lib().snch_query_silhouette(self._h, _ptr(p), _ptr(f), n, _ptr(dist), _ptr(edge), _stream(stream)))
         return dist, edge
+
+    def query_overlap(self, boxes, max_per_query=64, stream=None):
+        """query_device(overlaps(box)) query.cuh:177: (index [n, max] int32, -1 padded; count [n])."""
+        torch = _torch()
+        b = _dev(boxes, torch.float32, 6)
+        n = b.shape[0]
+        idx = torch.full((n, max_per_query), -1, dtype=torch.int32, device="cuda")
+        cnt = torch.empty(n, dtype=torch.int32, device="cuda")
+        check(lib().snch_query_overlap(self._h, _ptr(b), n, int(max_per_query), _ptr(idx), _ptr(cnt),
+                                       _stream(stream)))
+        return idx, cnt
+
+    def query_line(self, origins, dirs, max_per_query=64, stream=None):
+        """query_device(line_intersect(line)) query.cuh:15: (index [n, max], t [n, max], count [n])."""
+        torch = _torch()
+        o = _dev(origins, torch.float32, 3)
+        d = _dev(dirs, torch.float32, 3)
+        n = o.shape[0]
+        idx = torch.full((n, max_per_query), -1, dtype=torch.int32, device="cuda")
+        tt = torch.full((n, max_per_query), float("nan"), dtype=torch.float32, device="cuda")
+        cnt = torch.empty(n, dtype=torch.int32, device="cuda")
+        check(lib().snch_query_line(self._h, _ptr(o), _ptr(d), n, int(max_per_query), _ptr(idx), _ptr(tt), _ptr(cnt),
+                                    _stream(stream)))
+        return idx, tt, cnt
 
     def query_ray(self, origins, dirs, tmax, stream=None, out=None):
         """query_device(ray_intersect) query.cuh:82 -> (hit uint8, t, uv [n,2], index int32)."""

@@ -32,6 +32,7 @@ UNITS = [
     ("noalloc_sort.cu", []),
     ("mlp.cu", []),
     ("wost.cu", []),
+    ("io.cu", []),
 ]
 HEADERS = ["common.cuh", "internal.h", "tcgen05.cuh"]
 

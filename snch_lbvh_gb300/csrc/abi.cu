@@ -971,6 +971,40 @@ int snch_query_silhouette(snch_scene_t s, const float *pts, const uint8_t *flip,
     });
 }
 
+int snch_query_overlap(snch_scene_t s, const float *boxes, int64_t n, uint32_t max_per_query, uint32_t *out_index,
+                       uint32_t *out_count, snch_stream_t stream)
+{
+    int rc = check_built(s);
+    if (rc == SNCH_OK)
+        rc = check_n(n, {boxes, out_count});
+    if (rc == SNCH_OK && max_per_query > 0 && n > 0 && !out_index)
+        rc = fail(SNCH_ERR_INVALID_ARGUMENT, "out_index is NULL");
+    if (rc == SNCH_OK && s->num_meshes)
+        rc = fail(SNCH_ERR_INVALID_ARGUMENT, "enumeration queries take a plain scene");
+    if (rc != SNCH_OK || n == 0)
+        return rc;
+    SNCH_CUDA(launch_enumerate(s->view(), false, boxes, nullptr, n, max_per_query, out_index, nullptr, out_count,
+                               S(stream)));
+    return SNCH_OK;
+}
+
+int snch_query_line(snch_scene_t s, const float *origins, const float *dirs, int64_t n, uint32_t max_per_query,
+                    uint32_t *out_index, float *out_t, uint32_t *out_count, snch_stream_t stream)
+{
+    int rc = check_built(s);
+    if (rc == SNCH_OK)
+        rc = check_n(n, {origins, dirs, out_count});
+    if (rc == SNCH_OK && max_per_query > 0 && n > 0 && (!out_index || !out_t))
+        rc = fail(SNCH_ERR_INVALID_ARGUMENT, "out_index / out_t is NULL");
+    if (rc == SNCH_OK && s->num_meshes)
+        rc = fail(SNCH_ERR_INVALID_ARGUMENT, "enumeration queries take a plain scene");
+    if (rc != SNCH_OK || n == 0)
+        return rc;
+    SNCH_CUDA(launch_enumerate(s->view(), true, origins, dirs, n, max_per_query, out_index, out_t, out_count,
+                               S(stream)));
+    return SNCH_OK;
+}
+
 int snch_query_ray(snch_scene_t s, const float *o, const float *d, const float *tmax, int64_t n, uint8_t *hit, float *t,
                    float *uv, uint32_t *idx, snch_stream_t stream)
 {
@@ -1668,6 +1702,140 @@ int snch_graph_destroy(snch_graph_t g)
     if (g->graph)
         cudaGraphDestroy(g->graph);
     delete g;
+    return SNCH_OK;
+}
+
+// ---- flat binary file of a built scene: header, then the arrays below in order
+namespace
+{
+constexpr char kFileMagic[8] = {'S', 'N', 'C', 'H', 'B', 'V', 'H', '1'};
+struct FileHeader
+{
+    char magic[8];
+    uint32_t version, num_verts, num_tris, reserved;
+    int64_t num_edges;
+};
+struct FileArray
+{
+    void *dev;
+    size_t bytes;
+};
+std::vector<FileArray> file_arrays(snch_scene_s *s, int64_t num_edges)
+{
+    const size_t n = s->num_tris, nn = n ? 2 * n - 1 : 0, ni = n > 1 ? n - 1 : 0;
+    return {{s->verts, 12 * (size_t)s->num_verts}, {s->tris, 12 * n}, {s->tri_edges, 12 * n},
+            {s->tri_owned, 12 * n}, {s->edge_verts, 16 * (size_t)num_edges}, {s->keys, 4 * n}, {s->vals, 4 * n},
+            {s->nodes, sizeof(NodeRec) * nn}, {s->aabbs, sizeof(Box) * nn}, {s->cones, sizeof(Cone) * nn},
+            {s->inner, sizeof(InnerRec) * ni}, {s->inner_cones, sizeof(InnerConeRec) * ni},
+            {s->leaves, sizeof(LeafRec) * n}, {s->edges, sizeof(EdgeRec) * 3 * n}};
+}
+int64_t scene_num_edges(snch_scene_s *s)
+{
+    if (s->num_edges_host < 0)
+    {
+        uint32_t e = 0;
+        if (cudaMemcpy(&e, s->small + kWNumEdges, 4, cudaMemcpyDeviceToHost) != cudaSuccess)
+            return -1;
+        s->num_edges_host = e;
+    }
+    return s->num_edges_host;
+}
+}  // namespace
+
+int snch_scene_save(snch_scene_t s, const char *path, snch_stream_t stream)
+{
+    int rc = check_built(s);
+    if (rc != SNCH_OK)
+        return rc;
+    if (!path)
+        return fail(SNCH_ERR_INVALID_ARGUMENT, "path is NULL");
+    if (s->num_meshes)
+        return fail(SNCH_ERR_INVALID_ARGUMENT, "only plain scenes are saved");
+    SNCH_CUDA(cudaStreamSynchronize(S(stream)));
+    const int64_t ne = scene_num_edges(s);
+    if (ne < 0)
+        return fail(SNCH_ERR_CUDA, "reading the edge count failed");
+    FILE *fp = std::fopen(path, "wb");
+    if (!fp)
+        return fail(SNCH_ERR_INVALID_ARGUMENT, std::string("cannot write ") + path);
+    FileHeader h{};
+    std::memcpy(h.magic, kFileMagic, 8);
+    h.version = 1;
+    h.num_verts = s->num_verts;
+    h.num_tris = s->num_tris;
+    h.num_edges = ne;
+    bool ok = std::fwrite(&h, sizeof h, 1, fp) == 1;
+    std::vector<char> buf;
+    for (const FileArray &a : file_arrays(s, ne))
+    {
+        if (!ok || a.bytes == 0)
+            continue;
+        buf.resize(a.bytes);
+        ok = cudaMemcpy(buf.data(), a.dev, a.bytes, cudaMemcpyDeviceToHost) == cudaSuccess &&
+             std::fwrite(buf.data(), 1, a.bytes, fp) == a.bytes;
+    }
+    ok = (std::fclose(fp) == 0) && ok;
+    if (!ok)
+        return fail(SNCH_ERR_CUDA, std::string("writing ") + path + " failed");
+    return SNCH_OK;
+}
+
+int snch_scene_load(const char *path, snch_scene_t *out, snch_stream_t stream)
+{
+    if (!out || !path)
+        return fail(SNCH_ERR_INVALID_ARGUMENT, "path and out_scene are required");
+    *out = nullptr;
+    FILE *fp = std::fopen(path, "rb");
+    if (!fp)
+        return fail(SNCH_ERR_INVALID_ARGUMENT, std::string("cannot open ") + path);
+    FileHeader h{};
+    if (std::fread(&h, sizeof h, 1, fp) != 1 || std::memcmp(h.magic, kFileMagic, 8) != 0 || h.version != 1 ||
+        h.num_tris >= (1u << 30) || h.num_edges < 0 || h.num_edges > 3 * (int64_t)h.num_tris)
+    {
+        std::fclose(fp);
+        return fail(SNCH_ERR_INVALID_ARGUMENT, std::string(path) + " is not a scene file of this library");
+    }
+    snch_scene_s *s = new snch_scene_s();
+    s->num_verts = h.num_verts;
+    s->num_tris = h.num_tris;
+    int rc = allocate(s);
+    std::vector<char> buf;
+    cudaStream_t st = S(stream);
+    for (const FileArray &a : rc == SNCH_OK ? file_arrays(s, h.num_edges) : std::vector<FileArray>())
+    {
+        if (rc != SNCH_OK || a.bytes == 0)
+            continue;
+        buf.resize(a.bytes);
+        if (std::fread(buf.data(), 1, a.bytes, fp) != a.bytes)
+            rc = fail(SNCH_ERR_INVALID_ARGUMENT, std::string(path) + " is truncated");
+        else if (cudaMemcpy(a.dev, buf.data(), a.bytes, cudaMemcpyHostToDevice) != cudaSuccess)
+            rc = fail(SNCH_ERR_CUDA, "upload of the scene file failed");
+    }
+    char extra = 0;
+    if (rc == SNCH_OK && std::fread(&extra, 1, 1, fp) != 0)
+        rc = fail(SNCH_ERR_INVALID_ARGUMENT, std::string(path) + " has trailing bytes");
+    std::fclose(fp);
+    if (rc == SNCH_OK)
+    {
+        const uint32_t ne = (uint32_t)h.num_edges;
+        cudaError_t e = cudaMemcpyAsync(s->small + kWNumEdges, &ne, 4, cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess)
+            e = launch_ref_objects(s->verts, s->tris, s->tri_owned, s->edge_verts, s->num_tris, s->ref_objects,
+                                   s->ref_edges, st);
+        if (e == cudaSuccess)
+            e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess)
+            rc = fail(SNCH_ERR_CUDA, std::string("scene load: ") + cudaGetErrorString(e));
+    }
+    if (rc != SNCH_OK)
+    {
+        free_scene(s);
+        return rc;
+    }
+    s->num_edges_host = h.num_edges;
+    s->topology_ready = true;
+    s->built = true;
+    *out = s;
     return SNCH_OK;
 }
 

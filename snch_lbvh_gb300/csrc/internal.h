@@ -131,6 +131,10 @@ cudaError_t launch_ray(const TreeView &t, const float *o, const float *d, const 
                        float *tt, float *uv, uint32_t *idx, cudaStream_t st, uint32_t *stats = nullptr);
 cudaError_t launch_sample(const TreeView &t, const float *c, const float *r, const float *u, int64_t n, int32_t *idx,
                           float *pdf, cudaStream_t st, uint32_t *stats = nullptr);
+// overlap (line = false: q0 = boxes, lower xyz + upper xyz) / line (q0 = origins,
+// q1 = directions) enumeration: first max_out results per query, total count
+cudaError_t launch_enumerate(const TreeView &t, bool line, const float *q0, const float *q1, int64_t n,
+                             uint32_t max_out, uint32_t *idx, float *tt, uint32_t *count, cudaStream_t st);
 // Morton-sorted order of a query batch (thread i answers query order[i]);
 // scratch holds query_order_scratch_bytes(n) bytes and owns *order.
 size_t query_order_scratch_bytes(int64_t n);

@@ -644,9 +644,12 @@ __global__ void __launch_bounds__(kBlock, 1280 / kBlock) nearest_fast_kernel(Tre
             unpack_inner(load_inner(t.inner + node), lb, rb, L, R);
             if (kStats)
                 ++n_int;
+            // no minmaxdist sibling test (query.cuh:279, 297) here: it only removes
+            // subtrees whose every triangle is strictly farther than one in the
+            // sibling, which a near-first search never needs (same expansions, same
+            // answers and tie winners, measured 12 % faster without it)
             const float Lmd = mindist(lb, p), Rmd = mindist(rb, p);
-            const float Lmm = minmaxdist(lb, p), Rmm = minmaxdist(rb, p);
-            const bool aL = Lmd <= Rmm, aR = Rmd <= Lmm;  // query.cuh:279, 297
+            constexpr bool aL = true, aR = true;
             if (kPrefetchChildren)
             {
                 if (aL && L < ni && Lmd <= best)
@@ -1359,10 +1362,10 @@ __global__ void __launch_bounds__(128, SNCH_WIDE_MIN_BLOCKS)
 // entries in shared memory; at a node every lane whose bit is set applies its
 // own tests to the two children (the record is one broadcast load), the
 // ballots of the lanes that keep each child become the children's masks, and a
-// leaf is evaluated by the lanes that keep it. A lane therefore reaches exactly
-// the leaves its own binary search reaches, with the same tests (minmaxdist
-// sibling rule, cone tests, pruning by its own best), and its answer -- the
-// minimum over them, ties broken by leaf rank -- is the per-lane answer. The
+// leaf is evaluated by the lanes that keep it. A lane therefore reaches the
+// leaves its own per-lane search reaches, with the same tests (cone tests,
+// pruning by its own best), and its answer -- the minimum over them, ties
+// broken by leaf rank -- is the per-lane answer. The
 // warp visits the union of its lanes' nodes, in the order most of them prefer,
 // with every control decision uniform across the warp.
 
@@ -1441,9 +1444,7 @@ __global__ void __launch_bounds__(128, 10) nearest_packet_kernel(TreeView t, con
                     ++n_int;
                 Lmd = mindist(lb, p);
                 Rmd = mindist(rb, p);
-                const float Lmm = minmaxdist(lb, p), Rmm = minmaxdist(rb, p);
-                aL = Lmd <= Rmm;  // query.cuh:279, 297
-                aR = Rmd <= Lmm;
+                aL = aR = true;  // no minmaxdist sibling test: as nearest_fast_kernel
                 if (aL && L >= ni && Lmd <= best)
                 {
                     leaf_nearest_fast(t, L - ni, p, best, best_rank, nearest);
@@ -2297,6 +2298,151 @@ __global__ void query_keys_kernel(const float *__restrict__ pts, int64_t n, cons
     vals[i] = (uint32_t)i;
 }
 
+// ------------------------------------------------------------------ enumeration queries
+// query_device(overlaps(box)) query.cuh:177-231 and query_device(line_intersect(line),
+// element_test) query.cuh:15-77 over the scene's triangles. The reference's stack
+// discipline is kept (push L then R, pop the top; leaf children reported when their
+// parent is expanded, L before R), so the results come out in its order; the
+// first max_out go to the query's row, the total is counted (the reference's
+// return value). The line's element test is intersect_test's arithmetic
+// (scene.cuh:1005-1052) for a line: any t, returned with the triangle.
+
+// intersects(aabb, aabb) aabb.cuh:66-81 (query box first, as query.cuh:199)
+SNCH_DEV bool box_overlap(const Box &a, const Box &b)
+{
+    if (a.upper.x < b.lower.x || b.upper.x < a.lower.x)
+        return false;
+    if (a.upper.y < b.lower.y || b.upper.y < a.lower.y)
+        return false;
+    if (a.upper.z < b.lower.z || b.upper.z < a.lower.z)
+        return false;
+    return true;
+}
+// intersects(line<float,3>, aabb) aabb.cuh:329-348
+SNCH_DEV bool line_box(f3 o, f3 inv, const Box &b)
+{
+    float t1 = (b.lower.x - o.x) * inv.x, t2 = (b.upper.x - o.x) * inv.x;
+    float tmin = fminf(t1, t2), tmax = fmaxf(t1, t2);
+    t1 = (b.lower.y - o.y) * inv.y;
+    t2 = (b.upper.y - o.y) * inv.y;
+    tmin = fmaxf(tmin, fminf(t1, t2));
+    tmax = fminf(tmax, fmaxf(t1, t2));
+    t1 = (b.lower.z - o.z) * inv.z;
+    t2 = (b.upper.z - o.z) * inv.z;
+    tmin = fmaxf(tmin, fminf(t1, t2));
+    tmax = fminf(tmax, fmaxf(t1, t2));
+    return tmax >= tmin;
+}
+SNCH_DEV bool line_triangle(f3 o, f3 dir, f3 v0, f3 v1, f3 v2, float &t)
+{
+    const f3 e1 = sub(v1, v0), e2 = sub(v2, v0);
+    const f3 h = mk(dir.y * e2.z - dir.z * e2.y, dir.z * e2.x - dir.x * e2.z, dir.x * e2.y - dir.y * e2.x);
+    const float det = e1.x * h.x + e1.y * h.y + e1.z * h.z;
+    if (fabsf(det) < kEps)
+        return false;
+    const float inv_det = __frcp_rn(det);
+    const f3 sv = sub(o, v0);
+    const float u = (sv.x * h.x + sv.y * h.y + sv.z * h.z) * inv_det;
+    if (u < 0.0f || u > 1.0f)
+        return false;
+    const f3 qv = mk(sv.y * e1.z - sv.z * e1.y, sv.z * e1.x - sv.x * e1.z, sv.x * e1.y - sv.y * e1.x);
+    const float v = (dir.x * qv.x + dir.y * qv.y + dir.z * qv.z) * inv_det;
+    if (v < 0.0f || u + v > 1.0f)
+        return false;
+    t = (e2.x * qv.x + e2.y * qv.y + e2.z * qv.z) * inv_det;
+    return true;
+}
+
+template <bool kLine>
+__global__ void __launch_bounds__(128) enumerate_kernel(TreeView t, const float *__restrict__ q0,
+                                                        const float *__restrict__ q1, int64_t n, uint32_t max_out,
+                                                        uint32_t *__restrict__ out_idx, float *__restrict__ out_t,
+                                                        uint32_t *__restrict__ out_count)
+{
+    const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (q >= n)
+        return;
+    Box qb;
+    f3 o = mk(0.0f, 0.0f, 0.0f), dir = o, inv = o;
+    if (kLine)
+    {
+        o = load_point(q0, q);
+        dir = load_point(q1, q);
+        inv = mk(1.0f / dir.x, 1.0f / dir.y, 1.0f / dir.z);  // line ctor aabb.cuh:288-295
+    }
+    else
+    {
+        const float *x = q0 + 6 * q;
+        qb.lower = mk(__ldg(x), __ldg(x + 1), __ldg(x + 2));
+        qb.upper = mk(__ldg(x + 3), __ldg(x + 4), __ldg(x + 5));
+    }
+    uint32_t found = 0;
+    const uint64_t row = (uint64_t)q * max_out;
+    auto visit = [&](const Box &b) { return kLine ? line_box(o, inv, b) : box_overlap(qb, b); };
+    auto emit = [&](uint32_t pos) {
+        const float4 *lr = reinterpret_cast<const float4 *>(t.leaves + pos);
+        const float4 a = __ldg(lr);
+        float tt = 0.0f;
+        if (kLine)
+        {
+            const float4 b = __ldg(lr + 1), c = __ldg(lr + 2);
+            if (!line_triangle(o, dir, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), mk(c.x, c.y, c.z), tt))
+                return;
+        }
+        if (found < max_out)
+        {
+            out_idx[row + found] = __float_as_uint(a.w);
+            if (kLine)
+                out_t[row + found] = tt;
+        }
+        ++found;
+    };
+    const uint32_t N = t.num_tris, ni = N - 1;
+    if (N == 1)
+    {
+        if (visit(load_root_box(t.aabbs)))
+            emit(0);
+    }
+    else if (N > 1)
+    {
+        uint32_t stack[kStackDepth];
+        int sp = 0;
+        stack[sp++] = 0;
+        do
+        {
+            const uint32_t node = stack[--sp];
+            Box lb, rb;
+            uint32_t L, R;
+            unpack_inner(load_inner(t.inner + node), lb, rb, L, R);
+            bool full = false;
+            if (visit(lb))
+            {
+                if (L >= ni)
+                    emit(L - ni);
+                else if (sp < kStackDepth)
+                    stack[sp++] = L;
+                else
+                    full = true;
+            }
+            if (visit(rb))
+            {
+                if (R >= ni)
+                    emit(R - ni);
+                else if (sp < kStackDepth)
+                    stack[sp++] = R;
+                else
+                    full = true;
+            }
+            if (full)
+            {
+                atomicOr(t.status, kStatusStackOverflow);
+                break;
+            }
+        } while (sp > 0);
+    }
+    out_count[q] = found;
+}
+
 // ------------------------------------------------------------------ launchers
 namespace
 {
@@ -2462,6 +2608,19 @@ cudaError_t launch_sample(const TreeView &t, const float *c, const float *r, con
     note_launch();
     return cudaGetLastError();
 }
+cudaError_t launch_enumerate(const TreeView &t, bool line, const float *q0, const float *q1, int64_t n,
+                             uint32_t max_out, uint32_t *idx, float *tt, uint32_t *count, cudaStream_t st)
+{
+    if (n <= 0)
+        return cudaSuccess;
+    if (line)
+        enumerate_kernel<true><<<grid_for(n, 128), 128, 0, st>>>(t, q0, q1, n, max_out, idx, tt, count);
+    else
+        enumerate_kernel<false><<<grid_for(n, 128), 128, 0, st>>>(t, q0, q1, n, max_out, idx, tt, count);
+    note_launch();
+    return cudaGetLastError();
+}
+
 cudaError_t launch_query_order(const TreeView &t, const float *pts, int64_t n, void *scratch, uint32_t **order,
                                cudaStream_t st)
 {

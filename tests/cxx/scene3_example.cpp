@@ -129,8 +129,51 @@ int main(int argc, char **argv)
     cudaMemcpy(&sdist, d_dist, 4, cudaMemcpyDeviceToHost);
     cudaMemcpy(&sidx, d_idx, 4, cudaMemcpyDeviceToHost);
     std::printf("seeded: idx=%u dist=%.7f\n", sidx, sdist);
+    if (!(sidx == idx && sdist == dist))
+        return 7;
+
+    // scene_loader<3> round trip through an OBJ file, save / load of the built
+    // scene, and an overlap query on the loaded one
+    const std::string obj = "/tmp/snch_example_ico.obj", bin = "/tmp/snch_example_ico.snch";
+    if (FILE *fo = std::fopen(obj.c_str(), "w"))
+    {
+        for (auto &p : v)
+            std::fprintf(fo, "v %.9g %.9g %.9g\n", p.x, p.y, p.z);
+        for (auto &q : f)
+            std::fprintf(fo, "f %d %d %d\n", q.x + 1, q.y + 1, q.z + 1);
+        std::fclose(fo);
+    }
+    snch::scene_loader3<V3, I3> loader(obj);
+    if (loader.vertices_size() != 12 || loader.primitives_size() != 20 || loader.get_indices()[7].z != f[7].z)
+        return 8;
+    snch::scene3 from_file(loader.get_vertices().begin(), loader.get_vertices().end(), loader.get_indices().begin(),
+                           loader.get_indices().end());
+    from_file.compute_silhouettes();
+    from_file.build_bvh();
+    from_file.save(bin);
+    snch::scene3 loaded = snch::scene3::load(bin);
+    if (loaded.get_bvh_device_ptr().num_objects != 20)
+        return 9;
+    loaded.query_nearest(d_pts, 1, d_idx, d_dist);
+    float ldist = 0;
+    cudaMemcpy(&ldist, d_dist, 4, cudaMemcpyDeviceToHost);
+    const float hb[6] = {-2.f, -2.f, -2.f, 2.f, 2.f, 2.f};
+    float *dbox = nullptr;
+    uint32_t *dcnt = nullptr, *didx = nullptr;
+    cudaMalloc(&dbox, sizeof hb);
+    cudaMalloc(&dcnt, 4);
+    cudaMalloc(&didx, 4 * 32);
+    cudaMemcpy(dbox, hb, sizeof hb, cudaMemcpyHostToDevice);
+    loaded.query_overlap(dbox, 1, 32, didx, dcnt);
+    uint32_t cnt = 0;
+    cudaMemcpy(&cnt, dcnt, 4, cudaMemcpyDeviceToHost);
+    std::printf("loaded: dist=%.7f overlap count=%u\n", ldist, cnt);
+    for (void *q : {(void *)dbox, (void *)dcnt, (void *)didx})
+        cudaFree(q);
+    if (ldist != dist || cnt != 20)
+        return 10;
     for (void *q : {(void *)d_pts, (void *)d_dist, (void *)d_idx, (void *)d2, (void *)dd, (void *)dm, (void *)di,
                     (void *)dr})
         cudaFree(q);
-    return (sidx == idx && sdist == dist) ? 0 : 7;
+    return 0;
 }

@@ -39,15 +39,17 @@ def run_harness(verts, tris, q):
     nv, nt = len(verts), len(tris)
     n_near, n_sil, n_ray = len(q["near_pts"]), len(q["sil_pts"]), len(q["ray_o"])
     n_smp, n_obj = len(q["smp_c"]), len(q["obj_idx"])
+    n_box, n_line = len(q["box_q"]), len(q["line_o"])
     with tempfile.TemporaryDirectory() as td:
         fin, fout = os.path.join(td, "in.bin"), os.path.join(td, "out.bin")
         with open(fin, "wb") as f:
-            np.array([nv, nt, n_near, n_sil, n_ray, n_smp, n_obj], np.int64).tofile(f)
+            np.array([nv, nt, n_near, n_sil, n_ray, n_smp, n_obj, n_box, n_line, MAX_OUT], np.int64).tofile(f)
             for a, dt in [(verts, np.float32), (tris, np.int32), (q["near_pts"], np.float32),
                           (q["sil_pts"], np.float32), (q["sil_flip"], np.uint8), (q["ray_o"], np.float32),
                           (q["ray_d"], np.float32), (q["ray_tmax"], np.float32), (q["smp_c"], np.float32),
                           (q["smp_r"], np.float32), (q["smp_u"], np.float32), (q["obj_idx"], np.int32),
-                          (q["obj_u"], np.float32), (q["obj_v"], np.float32)]:
+                          (q["obj_u"], np.float32), (q["obj_v"], np.float32), (q["box_q"], np.float32),
+                          (q["line_o"], np.float32), (q["line_d"], np.float32)]:
                 np.ascontiguousarray(a, dtype=dt).tofile(f)
         subprocess.run([oracle.REF_HARNESS, fin, fout], check=True, stdout=subprocess.DEVNULL)
         buf = open(fout, "rb").read()
@@ -83,8 +85,55 @@ def run_harness(verts, tris, q):
     r["ref_smp_idx"] = rec[:, :4].copy().view(np.int32).reshape(-1)
     r["ref_smp_pdf"] = rec[:, 4:].copy().view(np.float32).reshape(-1)
     r["ref_obj_pts"] = take(np.float32, n_obj * 3).reshape(-1, 3)
+    # overlap / line enumerations: count per query and the first MAX_OUT results,
+    # stored padded (0xFFFFFFFF / NaN beyond min(count, MAX_OUT))
+    nb, nl = (n_box, n_line) if tree_ok else (0, 0)
+    r["ref_box_count"] = np.zeros(nb, np.uint32)
+    r["ref_box_idx"] = np.full((nb, MAX_OUT), 0xFFFFFFFF, np.uint32)
+    for k in range(nb):
+        c = int(take(np.uint32, 1)[0])
+        r["ref_box_count"][k] = c
+        r["ref_box_idx"][k, :min(c, MAX_OUT)] = take(np.uint32, min(c, MAX_OUT))
+    r["ref_line_count"] = np.zeros(nl, np.uint32)
+    r["ref_line_idx"] = np.full((nl, MAX_OUT), 0xFFFFFFFF, np.uint32)
+    r["ref_line_t"] = np.full((nl, MAX_OUT), np.nan, np.float32)
+    for k in range(nl):
+        c = int(take(np.uint32, 1)[0])
+        r["ref_line_count"][k] = c
+        rec = take(np.uint8, 8 * min(c, MAX_OUT)).reshape(-1, 8)
+        r["ref_line_idx"][k, :len(rec)] = rec[:, :4].copy().view(np.uint32).reshape(-1)
+        r["ref_line_t"][k, :len(rec)] = rec[:, 4:].copy().view(np.float32).reshape(-1)
     assert off == len(buf), (off, len(buf))
     return r
+
+
+MAX_OUT = 64  # results kept per overlap / line query (the count is the full one)
+
+
+def make_region_queries(verts, seed, n=256):
+    """AABB-overlap and line queries from their own generator (the point / ray
+    queries above keep their values): boxes of random centre and log-uniform
+    size, point boxes, a box holding everything and an empty one; lines through
+    random points with random and axis-aligned directions (zero components make
+    the slab test meet 0 * inf)."""
+    rng = np.random.default_rng(seed + 1000)
+    v = verts.astype(np.float64)
+    lo, hi = v.min(0), v.max(0)
+    c, h = 0.5 * (lo + hi), 0.5 * np.maximum(hi - lo, 1e-3) * 1.5
+    cen = c + (rng.random((n, 3)) * 2 - 1) * h
+    half = np.exp(rng.uniform(np.log(1e-3), np.log(h.max()), (n, 3)))
+    half[: n // 16] = 0.0  # point boxes
+    boxes = np.concatenate([cen - half, cen + half], 1)
+    boxes[-1] = np.concatenate([lo - 1, hi + 1])  # everything
+    boxes[-2] = np.concatenate([hi + 1, hi + 2])  # nothing
+    o = c + (rng.random((n, 3)) * 2 - 1) * h
+    d = rng.standard_normal((n, 3))
+    axis = rng.integers(0, 3, n)
+    axial = rng.random(n) < 0.2
+    d[axial] = 0.0
+    d[axial, axis[axial]] = 1.0
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    return {"box_q": boxes.astype(np.float32), "line_o": o.astype(np.float32), "line_d": d.astype(np.float32)}
 
 
 def make_queries(verts, tris, seed, n_rand=512, extra=True):
@@ -163,10 +212,56 @@ def cases():
     yield "cfg1_icosphere_l5", v, f, 19
 
 
+def write_obj_case(path, verts, tris):
+    """An OBJ file of a golden mesh in the forms the reference's reader handles:
+    comments, object / group / smoothing / normal / texture lines (ignored),
+    varied number formats and spacing, a 4th vertex coordinate, CRLF line ends,
+    quads (the first three indices count) and blank lines."""
+    rng = np.random.default_rng(99)
+    lines = ["# golden OBJ case", "o torus", "g part0", "s off", ""]
+    for k, p in enumerate(verts):
+        xs = [repr(float(x)) for x in p]
+        if k % 7 == 1:
+            xs = [f"{float(x):.9e}" for x in p]
+        sep = "\t" if k % 5 == 2 else "  " if k % 5 == 3 else " "
+        extra = " 1.0" if k % 11 == 4 else ""
+        lines.append("v" + sep + sep.join(xs) + extra + ("\r" if k % 13 == 6 else ""))
+        if k % 17 == 0:
+            lines.append(f"vn 0 0 1\nvt {rng.random():.3f} {rng.random():.3f}")
+    for k, t in enumerate(tris):
+        ids = [str(int(i) + 1) for i in t]
+        if k % 9 == 3:
+            ids.append(str(int(t[0]) + 1))  # a quad: the reader keeps the first three
+        lines.append("f " + " ".join(ids) + ("\r" if k % 10 == 7 else ""))
+        if k % 50 == 0:
+            lines.append("")
+    with open(path, "w", newline="") as f:
+        f.write("\n".join(lines) + "\n")
+
+
+def obj_case():
+    d = os.path.join(OUT, "obj")
+    os.makedirs(d, exist_ok=True)
+    v, f = meshes.noisy_torus(0.4, 0.1, 24, 12, 0.004, seed=6)
+    path = os.path.join(d, "torus.obj")
+    write_obj_case(path, v.astype(np.float32), f)
+    with tempfile.TemporaryDirectory() as td:
+        out = os.path.join(td, "out.bin")
+        subprocess.run([oracle.REF_HARNESS, "--obj", path, out], check=True)
+        buf = open(out, "rb").read()
+    nv, nt = np.frombuffer(buf, np.int64, 2)
+    rv = np.frombuffer(buf, np.float32, 3 * nv, 16).reshape(-1, 3)
+    rt = np.frombuffer(buf, np.int32, 3 * nt, 16 + 12 * nv).reshape(-1, 3)
+    np.savez_compressed(os.path.join(d, "torus_ref.npz"), ref_verts=rv, ref_tris=rt)
+    print(f"obj/torus.obj          verts={nv} tris={nt}")
+
+
 def main():
     oracle.build()
+    obj_case()
     for name, v, f, seed in cases():
         q = make_queries(v, f, seed, n_rand=2048 if name.startswith("cfg1") else 512)
+        q.update(make_region_queries(v, seed))
         tree = oracle.Tree(v, f)
         depth = tree.max_depth()
         assert depth < 60, f"{name}: tree depth {depth} would overflow the reference's 64-entry stacks"

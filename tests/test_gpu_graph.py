@@ -46,6 +46,7 @@ def test_graph_rebuild_and_queries(snch, width):
     out_n = (torch.empty(n, dtype=torch.int32, device="cuda"), torch.empty(n, dtype=torch.float32, device="cuda"))
     out_s = (torch.empty(n, dtype=torch.float32, device="cuda"), torch.empty(n, dtype=torch.int32, device="cuda"))
     st = torch.cuda.Stream()
+    torch.cuda.synchronize()  # the first build (current stream) is done before the graph's
     g = s.capture(True, pts, out_n, pts, flip, out_s, stream=st)
     for k in range(3):
         v = (v0 * np.float32(1.0 + 0.05 * k) + np.float32(0.01 * k)).astype(np.float32)  # moved vertices
@@ -89,6 +90,9 @@ def test_graph_batched_queries(snch):
     out_n = (torch.full((n,), 7, dtype=torch.int32, device="cuda"), torch.zeros(n, dtype=torch.float32, device="cuda"))
     out_s = (torch.zeros(n, dtype=torch.float32, device="cuda"), torch.zeros(n, dtype=torch.int32, device="cuda"))
     st = torch.cuda.Stream()
+    # the graph rebuilds the scene on another stream: the direct queries above
+    # (current stream) must be done before it runs
+    torch.cuda.synchronize()
     g = b.capture(True, pts, out_n, pts, flip, out_s, near_mesh=mesh, sil_mesh=mesh, stream=st)
     for _ in range(2):
         g.launch(st)

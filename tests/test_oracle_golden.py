@@ -99,3 +99,29 @@ def test_golden_cases_cover_edge_cases():
     assert len(np.unique(codes)) < len(codes), "duplicated case must force the 64-bit key path"
     grid = load_golden("open_grid")
     assert np.any(grid["ref_edge_verts"][:, 0] == -1) or np.any(grid["ref_edge_verts"][:, 3] == -1)
+
+
+def test_overlap_enumeration(case):
+    """query_device(overlaps(box)) query.cuh:177-231: the same triangles in the
+    same order, and the same total count, as the reference."""
+    name, g, t = case
+    if len(g["ref_box_count"]) == 0:
+        pytest.skip("one-triangle tree: the reference reads past its node array")
+    k = g["ref_box_idx"].shape[1]
+    idx, cnt = t.overlap(g["box_q"], k)
+    np.testing.assert_array_equal(cnt, g["ref_box_count"])
+    np.testing.assert_array_equal(idx, g["ref_box_idx"])
+
+
+def test_line_enumeration(case):
+    """query_device(line_intersect(line), element_test) query.cuh:15-77 with the
+    triangle test of intersect_test for a line: triangles, line parameters and
+    counts bit for bit, in the reference's order."""
+    name, g, t = case
+    if len(g["ref_line_count"]) == 0:
+        pytest.skip("one-triangle tree: the reference reads past its node array")
+    k = g["ref_line_idx"].shape[1]
+    idx, tt, cnt = t.line(g["line_o"], g["line_d"], k)
+    np.testing.assert_array_equal(cnt, g["ref_line_count"])
+    np.testing.assert_array_equal(idx, g["ref_line_idx"])
+    np.testing.assert_array_equal(bits(tt), bits(g["ref_line_t"]))
