@@ -196,13 +196,12 @@ int snch_set_traversal(snch_scene_t scene, int mode);
 /*   SNCH_OPT_PACKET           warp packets for the binary near-first nearest and
  *                             silhouette searches: a warp's 32 queries walk one shared
  *                             traversal, each lane applying its own tests and keeping its
- *                             own answer. 1: always; 2: for Morton-ordered batches (the
- *                             default of the silhouette search); 0: never (each lane
- *                             walks its own; the default of the nearest search). Same
- *                             distances; the silhouette edge id / nearest index equals
- *                             the per-lane one except on an exact distance tie that falls
- *                             on a rounding boundary of a box test, where the reference's
- *                             own choice depends on its visit order.
+ *                             own answer. 2 (default): for Morton-ordered batches; 1:
+ *                             always; 0: never (each lane walks its own). Same distances;
+ *                             the silhouette edge id / nearest index equals the per-lane
+ *                             one except on an exact distance tie that falls on a
+ *                             rounding boundary of a box test, where the reference's own
+ *                             choice depends on its visit order.
  *   SNCH_OPT_PACKET_NEAREST / _SILHOUETTE  the same for one query type. */
 #define SNCH_OPT_PACKET 12
 #define SNCH_OPT_PACKET_NEAREST 13
@@ -337,6 +336,44 @@ int snch_graph_create(snch_scene_t scene, int rebuild, const int32_t *near_mesh,
                       int32_t *sil_edge_or_null, snch_graph_t *out_graph, snch_stream_t stream);
 int snch_graph_launch(snch_graph_t graph, snch_stream_t stream);
 int snch_graph_destroy(snch_graph_t graph);
+
+/* ------------------------------------------------------------------ 2D scenes
+ * lbvh::scene<2> (scene.cuh:287-703): line segments (int2 vertex ids into float2
+ * vertices) with silhouette VERTICES. snch_scene2_build = compute_silhouettes()
+ * + build_bvh() (scene.cuh:642-683) on the GPU: the same topology, Morton codes,
+ * tree and boxes as the reference bit for bit. The queries replay the reference's
+ * traversals over the 2D functors: query_device(nearest) (segment index,
+ * distance), query_device(nearest_silhouette) (distance; also the silhouette
+ * vertex id), query_device(ray_intersect) (hit, t, segment parameter s of
+ * intersect_test scene.cuh:555-583, index) and sample_object_in_sphere with a
+ * circle (index, pdf; pdf 0 where none is hit), sample_on_object (a point on the
+ * segment). Vertices and segments are HOST buffers; everything else DEVICE
+ * buffers (float2 = 2 packed floats). A one-segment tree evaluates its segment
+ * (the reference reads past its node array there). */
+typedef struct snch_scene2_s *snch_scene2_t;
+int snch_scene2_create(const float *vertices_xy, int64_t num_vertices, const int32_t *segments,
+                       int64_t num_segments, snch_scene2_t *out_scene);
+int snch_scene2_destroy(snch_scene2_t scene);
+int snch_scene2_build(snch_scene2_t scene, snch_stream_t stream);
+int snch_scene2_get_device_status(snch_scene2_t scene, uint32_t *out_bits, int reset, snch_stream_t stream);
+/* silhouette vertices (V x int4 {prev, self, next, -1}), owned vertices per segment
+ * (N x int2), sorted Morton codes and segment indices (N), nodes ((2N-1) x 4),
+ * aabbs ((2N-1) x {upper.xy, lower.xy}), cones ((2N-1) x {axis.xy, half, radius})
+ * into caller DEVICE buffers; any may be NULL */
+int snch_scene2_export(snch_scene2_t scene, int32_t *silhouette_vertices, int32_t *segment_owned,
+                       uint32_t *sorted_morton, uint32_t *sorted_indices, uint32_t *nodes, float *aabbs,
+                       float *cones, snch_stream_t stream);
+int snch_scene2_query_nearest(snch_scene2_t scene, const float *points_xy, int64_t n, uint32_t *out_index,
+                              float *out_distance, snch_stream_t stream);
+int snch_scene2_query_silhouette(snch_scene2_t scene, const float *points_xy, const uint8_t *flip_or_null,
+                                 int64_t n, float *out_distance, int32_t *out_vertex_or_null, snch_stream_t stream);
+int snch_scene2_query_ray(snch_scene2_t scene, const float *origins_xy, const float *dirs_xy, const float *tmax,
+                          int64_t n, uint8_t *out_hit, float *out_t, float *out_segment_param, uint32_t *out_index,
+                          snch_stream_t stream);
+int snch_scene2_sample_in_circle(snch_scene2_t scene, const float *centers_xy, const float *radii, const float *u,
+                                 int64_t n, int32_t *out_index, float *out_pdf, snch_stream_t stream);
+int snch_scene2_sample_on_object(snch_scene2_t scene, const int32_t *index, const float *u, int64_t n,
+                                 float *out_points_xy, snch_stream_t stream);
 
 typedef struct snch_mlp_s *snch_mlp_t;
 

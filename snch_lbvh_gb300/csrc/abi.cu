@@ -98,7 +98,7 @@ struct snch_scene_s
     // and the wide records of the built tree: [0] 4-way, [1] 8-way
     int width_near = 2, width_sil = 2;
     int block_near = 128, block_sil = 128;  // threads per block of the binary searches
-    int packet_near = 0, packet_sil = 2;    // warp packets: 0 never, 1 always, 2 Morton-ordered batches
+    int packet_near = 2, packet_sil = 2;    // warp packets: 0 never, 1 always, 2 Morton-ordered batches
     float4 *wide[2] = {nullptr, nullptr};
     uint32_t *wide_idx[2] = {nullptr, nullptr};  // wide index of each wide-root binary node
     size_t wide_cap[2] = {0, 0};  // records allocated

@@ -5,7 +5,7 @@ import numpy as np
 import pytest
 
 from conftest import golden_names, load_golden
-from test_gpu_parity import bits, built_scene, check_edge_ids
+from test_gpu_parity import bits, built_scene, check_edge_ids, check_tri_ids
 
 pytestmark = pytest.mark.gpu
 
@@ -62,20 +62,22 @@ def check_batch(snch, ms, rng, per_mesh=3000):
     i, d = b.query_nearest_batch(mesh_ids[perm], pts[perm])
     sd, se = b.query_silhouette_batch(mesh_ids[perm], pts[perm], flips[perm])
     got = [x.cpu().numpy() for x in (i, d, sd, se)]
-    for g, e in zip(got[:3], exp[:3]):
+    for g, e in zip(got[1:3], exp[1:3]):
         np.testing.assert_array_equal(bits(g), bits(e[perm]))
     # silhouette edge ids, mesh by mesh: equal or an exact tie (warp packets)
     back = np.empty_like(perm)
     back[perm] = np.arange(len(perm))
-    se_in = got[3][back]
+    se_in, ni_in = got[3][back], got[0][back]
     start = 0
     for m, (v, f) in enumerate(ms):
         k = int((mesh_ids == m).sum())  # mesh_ids are mesh-major before the permutation
         sl = slice(start, start + k)
         if tops[m] is not None:
-            check_edge_ids(se_in[sl], exp[3][sl], exp[2][sl], pts[sl], v, tops[m])
+            check_tri_ids(ni_in[sl], exp[0][sl], exp[1][sl], pts[sl], v, f, max_frac=1e-2)
+            check_edge_ids(se_in[sl], exp[3][sl], exp[2][sl], pts[sl], v, tops[m], max_frac=1e-2)
         else:
             np.testing.assert_array_equal(se_in[sl], exp[3][sl])
+            np.testing.assert_array_equal(ni_in[sl], exp[0][sl])
         start += k
     assert b.device_status() == 0
     return b

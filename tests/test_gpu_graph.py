@@ -6,7 +6,7 @@ whose results are the plain ones."""
 import numpy as np
 import pytest
 
-from test_gpu_parity import bits, check_edge_ids
+from test_gpu_parity import bits, check_edge_ids, check_tri_ids
 
 pytestmark = pytest.mark.gpu
 
@@ -135,8 +135,9 @@ def test_autotune_keeps_results(snch):
     i, d = s.query_nearest(pts)
     sd, se = s.query_silhouette(pts, flip)
     got = [i.cpu().numpy(), bits(d.cpu().numpy()), bits(sd.cpu().numpy()), se.cpu().numpy()]
-    for x, y in zip(exp[:3], got[:3]):
+    for x, y in zip(exp[1:3], got[1:3]):
         np.testing.assert_array_equal(y, x)
+    check_tri_ids(got[0], exp[0], d.cpu().numpy(), pts, v, f)
     check_edge_ids(got[3], exp[3], sd.cpu().numpy(), pts, v, s.export_topology()[2])
     s.build_bvh()  # a rebuild keeps the chosen widths
     assert s.device_status() == 0

@@ -13,7 +13,7 @@ import numpy as np
 import pytest
 
 from oracle import mlp_oracle as mo
-from test_gpu_parity import bits, check_edge_ids, built_scene
+from test_gpu_parity import bits, check_edge_ids, check_tri_ids, built_scene
 
 pytestmark = pytest.mark.gpu
 
@@ -135,6 +135,7 @@ def trained():
     m = LearnedRadius(np.zeros(3), np.ones(3), seed=1)
     _, loss0 = m.gradient(train_pts, tgt, tau=0.9)
     loss = m.train(train_pts, tgt, epochs=12, batch=16384, lr=2e-3, tau=0.9)
+    s.faces = sc.faces  # for the tie checks
     return s, m, loss0, loss
 
 
@@ -153,8 +154,9 @@ def test_learned_radius_queries_identical(trained):
     i0, d0 = s.query_nearest(pts)
     nf = torch.zeros(1, dtype=torch.int32, device="cuda")
     i1, d1 = s.query_nearest_seeded(pts, rn, num_fallback=nf)
-    np.testing.assert_array_equal(i1.cpu().numpy(), i0.cpu().numpy())
     np.testing.assert_array_equal(bits(d1.cpu().numpy()), bits(d0.cpu().numpy()))
+    check_tri_ids(i1.cpu().numpy(), i0.cpu().numpy(), d0.cpu().numpy(), pts.cpu().numpy(),
+                  s.vertices().cpu().numpy(), s.faces)
     frac_near = int(nf.item()) / len(pts)
     sd0, se0 = s.query_silhouette(pts, flip)
     sd1, se1 = s.query_silhouette_seeded(pts, rs, flip, num_fallback=nf)

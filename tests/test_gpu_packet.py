@@ -8,7 +8,7 @@ import numpy as np
 import pytest
 
 from conftest import golden_names, load_golden
-from test_gpu_parity import bits, built_scene, check_edge_ids
+from test_gpu_parity import bits, built_scene, check_edge_ids, check_tri_ids
 from test_gpu_wide import answers, tie_probes
 
 pytestmark = pytest.mark.gpu
@@ -23,14 +23,15 @@ def snch():
     return snch_lbvh_gb300
 
 
-def check_packet(snch, s, pts, flip, verts):
+def check_packet(snch, s, pts, flip, verts, tris):
     s.set_option(snch.OPT_PACKET, 0)
     base = answers(s, pts, flip)
     s.set_option(snch.OPT_PACKET, 1)
     got = answers(s, pts, flip)
     s.set_option(snch.OPT_PACKET, 2)
-    for name, x, y in zip(("nearest idx", "nearest dist", "silhouette dist"), base, got):
+    for name, x, y in zip(("nearest dist", "silhouette dist"), base[1:3], got[1:3]):
         np.testing.assert_array_equal(y, x, err_msg=name)
+    check_tri_ids(got[0], base[0], base[1].view(np.float32), pts, verts, tris)
     check_edge_ids(got[3], base[3], base[2].view(np.float32), pts, verts, s.export_topology()[2])
     assert s.device_status() == 0
 
@@ -40,7 +41,7 @@ def test_packet_equals_per_lane_golden(snch, name):
     g = load_golden(name)
     s = built_scene(snch, g["verts"], g["tris"])
     pts = np.concatenate([g["near_pts"], g["sil_pts"], tie_probes(g["verts"], g["tris"])]).astype(np.float32)
-    check_packet(snch, s, pts, (np.arange(len(pts)) % 2).astype(np.uint8), g["verts"])
+    check_packet(snch, s, pts, (np.arange(len(pts)) % 2).astype(np.uint8), g["verts"], g["tris"])
 
 
 def test_packet_equals_per_lane_config1(snch):
@@ -48,7 +49,7 @@ def test_packet_equals_per_lane_config1(snch):
     v, f = meshes.noisy_icosphere(5, 1.0, 0.01, seed=0)
     pts = np.concatenate([meshes.box_queries(v, 1_000_000, 1.2, seed=1), tie_probes(v, f)])
     flip = (np.random.default_rng(2).random(len(pts)) < 0.5).astype(np.uint8)
-    check_packet(snch, built_scene(snch, v, f), pts, flip, v)
+    check_packet(snch, built_scene(snch, v, f), pts, flip, v, f)
 
 
 @pytest.mark.parametrize("ordered", [1, 0])
@@ -59,7 +60,7 @@ def test_packet_equals_per_lane_wost_scene(snch, ordered):
     s.set_option(snch.OPT_QUERY_ORDER, ordered)  # unordered: incoherent packets, same answers
     rng = np.random.default_rng(6)
     pts = rng.random((1_000_000 if ordered else 200_000, 3), dtype=np.float32)
-    check_packet(snch, s, pts, (rng.random(len(pts)) < 0.5).astype(np.uint8), sc.verts)
+    check_packet(snch, s, pts, (rng.random(len(pts)) < 0.5).astype(np.uint8), sc.verts, sc.faces)
 
 
 def test_packet_batched_and_seeded(snch):
@@ -91,13 +92,14 @@ def test_packet_batched_and_seeded(snch):
     base = run()
     b.set_option(snch.OPT_PACKET, 1)
     got = run()
-    for x, y in zip(base[:3], got[:3]):
+    for x, y in zip(base[1:3], got[1:3]):
         np.testing.assert_array_equal(y, x)
-    # edge ids per mesh: equal, or an exact tie (the duplicated-triangle golden mesh has them)
+    # indices per mesh: equal, or an exact tie (the duplicated-triangle golden mesh has them)
     for m, (v, f) in enumerate(ms):
         sel = np.nonzero(mesh == m)[0]
         if len(f) and len(sel):
             s1 = built_scene(snch, v, f)
+            check_tri_ids(got[0][sel], base[0][sel], base[1][sel].view(np.float32), pts[sel], v, f, max_frac=1e-2)
             check_edge_ids(got[3][sel], base[3][sel], base[2][sel].view(np.float32), pts[sel], v,
                            s1.export_topology()[2], max_frac=1e-2)
     assert b.device_status() == 0
@@ -112,8 +114,8 @@ def test_packet_batched_and_seeded(snch):
     s.set_option(snch.OPT_PACKET, 1)
     r, _ = radii_mix(d0.cpu().numpy(), rng)
     i1, d1 = s.query_nearest_seeded(q, r)
-    np.testing.assert_array_equal(i1.cpu().numpy(), i0.cpu().numpy())
     np.testing.assert_array_equal(bits(d1.cpu().numpy()), bits(d0.cpu().numpy()))
+    check_tri_ids(i1.cpu().numpy(), i0.cpu().numpy(), d0.cpu().numpy(), q, sc.verts, sc.faces)
     rs, _ = radii_mix(sd0.cpu().numpy(), rng)
     sd1, se1 = s.query_silhouette_seeded(q, rs, fl)
     np.testing.assert_array_equal(bits(sd1.cpu().numpy()), bits(sd0.cpu().numpy()))

@@ -64,6 +64,50 @@ def check_edge_ids(got, exp, dist, pts, verts, edge_verts, max_frac=1e-4):
     return len(bad)
 
 
+def tri_dist64(p, a, b, c):
+    """FP64 distance from points p (n, 3) to triangles a, b, c (n, 3 each):
+    the closest point by its Voronoi region (Ericson, Real-Time Collision
+    Detection 5.1.5), vectorised."""
+    p, a, b, c = (np.asarray(x, np.float64) for x in (p, a, b, c))
+    dot = lambda x, y: np.einsum("ij,ij->i", x, y)
+    ab, ac, ap = b - a, c - a, p - a
+    d1, d2 = dot(ab, ap), dot(ac, ap)
+    bp = p - b
+    d3, d4 = dot(ab, bp), dot(ac, bp)
+    cp = p - c
+    d5, d6 = dot(ab, cp), dot(ac, cp)
+    va, vb, vc = d3 * d6 - d5 * d4, d5 * d2 - d1 * d6, d1 * d4 - d3 * d2
+    den = np.where(va + vb + vc == 0, 1.0, va + vb + vc)
+    q = a + ab * (vb / den)[:, None] + ac * (vc / den)[:, None]  # face
+    w = np.clip(d2 / np.where(d2 - d6 == 0, 1, d2 - d6), 0, 1)
+    q = np.where(((vb <= 0) & (d2 >= 0) & (d6 <= 0))[:, None], a + ac * w[:, None], q)  # edge ac
+    w = np.clip((d4 - d3) / np.where((d4 - d3) + (d5 - d6) == 0, 1, (d4 - d3) + (d5 - d6)), 0, 1)
+    q = np.where(((va <= 0) & ((d4 - d3) >= 0) & ((d5 - d6) >= 0))[:, None], b + (c - b) * w[:, None], q)  # edge bc
+    w = np.clip(d1 / np.where(d1 - d3 == 0, 1, d1 - d3), 0, 1)
+    q = np.where(((vc <= 0) & (d1 >= 0) & (d3 <= 0))[:, None], a + ab * w[:, None], q)  # edge ab
+    q = np.where(((d6 >= 0) & (d5 <= d6))[:, None], c, q)
+    q = np.where(((d3 >= 0) & (d4 <= d3))[:, None], b, q)
+    q = np.where(((d1 <= 0) & (d2 <= 0))[:, None], a, q)
+    return np.linalg.norm(p - q, axis=1)
+
+
+def check_tri_ids(got, exp, dist, pts, verts, tris, max_frac=1e-4):
+    """Nearest-triangle indices of two searches with bit-identical distances:
+    equal, or both triangles at the returned distance (the tie case of
+    check_edge_ids), in at most max_frac of the queries."""
+    got, exp = np.asarray(got).view(np.int32), np.asarray(exp).view(np.int32)
+    bad = np.nonzero(got != exp)[0]
+    assert len(bad) <= max(3, max_frac * len(got)), f"{len(bad)} triangle indices differ"
+    if len(bad) == 0:
+        return 0
+    d = np.asarray(dist, np.float64)[bad]
+    for t in (got[bad], exp[bad]):
+        tv = np.asarray(tris)[t]
+        dt = tri_dist64(np.asarray(pts)[bad], verts[tv[:, 0]], verts[tv[:, 1]], verts[tv[:, 2]])
+        assert np.all(np.abs(dt - d) <= 1e-6 * np.maximum(d, 1e-3)), "differing triangles are not a distance tie"
+    return len(bad)
+
+
 def built_scene(snch, verts, tris):
     s = snch.Scene(verts, tris)
     s.compute_silhouettes()
@@ -150,8 +194,8 @@ def test_config1_workload_against_oracle(snch, oracle_mod):
     idx, dist = idx.cpu().numpy().view(np.uint32), dist.cpu().numpy()
     orc = oracle_mod.Tree(v, f)
     oi, od = orc.nearest(pts)
-    np.testing.assert_array_equal(idx, oi)
     np.testing.assert_array_equal(bits(dist), bits(od))
+    check_tri_ids(idx, oi, od, pts, v, f)
     # FP64 brute force on a subset: the reference algorithm's FP32 error. The
     # chosen triangle is compared through its FP64 distance, because exact ties
     # (a shared vertex or edge is the nearest feature) are common and brute
@@ -263,8 +307,9 @@ def test_near_first_equals_reference_order_config1(snch):
     s = built_scene(snch, v, f)
     a = run_all(s, q, snch.TRAVERSAL_REFERENCE_ORDER)
     b = run_all(s, q, snch.TRAVERSAL_NEAR_FIRST)
-    for x, y in zip(a[:3], b[:3]):
+    for x, y in zip(a[1:3], b[1:3]):
         np.testing.assert_array_equal(x, y)
+    check_tri_ids(b[0], a[0], a[1].view(np.float32), pts, v, f)
     check_edge_ids(b[3], a[3], a[2].view(np.float32), pts, v, s.export_topology()[2])
     assert s.device_status() == 0
 
@@ -290,8 +335,9 @@ def test_query_order_does_not_change_results(snch):
     s.set_option(snch.OPT_QUERY_ORDER, 1)
     b = everything()
     for k, (x, y) in enumerate(zip(a, b)):
-        if k != 3:  # silhouette edge ids: ordered batches run as warp packets
+        if k not in (0, 3):  # nearest index / silhouette edge id: ordered batches run as warp packets
             np.testing.assert_array_equal(x.view(np.uint8), y.view(np.uint8))
+    check_tri_ids(b[0], a[0], a[1], q["near_pts"], v, f)
     check_edge_ids(b[3], a[3], a[2], q["sil_pts"], v, s.export_topology()[2])
     assert s.device_status() == 0
 

@@ -5,7 +5,7 @@ properties of the tree."""
 import numpy as np
 import pytest
 
-from test_gpu_parity import bits, built_scene, check_cones, check_silhouette
+from test_gpu_parity import bits, built_scene, check_cones, check_silhouette, check_tri_ids
 
 pytestmark = pytest.mark.gpu
 
@@ -73,8 +73,8 @@ def test_queries_against_oracle_subset(big):
     q = meshes.wost_queries(200_000, 100_000, 200_000, 200_000, seed=11)
     idx, dist = s.query_nearest(q["near_pts"])
     oi, od = orc.nearest(q["near_pts"])
-    np.testing.assert_array_equal(idx.cpu().numpy().view(np.uint32), oi)
     np.testing.assert_array_equal(bits(dist.cpu().numpy()), bits(od))
+    check_tri_ids(idx.cpu().numpy(), oi, od, q["near_pts"], sc.verts, sc.faces)
     sd, _ = s.query_silhouette(q["sil_pts"], q["sil_flip"])
     osd, _ = orc.silhouette(q["sil_pts"], q["sil_flip"])
     check_silhouette(sd.cpu().numpy(), osd)

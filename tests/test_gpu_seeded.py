@@ -5,7 +5,7 @@ below, at and above the answer, tiny and huge, on the config-1 mesh and the
 import numpy as np
 import pytest
 
-from test_gpu_parity import bits, built_scene, check_edge_ids
+from test_gpu_parity import bits, built_scene, check_edge_ids, check_tri_ids
 
 pytestmark = pytest.mark.gpu
 
@@ -43,8 +43,8 @@ def test_seeded_equals_unseeded(mesh):
     r, kind = radii_mix(d0n, rng)
     nf = torch.zeros(1, dtype=torch.int32, device="cuda")
     i1, d1 = s.query_nearest_seeded(pts, r, num_fallback=nf)
-    np.testing.assert_array_equal(i1.cpu().numpy(), i0.cpu().numpy())
     np.testing.assert_array_equal(bits(d1.cpu().numpy()), bits(d0n))
+    check_tri_ids(i1.cpu().numpy(), i0.cpu().numpy(), d0n, pts, v, f)
     expect = int(((r * r) < (d0n * d0n)).sum())  # nothing inside the radius: fallback
     assert int(nf.item()) == expect
 
@@ -85,5 +85,6 @@ def test_seeded_reference_order_equals_unseeded():
     np.testing.assert_array_equal(se1.cpu().numpy(), se0.cpu().numpy())
     s.set_traversal(snch.TRAVERSAL_NEAR_FIRST)
     i2, d2 = s.query_nearest(pts)
-    np.testing.assert_array_equal(i2.cpu().numpy(), i0.cpu().numpy())
+    np.testing.assert_array_equal(bits(d2.cpu().numpy()), bits(d0n))
+    check_tri_ids(i2.cpu().numpy(), i0.cpu().numpy(), d0n, pts, v, f)
     assert s.device_status() == 0
