@@ -206,6 +206,76 @@ class scene_loader3
     std::vector<Int3> indices_;
 };
 
+// lbvh::scene<2> (scene.cuh:287-703): line segments with silhouette vertices.
+// Iterators over float2-like (x, y) vertices and int2-like (x, y) segments.
+class scene2
+{
+  public:
+    template <typename VertexIt, typename IndexIt>
+    scene2(VertexIt vertices_first, VertexIt vertices_last, IndexIt indices_first, IndexIt indices_last)
+    {
+        std::vector<float> v;
+        std::vector<int32_t> s;
+        for (auto it = vertices_first; it != vertices_last; ++it)
+        {
+            v.push_back(static_cast<float>(it->x));
+            v.push_back(static_cast<float>(it->y));
+        }
+        for (auto it = indices_first; it != indices_last; ++it)
+        {
+            s.push_back(static_cast<int32_t>(it->x));
+            s.push_back(static_cast<int32_t>(it->y));
+        }
+        check(snch_scene2_create(v.data(), static_cast<int64_t>(v.size() / 2), s.data(),
+                                 static_cast<int64_t>(s.size() / 2), &h_));
+    }
+    scene2(const scene2 &) = delete;
+    scene2 &operator=(const scene2 &) = delete;
+    scene2(scene2 &&o) noexcept : h_(std::exchange(o.h_, nullptr)), built_(o.built_) {}
+    ~scene2()
+    {
+        if (h_)
+            snch_scene2_destroy(h_);
+    }
+    // the silhouette vertices are derived on the GPU together with the tree
+    void compute_silhouettes(snch_stream_t = nullptr) {}
+    void build_bvh(snch_stream_t stream = nullptr)
+    {
+        check(snch_scene2_build(h_, stream));
+        built_ = true;
+    }
+    void query_nearest(const float *points_xy, int64_t n, uint32_t *index, float *distance,
+                       snch_stream_t stream = nullptr) const
+    {
+        check(snch_scene2_query_nearest(h_, points_xy, n, index, distance, stream));
+    }
+    void query_silhouette(const float *points_xy, const uint8_t *flip, int64_t n, float *distance,
+                          int32_t *vertex = nullptr, snch_stream_t stream = nullptr) const
+    {
+        check(snch_scene2_query_silhouette(h_, points_xy, flip, n, distance, vertex, stream));
+    }
+    void query_ray(const float *origins_xy, const float *dirs_xy, const float *tmax, int64_t n, uint8_t *hit,
+                   float *t, float *segment_param, uint32_t *index, snch_stream_t stream = nullptr) const
+    {
+        check(snch_scene2_query_ray(h_, origins_xy, dirs_xy, tmax, n, hit, t, segment_param, index, stream));
+    }
+    void sample_in_circle(const float *centers_xy, const float *radii, const float *u, int64_t n, int32_t *index,
+                          float *pdf, snch_stream_t stream = nullptr) const
+    {
+        check(snch_scene2_sample_in_circle(h_, centers_xy, radii, u, n, index, pdf, stream));
+    }
+    void sample_on_object(const int32_t *index, const float *u, int64_t n, float *points_xy,
+                          snch_stream_t stream = nullptr) const
+    {
+        check(snch_scene2_sample_on_object(h_, index, u, n, points_xy, stream));
+    }
+    snch_scene2_t handle() const { return h_; }
+
+  private:
+    snch_scene2_t h_ = nullptr;
+    bool built_ = false;
+};
+
 // Many independent meshes in one scene (snch_batch_*): one build, one query
 // launch per type; results per mesh as a scene3 of that mesh alone gives.
 class batch3 : public scene3

@@ -65,6 +65,13 @@ def _declare(L):
     L.orc_max_depth.restype = I
     L.orc_leaf_ranks.argtypes = [P, I64, P]
     L.orc_query_overlap.argtypes = [P, P, I64, I64, P, P, I]
+    L.orc2_topology.argtypes = [P, I64, I64, P, P]
+    L.orc2_build.argtypes = [P, P, I64, P, P, P, P, P, P, P, P]
+    L.orc2_build.restype = I
+    L.orc2_query_nearest.argtypes = [P, P, I64, P, P]
+    L.orc2_query_silhouette.argtypes = [P, P, P, I64, P, P]
+    L.orc2_query_ray.argtypes = [P, P, P, P, I64, P, P, P, P]
+    L.orc2_sample_in_circle.argtypes = [P, P, P, P, I64, P, P]
     L.orc_query_line.argtypes = [P, P, P, I64, I64, P, P, P, I]
 
 
@@ -212,3 +219,63 @@ def brute_ray_f64(verts, tris, origins, dirs, tmax, nthreads=None):
     lib().orc_brute_ray_f64(_p(v), _p(t), len(t.reshape(-1, 3)), _p(o), _p(d), _p(tm), n, _p(hit), _p(tt), _p(idx),
                             nthreads or nthreads_default())
     return hit, tt, idx
+
+
+class Orc2Scene(C.Structure):
+    _fields_ = [("num_segs", C.c_int64), ("num_verts", C.c_int64), ("verts", C.c_void_p), ("segs", C.c_void_p),
+                ("seg_owned", C.c_void_p), ("sv", C.c_void_p), ("nodes", C.c_void_p), ("aabbs", C.c_void_p),
+                ("cones", C.c_void_p)]
+
+
+class Tree2:
+    """The reference's scene<2> (scene.cuh:287-703): line segments, silhouette
+    vertices, the 2D LBVH and the four queries, restated in C (FP32)."""
+
+    def __init__(self, verts, segs):
+        L = lib()
+        self.verts = _c(verts, np.float32).reshape(-1, 2)
+        self.segs = _c(segs, np.int32).reshape(-1, 2)
+        n, nv = len(self.segs), len(self.verts)
+        self.sv = np.empty((max(nv, 1), 4), np.int32)[:nv]
+        self.seg_owned = np.empty((n, 2), np.int32)
+        L.orc2_topology(_p(self.segs), n, nv, _p(self.sv), _p(self.seg_owned))
+        nn = max(2 * n - 1, 0)
+        self.morton = np.empty(n, np.uint32)
+        self.sorted_idx = np.empty(n, np.uint32)
+        self.nodes = np.empty((nn, 4), np.uint32)
+        self.aabbs = np.empty((nn, 4), np.float32)
+        self.cones = np.empty((nn, 4), np.float32)
+        self.d1 = np.zeros(nn, np.uint8)
+        self.unique = bool(L.orc2_build(_p(self.verts), _p(self.segs), n, _p(self.seg_owned), _p(self.sv),
+                                        _p(self.morton), _p(self.sorted_idx), _p(self.nodes), _p(self.aabbs),
+                                        _p(self.cones), _p(self.d1)))
+        self._s = Orc2Scene(n, nv, _p(self.verts).value, _p(self.segs).value, _p(self.seg_owned).value,
+                            _p(self.sv).value, _p(self.nodes).value, _p(self.aabbs).value, _p(self.cones).value)
+
+    def nearest(self, pts):
+        p = _c(pts, np.float32).reshape(-1, 2)
+        idx, dist = np.empty(len(p), np.uint32), np.empty(len(p), np.float32)
+        lib().orc2_query_nearest(C.byref(self._s), _p(p), len(p), _p(idx), _p(dist))
+        return idx, dist
+
+    def silhouette(self, pts, flip=None):
+        p = _c(pts, np.float32).reshape(-1, 2)
+        fl = None if flip is None else _c(flip, np.uint8)
+        dist, vid = np.empty(len(p), np.float32), np.empty(len(p), np.int32)
+        lib().orc2_query_silhouette(C.byref(self._s), _p(p), _p(fl), len(p), _p(dist), _p(vid))
+        return dist, vid
+
+    def ray(self, origins, dirs, tmax):
+        o, d = _c(origins, np.float32).reshape(-1, 2), _c(dirs, np.float32).reshape(-1, 2)
+        tm = _c(tmax, np.float32)
+        n = len(o)
+        hit, t, sp, idx = np.empty(n, np.uint8), np.empty(n, np.float32), np.empty(n, np.float32), np.empty(n, np.uint32)
+        lib().orc2_query_ray(C.byref(self._s), _p(o), _p(d), _p(tm), n, _p(hit), _p(t), _p(sp), _p(idx))
+        return hit, t, sp, idx
+
+    def sample(self, centers, radii, u):
+        c = _c(centers, np.float32).reshape(-1, 2)
+        r, uu = _c(radii, np.float32), _c(u, np.float32)
+        idx, pdf = np.empty(len(c), np.int32), np.empty(len(c), np.float32)
+        lib().orc2_sample_in_circle(C.byref(self._s), _p(c), _p(r), _p(uu), len(c), _p(idx), _p(pdf))
+        return idx, pdf

@@ -84,10 +84,150 @@ static int read_obj_mode(const char *obj, const char *out_path)
     return 0;
 }
 
+// --2d in.bin out.bin: the reference's scene<2> (scene.cuh:287-703), its 2D build
+// and the four query templates over line segments. Input: int64 nv, nseg, n_near,
+// n_sil, n_ray, n_smp; float2 verts, int2 segments, near points, silhouette points
+// + uint8 flips, ray origins, directions, tmax, circle centres, radii, u.
+// Output: silhouette vertices (nv x int4), owned vertices (nseg x int2), Morton
+// codes, nodes, aabbs (upper.xy, lower.xy), cones (axis.xy, half, radius), then
+// (two or more segments) nearest (uint32, float), silhouette (float), ray
+// (uint8 hit, float t, float s, uint32 idx), sample (int32, float pdf).
+static int scene2d_mode(const char *in_path, const char *out_path)
+{
+    FILE *in = std::fopen(in_path, "rb");
+    if (!in)
+        return 3;
+    int64_t hdr[6];
+    if (std::fread(hdr, sizeof(int64_t), 6, in) != 6)
+        return 4;
+    const int64_t nv = hdr[0], nt = hdr[1], n_near = hdr[2], n_sil = hdr[3], n_ray = hdr[4], n_smp = hdr[5];
+    std::vector<float> verts, near_pts, sil_pts, ray_o, ray_d, ray_tmax, smp_c, smp_r, smp_u;
+    std::vector<int32_t> segs;
+    std::vector<uint8_t> sil_flip;
+    bool ok = read_n(in, verts, nv * 2) && read_n(in, segs, nt * 2) && read_n(in, near_pts, n_near * 2) &&
+              read_n(in, sil_pts, n_sil * 2) && read_n(in, sil_flip, n_sil) && read_n(in, ray_o, n_ray * 2) &&
+              read_n(in, ray_d, n_ray * 2) && read_n(in, ray_tmax, n_ray) && read_n(in, smp_c, n_smp * 2) &&
+              read_n(in, smp_r, n_smp) && read_n(in, smp_u, n_smp);
+    std::fclose(in);
+    if (!ok)
+        return 5;
+    std::vector<float2> v2(static_cast<size_t>(nv));
+    for (int64_t i = 0; i < nv; ++i)
+        v2[i] = make_float2(verts[2 * i], verts[2 * i + 1]);
+    std::vector<int2> s2(static_cast<size_t>(nt));
+    for (int64_t i = 0; i < nt; ++i)
+        s2[i] = make_int2(segs[2 * i], segs[2 * i + 1]);
+    lbvh::scene<2> sc(v2.data(), v2.data() + v2.size(), s2.data(), s2.data() + s2.size());
+    sc.compute_silhouettes();
+    sc.build_bvh();
+    const auto bvh = sc.get_bvh_device_ptr();
+    FILE *out = std::fopen(out_path, "wb");
+    if (!out)
+        return 6;
+    for (int64_t i = 0; i < nv; ++i)
+    {
+        const auto &q = sc.silhouettes_h[i].indices;
+        const int32_t w[4] = {q.x, q.y, q.z, q.w};
+        write_n(out, w, 4);
+    }
+    for (int64_t i = 0; i < nt; ++i)
+    {
+        const int32_t w[2] = {sc.lines[i].silhouette_indices.x, sc.lines[i].silhouette_indices.y};
+        write_n(out, w, 2);
+    }
+    {
+        using box_t = lbvh::aabb<float, 2>;
+        const float inf = std::numeric_limits<float>::infinity();
+        box_t whole;
+        whole.upper = make_float2(-inf, -inf);
+        whole.lower = make_float2(inf, inf);
+        std::vector<box_t> boxes(static_cast<size_t>(nt));
+        for (int64_t i = 0; i < nt; ++i)
+        {
+            boxes[i] = lbvh::scene<2>::aabb_getter()(sc.lines[i]);
+            whole = lbvh::merge(whole, boxes[i]);
+        }
+        lbvh::default_morton_code_calculator<float, 2, lbvh::scene<2>::line_segment> calc(whole);
+        for (int64_t i = 0; i < nt; ++i)
+        {
+            const uint32_t m = calc(sc.lines[i], boxes[i]);
+            write_n(out, &m, 1);
+        }
+    }
+    const int64_t NN = bvh.num_nodes;
+    for (int64_t i = 0; i < NN; ++i)
+    {
+        const auto &n = bvh.nodes[i];
+        const uint32_t q[4] = {n.parent_idx, n.left_idx, n.right_idx, n.object_idx};
+        write_n(out, q, 4);
+    }
+    for (int64_t i = 0; i < NN; ++i)
+    {
+        const auto &b = bvh.aabbs[i];
+        const float q[4] = {b.upper.x, b.upper.y, b.lower.x, b.lower.y};
+        write_n(out, q, 4);
+    }
+    for (int64_t i = 0; i < NN; ++i)
+    {
+        const auto &c = bvh.cones[i];
+        const float q[4] = {c.axis.x, c.axis.y, c.half_angle, c.radius};
+        write_n(out, q, 4);
+    }
+    if (nt >= 2)
+    {
+        for (int64_t q = 0; q < n_near; ++q)
+        {
+            const auto r = lbvh::query_device(bvh, lbvh::nearest(make_float2(near_pts[2 * q], near_pts[2 * q + 1])),
+                                              lbvh::scene<2>::distance_calculator());
+            const uint32_t idx = r.first;
+            const float d = r.second;
+            write_n(out, &idx, 1);
+            write_n(out, &d, 1);
+        }
+        for (int64_t q = 0; q < n_sil; ++q)
+        {
+            const float2 p = make_float2(sil_pts[2 * q], sil_pts[2 * q + 1]);
+            const float d = lbvh::query_device(bvh, lbvh::nearest_silhouette(p, sil_flip[q] != 0),
+                                               lbvh::scene<2>::silhouette_distance_calculator());
+            write_n(out, &d, 1);
+        }
+        for (int64_t q = 0; q < n_ray; ++q)
+        {
+            const float2 o = make_float2(ray_o[2 * q], ray_o[2 * q + 1]);
+            const float2 d = make_float2(ray_d[2 * q], ray_d[2 * q + 1]);
+            const auto r = lbvh::query_device(bvh, lbvh::ray_intersect(lbvh::ray<float, 2>(o, d), ray_tmax[q]),
+                                              lbvh::scene<2>::intersect_test());
+            const uint8_t hit = thrust::get<0>(r) ? 1 : 0;
+            const float t = thrust::get<1>(r);
+            const float sp = hit ? thrust::get<2>(r) : 0.0f;
+            const uint32_t idx = thrust::get<3>(r);
+            write_n(out, &hit, 1);
+            write_n(out, &t, 1);
+            write_n(out, &sp, 1);
+            write_n(out, &idx, 1);
+        }
+        for (int64_t q = 0; q < n_smp; ++q)
+        {
+            const float2 c = make_float2(smp_c[2 * q], smp_c[2 * q + 1]);
+            const auto r = lbvh::sample_object_in_sphere(
+                bvh, lbvh::sphere_intersect(lbvh::sphere<float, 2>(c, smp_r[q])), lbvh::scene<2>::intersect_sphere(),
+                lbvh::scene<2>::measurement_getter(), lbvh::scene<2>::green_weight(), smp_u[q]);
+            const int32_t idx = r.first;
+            const float pdf = idx >= 0 ? r.second : 0.0f;
+            write_n(out, &idx, 1);
+            write_n(out, &pdf, 1);
+        }
+    }
+    std::fclose(out);
+    return 0;
+}
+
 int main(int argc, char **argv)
 {
     if (argc == 4 && std::string(argv[1]) == "--obj")
         return read_obj_mode(argv[2], argv[3]);
+    if (argc == 4 && std::string(argv[1]) == "--2d")
+        return scene2d_mode(argv[2], argv[3]);
     if (argc != 3)
     {
         std::fprintf(stderr, "usage: %s in.bin out.bin\n", argv[0]);

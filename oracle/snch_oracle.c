@@ -1273,3 +1273,577 @@ void orc_query_line(const orc_scene *s, const float *origins, const float *dirs,
     enum_ctx c = {s, origins, dirs, max_out, idx, t, count, 1};
     orc_parallel(n, nthreads, enum_body, &c);
 }
+
+/* ================================================================ 2D scenes
+ * scene<2> (scene.cuh:287-703): line segments with silhouette VERTICES, the
+ * same LBVH build in 2D (bvh.cuh with aabb<float,2>, cone<float,2>) and the
+ * same four query templates (query.cuh, sample.cuh) over the 2D functors. */
+typedef struct { float x, y; } f2;
+typedef struct { f2 upper, lower; } box2;                    /* aabb<float,2>, upper first */
+typedef struct { f2 axis; float half_angle, radius; } cone2; /* cone<float,2> */
+#define ORC_BVH_OFFSET 1e-3f                                  /* bvh_offset scene.cuh:12 */
+
+static inline f2 mk2(float x, float y) { f2 r = {x, y}; return r; }
+static inline f2 sub2(f2 a, f2 b) { return mk2(a.x - b.x, a.y - b.y); }
+static inline float dot2(f2 a, f2 b) { return a.x * b.x + a.y * b.y; }
+static inline float len2(f2 a) { return sqrtf(a.x * a.x + a.y * a.y); }
+static inline f2 norm2(f2 v) { float n = len2(v); return mk2(v.x / n, v.y / n); }
+static inline f2 vload2(const float *v, int32_t i) { return mk2(v[2 * i], v[2 * i + 1]); }
+static inline f2 centroid2(box2 b) { return mk2((b.upper.x + b.lower.x) * 0.5f, (b.upper.y + b.lower.y) * 0.5f); }
+
+/* compute_silhouettes scene.cuh:642-664: one silhouette vertex per mesh vertex,
+ * {prev, self, next, -1}, later segments overwriting earlier ones; build_bvh
+ * scene.cuh:666-683: a segment owns the endpoints no earlier segment touched,
+ * in (x, y) order. sv: V x 4, seg_owned: N x 2 (-1 padded). */
+void orc2_topology(const int32_t *segs, int64_t n, int64_t nv, int32_t *sv, int32_t *seg_owned) {
+    for (int64_t v = 0; v < 4 * nv; ++v) sv[v] = -1;
+    for (int64_t i = 0; i < n; ++i) {
+        int32_t a = segs[2 * i], b = segs[2 * i + 1];
+        sv[4 * a + 1] = a; sv[4 * a + 2] = b;
+        sv[4 * b + 0] = a; sv[4 * b + 1] = b;
+    }
+    uint8_t *seen = (uint8_t *)calloc((size_t)(nv > 0 ? nv : 1), 1);
+    for (int64_t i = 0; i < n; ++i) {
+        int32_t own[2] = {-1, -1};
+        int k = 0;
+        for (int j = 0; j < 2; ++j) {
+            int32_t v = segs[2 * i + j];
+            if (!seen[v]) { seen[v] = 1; own[k++] = v; }
+        }
+        seg_owned[2 * i] = own[0];
+        seg_owned[2 * i + 1] = own[1];
+    }
+    free(seen);
+}
+
+/* silhouette_vertex scene.cuh:291-384 */
+static inline int sv_has_face(const int32_t *sv, int f) { return f == 0 ? sv[2] != -1 : sv[0] != -1; }
+static f2 sv_face_normal(const float *verts, const int32_t *sv, int f, int do_normalize) {
+    int i = f == 0 ? 1 : 0;
+    f2 pa = vload2(verts, sv[i]), pb = vload2(verts, sv[i + 1]);
+    f2 s = sub2(pb, pa);
+    f2 nn = mk2(s.y, -s.x);
+    return do_normalize ? norm2(nn) : nn;
+}
+static f2 sv_normal(const float *verts, const int32_t *sv) {
+    f2 nn = mk2(0.0f, 0.0f);
+    if (sv_has_face(sv, 0)) { f2 a = sv_face_normal(verts, sv, 0, 0); nn = mk2(nn.x + a.x, nn.y + a.y); }
+    if (sv_has_face(sv, 1)) { f2 a = sv_face_normal(verts, sv, 1, 0); nn = mk2(nn.x + a.x, nn.y + a.y); }
+    return norm2(nn);
+}
+
+/* aabb_getter scene.cuh:420-432 */
+static box2 seg_box(const float *verts, const int32_t *s) {
+    f2 p0 = vload2(verts, s[0]), p1 = vload2(verts, s[1]);
+    box2 b;
+    b.upper = mk2(fmaxf(p0.x, p1.x) + ORC_BVH_OFFSET, fmaxf(p0.y, p1.y) + ORC_BVH_OFFSET);
+    b.lower = mk2(fminf(p0.x, p1.x) - ORC_BVH_OFFSET, fminf(p0.y, p1.y) - ORC_BVH_OFFSET);
+    return b;
+}
+/* cone_getter scene.cuh:434-494 */
+static cone2 seg_cone(const float *verts, const int32_t *s, const int32_t *owned, const int32_t *svs) {
+    box2 bb = seg_box(verts, s);
+    f2 bc = centroid2(bb);
+    cone2 r;
+    r.axis = mk2(0.0f, 0.0f); r.half_angle = ORC_PI; r.radius = 0.0f;
+    int any = 0, all_two = 1;
+    for (int i = 0; i < 2; ++i) {
+        int32_t si = owned[i];
+        if (si == -1) continue;
+        const int32_t *sv = svs + 4 * (int64_t)si;
+        f2 nn = sv_normal(verts, sv);
+        r.axis.x += nn.x; r.axis.y += nn.y;
+        f2 c = vload2(verts, sv[1]);
+        r.radius = smax(r.radius, len2(mk2(c.x - bc.x, c.y - bc.y)));
+        all_two = all_two && sv_has_face(sv, 0) && sv_has_face(sv, 1);
+        any = 1;
+    }
+    if (!any) r.half_angle = -ORC_PI;
+    else if (!all_two) r.half_angle = ORC_PI;
+    else {
+        float an = len2(r.axis);
+        if (an > ORC_EPS) {
+            r.axis.x /= an; r.axis.y /= an;
+            r.half_angle = 0.0f;
+            for (int i = 0; i < 2; ++i) {
+                int32_t si = owned[i];
+                if (si == -1) continue;
+                const int32_t *sv = svs + 4 * (int64_t)si;
+                f2 fn[2];
+                fn[0] = sv_has_face(sv, 0) ? sv_face_normal(verts, sv, 0, 1) : mk2(0.0f, 0.0f);
+                fn[1] = sv_has_face(sv, 1) ? sv_face_normal(verts, sv, 1, 1) : mk2(0.0f, 0.0f);
+                for (int j = 0; j < 2; ++j) {
+                    float ang = acosf(smax(-1.0f, smin(1.0f, dot2(r.axis, fn[j]))));
+                    r.half_angle = smax(r.half_angle, ang);
+                }
+            }
+        }
+    }
+    return r;
+}
+void orc2_leaf_boxes(const float *verts, const int32_t *segs, int64_t n, float *out) {
+    for (int64_t i = 0; i < n; ++i) { box2 b = seg_box(verts, segs + 2 * i); memcpy(out + 4 * i, &b, sizeof b); }
+}
+
+/* morton_code(float2) morton_code.cuh:83-91 (the 3D bit spreading, x * 2 + y) */
+static uint32_t morton2(f2 p) {
+    const float res = 1024.0f;
+    p.x = fminf(fmaxf(p.x * res, 0.0f), res - 1.0f);
+    p.y = fminf(fmaxf(p.y * res, 0.0f), res - 1.0f);
+    return expand_bits((uint32_t)p.x) * 2 + expand_bits((uint32_t)p.y);
+}
+
+/* rotate(float2) cone.cuh:266-275 */
+static f2 rotate2(f2 u, f2 v, float theta) {
+    float det = u.x * v.y - u.y * v.x;
+    theta *= copysignf(1.0f, det);
+    float ct = cosf(theta), st = sinf(theta);
+    return mk2(ct * u.x - st * u.y, st * u.x + ct * u.y);
+}
+/* merge(cone<float,2>) cone.cuh:320-371; pi where the reference leaves the
+ * half angle unassigned (o_theta >= pi, lines 347-351) */
+static cone2 cone_merge2(cone2 a, cone2 b, f2 oa, f2 ob, f2 on, int *d1) {
+    cone2 r;
+    r.axis = mk2(0.0f, 0.0f); r.half_angle = 0.0f; r.radius = 0.0f;
+    int va = a.half_angle >= 0.0f, vb = b.half_angle >= 0.0f;
+    if (va && vb) {
+        f2 axis_a = a.axis, axis_b = b.axis;
+        float ha = a.half_angle, hb = b.half_angle;
+        f2 da = sub2(on, oa), db = sub2(on, ob);
+        r.radius = sqrtf(smax(a.radius * a.radius + (da.x * da.x + da.y * da.y),
+                              b.radius * b.radius + (db.x * db.x + db.y * db.y)));
+        if (hb > ha) { f2 t = axis_a; axis_a = axis_b; axis_b = t; float h = ha; ha = hb; hb = h; }
+        float theta = acosf(smax(-1.0f, smin(1.0f, dot2(axis_a, axis_b))));
+        if (smin(theta + hb, ORC_PI) <= ha) { r.axis = axis_a; r.half_angle = ha; return r; }
+        float o_theta = (ha + theta + hb) / 2.0f;
+        if (o_theta >= ORC_PI) { r.axis = axis_a; r.half_angle = ORC_PI; *d1 = 1; return r; }
+        float r_theta = o_theta - ha;
+        r.axis = rotate2(axis_a, axis_b, r_theta);
+        r.half_angle = o_theta;
+    } else if (va) {
+        r = a;
+    } else if (vb) {
+        r = b;
+    } else {
+        r.half_angle = -ORC_PI;
+    }
+    return r;
+}
+
+int orc2_build(const float *verts, const int32_t *segs, int64_t nseg, const int32_t *seg_owned, const int32_t *svs,
+               uint32_t *morton, uint32_t *sorted_idx, uint32_t *nodes, float *aabbs, float *cones,
+               uint8_t *d1_flags) {
+    if (nseg <= 0) return 1;
+    const unsigned N = (unsigned)nseg, NI = N - 1, NN = 2 * N - 1;
+    box2 *bx = (box2 *)aabbs;
+    cone2 *cn = (cone2 *)cones;
+    box2 *lb_ = (box2 *)malloc(sizeof(box2) * N);
+    cone2 *lc_ = (cone2 *)malloc(sizeof(cone2) * N);
+    box2 whole;
+    whole.upper = mk2(-INFINITY, -INFINITY);
+    whole.lower = mk2(INFINITY, INFINITY);
+    for (unsigned i = 0; i < N; ++i) {
+        lb_[i] = seg_box(verts, segs + 2 * (int64_t)i);
+        lc_[i] = seg_cone(verts, segs + 2 * (int64_t)i, seg_owned + 2 * (int64_t)i, svs);
+        whole.upper = mk2(fmaxf(whole.upper.x, lb_[i].upper.x), fmaxf(whole.upper.y, lb_[i].upper.y));
+        whole.lower = mk2(fminf(whole.lower.x, lb_[i].lower.x), fminf(whole.lower.y, lb_[i].lower.y));
+    }
+    /* default_morton_code_calculator<Real,2> bvh.cuh:257-279 */
+    for (unsigned i = 0; i < N; ++i) {
+        f2 p = centroid2(lb_[i]);
+        p.x -= whole.lower.x; p.y -= whole.lower.y;
+        p.x /= (whole.upper.x - whole.lower.x);
+        p.y /= (whole.upper.y - whole.lower.y);
+        morton[i] = morton2(p);
+    }
+    uint64_t *ck = (uint64_t *)malloc(sizeof(uint64_t) * N);
+    for (unsigned i = 0; i < N; ++i) ck[i] = ((uint64_t)morton[i] << 32) | i;
+    qsort(ck, N, sizeof(uint64_t), u64_cmp);
+    int unique = 1;
+    for (unsigned i = 0; i < N; ++i) {
+        sorted_idx[i] = (uint32_t)(ck[i] & 0xFFFFFFFFu);
+        if (i > 0 && (ck[i] >> 32) == (ck[i - 1] >> 32)) unique = 0;
+    }
+    uint64_t *keys = (uint64_t *)malloc(sizeof(uint64_t) * N);
+    for (unsigned i = 0; i < N; ++i) keys[i] = unique ? (ck[i] >> 32) : ck[i];
+    keyset ks = {keys, !unique};
+    for (unsigned i = 0; i < NN; ++i) {
+        nodes[4 * i] = nodes[4 * i + 1] = nodes[4 * i + 2] = nodes[4 * i + 3] = ORC_INVALID;
+        bx[i].upper = mk2(-INFINITY, -INFINITY);
+        bx[i].lower = mk2(INFINITY, INFINITY);
+        cn[i].axis = mk2(0.0f, 0.0f); cn[i].half_angle = ORC_PI; cn[i].radius = 0.0f;
+        if (d1_flags) d1_flags[i] = 0;
+    }
+    for (unsigned j = 0; j < N; ++j) {
+        nodes[4 * (NI + j) + 3] = sorted_idx[j];
+        bx[NI + j] = lb_[sorted_idx[j]];
+        cn[NI + j] = lc_[sorted_idx[j]];
+    }
+    for (unsigned idx = 0; idx < NI; ++idx) {
+        unsigned lo, hi;
+        determine_range(&ks, N, idx, &lo, &hi);
+        int gamma = (int)find_split(&ks, lo, hi);
+        uint32_t left = (uint32_t)gamma, right = (uint32_t)gamma + 1;
+        if ((lo < hi ? lo : hi) == (unsigned)gamma) left += NI;
+        if ((lo > hi ? lo : hi) == (unsigned)gamma + 1) right += NI;
+        nodes[4 * idx + 1] = left;
+        nodes[4 * idx + 2] = right;
+        nodes[4 * idx + 3] = ORC_INVALID;
+        nodes[4 * left] = idx;
+        nodes[4 * right] = idx;
+    }
+    if (NI > 0) {
+        uint32_t *stk = (uint32_t *)malloc(sizeof(uint32_t) * 2 * NN);
+        uint8_t *expanded = (uint8_t *)calloc(NN, 1);
+        int64_t sp = 0;
+        stk[sp++] = 0;
+        while (sp > 0) {
+            uint32_t p = stk[sp - 1];
+            uint32_t L = nodes[4 * p + 1], R = nodes[4 * p + 2];
+            if (!expanded[p]) {
+                expanded[p] = 1;
+                if (R < NI) stk[sp++] = R;
+                if (L < NI) stk[sp++] = L;
+                continue;
+            }
+            --sp;
+            box2 lb = bx[L], rb = bx[R], m;
+            m.upper = mk2(fmaxf(lb.upper.x, rb.upper.x), fmaxf(lb.upper.y, rb.upper.y));
+            m.lower = mk2(fminf(lb.lower.x, rb.lower.x), fminf(lb.lower.y, rb.lower.y));
+            bx[p] = m;
+            int d1 = 0;
+            cn[p] = cone_merge2(cn[L], cn[R], centroid2(lb), centroid2(rb), centroid2(m), &d1);
+            if (d1_flags) d1_flags[p] = (uint8_t)d1;
+        }
+        free(stk); free(expanded);
+    }
+    free(keys); free(ck); free(lb_); free(lc_);
+    return unique;
+}
+
+/* ---------------- 2D query math */
+static inline float mindist2(box2 b, f2 p) {  /* aabb.cuh:130-135 */
+    const float dx = fminf(b.upper.x, fmaxf(b.lower.x, p.x)) - p.x;
+    const float dy = fminf(b.upper.y, fmaxf(b.lower.y, p.y)) - p.y;
+    return dx * dx + dy * dy;
+}
+static inline float minmaxdist2(box2 b, f2 p) {  /* aabb.cuh:161-180 */
+    float rmx = (b.lower.x - p.x) * (b.lower.x - p.x), rmy = (b.lower.y - p.y) * (b.lower.y - p.y);
+    float rMx = (b.upper.x - p.x) * (b.upper.x - p.x), rMy = (b.upper.y - p.y) * (b.upper.y - p.y);
+    float t;
+    if ((b.upper.x + b.lower.x) * 0.5f < p.x) { t = rmx; rmx = rMx; rMx = t; }
+    if ((b.upper.y + b.lower.y) * 0.5f < p.y) { t = rmy; rmy = rMy; rMy = t; }
+    const float dx = rmx + rMy, dy = rMx + rmy;
+    return fminf(dx, dy);
+}
+/* find_closest_point_line_segment(float2) scene.cuh:176-199 */
+static float closest_point_segment2(f2 pa, f2 pb, f2 x) {
+    f2 u = sub2(pb, pa), v = sub2(x, pa);
+    float c1 = dot2(u, v);
+    if (c1 <= 0.0f) return len2(sub2(x, pa));
+    float c2 = dot2(u, u);
+    if (c2 <= c1) return len2(sub2(x, pb));
+    float t = c1 / c2;
+    f2 pt = mk2(pa.x + u.x * t, pa.y + u.y * t);
+    return len2(mk2(x.x - pt.x, x.y - pt.y));
+}
+/* is_silhouette_vertex scene.cuh:112-141 */
+static int is_silhouette_vertex(f2 n0, f2 n1, f2 view_dir, float d, int flip) {
+    const float precision = 1e-3f;
+    float sign = flip ? 1.0f : -1.0f;
+    if (d <= precision) {
+        float det = n0.x * n1.y - n0.y * n1.x;
+        return sign * det > precision;
+    }
+    f2 vu = mk2(view_dir.x / d, view_dir.y / d);
+    float dot0 = dot2(vu, n0), dot1 = dot2(vu, n1);
+    if (fabsf(dot0) <= precision) return sign * dot1 > precision;
+    if (fabsf(dot1) <= precision) return sign * dot0 > precision;
+    return dot0 * dot1 < 0.0f;
+}
+/* overlap(cone<float,2>) cone.cuh:78-120 with project_to_plane(float2) 44-49 */
+static int cone_overlap2(cone2 bc, f2 o, box2 b, float dist_to_box) {
+    if (bc.half_angle >= ORC_PI_2 || dist_to_box < ORC_EPS) return 1;
+    f2 c = centroid2(b);
+    f2 v = mk2(c.x - o.x, c.y - o.y);
+    float l = len2(v);
+    v.x /= l; v.y /= l;
+    float dax = acosf(smax(-1.0f, smin(1.0f, dot2(bc.axis, v))));
+    if (inrange(ORC_PI_2, dax - bc.half_angle, dax + bc.half_angle)) return 1;
+    if (l > bc.radius) {
+        float vch = asinf(bc.radius / l);
+        float hs = bc.half_angle + vch;
+        return hs >= ORC_PI_2 ? 1 : inrange(ORC_PI_2, dax - hs, dax + hs);
+    }
+    f2 e = mk2(b.upper.x - c.x, b.upper.y - c.y);
+    float d = dot2(e, mk2(fabsf(v.x), fabsf(v.y)));
+    float s = l - d;
+    if (s <= 0.0f) return 1;
+    f2 bb = mk2(-v.y, v.x);
+    d = fabsf(dot2(e, mk2(fabsf(bb.x), fabsf(bb.y))));
+    float vch = atan2f(d, s);
+    float hs = bc.half_angle + vch;
+    return hs >= ORC_PI_2 ? 1 : inrange(ORC_PI_2, dax - hs, dax + hs);
+}
+
+typedef struct {
+    int64_t num_segs, num_verts;
+    const float *verts;        /* V x 2 */
+    const int32_t *segs;       /* N x 2 */
+    const int32_t *seg_owned;  /* N x 2 owned silhouette vertices, -1 padded */
+    const int32_t *sv;         /* V x 4 {prev, self, next, -1} */
+    const uint32_t *nodes;     /* (2N-1) x 4 */
+    const float *aabbs;        /* (2N-1) x {upper.xy, lower.xy} */
+    const float *cones;        /* (2N-1) x {axis.xy, half_angle, radius} */
+} orc2_scene;
+
+static inline box2 node_box2(const orc2_scene *s, uint32_t n) { box2 b; memcpy(&b, s->aabbs + 4 * (int64_t)n, sizeof b); return b; }
+static inline cone2 node_cone2(const orc2_scene *s, uint32_t n) { cone2 c; memcpy(&c, s->cones + 4 * (int64_t)n, sizeof c); return c; }
+static inline float seg_distance(const orc2_scene *s, uint32_t obj, f2 p) {
+    const int32_t *g = s->segs + 2 * (int64_t)obj;
+    return closest_point_segment2(vload2(s->verts, g[0]), vload2(s->verts, g[1]), p);
+}
+
+/* query_device(nearest) query.cuh:239-318 over segments */
+void orc2_query_nearest(const orc2_scene *s, const float *pts, int64_t n, uint32_t *idx, float *dist) {
+    typedef struct { uint32_t n; float d; } ent;
+    ent stk[ORC_STACK];
+    for (int64_t q = 0; q < n; ++q) {
+        f2 p = mk2(pts[2 * q], pts[2 * q + 1]);
+        uint32_t nearest = ORC_INVALID;
+        float best = INFINITY;
+        if (s->num_segs == 1) {
+            float d = seg_distance(s, s->nodes[3], p);
+            best = d * d; nearest = s->nodes[3];
+        } else if (s->num_segs > 1) {
+            int sp = 0;
+            stk[sp].n = 0; stk[sp].d = mindist2(node_box2(s, 0), p); ++sp;
+            do {
+                ent nd = stk[--sp];
+                if (nd.d > best) continue;
+                uint32_t L = s->nodes[4 * nd.n + 1], R = s->nodes[4 * nd.n + 2];
+                box2 lb = node_box2(s, L), rb = node_box2(s, R);
+                float Lmd = mindist2(lb, p), Rmd = mindist2(rb, p);
+                float Lmm = minmaxdist2(lb, p), Rmm = minmaxdist2(rb, p);
+                uint32_t ch[2] = {L, R};
+                int ok[2] = {Lmd <= Rmm, Rmd <= Lmm};
+                float md[2] = {Lmd, Rmd};
+                for (int k = 0; k < 2; ++k) {
+                    if (!ok[k]) continue;
+                    uint32_t obj = s->nodes[4 * ch[k] + 3];
+                    if (obj != ORC_INVALID) {
+                        float d = seg_distance(s, obj, p);
+                        d *= d;
+                        if (d <= best) { best = d; nearest = obj; }
+                    } else { stk[sp].n = ch[k]; stk[sp].d = md[k]; ++sp; }
+                }
+                if (sp >= ORC_STACK - 2) { nearest = ORC_INVALID; best = NAN; break; }
+            } while (sp > 0);
+        }
+        idx[q] = nearest;
+        dist[q] = sqrtf(best);
+    }
+}
+
+/* silhouette_vertex::find_closest_silhouette_point scene.cuh:354-381 */
+static int sv_closest(const orc2_scene *s, int32_t si, f2 o, float max_r2, float *dist, int flip) {
+    if (0.0f >= max_r2) return 0;
+    const int32_t *sv = s->sv + 4 * (int64_t)si;
+    f2 p = vload2(s->verts, sv[1]);
+    f2 vd = mk2(o.x - p.x, o.y - p.y);
+    float d = len2(vd);
+    if (d * d > max_r2) return 0;
+    int is_sil = !sv_has_face(sv, 0) || !sv_has_face(sv, 1);
+    if (!is_sil)
+        is_sil = is_silhouette_vertex(sv_face_normal(s->verts, sv, 0, 1), sv_face_normal(s->verts, sv, 1, 1), vd, d, flip);
+    if (is_sil && d * d <= max_r2) { *dist = d; return 1; }
+    return 0;
+}
+/* silhouette_distance_calculator scene.cuh:512-532 */
+static int leaf_silhouette2(const orc2_scene *s, uint32_t obj, f2 o, float max_r2, float *dist, int flip, int32_t *vid) {
+    const int32_t *own = s->seg_owned + 2 * (int64_t)obj;
+    float mr2 = max_r2;
+    int ret = 0;
+    for (int i = 0; i < 2; ++i) {
+        if (own[i] == -1) continue;
+        if (sv_closest(s, own[i], o, mr2, dist, flip)) { ret = 1; mr2 = *dist * *dist; *vid = own[i]; }
+    }
+    return ret;
+}
+/* query_device(nearest_silhouette) query.cuh:326-423 over segments; vid: the
+ * silhouette vertex (mesh vertex id) that gave the distance */
+void orc2_query_silhouette(const orc2_scene *s, const float *pts, const uint8_t *flip, int64_t n, float *dist,
+                           int32_t *vid) {
+    typedef struct { uint32_t n; float d; } ent;
+    ent stk[ORC_STACK];
+    for (int64_t q = 0; q < n; ++q) {
+        f2 p = mk2(pts[2 * q], pts[2 * q + 1]);
+        int fl = flip ? flip[q] != 0 : 0;
+        float best = INFINITY;
+        int32_t bv = -1;
+        if (s->num_segs == 1) {
+            float d = INFINITY; int32_t v = -1;
+            if (leaf_silhouette2(s, s->nodes[3], p, best * best, &d, fl, &v) && d <= best) { best = d; bv = v; }
+        } else if (s->num_segs > 1) {
+            int sp = 0;
+            stk[sp].n = 0; stk[sp].d = mindist2(node_box2(s, 0), p); ++sp;
+            do {
+                ent nd = stk[--sp];
+                if (nd.d > best * best) continue;
+                uint32_t L = s->nodes[4 * nd.n + 1], R = s->nodes[4 * nd.n + 2];
+                box2 lb = node_box2(s, L), rb = node_box2(s, R);
+                cone2 lc = node_cone2(s, L), rc = node_cone2(s, R);
+                float Lmd = mindist2(lb, p), Rmd = mindist2(rb, p);
+                int hit[2] = {lc.half_angle >= 0.0f && cone_overlap2(lc, p, lb, Lmd),
+                              rc.half_angle >= 0.0f && cone_overlap2(rc, p, rb, Rmd)};
+                uint32_t ch[2] = {L, R};
+                float md[2] = {Lmd, Rmd};
+                for (int k = 0; k < 2; ++k) {
+                    if (!hit[k]) continue;
+                    uint32_t obj = s->nodes[4 * ch[k] + 3];
+                    if (obj != ORC_INVALID) {
+                        float d = INFINITY; int32_t v = -1;
+                        if (leaf_silhouette2(s, obj, p, best * best, &d, fl, &v) && d <= best) { best = d; bv = v; }
+                    } else { stk[sp].n = ch[k]; stk[sp].d = md[k]; ++sp; }
+                }
+                if (sp >= ORC_STACK - 2) { best = NAN; bv = -1; break; }
+            } while (sp > 0);
+        }
+        dist[q] = best;
+        if (vid) vid[q] = bv;
+    }
+}
+
+/* intersects_d(ray<float,2>) aabb.cuh:366-390 */
+static int ray_box2(f2 o, f2 inv, box2 b, float max_dist, float *dist) {
+    float t1 = (b.lower.x - o.x) * inv.x, t2 = (b.upper.x - o.x) * inv.x;
+    float tmin = fminf(t1, t2), tmax = fmaxf(t1, t2);
+    t1 = (b.lower.y - o.y) * inv.y; t2 = (b.upper.y - o.y) * inv.y;
+    tmin = fmaxf(tmin, fminf(t1, t2)); tmax = fminf(tmax, fmaxf(t1, t2));
+    if (tmax >= tmin && tmax >= 0.0f && tmin <= max_dist) { *dist = tmin >= 0.0f ? tmin : 0.0f; return 1; }
+    return 0;
+}
+/* scene<2>::intersect_test scene.cuh:555-583: (hit, t, segment parameter s) */
+static int ray_segment(f2 o, f2 dir, f2 p0, f2 p1, float *t, float *sp) {
+    f2 sd = sub2(p1, p0);
+    float D = dir.x * (-sd.y) + dir.y * sd.x;
+    if (fabsf(D) < ORC_EPS) return 0;
+    float invD = 1.0f / D;
+    float tt = ((p0.x - o.x) * (-sd.y) - (p0.y - o.y) * (-sd.x)) * invD;
+    float ss = (dir.x * (p0.y - o.y) - dir.y * (p0.x - o.x)) * invD;
+    if (ss >= -1e-3f && ss <= 1.0f + 1e-3f && tt >= 0.0f) { *t = tt; *sp = ss; return 1; }
+    return 0;
+}
+/* query_device(ray_intersect) query.cuh:82-169 over segments */
+void orc2_query_ray(const orc2_scene *s, const float *origins, const float *dirs, const float *tmax, int64_t n,
+                    uint8_t *hit, float *t, float *sparam, uint32_t *idx) {
+    typedef struct { uint32_t n; float d; } ent;
+    ent stk[ORC_STACK];
+    for (int64_t q = 0; q < n; ++q) {
+        f2 o = mk2(origins[2 * q], origins[2 * q + 1]);
+        f2 dir = mk2(dirs[2 * q], dirs[2 * q + 1]);
+        f2 inv = mk2(1 / dir.x, 1 / dir.y);
+        float max_dist = tmax[q], min_dist = INFINITY, bs = 0.0f;
+        int found = 0;
+        uint32_t nearest = ORC_INVALID;
+        if (s->num_segs > 0) {
+            int sp = 0;
+            stk[sp].n = 0; stk[sp].d = INFINITY; ++sp;
+            do {
+                ent nd = stk[--sp];
+                if (nd.d > min_dist) continue;
+                uint32_t obj = s->nodes[4 * nd.n + 3];
+                if (obj != ORC_INVALID) {
+                    const int32_t *g = s->segs + 2 * (int64_t)obj;
+                    float tt, ss;
+                    if (ray_segment(o, dir, vload2(s->verts, g[0]), vload2(s->verts, g[1]), &tt, &ss) &&
+                        tt < max_dist && tt < min_dist) {
+                        min_dist = tt; found = 1; bs = ss; nearest = obj;
+                    }
+                } else {
+                    uint32_t L = s->nodes[4 * nd.n + 1], R = s->nodes[4 * nd.n + 2];
+                    float Ld = 0.0f, Rd = 0.0f;
+                    int Lh = ray_box2(o, inv, node_box2(s, L), max_dist, &Ld);
+                    int Rh = ray_box2(o, inv, node_box2(s, R), max_dist, &Rd);
+                    if (Lh && Rh) {
+                        uint32_t closer = L, other = R;
+                        if (Rd < Ld) { float tmp = Ld; Ld = Rd; Rd = tmp; closer = R; other = L; }
+                        stk[sp].n = other; stk[sp].d = Rd; ++sp;
+                        stk[sp].n = closer; stk[sp].d = Ld; ++sp;
+                    } else if (Lh) { stk[sp].n = L; stk[sp].d = Ld; ++sp; }
+                    else if (Rh) { stk[sp].n = R; stk[sp].d = Rd; ++sp; }
+                }
+                if (sp >= ORC_STACK - 2) { found = 0; nearest = ORC_INVALID; min_dist = NAN; break; }
+            } while (sp > 0);
+        }
+        hit[q] = (uint8_t)found;
+        t[q] = min_dist;
+        sparam[q] = bs;
+        idx[q] = nearest;
+    }
+}
+
+/* intersect_sphere(sphere<float,2>, aabb) aabb.cuh:433-449 */
+static int circle_box(f2 c, float r, box2 b) {
+    float cx = smax(b.lower.x, smin(c.x, b.upper.x));
+    float cy = smax(b.lower.y, smin(c.y, b.upper.y));
+    float dx = cx - c.x, dy = cy - c.y;
+    return dx * dx + dy * dy <= (r * r);
+}
+/* scene<2>::intersect_sphere scene.cuh:585-608 */
+static int circle_segment(f2 c, float radius, f2 p1, f2 p2) {
+    f2 d = sub2(p2, p1);
+    float len_sq = d.x * d.x + d.y * d.y;
+    float t = ((c.x - p1.x) * d.x + (c.y - p1.y) * d.y) / len_sq;
+    t = smax(0.0f, smin(1.0f, t));
+    f2 cp = mk2(p1.x + t * d.x, p1.y + t * d.y);
+    float dx = cp.x - c.x, dy = cp.y - c.y;
+    return dx * dx + dy * dy <= (radius * radius);
+}
+/* scene<2>::green_weight scene.cuh:610-617: |log(max(|x - y|, 1e-2)) / (2 pi)| */
+static inline float green_weight2(f2 x, f2 y) {
+    float r = smax(len2(mk2(x.x - y.x, x.y - y.y)), 1e-2f);
+    return fabsf(logf(r) / (3.14159265358979323846f * 2.0f));
+}
+/* sample_object_in_sphere sample.cuh:23-91 over segments (measurement = length) */
+void orc2_sample_in_circle(const orc2_scene *s, const float *centers, const float *radii, const float *u_in,
+                           int64_t n, int32_t *idx, float *pdf) {
+    for (int64_t q = 0; q < n; ++q) {
+        f2 ctr = mk2(centers[2 * q], centers[2 * q + 1]);
+        float rad = radii[q], u = u_in[q];
+        int32_t oi = -1;
+        float opdf = 0.0f;
+        if (s->num_segs > 0) {
+            uint32_t node = 0;
+            float npdf = 1.0f;
+            int have = 1;
+            while (have) {
+                have = 0;
+                uint32_t obj = s->nodes[4 * node + 3];
+                if (obj != ORC_INVALID) {
+                    const int32_t *g = s->segs + 2 * (int64_t)obj;
+                    f2 p0 = vload2(s->verts, g[0]), p1 = vload2(s->verts, g[1]);
+                    if (circle_segment(ctr, rad, p0, p1)) {
+                        oi = (int32_t)obj;
+                        opdf = npdf;
+                        opdf /= len2(mk2(p0.x - p1.x, p0.y - p1.y));
+                    }
+                } else {
+                    uint32_t L = s->nodes[4 * node + 1], R = s->nodes[4 * node + 2];
+                    box2 lb = node_box2(s, L), rb = node_box2(s, R);
+                    float Lw = circle_box(ctr, rad, lb) ? green_weight2(ctr, centroid2(lb)) : 0;
+                    float Rw = circle_box(ctr, rad, rb) ? green_weight2(ctr, centroid2(rb)) : 0;
+                    float tw = Lw + Rw;
+                    if (tw > 0) {
+                        float Lp = Lw / tw;
+                        if (u < Lp) { u /= Lp; node = L; npdf = Lp * npdf; }
+                        else { float Rp = 1.0f - Lp; u = (u - Lp) / Rp; node = R; npdf = Rp * npdf; }
+                        have = 1;
+                    }
+                }
+            }
+        }
+        idx[q] = oi;
+        pdf[q] = opdf;
+    }
+}

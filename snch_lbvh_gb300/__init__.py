@@ -20,7 +20,7 @@ import numpy as np
 
 from ._ffi import BvhView, SnchError, check, lib  # noqa: F401
 
-__all__ = ["Scene", "BatchedScene", "Graph", "SnchError", "BvhView", "lib", "read_obj"]
+__all__ = ["Scene", "BatchedScene", "Scene2", "Graph", "SnchError", "BvhView", "lib", "read_obj"]
 
 INVALID = 0xFFFFFFFF
 TRAVERSAL_NEAR_FIRST = 0
@@ -519,3 +519,102 @@ class BatchedScene(Scene):
         check(lib().snch_batch_query_silhouette(self._h, _ptr(m), _ptr(p), _ptr(f), n, _ptr(dist), _ptr(edge),
                                                 _stream(stream)))
         return dist, edge
+
+
+class Scene2:
+    """lbvh::scene<2> (scene.cuh:287-703): line segments with silhouette vertices
+    and their SNCH-LBVH; queries on CUDA tensors of 2D points."""
+
+    def __init__(self, vertices, segments):
+        self._h = C.c_void_p()
+        v = _host(vertices, np.float32, 2)
+        s = _host(segments, np.int32, 2)
+        check(lib().snch_scene2_create(v.ctypes.data_as(C.c_void_p), len(v), s.ctypes.data_as(C.c_void_p), len(s),
+                                       C.byref(self._h)))
+        self.num_vertices, self.num_segments = len(v), len(s)
+
+    def close(self):
+        if self._h:
+            lib().snch_scene2_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def build(self, stream=None):
+        """compute_silhouettes() + build_bvh() scene.cuh:642-683."""
+        check(lib().snch_scene2_build(self._h, _stream(stream)))
+
+    def device_status(self, reset=True, stream=None) -> int:
+        b = C.c_uint32()
+        check(lib().snch_scene2_get_device_status(self._h, C.byref(b), int(reset), _stream(stream)))
+        return int(b.value)
+
+    def export(self, stream=None):
+        torch = _torch()
+        n, nv = self.num_segments, self.num_vertices
+        nn = max(2 * n - 1, 0)
+        out = {"sv": torch.empty((nv, 4), dtype=torch.int32, device="cuda"),
+               "seg_owned": torch.empty((n, 2), dtype=torch.int32, device="cuda"),
+               "morton": torch.empty(n, dtype=torch.int32, device="cuda"),
+               "sorted_idx": torch.empty(n, dtype=torch.int32, device="cuda"),
+               "nodes": torch.empty((nn, 4), dtype=torch.int32, device="cuda"),
+               "aabbs": torch.empty((nn, 4), dtype=torch.float32, device="cuda"),
+               "cones": torch.empty((nn, 4), dtype=torch.float32, device="cuda")}
+        check(lib().snch_scene2_export(self._h, *[_ptr(out[k]) for k in ("sv", "seg_owned", "morton", "sorted_idx",
+                                                                         "nodes", "aabbs", "cones")],
+                                       _stream(stream)))
+        torch.cuda.synchronize()
+        r = {k: x.cpu().numpy() for k, x in out.items()}
+        for k in ("morton", "sorted_idx", "nodes"):
+            r[k] = r[k].view(np.uint32)
+        return r
+
+    def query_nearest(self, points, stream=None):
+        torch = _torch()
+        p = _dev(points, torch.float32, 2)
+        n = p.shape[0]
+        idx, dist = torch.empty(n, dtype=torch.int32, device="cuda"), torch.empty(n, dtype=torch.float32, device="cuda")
+        check(lib().snch_scene2_query_nearest(self._h, _ptr(p), n, _ptr(idx), _ptr(dist), _stream(stream)))
+        return idx, dist
+
+    def query_silhouette(self, points, flip=None, stream=None):
+        torch = _torch()
+        p = _dev(points, torch.float32, 2)
+        n = p.shape[0]
+        f = None if flip is None else _dev(flip, torch.uint8)
+        dist, vid = torch.empty(n, dtype=torch.float32, device="cuda"), torch.empty(n, dtype=torch.int32, device="cuda")
+        check(lib().snch_scene2_query_silhouette(self._h, _ptr(p), _ptr(f), n, _ptr(dist), _ptr(vid),
+                                                 _stream(stream)))
+        return dist, vid
+
+    def query_ray(self, origins, dirs, tmax, stream=None):
+        torch = _torch()
+        o, d, tm = _dev(origins, torch.float32, 2), _dev(dirs, torch.float32, 2), _dev(tmax, torch.float32)
+        n = o.shape[0]
+        hit = torch.empty(n, dtype=torch.uint8, device="cuda")
+        t, sp = torch.empty(n, dtype=torch.float32, device="cuda"), torch.empty(n, dtype=torch.float32, device="cuda")
+        idx = torch.empty(n, dtype=torch.int32, device="cuda")
+        check(lib().snch_scene2_query_ray(self._h, _ptr(o), _ptr(d), _ptr(tm), n, _ptr(hit), _ptr(t), _ptr(sp),
+                                          _ptr(idx), _stream(stream)))
+        return hit, t, sp, idx
+
+    def sample_in_circle(self, centers, radii, u, stream=None):
+        torch = _torch()
+        c, r, uu = _dev(centers, torch.float32, 2), _dev(radii, torch.float32), _dev(u, torch.float32)
+        n = c.shape[0]
+        idx, pdf = torch.empty(n, dtype=torch.int32, device="cuda"), torch.empty(n, dtype=torch.float32, device="cuda")
+        check(lib().snch_scene2_sample_in_circle(self._h, _ptr(c), _ptr(r), _ptr(uu), n, _ptr(idx), _ptr(pdf),
+                                                 _stream(stream)))
+        return idx, pdf
+
+    def sample_on_object(self, index, u, stream=None):
+        torch = _torch()
+        i, uu = _dev(index, torch.int32), _dev(u, torch.float32)
+        n = i.shape[0]
+        out = torch.empty((n, 2), dtype=torch.float32, device="cuda")
+        check(lib().snch_scene2_sample_on_object(self._h, _ptr(i), _ptr(uu), n, _ptr(out), _stream(stream)))
+        return out

@@ -50,7 +50,7 @@ def _ctype(arg: str):
     t = a.split()[0]
     return {"int64_t": I64, "int": I, "int32_t": C.c_int32, "size_t": C.c_size_t, "snch_scene_t": P, "snch_stream_t": P,
             "uint32_t": C.c_uint32, "uint64_t": C.c_uint64, "float": C.c_float, "snch_mlp_t": P,
-            "snch_graph_t": P}[t]
+            "snch_graph_t": P, "snch_scene2_t": P}[t]
 
 
 _lib = None

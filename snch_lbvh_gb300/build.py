@@ -33,6 +33,7 @@ UNITS = [
     ("mlp.cu", []),
     ("wost.cu", []),
     ("io.cu", []),
+    ("scene2d.cu", ["-fmad=false"]),
 ]
 HEADERS = ["common.cuh", "internal.h", "tcgen05.cuh"]
 

@@ -911,6 +911,16 @@ cudaError_t launch_wide_fill(const WideArgs &a, cudaStream_t st)
 }
 
 // ------------------------------------------------------------------ launchers
+// Karras internal nodes alone, over a.keys / a.vals (sorted), into a.nodes and
+// a.sizes: the 2D build shares it (the construction does not depend on the
+// dimension)
+cudaError_t launch_karras(const BuildArgs &a, cudaStream_t st)
+{
+    karras_kernel<<<(a.num_tris + 255) / 256, 256, 0, st>>>(a);
+    note_launch();
+    return cudaGetLastError();
+}
+
 cudaError_t launch_build_front(const BuildArgs &a, cudaStream_t st)
 {
     const uint32_t n = a.num_tris;

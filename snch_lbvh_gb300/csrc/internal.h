@@ -82,6 +82,7 @@ cudaError_t launch_wide_count(const WideArgs &a, cudaStream_t st);
 cudaError_t launch_wide_fill(const WideArgs &a, cudaStream_t st);
 
 // ---- build.cu
+cudaError_t launch_karras(const BuildArgs &a, cudaStream_t st);  // keys, vals, nodes, sizes, num_tris
 cudaError_t launch_build_front(const BuildArgs &a, cudaStream_t st);
 cudaError_t launch_build_back(const BuildArgs &a, cudaStream_t st);
 // batched scenes: after the Morton sort, the stable pass by mesh id

@@ -172,6 +172,23 @@ int main(int argc, char **argv)
         cudaFree(q);
     if (ldist != dist || cnt != 20)
         return 10;
+
+    // scene<2>: a unit square; the nearest distance from its centre is 0.5
+    struct V2 { float x, y; };
+    struct I2 { int x, y; };
+    const std::vector<V2> sq = {{0.f, 0.f}, {1.f, 0.f}, {1.f, 1.f}, {0.f, 1.f}};
+    const std::vector<I2> sg = {{0, 1}, {1, 2}, {2, 3}, {3, 0}};
+    snch::scene2 sq2(sq.begin(), sq.end(), sg.begin(), sg.end());
+    sq2.compute_silhouettes();
+    sq2.build_bvh();
+    const float c2[2] = {0.5f, 0.5f};
+    cudaMemcpy(d_pts, c2, sizeof c2, cudaMemcpyHostToDevice);
+    sq2.query_nearest(d_pts, 1, d_idx, d_dist);
+    float d2d = 0;
+    cudaMemcpy(&d2d, d_dist, 4, cudaMemcpyDeviceToHost);
+    std::printf("2d: dist=%.7f\n", d2d);
+    if (d2d != 0.5f)
+        return 11;
     for (void *q : {(void *)d_pts, (void *)d_dist, (void *)d_idx, (void *)d2, (void *)dd, (void *)dm, (void *)di,
                     (void *)dr})
         cudaFree(q);

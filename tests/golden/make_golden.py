@@ -256,8 +256,135 @@ def obj_case():
     print(f"obj/torus.obj          verts={nv} tris={nt}")
 
 
+# ---------------------------------------------------------------- 2D scenes
+def polygon(n, r=1.0, c=(0.0, 0.0), noise=0.0, seed=0, reverse=False):
+    rng = np.random.default_rng(seed)
+    a = np.linspace(0, 2 * np.pi, n, endpoint=False)
+    rr = r * (1 + noise * rng.standard_normal(n))
+    v = np.stack([c[0] + rr * np.cos(a), c[1] + rr * np.sin(a)], 1)
+    s = np.stack([np.arange(n), (np.arange(n) + 1) % n], 1)
+    if reverse:
+        s = s[:, ::-1]
+    return v, s
+
+
+def cases_2d():
+    yield "square", np.array([[0, 0], [1, 0], [1, 1], [0, 1]], np.float32), \
+        np.array([[0, 1], [1, 2], [2, 3], [3, 0]], np.int32), 31
+    yield "single_seg", np.array([[0, 0], [1, 0.5]], np.float32), np.array([[0, 1]], np.int32), 32
+    yield "two_seg", np.array([[0, 0], [1, 0], [1, 1]], np.float32), np.array([[0, 1], [1, 2]], np.int32), 33
+    v, s = polygon(64, noise=0.02, seed=1)
+    yield "circle64", v.astype(np.float32), s.astype(np.int32), 34
+    # a domain with a hole: outer loop counter-clockwise, inner loop clockwise
+    vo, so = polygon(48, 1.0, noise=0.01, seed=2)
+    vi, si = polygon(24, 0.4, c=(0.1, -0.05), noise=0.01, seed=3, reverse=True)
+    yield "two_loops", np.concatenate([vo, vi]).astype(np.float32), \
+        np.concatenate([so, si + len(vo)]).astype(np.int32), 35
+    # open zig-zag polyline: end vertices have one segment
+    x = np.linspace(0, 2, 41)
+    v = np.stack([x, 0.2 * (np.arange(41) % 2)], 1)
+    yield "open_polyline", v.astype(np.float32), np.stack([np.arange(40), np.arange(1, 41)], 1).astype(np.int32), 36
+    # independent random segments (every vertex is an end point)
+    rng = np.random.default_rng(7)
+    a = rng.random((150, 2))
+    b = a + 0.05 * rng.standard_normal((150, 2))
+    v = np.concatenate([a, b]).astype(np.float32)
+    yield "random_segments", v, np.stack([np.arange(150), np.arange(150, 300)], 1).astype(np.int32), 37
+    # every segment twice: equal Morton codes (the 64-bit key path) and shared vertices
+    v, s = polygon(32, noise=0.03, seed=4)
+    yield "duplicated_2d", v.astype(np.float32), np.concatenate([s, s]).astype(np.int32), 38
+    v, s = polygon(4096, noise=0.005, seed=5)
+    yield "circle4096", v.astype(np.float32), s.astype(np.int32), 39
+
+
+def make_queries_2d(verts, segs, seed, n_rand=512):
+    """Points in the box x 1.5 plus vertex, midpoint and offset probes; rays
+    (random and axis-aligned); circles with log-uniform radii."""
+    rng = np.random.default_rng(seed)
+    v = verts.astype(np.float64)
+    lo, hi = v.min(0), v.max(0)
+    c, h = 0.5 * (lo + hi), 0.5 * np.maximum(hi - lo, 1e-3) * 1.5
+    k = min(len(segs), 64)
+    sel = rng.choice(len(segs), k, replace=False)
+    a, b = v[segs[sel, 0]], v[segs[sel, 1]]
+    d = b - a
+    nrm = np.stack([d[:, 1], -d[:, 0]], 1)
+    nn = np.linalg.norm(nrm, axis=1, keepdims=True)
+    nrm = np.where(nn > 0, nrm / np.where(nn > 0, nn, 1), 0)
+    pts = np.concatenate([c + (rng.random((n_rand, 2)) * 2 - 1) * h, a, 0.5 * (a + b),
+                          0.5 * (a + b) + 0.01 * nrm, a - 0.02 * nrm]).astype(np.float32)
+    nr = len(pts)
+    dd = rng.standard_normal((nr, 2))
+    axial = rng.random(nr) < 0.15
+    ax = rng.integers(0, 2, nr)
+    dd[axial] = 0.0
+    dd[axial, ax[axial]] = np.where(rng.random(axial.sum()) < 0.5, -1.0, 1.0)
+    dd /= np.linalg.norm(dd, axis=1, keepdims=True)
+    return {"near_pts": pts, "sil_pts": pts, "sil_flip": (rng.random(nr) < 0.5).astype(np.uint8),
+            "ray_o": pts, "ray_d": dd.astype(np.float32),
+            "ray_tmax": np.where(rng.random(nr) < 0.2, np.float32(np.inf),
+                                 np.exp(rng.uniform(np.log(1e-3), np.log(4 * h.max()), nr))).astype(np.float32),
+            "smp_c": pts, "smp_r": np.exp(rng.uniform(np.log(1e-3), np.log(2 * h.max()), nr)).astype(np.float32),
+            "smp_u": rng.random(nr).astype(np.float32)}
+
+
+def run_harness_2d(verts, segs, q):
+    nv, nt = len(verts), len(segs)
+    nq = len(q["near_pts"])
+    with tempfile.TemporaryDirectory() as td:
+        fin, fout = os.path.join(td, "in.bin"), os.path.join(td, "out.bin")
+        with open(fin, "wb") as f:
+            np.array([nv, nt, nq, nq, nq, nq], np.int64).tofile(f)
+            for a, dt in [(verts, np.float32), (segs, np.int32), (q["near_pts"], np.float32),
+                          (q["sil_pts"], np.float32), (q["sil_flip"], np.uint8), (q["ray_o"], np.float32),
+                          (q["ray_d"], np.float32), (q["ray_tmax"], np.float32), (q["smp_c"], np.float32),
+                          (q["smp_r"], np.float32), (q["smp_u"], np.float32)]:
+                np.ascontiguousarray(a, dtype=dt).tofile(f)
+        subprocess.run([oracle.REF_HARNESS, "--2d", fin, fout], check=True, stdout=subprocess.DEVNULL)
+        buf = open(fout, "rb").read()
+    off = 0
+
+    def take(dt, n):
+        nonlocal off
+        a = np.frombuffer(buf, dtype=dt, count=n, offset=off)
+        off += a.nbytes
+        return a.copy()
+
+    nn = 2 * nt - 1
+    r = {"ref_sv": take(np.int32, 4 * nv).reshape(nv, 4), "ref_seg_owned": take(np.int32, 2 * nt).reshape(nt, 2),
+         "ref_morton": take(np.uint32, nt), "ref_nodes": take(np.uint32, 4 * nn).reshape(nn, 4),
+         "ref_aabbs": take(np.float32, 4 * nn).reshape(nn, 4), "ref_cones": take(np.float32, 4 * nn).reshape(nn, 4)}
+    m = nq if nt >= 2 else 0
+    rec = take(np.uint8, 8 * m).reshape(-1, 8)
+    r["ref_near_idx"] = rec[:, :4].copy().view(np.uint32).reshape(-1)
+    r["ref_near_dist"] = rec[:, 4:].copy().view(np.float32).reshape(-1)
+    r["ref_sil_dist"] = take(np.float32, m)
+    rec = take(np.uint8, 13 * m).reshape(-1, 13)
+    r["ref_ray_hit"] = rec[:, 0].copy()
+    r["ref_ray_t"] = rec[:, 1:5].copy().view(np.float32).reshape(-1)
+    r["ref_ray_s"] = rec[:, 5:9].copy().view(np.float32).reshape(-1)
+    r["ref_ray_idx"] = rec[:, 9:13].copy().view(np.uint32).reshape(-1)
+    rec = take(np.uint8, 8 * m).reshape(-1, 8)
+    r["ref_smp_idx"] = rec[:, :4].copy().view(np.int32).reshape(-1)
+    r["ref_smp_pdf"] = rec[:, 4:].copy().view(np.float32).reshape(-1)
+    assert off == len(buf), (off, len(buf))
+    return r
+
+
+def main_2d():
+    d = os.path.join(OUT, "2d")
+    os.makedirs(d, exist_ok=True)
+    for name, v, sg, seed in cases_2d():
+        q = make_queries_2d(v, sg, seed, n_rand=2048 if name == "circle4096" else 512)
+        r = run_harness_2d(v, sg, q)
+        path = os.path.join(d, f"{name}.npz")
+        np.savez_compressed(path, verts=v, segs=sg, **q, **r)
+        print(f"2d/{name:20s} segs={len(sg):6d} -> {os.path.getsize(path)/1024:.0f} KiB")
+
+
 def main():
     oracle.build()
+    main_2d()
     obj_case()
     for name, v, f, seed in cases():
         q = make_queries(v, f, seed, n_rand=2048 if name.startswith("cfg1") else 512)
