@@ -74,6 +74,15 @@ def workload_name(counts, ntri):
             f"{counts['ray']:,} ray + {counts['smp']:,} sphere-sample queries")
 
 
+def bit_mismatches(a, b):
+    """Number of entries of a and b (same shape and dtype) whose bits differ."""
+    a, b = np.ascontiguousarray(a), np.ascontiguousarray(b)
+    if a.shape != b.shape or a.dtype.itemsize != b.dtype.itemsize:
+        return -1
+    w = {1: np.uint8, 2: np.uint16, 4: np.uint32, 8: np.uint64}[a.dtype.itemsize]
+    return int(np.count_nonzero(a.view(w) != b.view(w)))
+
+
 def make_workload(scale, seed):
     from snch_lbvh_gb300 import meshes
     sc = meshes.wost_scene(seed=0)
@@ -627,6 +636,10 @@ def run_ours(args):
     barrier()
     launches = L.snch_kernel_launch_count() - launches0
     clk = clocks.stop()
+    # answers of the last timed step; the e2e leg's host-buffer answers must equal them
+    device_answers = {"near_dist": out["near"][1].cpu().numpy(), "sil_dist": out["sil"][0].cpu().numpy(),
+                      "ray_hit": out["ray"][0].cpu().numpy(), "ray_t": out["ray"][1].cpu().numpy(),
+                      "smp_idx": out["smp"][0].cpu().numpy(), "smp_pdf": out["smp"][1].cpu().numpy()}
     status |= scene.device_status()
     elapsed_ms = t_start.elapsed_time(t_end)
     if ws > 1:
@@ -710,9 +723,14 @@ def run_ours(args):
             e2e_s = float(t.item())
         h2d = sc.verts.nbytes + sc.faces.nbytes + sum(v.nbytes for v in q.values())
         d2h = sum(a.nbytes for v in hout.values() for a in v)
+        host_answers = {"near_dist": hout["near"][1], "sil_dist": hout["sil"][0], "ray_hit": hout["ray"][0],
+                        "ray_t": hout["ray"][1], "smp_idx": hout["smp"][0], "smp_pdf": hout["smp"][1]}
+        mismatch = {k: bit_mismatches(v, device_answers[k]) for k, v in host_answers.items()}
         e2e = {"value": total_q * ws * e2e_steps / e2e_s, "unit": "queries/s", "h2d_bytes_per_step": int(h2d),
                "d2h_bytes_per_step": int(d2h), "steps": e2e_steps,
-               "note": "scene upload + build + snch_*_host queries from pinned host memory, wall clock"}
+               "mismatches_vs_device_forms": mismatch,
+               "note": "scene upload + build + snch_*_host queries from pinned host memory, wall clock; "
+                       "answers compared bit for bit with the device forms' answers of the timed step"}
 
     if rank != 0:
         if ws > 1:

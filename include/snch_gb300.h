@@ -206,6 +206,12 @@ int snch_set_traversal(snch_scene_t scene, int mode);
 #define SNCH_OPT_PACKET 12
 #define SNCH_OPT_PACKET_NEAREST 13
 #define SNCH_OPT_PACKET_SILHOUETTE 14
+/*   SNCH_OPT_HOST_CHUNK       queries per chunk of the *_host forms (default 2^24, at
+ *                             most 29 bytes in and 17 out per query on each of two
+ *                             streams): chunk i's input copy, search and output copy run
+ *                             on stream i % 2, so copies overlap searches; a larger chunk
+ *                             gives each Morton-ordered search a denser batch. */
+#define SNCH_OPT_HOST_CHUNK 15
 int snch_set_option(snch_scene_t scene, int option, int64_t value);
 
 /* Position of each sorted leaf in the reference's depth-first visit order,
@@ -453,6 +459,9 @@ int snch_gemm_bf16(const void *A, const void *B, float *C, int64_t M, int64_t N,
 
 /* Host-buffer forms of the four queries: copy in, run, copy out in pipelined
  * chunks on the scene's own streams; return when results are in host memory.
+ * The scene's streams are ordered after work queued on the legacy default
+ * stream (stream 0, where a NULL snch_stream_t builds); a build queued on any
+ * other stream must be complete before the call.
  * This is the call shape of the reference's benchmark loop (benchmark.cu:395-409). */
 int snch_query_nearest_host(snch_scene_t scene, const float *points_xyz, int64_t n, uint32_t *out_index,
                             float *out_distance);
@@ -484,6 +493,17 @@ int snch_sort_pairs(uint32_t *keys, uint32_t *values, uint32_t *keys_tmp, uint32
 
 /* Number of kernels this library has launched in this process (all scenes). */
 uint64_t snch_kernel_launch_count(void);
+
+/* Device memory held for reuse. A destroyed scene's arrays and its host-form
+ * staging buffers stay allocated for the next scene of similar size (a scene
+ * rebuilt from scratch every batch then pays no cudaMalloc / cudaFree), and
+ * per-call scratch comes from a pool that keeps its pages mapped.
+ * snch_cached_memory_bytes: bytes of released scene blocks held now (the
+ * scratch pool is not counted). snch_release_cached_memory: waits for the
+ * device, then returns both to the driver (like emptying a caching
+ * allocator). A cudaMalloc that runs out of memory does the same and retries. */
+int64_t snch_cached_memory_bytes(void);
+int snch_release_cached_memory(void);
 
 /* snch_sort_pairs for callers that cannot allocate GPU memory -- a real-time
  * solver loop that must never stall the device (cudaMalloc/cudaFree can

@@ -20,7 +20,8 @@ import numpy as np
 
 from ._ffi import BvhView, SnchError, check, lib  # noqa: F401
 
-__all__ = ["Scene", "BatchedScene", "Scene2", "Graph", "SnchError", "BvhView", "lib", "read_obj"]
+__all__ = ["Scene", "BatchedScene", "Scene2", "Graph", "SnchError", "BvhView", "lib", "read_obj",
+           "cached_memory_bytes", "release_cached_memory"]
 
 INVALID = 0xFFFFFFFF
 TRAVERSAL_NEAR_FIRST = 0
@@ -29,6 +30,7 @@ OPT_TRAVERSAL, OPT_QUERY_ORDER, OPT_ORDER_MIN_BATCH, OPT_PERSISTENT, OPT_TAIL_CA
 OPT_NODE_WIDTH, OPT_NODE_WIDTH_NEAREST, OPT_NODE_WIDTH_SILHOUETTE = 6, 7, 8
 OPT_BLOCK, OPT_BLOCK_NEAREST, OPT_BLOCK_SILHOUETTE = 9, 10, 11
 OPT_PACKET, OPT_PACKET_NEAREST, OPT_PACKET_SILHOUETTE = 12, 13, 14
+OPT_HOST_CHUNK = 15
 
 
 def _torch():
@@ -74,6 +76,16 @@ def read_obj(path):
     check(L.snch_obj_read(p, v.ctypes.data_as(C.c_void_p), nv.value, t.ctypes.data_as(C.c_void_p), nt.value,
                           C.byref(nv), C.byref(nt)))
     return v, t
+
+
+def cached_memory_bytes():
+    """Bytes of released scene arrays this library holds for reuse."""
+    return int(lib().snch_cached_memory_bytes())
+
+
+def release_cached_memory():
+    """Return the held scene arrays and the scratch pool to the driver."""
+    check(lib().snch_release_cached_memory())
 
 
 class Scene:

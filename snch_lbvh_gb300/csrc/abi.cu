@@ -8,6 +8,9 @@
 #include <cmath>
 
 #include <atomic>
+#include <map>
+#include <mutex>
+#include <unordered_map>
 
 #include "internal.h"
 
@@ -51,7 +54,7 @@ inline cudaStream_t S(snch_stream_t s) { return static_cast<cudaStream_t>(s); }
 constexpr size_t kSmallWords = 1056;
 constexpr size_t kWStatus = 1040, kWNumEdges = 1041, kWBad = 1042, kWHist = 8;
 
-constexpr int64_t kHostChunk = 1 << 21;  // queries per pipelined host-form chunk
+constexpr int64_t kHostChunk = 1 << 24;  // queries per pipelined host-form chunk
 
 struct HostStage
 {
@@ -85,6 +88,7 @@ struct snch_scene_s
     int traversal = SNCH_TRAVERSAL_NEAR_FIRST;
     int query_order = 1;             // Morton-sort batches of at least order_min queries
     int64_t order_min = 65536;
+    int64_t host_chunk = kHostChunk;  // queries per pipelined host-form chunk
     int persistent = 0;              // lane-refill nearest/silhouette kernels (measured slower: off)
     int64_t tail_cap = 0;            // near-first expansions before a query is deferred (0: off; measured slower)
     // batched scene (num_meshes > 0): independent meshes, one build, per-mesh queries
@@ -139,13 +143,166 @@ struct snch_scene_s
 
 namespace
 {
+// Scene arrays and host-form staging buffers come from a cache of released
+// device blocks: a scene created and destroyed once per batch of work reuses
+// the previous scene's blocks instead of paying cudaMalloc / cudaFree (and the
+// device-wide synchronisation of cudaFree) each time. A block is released to
+// the cache only when no queued device work uses it; a request takes the
+// smallest cached block of at least its size and at most 1/8 larger. A failed
+// cudaMalloc returns the cache to the driver and tries once more;
+// snch_release_cached_memory() does the same on request.
+struct BlockCache
+{
+    std::mutex mu;
+    std::multimap<size_t, void *> free_blocks;        // size -> block
+    std::unordered_map<void *, size_t> live;          // block -> size
+    size_t cached_bytes = 0;
+};
+BlockCache &block_cache()
+{
+    static BlockCache *c = new BlockCache();  // never destroyed: scenes may outlive static destructors
+    return *c;
+}
+
+void cache_trim_locked(BlockCache &c)
+{
+    for (auto &kv : c.free_blocks)
+        cudaFree(kv.second);
+    c.free_blocks.clear();
+    c.cached_bytes = 0;
+}
+
+cudaError_t cache_alloc(void **p, size_t bytes)
+{
+    *p = nullptr;
+    bytes = (std::max<size_t>(bytes, 1) + 255) & ~size_t(255);
+    BlockCache &c = block_cache();
+    std::lock_guard<std::mutex> lock(c.mu);
+    auto it = c.free_blocks.lower_bound(bytes);
+    if (it != c.free_blocks.end() && it->first <= bytes + bytes / 8)
+    {
+        *p = it->second;
+        c.live[it->second] = it->first;
+        c.cached_bytes -= it->first;
+        c.free_blocks.erase(it);
+        return cudaSuccess;
+    }
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e == cudaErrorMemoryAllocation && !c.free_blocks.empty())
+    {
+        cudaGetLastError();
+        cache_trim_locked(c);
+        e = cudaMalloc(p, bytes);
+    }
+    if (e != cudaSuccess)
+    {
+        *p = nullptr;
+        return e;
+    }
+    c.live[*p] = bytes;
+    return cudaSuccess;
+}
+
+// p must be idle: no queued device work may read or write it
+void cache_release(void *p)
+{
+    if (!p)
+        return;
+    BlockCache &c = block_cache();
+    std::lock_guard<std::mutex> lock(c.mu);
+    auto it = c.live.find(p);
+    if (it == c.live.end())
+    {
+        cudaFree(p);  // not from the cache
+        return;
+    }
+    c.free_blocks.emplace(it->second, p);
+    c.cached_bytes += it->second;
+    c.live.erase(it);
+}
+
+// Per-call scratch (query orders, deferred lists, workspaces) is stream-ordered
+// and comes from this library's own memory pool on the current device, which
+// keeps released memory mapped (release threshold: unlimited) so a call does
+// not map fresh pages each time. Under stream capture the allocation is left
+// to the graph (cudaMallocAsync). Released by snch_release_cached_memory().
+constexpr int kMaxDevices = 64;
+cudaMemPool_t g_pool[kMaxDevices] = {};
+std::mutex g_pool_mu;
+
+cudaMemPool_t scratch_pool()
+{
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
+        return nullptr;
+    std::lock_guard<std::mutex> lock(g_pool_mu);
+    if (!g_pool[dev])
+    {
+        cudaMemPoolProps props = {};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = dev;
+        cudaMemPool_t pool = nullptr;
+        if (cudaMemPoolCreate(&pool, &props) != cudaSuccess)
+        {
+            cudaGetLastError();
+            return nullptr;
+        }
+        uint64_t keep = UINT64_MAX;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+        g_pool[dev] = pool;
+    }
+    return g_pool[dev];
+}
+
+void trim_pools()
+{
+    std::lock_guard<std::mutex> lock(g_pool_mu);
+    for (cudaMemPool_t pool : g_pool)
+        if (pool)
+            cudaMemPoolTrimTo(pool, 0);
+}
+
+cudaError_t scratch_alloc_raw(void **pp, size_t bytes, cudaStream_t st)
+{
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(st, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone)
+        return cudaMallocAsync(pp, bytes, st);
+    cudaMemPool_t pool = scratch_pool();
+    if (!pool)
+        return cudaMallocAsync(pp, bytes, st);
+    cudaError_t e = cudaMallocFromPoolAsync(pp, bytes, pool, st);
+    if (e == cudaErrorMemoryAllocation)
+    {
+        cudaGetLastError();
+        {
+            BlockCache &c = block_cache();
+            std::lock_guard<std::mutex> lock(c.mu);
+            cache_trim_locked(c);
+        }
+        cudaStreamSynchronize(st);
+        cudaMemPoolTrimTo(pool, 0);
+        e = cudaMallocFromPoolAsync(pp, bytes, pool, st);
+    }
+    return e;
+}
+
+template <typename T>
+cudaError_t scratch_alloc(T **p, size_t bytes, cudaStream_t st)
+{
+    void *q = nullptr;
+    const cudaError_t e = scratch_alloc_raw(&q, bytes, st);
+    *p = static_cast<T *>(q);
+    return e;
+}
+
 template <typename T>
 cudaError_t dalloc(T **p, size_t count)
 {
-    *p = nullptr;
-    if (count == 0)
-        count = 1;
-    return cudaMalloc(reinterpret_cast<void **>(p), sizeof(T) * count);
+    void *q = nullptr;
+    const cudaError_t e = cache_alloc(&q, sizeof(T) * std::max<size_t>(count, 1));
+    *p = static_cast<T *>(q);
+    return e;
 }
 
 void free_scene(snch_scene_s *s)
@@ -157,9 +314,9 @@ void free_scene(snch_scene_s *s)
                     s->tri_mesh, s->mesh_tri_start, s->mesh_box, s->sorted_mesh, s->mesh_root, s->perm,
                     s->perm_tmp, s->mkey_tmp, s->mesh_edge_start, s->wide[0], s->wide[1], s->wide_idx[0],
                     s->wide_idx[1]};
+    cudaDeviceSynchronize();  // the scene's queued work ends before its blocks are reused
     for (void *p : ptrs)
-        if (p)
-            cudaFree(p);
+        cache_release(p);
     for (cudaStream_t st : s->pipe)
         if (st)
             cudaStreamDestroy(st);
@@ -192,7 +349,7 @@ int allocate(snch_scene_s *s)
     SNCH_CUDA(dalloc(&s->ref_objects, n));
     SNCH_CUDA(dalloc(&s->ref_edges, 3 * n));
     const size_t scratch = std::max(topology_scratch_bytes((uint32_t)n), sort_scratch_bytes((uint32_t)n, 30));
-    SNCH_CUDA(cudaMalloc(&s->scratch, scratch));
+    SNCH_CUDA(cache_alloc(&s->scratch, scratch));
     SNCH_CUDA(cudaMemset(s->small, 0, kSmallWords * 4));
     return SNCH_OK;
 }
@@ -225,10 +382,19 @@ int create_common(const float *v, int64_t nv, const int32_t *t, int64_t nt, snch
     if (nt >= (int64_t(1) << 30) || nv >= (int64_t(1) << 31))
         return fail(SNCH_ERR_TOO_LARGE, "at most 2^30 - 1 triangles and 2^31 - 1 vertices are supported");
     if (!device)
+    {
+        // one branch-free pass (an unsigned compare also catches negative
+        // indices), then a search for the first bad index only on failure
+        uint32_t any_bad = 0;
+        const uint32_t unv = (uint32_t)nv;
         for (int64_t i = 0; i < 3 * nt; ++i)
-            if (t[i] < 0 || t[i] >= nv)
-                return fail(SNCH_ERR_INVALID_ARGUMENT,
-                            "triangle vertex index out of range at triangle " + std::to_string(i / 3));
+            any_bad |= (uint32_t)((uint32_t)t[i] >= unv);
+        if (any_bad)
+            for (int64_t i = 0; i < 3 * nt; ++i)
+                if (t[i] < 0 || t[i] >= nv)
+                    return fail(SNCH_ERR_INVALID_ARGUMENT,
+                                "triangle vertex index out of range at triangle " + std::to_string(i / 3));
+    }
     snch_scene_s *s = new snch_scene_s();
     s->num_verts = (uint32_t)nv;
     s->num_tris = (uint32_t)nt;
@@ -363,7 +529,7 @@ int ensure_wide(snch_scene_s *s, int W, cudaStream_t st)
     a.out = s->wide[k];
     a.status = s->small + kWStatus;
     char *scratch = nullptr;
-    SNCH_CUDA(cudaMallocAsync(reinterpret_cast<void **>(&scratch), wide_scratch_bytes(s->num_tris) + 256, st));
+    SNCH_CUDA(scratch_alloc(&scratch, wide_scratch_bytes(s->num_tris) + 256, st));
     a.count = reinterpret_cast<uint32_t *>(scratch);
     a.scratch = scratch + 256;
     cudaError_t e = launch_wide_count(a, st);
@@ -438,7 +604,7 @@ cudaError_t batch_view(const snch_scene_s *s, const float *keys_from, int64_t n,
     }
     if (!s->query_order || n < s->order_min || n >= (int64_t(1) << 30) || s->num_tris < 2)
         return cudaSuccess;
-    cudaError_t e = cudaMallocAsync(&b.scratch, query_order_scratch_bytes(n), st);
+    cudaError_t e = scratch_alloc(&b.scratch, query_order_scratch_bytes(n), st);
     if (e != cudaSuccess)
         return e;
     uint32_t *order = nullptr;
@@ -469,7 +635,7 @@ int run_query(snch_scene_s *s, const float *pts, const float *radius, int64_t n,
     }
     char *scratch = nullptr;
     const size_t lists = (radius ? 1 : 0) + (capped ? 3 : 0);
-    SNCH_CUDA(cudaMallocAsync(reinterpret_cast<void **>(&scratch), 256 + lists * (4 * (size_t)n + 256), st));
+    SNCH_CUDA(scratch_alloc(&scratch, 256 + lists * (4 * (size_t)n + 256), st));
     uint32_t *fail_count = reinterpret_cast<uint32_t *>(scratch), *defer_count = fail_count + 1;
     char *next = scratch + 256;
     auto take = [&]() {
@@ -592,32 +758,41 @@ MlpWorkspace mlp_workspace(char *base, int64_t rows)
     return w;
 }
 
-// ---- host-form pipeline: chunk i runs on pipe[i % 2]: H2D inputs, kernel, D2H outputs
+// ---- host-form pipeline: chunk i runs on pipe[i % 2]: H2D inputs, kernel, D2H outputs.
+// The pipes are blocking streams: their work starts after what is queued on the
+// legacy default stream (a build with a NULL stream) and needs no event.
 int ensure_stage(snch_scene_s *s, size_t in_bytes, size_t out_bytes)
 {
     for (int k = 0; k < 2; ++k)
         if (!s->pipe[k])
-            SNCH_CUDA(cudaStreamCreateWithFlags(&s->pipe[k], cudaStreamNonBlocking));
+            SNCH_CUDA(cudaStreamCreateWithFlags(&s->pipe[k], cudaStreamDefault));
+    if (in_bytes <= s->stage.in_bytes && out_bytes <= s->stage.out_bytes)
+        return SNCH_OK;
+    // a call that failed part-way may have left copies queued on the stage
+    for (int k = 0; k < 2; ++k)
+        SNCH_CUDA(cudaStreamSynchronize(s->pipe[k]));
     if (in_bytes > s->stage.in_bytes)
     {
         for (int k = 0; k < 2; ++k)
         {
-            if (s->stage.in[k])
-                cudaFree(s->stage.in[k]);
+            cache_release(s->stage.in[k]);
             s->stage.in[k] = nullptr;
-            SNCH_CUDA(cudaMalloc(&s->stage.in[k], in_bytes));
         }
+        s->stage.in_bytes = 0;
+        for (int k = 0; k < 2; ++k)
+            SNCH_CUDA(cache_alloc(&s->stage.in[k], in_bytes));
         s->stage.in_bytes = in_bytes;
     }
     if (out_bytes > s->stage.out_bytes)
     {
         for (int k = 0; k < 2; ++k)
         {
-            if (s->stage.out[k])
-                cudaFree(s->stage.out[k]);
+            cache_release(s->stage.out[k]);
             s->stage.out[k] = nullptr;
-            SNCH_CUDA(cudaMalloc(&s->stage.out[k], out_bytes));
         }
+        s->stage.out_bytes = 0;
+        for (int k = 0; k < 2; ++k)
+            SNCH_CUDA(cache_alloc(&s->stage.out[k], out_bytes));
         s->stage.out_bytes = out_bytes;
     }
     return SNCH_OK;
@@ -641,7 +816,7 @@ int run_host_pipeline(snch_scene_s *s, int64_t n, const Field *ins, int nin, con
         in_per += ins[i].elem;
     for (int i = 0; i < nout; ++i)
         out_per += outs[i].elem;
-    const int64_t chunk = std::min<int64_t>(n, kHostChunk);
+    const int64_t chunk = std::min<int64_t>(n, s->host_chunk);
     int rc = ensure_stage(s, in_per * chunk + 256 * nin, out_per * chunk + 256 * nout);
     if (rc != SNCH_OK)
         return rc;
@@ -688,6 +863,25 @@ extern "C" {
 const char *snch_version(void) { return "snch_gb300 0.1 (sm_103a)"; }
 
 const char *snch_last_error(void) { return g_error.c_str(); }
+
+int64_t snch_cached_memory_bytes(void)
+{
+    BlockCache &c = block_cache();
+    std::lock_guard<std::mutex> lock(c.mu);
+    return (int64_t)c.cached_bytes;
+}
+
+int snch_release_cached_memory(void)
+{
+    BlockCache &c = block_cache();
+    {
+        std::lock_guard<std::mutex> lock(c.mu);
+        cache_trim_locked(c);
+    }
+    cudaDeviceSynchronize();
+    trim_pools();
+    return SNCH_OK;
+}
 
 uint64_t snch_kernel_launch_count(void) { return g_kernel_launches.load(std::memory_order_relaxed); }
 
@@ -772,6 +966,11 @@ int snch_set_option(snch_scene_t s, int option, int64_t value)
         if (value < 0)
             return fail(SNCH_ERR_INVALID_ARGUMENT, "SNCH_OPT_ORDER_MIN_BATCH must be >= 0");
         s->order_min = value;
+        return SNCH_OK;
+    case SNCH_OPT_HOST_CHUNK:
+        if (value < 1024 || value >= (int64_t(1) << 30))
+            return fail(SNCH_ERR_INVALID_ARGUMENT, "SNCH_OPT_HOST_CHUNK must be in [1024, 2^30)");
+        s->host_chunk = value;
         return SNCH_OK;
     case SNCH_OPT_TAIL_CAP:
         if (value < 0 || value > (int64_t(1) << 30))
@@ -1167,7 +1366,7 @@ int snch_query_visits(snch_scene_t s, int kind, const float *in0, const float *i
     cudaStream_t st = S(stream);
     // result buffers of the counted launch (discarded)
     char *scratch = nullptr;
-    SNCH_CUDA(cudaMallocAsync(reinterpret_cast<void **>(&scratch), 32 * (size_t)n + 256, st));
+    SNCH_CUDA(scratch_alloc(&scratch, 32 * (size_t)n + 256, st));
     // nearest / silhouette batches are counted in the order a query call runs them
     // (Morton-ordered above the ordering threshold, which selects the packet form)
     BatchView b;
@@ -1317,7 +1516,7 @@ int snch_mlp_gradient(snch_mlp_t m, const float *pts, const float *targets, int6
     cudaStream_t st = S(stream);
     const int64_t rows = (n + 127) / 128 * 128;
     char *ws = nullptr;
-    SNCH_CUDA(cudaMallocAsync(reinterpret_cast<void **>(&ws), mlp_workspace_bytes(rows), st));
+    SNCH_CUDA(scratch_alloc(&ws, mlp_workspace_bytes(rows), st));
     cudaError_t e = mlp_forward_backward(m->st.params, m->st.grad, pts, targets, n, rows, m->st.center,
                                          m->st.inv_half, tau, mlp_workspace(ws, rows), m->st.loss, m->st.status, st);
     if (e == cudaSuccess && host_grad)
@@ -1341,8 +1540,8 @@ int snch_mlp_train(snch_mlp_t m, const float *pts, const float *targets, int64_t
     char *ws = nullptr;
     const int64_t steps = (n + batch - 1) / batch;
     float *losses = nullptr;
-    SNCH_CUDA(cudaMallocAsync(reinterpret_cast<void **>(&ws), mlp_workspace_bytes(rows_max), st));
-    cudaError_t e = cudaMallocAsync(reinterpret_cast<void **>(&losses), 4 * (size_t)steps, st);
+    SNCH_CUDA(scratch_alloc(&ws, mlp_workspace_bytes(rows_max), st));
+    cudaError_t e = scratch_alloc(&losses, 4 * (size_t)steps, st);
     const MlpWorkspace w = mlp_workspace(ws, rows_max);
     for (int ep = 0; ep < epochs && e == cudaSuccess; ++ep)
         for (int64_t s = 0; s < steps && e == cudaSuccess; ++s)
@@ -1425,7 +1624,7 @@ int snch_batch_create(const float *v, int64_t nv, const int32_t *t, int64_t nt, 
         e = cudaMemcpyAsync(s->verts, v, 12 * (size_t)nv, device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
                             st);
     if (e == cudaSuccess)
-        e = cudaMallocAsync(reinterpret_cast<void **>(&vs_dev), 8 * (size_t)(num_meshes + 1), st);
+        e = scratch_alloc(&vs_dev, 8 * (size_t)(num_meshes + 1), st);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(vs_dev, mesh_vert_start, 8 * (size_t)(num_meshes + 1), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess)
@@ -1521,7 +1720,7 @@ int snch_autotune(snch_scene_t s, const int32_t *near_mesh, const float *near_pt
     float ms[2][kConfigs] = {};
     char *out = nullptr;
     const int64_t nmax = std::max<int64_t>(1, std::max(n_near, n_sil));
-    SNCH_CUDA(cudaMallocAsync(reinterpret_cast<void **>(&out), 8 * (size_t)nmax, st));
+    SNCH_CUDA(scratch_alloc(&out, 8 * (size_t)nmax, st));
     uint32_t *o_idx = reinterpret_cast<uint32_t *>(out);
     float *o_dist = reinterpret_cast<float *>(out + 4 * (size_t)nmax);
     cudaEvent_t ev[2] = {nullptr, nullptr};
@@ -1604,8 +1803,8 @@ int snch_autotune(snch_scene_t s, const int32_t *near_mesh, const float *near_pt
         const int w = k == 0 ? 4 : 8;
         if (s->width_near != w && s->width_sil != w && s->wide[k])
         {
-            cudaFree(s->wide[k]);
-            cudaFree(s->wide_idx[k]);
+            cache_release(s->wide[k]);
+            cache_release(s->wide_idx[k]);
             s->wide[k] = nullptr;
             s->wide_idx[k] = nullptr;
             s->wide_cap[k] = 0;
@@ -1901,7 +2100,7 @@ int snch_wost_trace(snch_scene_t dir, snch_scene_t neu, snch_mlp_t mlp, const sn
     const size_t per = 2 * (12 + 12 + 1 + 4 + 4) + 4 + 4 + 4 + 4 + 4 + 4 + 12 + 4 + 4 + 4 + 4 + 1 + 4 + 8 + 4 + 4 + 4 +
                        12 + 4 + 4;
     char *blk = nullptr;
-    SNCH_CUDA(cudaMallocAsync(reinterpret_cast<void **>(&blk), per * n + 64 * 256, st));
+    SNCH_CUDA(scratch_alloc(&blk, per * n + 64 * 256, st));
     size_t off = 0;
     auto take = [&](size_t bytes) {
         char *q = blk + off;
