@@ -392,11 +392,27 @@ def batched_leg(scale, per_tri=8):
             and torch.equal(se, torch.cat([o[1] for o in outs2])))
     for s_ in scenes:
         s_.close()
-    # autotuned (node width, threads per block) on a 1/256 sample of each mesh's queries
-    tsub = [p_[: max(1, len(p_) // 256)] for p_ in pts]
-    Pt, Mt = torch.cat(tsub), torch.cat([m_[: len(p_)] for m_, p_ in zip(mid, tsub)])
+    # autotuned (node width, threads per block, packets, persistent) on every query of
+    # every 32nd mesh: the sample keeps the batch's query density, which decides
+    # whether warp packets pay (a thin slice of every mesh's queries would not)
+    tsel = range(0, len(pts), 32)
+    Pt, Mt = torch.cat([pts[m_] for m_ in tsel]), torch.cat([mid[m_] for m_ in tsel])
     tuned = b.autotune(Pt, Pt, None, near_mesh=Mt, sil_mesh=Mt)
-    chosen = {"near": "w%d_b%d" % b.search_config("nearest"), "sil": "w%d_b%d" % b.search_config("silhouette")}
+
+    def cfg_name(w, bk, pk, pers):
+        return f"w{w}_b{bk}_" + ("packet" if pk else "persistent" if pers else "lane")
+
+    chosen = {"near": cfg_name(*b.search_config("nearest")), "sil": cfg_name(*b.search_config("silhouette"))}
+    # the full batches again in the chosen configurations
+    te = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    torch.cuda.synchronize()
+    te[0].record()
+    b.query_nearest_batch(M, P)
+    te[1].record()
+    b.query_silhouette_batch(M, P)
+    te[2].record()
+    torch.cuda.synchronize()
+    tuned_ms = [te[0].elapsed_time(te[1]), te[1].elapsed_time(te[2])]
     # the whole step (topology + build of all meshes + both query batches) as one
     # captured CUDA graph, launched once to warm up and once timed
     gst = torch.cuda.Stream()
@@ -427,10 +443,11 @@ def batched_leg(scale, per_tri=8):
             "batched_subset_qps": {"near": ns / (bsub[0] / 1e3), "sil": ns / (bsub[1] / 1e3)},
             "build_speedup": single[0] / batched[0],
             "identical_to_per_mesh": bool(same),
-            "autotune_ms": {"sample": f"{len(Pt):,} queries per type",
-                            "near": {f"w{w}_b{bk}": t for (w, bk), t in tuned["nearest"].items()},
-                            "sil": {f"w{w}_b{bk}": t for (w, bk), t in tuned["silhouette"].items()},
+            "autotune_ms": {"sample": f"{len(Pt):,} queries per type (all queries of every 32nd mesh)",
+                            "near": {cfg_name(*c): t for c, t in tuned["nearest"].items()},
+                            "sil": {cfg_name(*c): t for c, t in tuned["silhouette"].items()},
                             "chosen": chosen},
+            "tuned_qps": {"near": n / (tuned_ms[0] / 1e3), "sil": n / (tuned_ms[1] / 1e3)},
             "graph": {"step_ms": graph_ms, "qps": 2 * n / (graph_ms / 1e3),
                       "what": "one CUDA-graph launch: topology + build of all meshes + both query batches",
                       "identical": bool(graph_same)},

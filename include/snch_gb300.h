@@ -161,12 +161,17 @@ int snch_set_traversal(snch_scene_t scene, int mode);
 #define SNCH_OPT_TRAVERSAL 1
 #define SNCH_OPT_QUERY_ORDER 2
 #define SNCH_OPT_ORDER_MIN_BATCH 3
-/*   SNCH_OPT_PERSISTENT       1: near-first nearest/silhouette batches run as persistent
- *                             kernels whose lanes take the next query when their own is
- *                             done; 0 (default): one thread per query. Same results; on
- *                             the 2M-triangle scene with Morton-ordered batches the
- *                             refilled lanes lose their warp's coherence and run slower. */
+/*   SNCH_OPT_PERSISTENT       1: near-first nearest/silhouette batches (plain or batched
+ *                             scenes) run as persistent work-stealing kernels: a warp
+ *                             takes 32 queries at a time from a batch-wide counter and a
+ *                             lane takes the next query when its own is done; 0
+ *                             (default): one thread per query. Same results; on the
+ *                             2M-triangle scene with Morton-ordered batches the refilled
+ *                             lanes lose their warp's coherence and run slower.
+ *   SNCH_OPT_PERSISTENT_NEAREST / _SILHOUETTE  the same for one query type. */
 #define SNCH_OPT_PERSISTENT 4
+#define SNCH_OPT_PERSISTENT_NEAREST 16
+#define SNCH_OPT_PERSISTENT_SILHOUETTE 17
 /*   SNCH_OPT_TAIL_CAP         near-first nearest/silhouette searches still running after
  *                             this many node expansions (0 = no cap, the default) are
  *                             finished by a second pass seeded with the best distance
@@ -213,6 +218,9 @@ int snch_set_traversal(snch_scene_t scene, int mode);
  *                             gives each Morton-ordered search a denser batch. */
 #define SNCH_OPT_HOST_CHUNK 15
 int snch_set_option(snch_scene_t scene, int option, int64_t value);
+/* current value of an option (SNCH_OPT_NODE_WIDTH / _BLOCK / _PACKET read the
+ * nearest search's) */
+int snch_get_option(snch_scene_t scene, int option, int64_t *value);
 
 /* Position of each sorted leaf in the reference's depth-first visit order,
  * copied to a HOST buffer of N entries (synchronous). */
@@ -308,15 +316,23 @@ int snch_batch_query_silhouette(snch_scene_t scene, const int32_t *mesh, const f
 
 /* Autotuner (no reference counterpart): times this scene's nearest and
  * silhouette searches in SNCH_AUTOTUNE_CONFIGS configurations -- (node width,
- * threads per block) = (2, 128), (4, 128), (8, 128), (2, 64), (2, 256) -- on
- * caller sample batches (DEVICE buffers; for a batched scene near_mesh /
- * sil_mesh give each query's mesh, else NULL; a count of 0 skips that query
- * type), keeps the fastest configuration per query type (SNCH_OPT_NODE_WIDTH_*,
- * SNCH_OPT_BLOCK_*) and releases the wide records no type keeps. out_ms (HOST,
- * may be NULL): 2 x SNCH_AUTOTUNE_CONFIGS floats, milliseconds per batch in that
- * order for nearest, then silhouette. Synchronous. Results are the same in
- * every configuration; only their speed differs. */
-#define SNCH_AUTOTUNE_CONFIGS 5
+ * threads per block, SNCH_OPT_PACKET, SNCH_OPT_PERSISTENT) = (2, 128, 2, 0)
+ * [warp packets: 32 queries per traversal], (2, 128, 0, 0), (4, 128, 0, 0),
+ * (8, 128, 0, 0), (2, 64, 0, 0), (2, 256, 0, 0) [one query per traversal],
+ * (2, 128, 0, 1) [persistent work-stealing lanes] -- on caller sample batches
+ * (DEVICE buffers; for a batched scene near_mesh / sil_mesh give each query's
+ * mesh, else NULL; a count of 0 skips that query type), keeps the fastest
+ * configuration per query type (SNCH_OPT_NODE_WIDTH_*, SNCH_OPT_BLOCK_*,
+ * SNCH_OPT_PACKET_*, SNCH_OPT_PERSISTENT_*) and releases the wide records no
+ * type keeps. out_ms (HOST, may be NULL): 2 x SNCH_AUTOTUNE_CONFIGS floats,
+ * milliseconds per batch in that order for nearest, then silhouette.
+ * Synchronous. Distances are the same in every configuration (indices too, up
+ * to the exact ties described under SNCH_OPT_PACKET); only their speed
+ * differs. Stack depth is not a candidate: a search touches its stack only to
+ * the depth it reaches. Give a sample with the query density of the real
+ * batches (for a batched scene, all queries of some meshes rather than a few
+ * of every mesh's): warp packets gain with density and lose on sparse batches. */
+#define SNCH_AUTOTUNE_CONFIGS 7
 int snch_autotune(snch_scene_t scene, const int32_t *near_mesh, const float *near_points, int64_t n_near,
                   const int32_t *sil_mesh, const float *sil_points, const uint8_t *sil_flip_or_null, int64_t n_sil,
                   float *out_ms, snch_stream_t stream);

@@ -31,6 +31,7 @@ OPT_NODE_WIDTH, OPT_NODE_WIDTH_NEAREST, OPT_NODE_WIDTH_SILHOUETTE = 6, 7, 8
 OPT_BLOCK, OPT_BLOCK_NEAREST, OPT_BLOCK_SILHOUETTE = 9, 10, 11
 OPT_PACKET, OPT_PACKET_NEAREST, OPT_PACKET_SILHOUETTE = 12, 13, 14
 OPT_HOST_CHUNK = 15
+OPT_PERSISTENT_NEAREST, OPT_PERSISTENT_SILHOUETTE = 16, 17
 
 
 def _torch():
@@ -241,23 +242,34 @@ class Scene:
         return Graph(self, rebuild, near_points, near_out, sil_points, sil_flip, sil_out, near_mesh, sil_mesh,
                      stream)
 
+    def get_option(self, option):
+        v = C.c_int64()
+        check(lib().snch_get_option(self._h, option, C.byref(v)))
+        return int(v.value)
+
     def search_config(self, which: str = "nearest"):
-        """(node width, threads per block) of the nearest or silhouette search."""
+        """(node width, threads per block, OPT_PACKET mode, OPT_PERSISTENT) of the
+        nearest or silhouette search."""
         w, b = C.c_int32(), C.c_int32()
-        check(lib().snch_get_search_config(self._h, {"nearest": 0, "silhouette": 1}[which], C.byref(w), C.byref(b)))
-        return int(w.value), int(b.value)
+        k = {"nearest": 0, "silhouette": 1}[which]
+        check(lib().snch_get_search_config(self._h, k, C.byref(w), C.byref(b)))
+        return (int(w.value), int(b.value), self.get_option((OPT_PACKET_NEAREST, OPT_PACKET_SILHOUETTE)[k]),
+                self.get_option((OPT_PERSISTENT_NEAREST, OPT_PERSISTENT_SILHOUETTE)[k]))
 
     def node_width(self, which: str = "nearest") -> int:
         return self.search_config(which)[0]
 
-    AUTOTUNE_CONFIGS = ((2, 128), (4, 128), (8, 128), (2, 64), (2, 256))
+    # (node width, threads per block, OPT_PACKET, OPT_PERSISTENT): warp packets, one query
+    # per traversal, persistent work-stealing lanes
+    AUTOTUNE_CONFIGS = ((2, 128, 2, 0), (2, 128, 0, 0), (4, 128, 0, 0), (8, 128, 0, 0), (2, 64, 0, 0),
+                        (2, 256, 0, 0), (2, 128, 0, 1))
 
     def autotune(self, near_points=None, sil_points=None, sil_flip=None, near_mesh=None, sil_mesh=None,
                  stream=None):
         """Times the nearest / silhouette searches in each (node width, threads per
-        block) of AUTOTUNE_CONFIGS on these sample batches and keeps the fastest per
-        type (same results in every configuration). Returns
-        {"nearest": {(width, block): ms, ...}, "silhouette": {...}}."""
+        block, packet mode, persistent) of AUTOTUNE_CONFIGS on these sample batches and
+        keeps the fastest per type (same distances in every configuration). Returns
+        {"nearest": {(width, block, packet, persistent): ms, ...}, "silhouette": {...}}."""
         torch = _torch()
         pn = None if near_points is None else _dev(near_points, torch.float32, 3)
         ps = None if sil_points is None else _dev(sil_points, torch.float32, 3)

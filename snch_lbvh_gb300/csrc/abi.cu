@@ -89,7 +89,7 @@ struct snch_scene_s
     int query_order = 1;             // Morton-sort batches of at least order_min queries
     int64_t order_min = 65536;
     int64_t host_chunk = kHostChunk;  // queries per pipelined host-form chunk
-    int persistent = 0;              // lane-refill nearest/silhouette kernels (measured slower: off)
+    int persistent_near = 0, persistent_sil = 0;  // lane-refill (work-stealing) searches
     int64_t tail_cap = 0;            // near-first expansions before a query is deferred (0: off; measured slower)
     // batched scene (num_meshes > 0): independent meshes, one build, per-mesh queries
     uint32_t num_meshes = 0;
@@ -120,7 +120,7 @@ struct snch_scene_s
         t.edges = edges;
         t.status = small + kWStatus;
         t.near_first = traversal == SNCH_TRAVERSAL_NEAR_FIRST ? 1 : 0;
-        t.persistent = persistent;
+        t.persistent = (persistent_near ? 1 : 0) | (persistent_sil ? 2 : 0);
         t.width_near = width_near;
         t.width_sil = width_sil;
         t.block_near = block_near;
@@ -600,7 +600,6 @@ cudaError_t batch_view(const snch_scene_s *s, const float *keys_from, int64_t n,
         b.t.mesh_edge_start = s->mesh_edge_start;
         b.t.num_meshes = s->num_meshes;
         b.t.near_first = 1;
-        b.t.persistent = 0;
     }
     if (!s->query_order || n < s->order_min || n >= (int64_t(1) << 30) || s->num_tris < 2)
         return cudaSuccess;
@@ -622,10 +621,11 @@ cudaError_t batch_view(const snch_scene_s *s, const float *keys_from, int64_t n,
 //   3. with a user radius: the queries with nothing inside it, unbounded.
 // Every pass reads its query list and count on the device: no host sync.
 template <typename Launch>
-int run_query(snch_scene_s *s, const float *pts, const float *radius, int64_t n, uint32_t *num_fallback,
+int run_query(snch_scene_s *s, int kind, const float *pts, const float *radius, int64_t n, uint32_t *num_fallback,
               cudaStream_t st, Launch launch, const uint32_t *query_mesh = nullptr)
 {
-    const bool capped = s->tail_cap > 0 && s->traversal == SNCH_TRAVERSAL_NEAR_FIRST && !s->persistent;
+    const bool persistent = kind == 0 ? s->persistent_near : s->persistent_sil;
+    const bool capped = s->tail_cap > 0 && s->traversal == SNCH_TRAVERSAL_NEAR_FIRST && !persistent;
     BatchView b;
     if (!capped && !radius)
     {
@@ -978,9 +978,14 @@ int snch_set_option(snch_scene_t s, int option, int64_t value)
         s->tail_cap = value;
         return SNCH_OK;
     case SNCH_OPT_PERSISTENT:
+    case SNCH_OPT_PERSISTENT_NEAREST:
+    case SNCH_OPT_PERSISTENT_SILHOUETTE:
         if (value != 0 && value != 1)
             return fail(SNCH_ERR_INVALID_ARGUMENT, "SNCH_OPT_PERSISTENT takes 0 or 1");
-        s->persistent = (int)value;
+        if (option != SNCH_OPT_PERSISTENT_SILHOUETTE)
+            s->persistent_near = (int)value;
+        if (option != SNCH_OPT_PERSISTENT_NEAREST)
+            s->persistent_sil = (int)value;
         return SNCH_OK;
     case SNCH_OPT_PACKET:
     case SNCH_OPT_PACKET_NEAREST:
@@ -1150,7 +1155,7 @@ int snch_query_nearest(snch_scene_t s, const float *pts, int64_t n, uint32_t *id
         return rc;
     if (n == 0)
         return SNCH_OK;
-    return run_query(s, pts, nullptr, n, nullptr, S(stream), [&](const TreeView &t, const SeedArgs &seed) {
+    return run_query(s, 0, pts, nullptr, n, nullptr, S(stream), [&](const TreeView &t, const SeedArgs &seed) {
         return launch_nearest(t, pts, n, idx, dist, S(stream), nullptr, seed);
     });
 }
@@ -1165,7 +1170,7 @@ int snch_query_silhouette(snch_scene_t s, const float *pts, const uint8_t *flip,
         return rc;
     if (n == 0)
         return SNCH_OK;
-    return run_query(s, pts, nullptr, n, nullptr, S(stream), [&](const TreeView &t, const SeedArgs &seed) {
+    return run_query(s, 1, pts, nullptr, n, nullptr, S(stream), [&](const TreeView &t, const SeedArgs &seed) {
         return launch_silhouette(t, pts, flip, n, dist, edge, S(stream), nullptr, seed);
     });
 }
@@ -1333,7 +1338,7 @@ int snch_query_nearest_seeded(snch_scene_t s, const float *pts, const float *rad
         rc = check_n(n, {pts, radius, idx, dist});
     if (rc != SNCH_OK || n == 0)
         return rc;
-    return run_query(s, pts, radius, n, num_fallback, S(stream), [&](const TreeView &t, const SeedArgs &seed) {
+    return run_query(s, 0, pts, radius, n, num_fallback, S(stream), [&](const TreeView &t, const SeedArgs &seed) {
         return launch_nearest(t, pts, n, idx, dist, S(stream), nullptr, seed);
     });
 }
@@ -1346,7 +1351,7 @@ int snch_query_silhouette_seeded(snch_scene_t s, const float *pts, const uint8_t
         rc = check_n(n, {pts, radius, dist});
     if (rc != SNCH_OK || n == 0)
         return rc;
-    return run_query(s, pts, radius, n, num_fallback, S(stream), [&](const TreeView &t, const SeedArgs &seed) {
+    return run_query(s, 1, pts, radius, n, num_fallback, S(stream), [&](const TreeView &t, const SeedArgs &seed) {
         return launch_silhouette(t, pts, flip, n, dist, edge, S(stream), nullptr, seed);
     });
 }
@@ -1675,7 +1680,7 @@ int snch_batch_query_nearest(snch_scene_t s, const int32_t *mesh, const float *p
     if (rc != SNCH_OK || n == 0)
         return rc;
     return run_query(
-        s, pts, nullptr, n, nullptr, S(stream),
+        s, 0, pts, nullptr, n, nullptr, S(stream),
         [&](const TreeView &t, const SeedArgs &seed) {
             return launch_nearest(t, pts, n, reinterpret_cast<uint32_t *>(idx), dist, S(stream), nullptr, seed);
         },
@@ -1693,7 +1698,7 @@ int snch_batch_query_silhouette(snch_scene_t s, const int32_t *mesh, const float
     if (rc != SNCH_OK || n == 0)
         return rc;
     return run_query(
-        s, pts, nullptr, n, nullptr, S(stream),
+        s, 1, pts, nullptr, n, nullptr, S(stream),
         [&](const TreeView &t, const SeedArgs &seed) {
             return launch_silhouette(t, pts, flip, n, dist, edge, S(stream), nullptr, seed);
         },
@@ -1714,9 +1719,13 @@ int snch_autotune(snch_scene_t s, const int32_t *near_mesh, const float *near_pt
     if (rc != SNCH_OK)
         return rc;
     cudaStream_t st = S(stream);
-    // candidates (node width, threads per block); the block size applies to the binary searches
+    // candidates (node width, threads per block, SNCH_OPT_PACKET, SNCH_OPT_PERSISTENT):
+    // warp packets (2: for Morton-ordered batches, as the sample is), one search
+    // per lane, or persistent work-stealing lanes; the block size applies to the
+    // per-lane binary searches
     constexpr int kConfigs = SNCH_AUTOTUNE_CONFIGS;
-    const int cw[kConfigs] = {2, 4, 8, 2, 2}, cb[kConfigs] = {128, 128, 128, 64, 256};
+    const int cw[kConfigs] = {2, 2, 4, 8, 2, 2, 2}, cb[kConfigs] = {128, 128, 128, 128, 64, 256, 128},
+              cp[kConfigs] = {2, 0, 0, 0, 0, 0, 0}, cr[kConfigs] = {0, 0, 0, 0, 0, 0, 1};
     float ms[2][kConfigs] = {};
     char *out = nullptr;
     const int64_t nmax = std::max<int64_t>(1, std::max(n_near, n_sil));
@@ -1727,7 +1736,8 @@ int snch_autotune(snch_scene_t s, const int32_t *near_mesh, const float *near_pt
     cudaError_t e = cudaEventCreate(&ev[0]);
     if (e == cudaSuccess)
         e = cudaEventCreate(&ev[1]);
-    const int saved[4] = {s->width_near, s->width_sil, s->block_near, s->block_sil};
+    const int saved[8] = {s->width_near, s->width_sil,  s->block_near,      s->block_sil,
+                          s->packet_near, s->packet_sil, s->persistent_near, s->persistent_sil};
     auto run = [&](int kind) -> int {
         if (kind == 0)
             return s->num_meshes
@@ -1746,6 +1756,8 @@ int snch_autotune(snch_scene_t s, const int32_t *near_mesh, const float *near_pt
             rc = alloc_wide(s, w);
         s->width_near = s->width_sil = w;
         s->block_near = s->block_sil = cb[c];
+        s->packet_near = s->packet_sil = cp[c];
+        s->persistent_near = s->persistent_sil = cr[c];
         if (rc == SNCH_OK)
             rc = ensure_widths(s, st);
         for (int kind = 0; kind < 2 && rc == SNCH_OK && e == cudaSuccess; ++kind)
@@ -1778,6 +1790,10 @@ int snch_autotune(snch_scene_t s, const int32_t *near_mesh, const float *near_pt
         s->width_sil = saved[1];
         s->block_near = saved[2];
         s->block_sil = saved[3];
+        s->packet_near = saved[4];
+        s->packet_sil = saved[5];
+        s->persistent_near = saved[6];
+        s->persistent_sil = saved[7];
         if (rc != SNCH_OK)
             return rc;
         SNCH_CUDA(e);
@@ -1796,6 +1812,10 @@ int snch_autotune(snch_scene_t s, const int32_t *near_mesh, const float *near_pt
     s->block_near = best[0] < 0 ? saved[2] : cb[best[0]];
     s->width_sil = best[1] < 0 ? saved[1] : cw[best[1]];
     s->block_sil = best[1] < 0 ? saved[3] : cb[best[1]];
+    s->packet_near = best[0] < 0 ? saved[4] : cp[best[0]];
+    s->packet_sil = best[1] < 0 ? saved[5] : cp[best[1]];
+    s->persistent_near = best[0] < 0 ? saved[6] : cr[best[0]];
+    s->persistent_sil = best[1] < 0 ? saved[7] : cr[best[1]];
     // records of a width no query type keeps are released
     SNCH_CUDA(cudaStreamSynchronize(st));
     for (int k = 0; k < 2; ++k)
@@ -2043,6 +2063,34 @@ int snch_scene_vertices(snch_scene_t s, float **out)
     if (!s || !out)
         return fail(SNCH_ERR_INVALID_ARGUMENT, "scene and out are required");
     *out = s->verts;
+    return SNCH_OK;
+}
+
+int snch_get_option(snch_scene_t s, int option, int64_t *value)
+{
+    if (!s || !value)
+        return fail(SNCH_ERR_INVALID_ARGUMENT, "scene and value are required");
+    switch (option)
+    {
+    case SNCH_OPT_TRAVERSAL: *value = s->traversal; break;
+    case SNCH_OPT_QUERY_ORDER: *value = s->query_order; break;
+    case SNCH_OPT_ORDER_MIN_BATCH: *value = s->order_min; break;
+    case SNCH_OPT_PERSISTENT:
+    case SNCH_OPT_PERSISTENT_NEAREST: *value = s->persistent_near; break;
+    case SNCH_OPT_PERSISTENT_SILHOUETTE: *value = s->persistent_sil; break;
+    case SNCH_OPT_TAIL_CAP: *value = s->tail_cap; break;
+    case SNCH_OPT_NODE_WIDTH:
+    case SNCH_OPT_NODE_WIDTH_NEAREST: *value = s->width_near; break;
+    case SNCH_OPT_NODE_WIDTH_SILHOUETTE: *value = s->width_sil; break;
+    case SNCH_OPT_BLOCK:
+    case SNCH_OPT_BLOCK_NEAREST: *value = s->block_near; break;
+    case SNCH_OPT_BLOCK_SILHOUETTE: *value = s->block_sil; break;
+    case SNCH_OPT_PACKET:
+    case SNCH_OPT_PACKET_NEAREST: *value = s->packet_near; break;
+    case SNCH_OPT_PACKET_SILHOUETTE: *value = s->packet_sil; break;
+    case SNCH_OPT_HOST_CHUNK: *value = s->host_chunk; break;
+    default: return fail(SNCH_ERR_INVALID_ARGUMENT, "unknown option " + std::to_string(option));
+    }
     return SNCH_OK;
 }
 

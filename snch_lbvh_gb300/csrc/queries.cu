@@ -1723,8 +1723,35 @@ struct SilState
     float best;
     uint32_t best_key;
     int32_t best_edge;
+    int32_t edge_off;  // batched scenes: first edge id of the query's mesh
     int sp;
 };
+
+// Starts the search of query q at its (mesh's) root. Returns false when the
+// answer is already known -- no tree, or a one-triangle tree or mesh, whose
+// single leaf is evaluated here -- and true when nodes are left to expand.
+SNCH_DEV bool start_silhouette(const TreeView &t, SilState &s, uint32_t *sn, float *sd, const SeedArgs &seed)
+{
+    const uint32_t ni = t.num_tris - 1;
+    s.best = seed.radius ? __ldg(seed.radius + s.q) : INFINITY;
+    s.best_key = 0;
+    s.best_edge = -1;
+    s.sp = 0;
+    const QueryRoot qr = query_root(t, s.q);
+    s.edge_off = qr.edge_off;
+    if (qr.node == kInvalid)
+        return false;
+    if (qr.node >= ni)
+    {
+        uint32_t dummy = 0;
+        leaf_silhouette_fast(t, qr.node - ni, s.p, s.flip, s.best, s.best_key, s.best_edge, dummy);
+        return false;
+    }
+    sn[0] = qr.node;
+    sd[0] = mindist(load_root_box(t.aabbs + qr.node), s.p);
+    s.sp = 1;
+    return true;
+}
 
 template <bool kSeed>
 __global__ void __launch_bounds__(128) silhouette_persistent_kernel(TreeView t, const float *__restrict__ pts,
@@ -1746,72 +1773,74 @@ __global__ void __launch_bounds__(128) silhouette_persistent_kernel(TreeView t, 
     for (;;)
     {
         const int64_t qi = take_query(wq, total, counter, !active);
+        bool done = false;
         if (qi >= 0)
         {
             s.q = query_index(t, qi);
             s.p = load_point(pts, s.q);
             s.flip = flips ? __ldg(flips + s.q) != 0 : false;
-            s.best = kSeed ? __ldg(seed.radius + s.q) : INFINITY;
-            s.best_key = 0;
-            s.best_edge = -1;
-            sn[0] = 0;
-            sd[0] = mindist(load_root_box(t.aabbs), s.p);
-            s.sp = 1;
             active = true;
+            done = !start_silhouette(t, s, sn, sd, seed);
         }
         if (!__any_sync(0xFFFFFFFFu, active))
-            break;
+        {
+            if (wq.exhausted)
+                break;
+            continue;
+        }
         if (!active)
             continue;
-        bool done = false;
-        --s.sp;
-        const uint32_t node = sn[s.sp];
-        if (!(sd[s.sp] > s.best * s.best))
+        if (!done)
         {
-            if (s.sp > kStackDepth - 2)
+            --s.sp;
+            const uint32_t node = sn[s.sp];
+            if (!(sd[s.sp] > s.best * s.best))
             {
-                atomicOr(t.status, kStatusStackOverflow);
-                s.best = NAN;
-                s.best_edge = -1;
-                done = true;
-            }
-            else
-            {
-                Box lb, rb;
-                uint32_t L, R;
-                unpack_inner(load_inner(t.inner + node), lb, rb, L, R);
-                const float4 *cr = reinterpret_cast<const float4 *>(t.inner_cones + node);
-                InnerConeRec icr;
-                icr.a = __ldg(cr);
-                icr.b = __ldg(cr + 1);
-                icr.c = __ldg(cr + 2);
-                Cone lc, rc;
-                unpack_cones(icr, lc, rc);
-                const f3 p = s.p;
-                const float Lmd = mindist(lb, p), Rmd = mindist(rb, p);
-                const float b2 = s.best * s.best;
-                const bool hitL = Lmd <= b2 && lc.half_angle >= 0.0f && cone_test(lc, p, lb, Lmd);
-                const bool hitR = Rmd <= b2 && rc.half_angle >= 0.0f && cone_test(rc, p, rb, Rmd);
-                if (hitL && L >= ni)
-                    leaf_silhouette_fast(t, L - ni, p, s.flip, s.best, s.best_key, s.best_edge, dummy);
-                if (hitR && R >= ni)
-                    leaf_silhouette_fast(t, R - ni, p, s.flip, s.best, s.best_key, s.best_edge, dummy);
-                const float b2n = s.best * s.best;
-                const bool pL = hitL && L < ni && Lmd <= b2n, pR = hitR && R < ni && Rmd <= b2n;
-                if (pL && pR)
+                if (s.sp > kStackDepth - 2)
                 {
-                    const bool l_first = Lmd <= Rmd;
-                    sn[s.sp] = l_first ? R : L;
-                    sd[s.sp] = l_first ? Rmd : Lmd;
-                    sn[s.sp + 1] = l_first ? L : R;
-                    sd[s.sp + 1] = l_first ? Lmd : Rmd;
-                    s.sp += 2;
+                    atomicOr(t.status, kStatusStackOverflow);
+                    s.best = NAN;
+                    s.best_edge = -1;
+                    done = true;
                 }
-                else if (pL || pR)
+                else
                 {
-                    sn[s.sp] = pL ? L : R;
-                    sd[s.sp] = pL ? Lmd : Rmd;
-                    ++s.sp;
+                    Box lb, rb;
+                    uint32_t L, R;
+                    unpack_inner(load_inner(t.inner + node), lb, rb, L, R);
+                    const float4 *cr = reinterpret_cast<const float4 *>(t.inner_cones + node);
+                    InnerConeRec icr;
+                    icr.a = __ldg(cr);
+                    icr.b = __ldg(cr + 1);
+                    icr.c = __ldg(cr + 2);
+                    Cone lc, rc;
+                    unpack_cones(icr, lc, rc);
+                    const f3 p = s.p;
+                    const float Lmd = mindist(lb, p), Rmd = mindist(rb, p);
+                    const float b2 = s.best * s.best;
+                    const bool hitL = Lmd <= b2 && lc.half_angle >= 0.0f && cone_test(lc, p, lb, Lmd);
+                    const bool hitR = Rmd <= b2 && rc.half_angle >= 0.0f && cone_test(rc, p, rb, Rmd);
+                    if (hitL && L >= ni)
+                        leaf_silhouette_fast(t, L - ni, p, s.flip, s.best, s.best_key, s.best_edge, dummy);
+                    if (hitR && R >= ni)
+                        leaf_silhouette_fast(t, R - ni, p, s.flip, s.best, s.best_key, s.best_edge, dummy);
+                    const float b2n = s.best * s.best;
+                    const bool pL = hitL && L < ni && Lmd <= b2n, pR = hitR && R < ni && Rmd <= b2n;
+                    if (pL && pR)
+                    {
+                        const bool l_first = Lmd <= Rmd;
+                        sn[s.sp] = l_first ? R : L;
+                        sd[s.sp] = l_first ? Rmd : Lmd;
+                        sn[s.sp + 1] = l_first ? L : R;
+                        sd[s.sp + 1] = l_first ? Lmd : Rmd;
+                        s.sp += 2;
+                    }
+                    else if (pL || pR)
+                    {
+                        sn[s.sp] = pL ? L : R;
+                        sd[s.sp] = pL ? Lmd : Rmd;
+                        ++s.sp;
+                    }
                 }
             }
         }
@@ -1821,7 +1850,7 @@ __global__ void __launch_bounds__(128) silhouette_persistent_kernel(TreeView t, 
                 s.best = INFINITY;  // nothing within the seed radius: the fallback pass answers it
             out_dist[s.q] = s.best;
             if (out_edge)
-                out_edge[s.q] = s.best_edge;
+                out_edge[s.q] = s.best_edge < 0 ? s.best_edge : s.best_edge - s.edge_off;
             if (kSeed && seed.fail_list)
                 append_failed(seed.fail_list, seed.fail_count, (uint32_t)s.q, s.best_edge < 0);
             active = false;
@@ -1841,7 +1870,7 @@ __global__ void __launch_bounds__(128) nearest_persistent_kernel(TreeView t, con
     float sd[kStackDepth];
     int64_t q = -1;
     f3 p = mk(0.f, 0.f, 0.f);
-    uint32_t nearest = kInvalid, best_rank = 0;
+    uint32_t nearest = kInvalid, best_rank = 0, tri_off = 0;
     float best = INFINITY;
     int sp = 0;
     bool active = false;
@@ -1849,6 +1878,7 @@ __global__ void __launch_bounds__(128) nearest_persistent_kernel(TreeView t, con
     for (;;)
     {
         const int64_t qi = take_query(wq, total, counter, !active);
+        bool done = false;
         if (qi >= 0)
         {
             q = query_index(t, qi);
@@ -1861,54 +1891,75 @@ __global__ void __launch_bounds__(128) nearest_persistent_kernel(TreeView t, con
                 const float r = __ldg(seed.radius + q);
                 best = r * r;
             }
-            sn[0] = 0;
-            sd[0] = mindist(load_root_box(t.aabbs), p);
-            sp = 1;
             active = true;
-        }
-        if (!__any_sync(0xFFFFFFFFu, active))
-            break;
-        if (!active)
-            continue;
-        bool done = false;
-        --sp;
-        const uint32_t node = sn[sp];
-        if (!(sd[sp] > best))
-        {
-            if (sp > kStackDepth - 2)
+            // start at the query's (mesh's) root; no tree, or a one-triangle
+            // tree or mesh, is answered here
+            const QueryRoot qr = query_root(t, q);
+            tri_off = qr.tri_off;
+            sp = 0;
+            if (qr.node == kInvalid)
+                done = true;
+            else if (qr.node >= ni)
             {
-                atomicOr(t.status, kStatusStackOverflow);
-                nearest = kInvalid;
-                best = NAN;
+                leaf_nearest_fast(t, qr.node - ni, p, best, best_rank, nearest);
                 done = true;
             }
             else
             {
-                Box lb, rb;
-                uint32_t L, R;
-                unpack_inner(load_inner(t.inner + node), lb, rb, L, R);
-                const float Lmd = mindist(lb, p), Rmd = mindist(rb, p);
-                const float Lmm = minmaxdist(lb, p), Rmm = minmaxdist(rb, p);
-                const bool aL = Lmd <= Rmm, aR = Rmd <= Lmm;  // query.cuh:279, 297
-                if (aL && L >= ni && Lmd <= best)
-                    leaf_nearest_fast(t, L - ni, p, best, best_rank, nearest);
-                if (aR && R >= ni && Rmd <= best)
-                    leaf_nearest_fast(t, R - ni, p, best, best_rank, nearest);
-                const bool pL = aL && L < ni && Lmd <= best, pR = aR && R < ni && Rmd <= best;
-                if (pL && pR)
+                sn[0] = qr.node;
+                sd[0] = mindist(load_root_box(t.aabbs + qr.node), p);
+                sp = 1;
+            }
+        }
+        if (!__any_sync(0xFFFFFFFFu, active))
+        {
+            if (wq.exhausted)
+                break;
+            continue;
+        }
+        if (!active)
+            continue;
+        if (!done)
+        {
+            --sp;
+            const uint32_t node = sn[sp];
+            if (!(sd[sp] > best))
+            {
+                if (sp > kStackDepth - 2)
                 {
-                    const bool l_first = Lmd <= Rmd;
-                    sn[sp] = l_first ? R : L;
-                    sd[sp] = l_first ? Rmd : Lmd;
-                    sn[sp + 1] = l_first ? L : R;
-                    sd[sp + 1] = l_first ? Lmd : Rmd;
-                    sp += 2;
+                    atomicOr(t.status, kStatusStackOverflow);
+                    nearest = kInvalid;
+                    best = NAN;
+                    done = true;
                 }
-                else if (pL || pR)
+                else
                 {
-                    sn[sp] = pL ? L : R;
-                    sd[sp] = pL ? Lmd : Rmd;
-                    ++sp;
+                    // near-first without the minmaxdist sibling test, as
+                    // nearest_fast_kernel: the same leaves decide the answer
+                    Box lb, rb;
+                    uint32_t L, R;
+                    unpack_inner(load_inner(t.inner + node), lb, rb, L, R);
+                    const float Lmd = mindist(lb, p), Rmd = mindist(rb, p);
+                    if (L >= ni && Lmd <= best)
+                        leaf_nearest_fast(t, L - ni, p, best, best_rank, nearest);
+                    if (R >= ni && Rmd <= best)
+                        leaf_nearest_fast(t, R - ni, p, best, best_rank, nearest);
+                    const bool pL = L < ni && Lmd <= best, pR = R < ni && Rmd <= best;
+                    if (pL && pR)
+                    {
+                        const bool l_first = Lmd <= Rmd;
+                        sn[sp] = l_first ? R : L;
+                        sd[sp] = l_first ? Rmd : Lmd;
+                        sn[sp + 1] = l_first ? L : R;
+                        sd[sp + 1] = l_first ? Lmd : Rmd;
+                        sp += 2;
+                    }
+                    else if (pL || pR)
+                    {
+                        sn[sp] = pL ? L : R;
+                        sd[sp] = pL ? Lmd : Rmd;
+                        ++sp;
+                    }
                 }
             }
         }
@@ -1916,7 +1967,7 @@ __global__ void __launch_bounds__(128) nearest_persistent_kernel(TreeView t, con
         {
             if (kSeed && nearest == kInvalid)
                 best = INFINITY;  // nothing within the seed radius: the fallback pass answers it
-            out_idx[q] = nearest;
+            out_idx[q] = nearest == kInvalid ? kInvalid : nearest - tri_off;
             out_dist[q] = sqrtf(best);
             if (kSeed && seed.fail_list)
                 append_failed(seed.fail_list, seed.fail_count, (uint32_t)q, nearest == kInvalid);
@@ -2448,16 +2499,16 @@ namespace
 {
 inline unsigned grid_for(int64_t n, int b) { return (unsigned)((n + b - 1) / b); }
 // the packet searches serve near-first, binary-record, uncapped launches
-inline bool packet_ok(const TreeView &t, int packet, int width, const SeedArgs &seed)
+inline bool packet_ok(const TreeView &t, int packet, int width, bool persistent, const SeedArgs &seed)
 {
     const bool on = packet == 1 || (packet == 2 && t.order_coherent);
-    return on && width == 2 && t.near_first && !t.persistent && !seed.cap && t.num_tris > 1;
+    return on && width == 2 && t.near_first && !persistent && !seed.cap && t.num_tris > 1;
 }
 // the wide searches serve near-first, one-thread-per-query, uncapped launches
 // over a tree whose wide records of that width exist
-inline bool wide_ok(const TreeView &t, int width, const SeedArgs &seed)
+inline bool wide_ok(const TreeView &t, int width, bool persistent, const SeedArgs &seed)
 {
-    if (!t.near_first || t.persistent || seed.cap || t.num_tris < 2)
+    if (!t.near_first || persistent || seed.cap || t.num_tris < 2)
         return false;
     return (width == 4 && t.wide4 && t.wide4_of) || (width == 8 && t.wide8 && t.wide8_of);
 }
@@ -2497,14 +2548,15 @@ cudaError_t launch_nearest(const TreeView &t, const float *pts, int64_t n, uint3
 {
     if (n <= 0)
         return cudaSuccess;
-    if (packet_ok(t, t.packet_near, t.width_near, seed))
+    const bool persistent = (t.persistent & 1) != 0;
+    if (packet_ok(t, t.packet_near, t.width_near, persistent, seed))
     {
         if (stats)
             nearest_packet_kernel<true><<<grid_for(n, 128), 128, 0, st>>>(t, pts, n, idx, dist, stats, seed);
         else
             nearest_packet_kernel<false><<<grid_for(n, 128), 128, 0, st>>>(t, pts, n, idx, dist, nullptr, seed);
     }
-    else if (wide_ok(t, t.width_near, seed))
+    else if (wide_ok(t, t.width_near, persistent, seed))
     {
         const unsigned g = grid_for(n, 128);
         if (t.width_near == 4)
@@ -2516,7 +2568,7 @@ cudaError_t launch_nearest(const TreeView &t, const float *pts, int64_t n, uint3
     }
     else if (stats)
         nearest_fast_kernel<true><<<grid_for(n, 128), 128, 0, st>>>(t, pts, n, idx, dist, stats, seed);
-    else if (t.near_first && t.num_tris > 1 && t.persistent)
+    else if (t.near_first && t.num_tris > 1 && persistent)
     {
         return seed.radius ? launch_persistent(nearest_persistent_kernel<true>, n, st, t, pts, n, idx, dist, seed)
                            : launch_persistent(nearest_persistent_kernel<false>, n, st, t, pts, n, idx, dist, seed);
@@ -2537,7 +2589,8 @@ cudaError_t launch_silhouette(const TreeView &t, const float *pts, const uint8_t
 {
     if (n <= 0)
         return cudaSuccess;
-    if (packet_ok(t, t.packet_sil, t.width_sil, seed))
+    const bool persistent = (t.persistent & 2) != 0;
+    if (packet_ok(t, t.packet_sil, t.width_sil, persistent, seed))
     {
         if (stats)
             silhouette_packet_kernel<true>
@@ -2546,7 +2599,7 @@ cudaError_t launch_silhouette(const TreeView &t, const float *pts, const uint8_t
             silhouette_packet_kernel<false>
                 <<<grid_for(n, 128), 128, 0, st>>>(t, pts, flip, n, dist, edge, nullptr, seed);
     }
-    else if (wide_ok(t, t.width_sil, seed))
+    else if (wide_ok(t, t.width_sil, persistent, seed))
     {
         const unsigned g = grid_for(n, 128);
         if (t.width_sil == 4)
@@ -2558,7 +2611,7 @@ cudaError_t launch_silhouette(const TreeView &t, const float *pts, const uint8_t
     }
     else if (stats)
         silhouette_fast_kernel<true><<<grid_for(n, 128), 128, 0, st>>>(t, pts, flip, n, dist, edge, stats, seed);
-    else if (t.near_first && t.num_tris > 1 && t.persistent)
+    else if (t.near_first && t.num_tris > 1 && persistent)
     {
         return seed.radius
                    ? launch_persistent(silhouette_persistent_kernel<true>, n, st, t, pts, flip, n, dist, edge, seed)

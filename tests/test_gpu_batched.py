@@ -30,10 +30,12 @@ def mixed_meshes(rng, count):
     return out
 
 
-def check_batch(snch, ms, rng, per_mesh=3000):
+def check_batch(snch, ms, rng, per_mesh=3000, options=None):
     b = snch.BatchedScene(ms)
     b.compute_silhouettes()
     b.build_bvh()
+    for k, val in (options or {}).items():
+        b.set_option(k, val)
     assert b.num_meshes == len(ms)
     mesh_ids, pts, flips, expect, tops = [], [], [], [], []
     for m, (v, f) in enumerate(ms):
@@ -110,6 +112,35 @@ def test_batched_many_meshes_ordered_batch(snch_mod):
         v, f, _ = meshes.icosphere(int(rng.integers(0, 3)), float(rng.uniform(0.1, 1)))
         ms.append(((v + rng.uniform(-1, 1, 3)).astype(np.float32), f.astype(np.int32)))
     check_batch(snch_mod, ms, rng, per_mesh=400)
+
+
+def test_batched_persistent_work_stealing(snch_mod):
+    """Persistent work-stealing searches (SNCH_OPT_PERSISTENT) on a batched scene:
+    per-mesh roots, empty and one-triangle meshes, results as single scenes give,
+    and bit for bit the one-thread-per-query searches' results."""
+    snch = snch_mod
+    rng = np.random.default_rng(3)
+    ms = mixed_meshes(rng, 18)
+    ms.insert(4, (np.zeros((0, 3), np.float32), np.zeros((0, 3), np.int32)))
+    ms.insert(7, (np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], np.float32), np.array([[0, 1, 2]], np.int32)))
+    b = check_batch(snch, ms, rng, per_mesh=2000, options={snch.OPT_PERSISTENT: 1})
+    n = 100_000
+    mesh = rng.integers(0, len(ms), n).astype(np.int32)
+    pts = rng.uniform(-3, 3, (n, 3)).astype(np.float32)
+    flip = (rng.random(n) < 0.5).astype(np.uint8)
+
+    def run():
+        out = list(b.query_nearest_batch(mesh, pts)) + list(b.query_silhouette_batch(mesh, pts, flip))
+        return [x.cpu().numpy() for x in out]
+
+    got = run()
+    b.set_option(snch.OPT_PERSISTENT, 0)
+    b.set_option(snch.OPT_PACKET, 0)
+    want = run()
+    for x, y in zip(got, want):
+        np.testing.assert_array_equal(x.view(np.uint8), y.view(np.uint8))
+    assert b.device_status() == 0
+    b.close()
 
 
 def test_batched_rejects_bad_input(snch_mod):

@@ -203,7 +203,7 @@ def test_block_size_same_results(snch, block):
     s = built_scene(snch, v, f)
     base = answers(s, pts, flip)
     s.set_option(snch.OPT_BLOCK, block)
-    assert s.search_config("nearest") == (2, block) and s.search_config("silhouette") == (2, block)
+    assert s.search_config("nearest")[:2] == (2, block) and s.search_config("silhouette")[:2] == (2, block)
     for x, y in zip(base, answers(s, pts, flip)):
         np.testing.assert_array_equal(y, x)
     with pytest.raises(snch.SnchError):
