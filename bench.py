@@ -715,15 +715,25 @@ def run_ours(args):
                     torch.empty(n["smp"], dtype=torch.float32).pin_memory().numpy()),
         }
 
+        e2e_parts = []
+
         def e2e_step():
+            t = [time.perf_counter()]
             s = snch.Scene(pin_v, pin_f)
             s.compute_silhouettes()
             s.build_bvh()
+            t.append(time.perf_counter())
             s.query_nearest_host(pin["near_pts"], out=hout["near"])
+            t.append(time.perf_counter())
             s.query_silhouette_host(pin["sil_pts"], pin["sil_flip"], out=hout["sil"])
+            t.append(time.perf_counter())
             s.query_ray_host(pin["ray_o"], pin["ray_d"], pin["ray_tmax"], out=hout["ray"])
+            t.append(time.perf_counter())
             s.sample_in_sphere_host(pin["smp_c"], pin["smp_r"], pin["smp_u"], out=hout["smp"])
+            t.append(time.perf_counter())
             s.close()
+            t.append(time.perf_counter())
+            e2e_parts.append([1e3 * (b_ - a_) for a_, b_ in zip(t, t[1:])])
 
         e2e_steps = max(1, min(args.steps, 3))
         e2e_step()
@@ -746,6 +756,8 @@ def run_ours(args):
         e2e = {"value": total_q * ws * e2e_steps / e2e_s, "unit": "queries/s", "h2d_bytes_per_step": int(h2d),
                "d2h_bytes_per_step": int(d2h), "steps": e2e_steps,
                "mismatches_vs_device_forms": mismatch,
+               "phase_ms": dict(zip(["create+build", "near", "sil", "ray", "smp", "close"],
+                                    np.round(np.mean(e2e_parts[1:], 0), 2).tolist())),
                "note": "scene upload + build + snch_*_host queries from pinned host memory, wall clock; "
                        "answers compared bit for bit with the device forms' answers of the timed step"}
 

@@ -211,11 +211,12 @@ int snch_set_traversal(snch_scene_t scene, int mode);
 #define SNCH_OPT_PACKET 12
 #define SNCH_OPT_PACKET_NEAREST 13
 #define SNCH_OPT_PACKET_SILHOUETTE 14
-/*   SNCH_OPT_HOST_CHUNK       queries per chunk of the *_host forms (default 2^24, at
- *                             most 29 bytes in and 17 out per query on each of two
- *                             streams): chunk i's input copy, search and output copy run
- *                             on stream i % 2, so copies overlap searches; a larger chunk
- *                             gives each Morton-ordered search a denser batch. */
+/*   SNCH_OPT_HOST_CHUNK       queries per chunk of the *_host forms (at most 29 bytes in
+ *                             and 17 out per query on each of two streams): chunk i's
+ *                             input copy, search and output copy run on stream i % 2, so
+ *                             copies overlap searches; a larger chunk gives each
+ *                             Morton-ordered search a denser batch. 0 (default): 2^24
+ *                             for nearest / silhouette, 2^22 for ray / sphere sample. */
 #define SNCH_OPT_HOST_CHUNK 15
 int snch_set_option(snch_scene_t scene, int option, int64_t value);
 /* current value of an option (SNCH_OPT_NODE_WIDTH / _BLOCK / _PACKET read the

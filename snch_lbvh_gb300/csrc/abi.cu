@@ -54,7 +54,10 @@ inline cudaStream_t S(snch_stream_t s) { return static_cast<cudaStream_t>(s); }
 constexpr size_t kSmallWords = 1056;
 constexpr size_t kWStatus = 1040, kWNumEdges = 1041, kWBad = 1042, kWHist = 8;
 
-constexpr int64_t kHostChunk = 1 << 24;  // queries per pipelined host-form chunk
+// queries per pipelined host-form chunk when SNCH_OPT_HOST_CHUNK is 0 (auto):
+// nearest / silhouette searches gain from a dense Morton-ordered batch, ray and
+// sphere-sample batches from copies that overlap the next chunk's search
+constexpr int64_t kHostChunkSearch = 1 << 24, kHostChunkRay = 1 << 22;
 
 struct HostStage
 {
@@ -88,7 +91,7 @@ struct snch_scene_s
     int traversal = SNCH_TRAVERSAL_NEAR_FIRST;
     int query_order = 1;             // Morton-sort batches of at least order_min queries
     int64_t order_min = 65536;
-    int64_t host_chunk = kHostChunk;  // queries per pipelined host-form chunk
+    int64_t host_chunk = 0;  // queries per pipelined host-form chunk; 0: per query type
     int persistent_near = 0, persistent_sil = 0;  // lane-refill (work-stealing) searches
     int64_t tail_cap = 0;            // near-first expansions before a query is deferred (0: off; measured slower)
     // batched scene (num_meshes > 0): independent meshes, one build, per-mesh queries
@@ -807,7 +810,8 @@ struct Field
 
 // Runs `body(chunk_begin, count, dev_in[], dev_out[], stream)` over chunks.
 template <typename Body>
-int run_host_pipeline(snch_scene_s *s, int64_t n, const Field *ins, int nin, const Field *outs, int nout, Body body)
+int run_host_pipeline(snch_scene_s *s, int64_t n, int64_t auto_chunk, const Field *ins, int nin, const Field *outs,
+                      int nout, Body body)
 {
     if (n == 0)
         return SNCH_OK;
@@ -816,7 +820,7 @@ int run_host_pipeline(snch_scene_s *s, int64_t n, const Field *ins, int nin, con
         in_per += ins[i].elem;
     for (int i = 0; i < nout; ++i)
         out_per += outs[i].elem;
-    const int64_t chunk = std::min<int64_t>(n, s->host_chunk);
+    const int64_t chunk = std::min<int64_t>(n, s->host_chunk > 0 ? s->host_chunk : auto_chunk);
     int rc = ensure_stage(s, in_per * chunk + 256 * nin, out_per * chunk + 256 * nout);
     if (rc != SNCH_OK)
         return rc;
@@ -968,8 +972,8 @@ int snch_set_option(snch_scene_t s, int option, int64_t value)
         s->order_min = value;
         return SNCH_OK;
     case SNCH_OPT_HOST_CHUNK:
-        if (value < 1024 || value >= (int64_t(1) << 30))
-            return fail(SNCH_ERR_INVALID_ARGUMENT, "SNCH_OPT_HOST_CHUNK must be in [1024, 2^30)");
+        if (value != 0 && (value < 1024 || value >= (int64_t(1) << 30)))
+            return fail(SNCH_ERR_INVALID_ARGUMENT, "SNCH_OPT_HOST_CHUNK must be 0 or in [1024, 2^30)");
         s->host_chunk = value;
         return SNCH_OK;
     case SNCH_OPT_TAIL_CAP:
@@ -1266,7 +1270,8 @@ int snch_query_nearest_host(snch_scene_t s, const float *pts, int64_t n, uint32_
         return rc;
     const Field ins[] = {{pts, nullptr, 12}};
     const Field outs[] = {{nullptr, idx, 4}, {nullptr, dist, 4}};
-    return run_host_pipeline(s, n, ins, 1, outs, 2, [&](int64_t m, void **di, void **dout, cudaStream_t st) {
+    return run_host_pipeline(s, n, kHostChunkSearch, ins, 1, outs, 2,
+                             [&](int64_t m, void **di, void **dout, cudaStream_t st) {
         BatchView b;
         cudaError_t e = batch_view(s, (const float *)di[0], m, st, b);
         return e != cudaSuccess ? e : launch_nearest(b.t, (const float *)di[0], m, (uint32_t *)dout[0],
@@ -1284,7 +1289,8 @@ int snch_query_silhouette_host(snch_scene_t s, const float *pts, const uint8_t *
         return rc;
     const Field ins[] = {{pts, nullptr, 12}, {flip, nullptr, 1}};
     const Field outs[] = {{nullptr, dist, 4}, {nullptr, edge, 4}};
-    return run_host_pipeline(s, n, ins, 2, outs, 2, [&](int64_t m, void **di, void **dout, cudaStream_t st) {
+    return run_host_pipeline(s, n, kHostChunkSearch, ins, 2, outs, 2,
+                             [&](int64_t m, void **di, void **dout, cudaStream_t st) {
         BatchView b;
         cudaError_t e = batch_view(s, (const float *)di[0], m, st, b);
         return e != cudaSuccess ? e : launch_silhouette(b.t, (const float *)di[0], (const uint8_t *)di[1], m,
@@ -1302,7 +1308,8 @@ int snch_query_ray_host(snch_scene_t s, const float *o, const float *d, const fl
         return rc;
     const Field ins[] = {{o, nullptr, 12}, {d, nullptr, 12}, {tmax, nullptr, 4}};
     const Field outs[] = {{nullptr, hit, 1}, {nullptr, t, 4}, {nullptr, uv, 8}, {nullptr, idx, 4}};
-    return run_host_pipeline(s, n, ins, 3, outs, 4, [&](int64_t m, void **di, void **dout, cudaStream_t st) {
+    return run_host_pipeline(s, n, kHostChunkRay, ins, 3, outs, 4,
+                             [&](int64_t m, void **di, void **dout, cudaStream_t st) {
         BatchView b;
         cudaError_t e = batch_view(s, (const float *)di[0], m, st, b);
         return e != cudaSuccess ? e
@@ -1322,7 +1329,8 @@ int snch_sample_in_sphere_host(snch_scene_t s, const float *c, const float *r, c
         return rc;
     const Field ins[] = {{c, nullptr, 12}, {r, nullptr, 4}, {u, nullptr, 4}};
     const Field outs[] = {{nullptr, idx, 4}, {nullptr, pdf, 4}};
-    return run_host_pipeline(s, n, ins, 3, outs, 2, [&](int64_t m, void **di, void **dout, cudaStream_t st) {
+    return run_host_pipeline(s, n, kHostChunkRay, ins, 3, outs, 2,
+                             [&](int64_t m, void **di, void **dout, cudaStream_t st) {
         BatchView b;
         cudaError_t e = batch_view(s, (const float *)di[0], m, st, b);
         return e != cudaSuccess ? e : launch_sample(b.t, (const float *)di[0], (const float *)di[1],
