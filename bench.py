@@ -11,9 +11,14 @@ and 16M ray queries and 4M SampleTriangleInSphere draws.
            ranks / max rank time; each rank runs the full step: weak scaling);
   e2e    = the same through the host-buffer C-ABI calls (scene upload, build,
            snch_*_host queries with their H2D/D2H copies) on pinned host memory;
-  roofline = algorithmic bytes of the dominant query kernel (visits counted by
-           the instrumented CPU restatement on a sample) / its event time;
+  roofline = algorithmic bytes of the dominant query kernel (reference record
+           sizes x the kernel's own per-query visit counts) / its event time;
   cpu_baseline = the CPU restatement (oracle/) on the host cores, bounded sample.
+
+Outside the timed step (single GPU): the learned radius on the same batches,
+the 20,480-triangle icosphere (1M nearest queries; learned radius on 16M
+points), 256 batched meshes (autotuned, graph-captured) and a 1M-walker
+walk-on-stars trace.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--scale F]
 """
@@ -60,6 +65,7 @@ def parse():
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-radius leg")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-meshes leg")
     ap.add_argument("--no-wost", action="store_true", help="skip the walk-on-stars leg")
+    ap.add_argument("--no-icosphere", action="store_true", help="skip the 20,480-triangle icosphere leg")
     return ap.parse_args()
 
 
@@ -320,6 +326,119 @@ def learned_on_reference_order(scene, model, dev, margin, mlp_ms, counts, sub=2_
     finally:
         scene.set_traversal(snch.TRAVERSAL_NEAR_FIRST)
     return out
+
+
+# --------------------------------------------------------------------- icosphere (configs 1 and 4)
+def time_events(fn, reps, stream):
+    """Mean milliseconds of fn() over reps runs after one warm-up, CUDA events."""
+    import torch
+    fn()
+    e = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    torch.cuda.synchronize()
+    e[0].record(stream)
+    for _ in range(reps):
+        fn()
+    e[1].record(stream)
+    torch.cuda.synchronize()
+    return e[0].elapsed_time(e[1]) / reps
+
+
+def l2_copy_gbs(stream, mb=24, reps=50):
+    """Copy bandwidth of a buffer pair that stays in L2 (read + write bytes / time)."""
+    import torch
+    a = torch.empty(mb << 20, dtype=torch.uint8, device="cuda")
+    b = torch.empty_like(a)
+    ms = time_events(lambda: b.copy_(a), reps, stream)
+    return 2 * a.numel() / (ms / 1e3) / 1e9
+
+
+def icosphere_leg(scale, n_plain=1_000_000, n_eval=16_000_000, reps=5):
+    """The 20,480-triangle noisy icosphere (level 5, radius 1, sigma 0.01): 1M
+    nearest queries uniform in its box x 1.2, both traversal orders (config 1;
+    the tree is L2-resident, so the algorithmic bytes are set against an L2 copy
+    bandwidth measured here), and the learned radius trained on 8M (point, exact
+    distance) pairs from the plain queries -- half uniform in the box, half within
+    0.05 of the surface -- evaluated on 16M fresh points: learned vs plain, both
+    traversal orders, identical results (config 4)."""
+    import torch
+    import snch_lbvh_gb300 as snch
+    from snch_lbvh_gb300 import meshes
+    from snch_lbvh_gb300.learned import LearnedRadius, targets_from_scene, training_points
+    stream = torch.cuda.current_stream()
+    v, f = meshes.noisy_icosphere(5, 1.0, 0.01, seed=0)
+    s = snch.Scene(torch.from_numpy(v).cuda(), torch.from_numpy(f).cuda())
+    s.compute_silhouettes()
+    s.build_bvh()
+    n1 = max(1024, int(n_plain * scale))
+    p1 = torch.from_numpy(meshes.box_queries(v, n1, 1.2, seed=1)).cuda()
+    res = {"workload": f"{len(f):,}-triangle noisy icosphere; {n1:,} nearest queries uniform in its box x 1.2"}
+    plain = {}
+    for name, mode in (("near_first", snch.TRAVERSAL_NEAR_FIRST), ("reference_order", snch.TRAVERSAL_REFERENCE_ORDER)):
+        s.set_traversal(mode)
+        ms = time_events(lambda: s.query_nearest(p1), reps, stream)
+        vis = s.query_visits("nearest", p1[: min(n1, 1_000_000)]).astype(np.float64).mean(0)
+        alg = 20 + 56 * vis[0] + 48 * vis[1]  # in/out + per expanded node + per leaf triangle
+        plain[name] = {"qps": n1 / (ms / 1e3), "ms": ms, "visits_per_query": vis[:2].tolist(),
+                       "algorithmic_bytes_per_query": float(alg), "achieved_GBs": n1 * alg / (ms / 1e3) / 1e9}
+    s.set_traversal(snch.TRAVERSAL_NEAR_FIRST)
+    l2 = l2_copy_gbs(stream)
+    for r in plain.values():
+        r["l2_frac"] = r["achieved_GBs"] / l2
+    res["nearest"] = plain
+    res["l2_copy_GBs"] = l2
+
+    # learned radius (config 4)
+    cfg = dict(LEARNED_TRAIN)
+    lo, hi = v.min(0), v.max(0)
+    c, h = (lo + hi) / 2, (hi - lo) / 2 * 1.2
+    nu, ns = max(4096, int(cfg["uniform"] * scale)), max(4096, int(cfg["surface"] * scale))
+    tp = torch.from_numpy(training_points(v, f, nu, ns, cfg["band"], lo=c - h, hi=c + h, seed=78)).cuda()
+    tgt = targets_from_scene(s, tp)
+    model = LearnedRadius(c - h, c + h, seed=4)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    loss = model.train(tp, tgt, epochs=cfg["epochs"], batch=cfg["batch"], lr=cfg["lr"], tau=cfg["tau"])
+    torch.cuda.synchronize()
+    res["training"] = {**cfg, "uniform": nu, "surface": ns, "final_loss": loss,
+                       "train_s": time.perf_counter() - t0}
+    del tp, tgt
+    ne = max(1024, int(n_eval * scale))
+    pe = torch.from_numpy(meshes.box_queries(v, ne, 1.2, seed=2)).cuda()
+    fe = (torch.arange(ne, device="cuda") % 2).to(torch.uint8)
+    learned = {}
+    for name, mode in (("near_first", snch.TRAVERSAL_NEAR_FIRST), ("reference_order", snch.TRAVERSAL_REFERENCE_ORDER)):
+        s.set_traversal(mode)
+        pn, ps = s.query_nearest(pe), s.query_silhouette(pe, fe)
+        plain_ms = [time_events(lambda: s.query_nearest(pe), reps, stream),
+                    time_events(lambda: s.query_silhouette(pe, fe), reps, stream)]
+        best = None
+        for margin in (1.1, 1.25, 1.5):
+            rn, rs = model.predict(pe, margin=margin, floor=1e-4)
+            nf = torch.zeros(2, dtype=torch.int32, device="cuda")
+            sn = s.query_nearest_seeded(pe, rn, num_fallback=nf[0:1])
+            ss = s.query_silhouette_seeded(pe, rs, fe, num_fallback=nf[1:2])
+            same = (torch.equal(sn[0], pn[0]) and torch.equal(sn[1].view(torch.int32), pn[1].view(torch.int32))
+                    and torch.equal(ss[0].view(torch.int32), ps[0].view(torch.int32)) and torch.equal(ss[1], ps[1]))
+            mlp_ms = time_events(lambda: model.predict(pe, margin=margin, floor=1e-4, out=(rn, rs)), reps, stream)
+            seeded_ms = [time_events(lambda: s.query_nearest_seeded(pe, rn), reps, stream),
+                         time_events(lambda: s.query_silhouette_seeded(pe, rs, fe), reps, stream)]
+            fb = nf.cpu().numpy() / ne
+            # the model predicts both radii in one pass: half its time is charged to each type
+            r = {"margin": margin, "near_qps": ne / ((seeded_ms[0] + mlp_ms / 2) / 1e3),
+                 "sil_qps": ne / ((seeded_ms[1] + mlp_ms / 2) / 1e3), "mlp_ms_both": mlp_ms,
+                 "fallback_frac": {"near": float(fb[0]), "sil": float(fb[1])}, "identical_to_plain": bool(same)}
+            if best is None or r["near_qps"] + r["sil_qps"] > best["near_qps"] + best["sil_qps"]:
+                best = r
+        best["plain_qps"] = {"near": ne / (plain_ms[0] / 1e3), "sil": ne / (plain_ms[1] / 1e3)}
+        best["speedup"] = {"near": best["near_qps"] / best["plain_qps"]["near"],
+                           "sil": best["sil_qps"] / best["plain_qps"]["sil"]}
+        learned[name] = best
+    s.set_traversal(snch.TRAVERSAL_NEAR_FIRST)
+    res["learned"] = {"eval_points": ne, **learned}
+    res["device_status"] = int(s.device_status())
+    model.close()
+    s.close()
+    return res
 
 
 # --------------------------------------------------------------------- batched meshes
@@ -689,8 +808,10 @@ def run_ours(args):
                               "sil": learned["sil_qps"] / per_type["sil"]}
         learned["status"] = int(scene.device_status())
 
-    # ---- batched meshes and walk-on-stars (single GPU only; outside the timed step)
-    batched = wost_res = None
+    # ---- icosphere, batched meshes and walk-on-stars (single GPU only; outside the timed step)
+    batched = wost_res = ico = None
+    if ws == 1 and not args.no_icosphere:
+        ico = icosphere_leg(args.scale)
     if ws == 1 and not args.no_batched:
         batched = batched_leg(args.scale)
     if ws == 1 and not args.no_wost:
@@ -807,6 +928,7 @@ def run_ours(args):
         "roofline": roof,
         "e2e": e2e,
         "learned": learned,
+        "icosphere": ico,
         "batched": batched,
         "wost": wost_res,
     }

@@ -636,26 +636,31 @@ int run_query(snch_scene_s *s, int kind, const float *pts, const float *radius, 
         SNCH_CUDA(launch(b.t, SeedArgs()));
         return SNCH_OK;
     }
+    // scratch: [counts][fail_flag][fail_list][list-building scratch][defer_list][defer_radius]
+    const size_t per = 4 * (size_t)n + 256;
+    const size_t fl_bytes = radius ? 2 * per + failed_list_scratch_bytes(n) + 256 : 0;
     char *scratch = nullptr;
-    const size_t lists = (radius ? 1 : 0) + (capped ? 3 : 0);
-    SNCH_CUDA(scratch_alloc(&scratch, 256 + lists * (4 * (size_t)n + 256), st));
-    uint32_t *fail_count = reinterpret_cast<uint32_t *>(scratch), *defer_count = fail_count + 1;
+    SNCH_CUDA(scratch_alloc(&scratch, 256 + fl_bytes + (capped ? 2 * per : 0), st));
+    uint32_t *defer_count = reinterpret_cast<uint32_t *>(scratch), *fail_count = defer_count + 1;
     char *next = scratch + 256;
-    auto take = [&]() {
+    auto take = [&](size_t bytes) {
         char *q = next;
-        next += 4 * (size_t)n + 256;
+        next += (bytes + 255) & ~size_t(255);
         return q;
     };
-    uint32_t *fail_list = radius ? reinterpret_cast<uint32_t *>(take()) : nullptr;
-    uint32_t *defer_list = capped ? reinterpret_cast<uint32_t *>(take()) : nullptr;
-    float *defer_radius = capped ? reinterpret_cast<float *>(take()) : nullptr;
+    uint32_t *fail_flag = radius ? reinterpret_cast<uint32_t *>(take(per)) : nullptr;
+    uint32_t *fail_list = radius ? reinterpret_cast<uint32_t *>(take(per)) : nullptr;
+    void *list_scratch = radius ? take(failed_list_scratch_bytes(n)) : nullptr;
+    uint32_t *defer_list = capped ? reinterpret_cast<uint32_t *>(take(per)) : nullptr;
+    float *defer_radius = capped ? reinterpret_cast<float *>(take(per)) : nullptr;
     cudaError_t e = cudaMemsetAsync(scratch, 0, 256, st);
+    if (e == cudaSuccess && radius)  // a deferred query's flag is written by the second pass
+        e = cudaMemsetAsync(fail_flag, 0, 4 * (size_t)n, st);
     if (e == cudaSuccess)
         e = batch_view(s, pts, n, st, b, query_mesh);
     SeedArgs s1;
     s1.radius = radius;
-    s1.fail_list = fail_list;
-    s1.fail_count = radius ? fail_count : nullptr;
+    s1.fail_flag = fail_flag;
     if (capped)
     {
         s1.cap = (uint32_t)s->tail_cap;
@@ -673,17 +678,19 @@ int run_query(snch_scene_s *s, int kind, const float *pts, const float *radius, 
         t2.order_coherent = 0;
         SeedArgs s2;
         s2.radius = defer_radius;
-        s2.fail_list = fail_list;
-        s2.fail_count = radius ? fail_count : nullptr;
+        s2.fail_flag = fail_flag;
         e = launch(t2, s2);
     }
     if (e == cudaSuccess && radius)
     {
+        // the fallback pass runs the failed queries in the batch's own (Morton)
+        // order, so its warps stay as coherent as the batch's
+        e = launch_failed_list(b.t.order, fail_flag, n, fail_list, fail_count, list_scratch, b.t.status, st);
         TreeView t3 = b.t;
         t3.order = fail_list;
         t3.order_count = fail_count;
-        t3.order_coherent = 0;
-        e = launch(t3, SeedArgs());
+        if (e == cudaSuccess)
+            e = launch(t3, SeedArgs());
     }
     if (e == cudaSuccess && num_fallback)
         e = cudaMemcpyAsync(num_fallback, fail_count, 4, cudaMemcpyDeviceToDevice, st);

@@ -182,12 +182,11 @@ SNCH_DEV QueryRoot query_root(const TreeView &t, int64_t q)
 }
 
 // Seeded search: per-query initial radius, and where queries that find
-// nothing inside it are listed for the unbounded fallback pass.
+// nothing inside it are marked for the unbounded fallback pass.
 struct SeedArgs
 {
     const float *radius = nullptr;   // nullptr: unbounded
-    uint32_t *fail_list = nullptr;   // query indices with an empty seeded result (finite radius)
-    uint32_t *fail_count = nullptr;
+    uint32_t *fail_flag = nullptr;   // per query index: 1 = empty seeded result (finite radius)
     // Tail cap (near-first kernels): a query still searching after `cap` node
     // expansions stops, writes the distance of the best candidate it has (an
     // upper bound of its answer; +inf if none) to defer_radius[q] and is listed

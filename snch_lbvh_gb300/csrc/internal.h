@@ -137,6 +137,11 @@ cudaError_t launch_sample(const TreeView &t, const float *c, const float *r, con
 cudaError_t launch_enumerate(const TreeView &t, bool line, const float *q0, const float *q1, int64_t n,
                              uint32_t max_out, uint32_t *idx, float *tt, uint32_t *count, cudaStream_t st);
 // Morton-sorted order of a query batch (thread i answers query order[i]);
+// The queries of a seeded batch whose fail_flag is set, listed in batch order
+// (order[i], or i without an order) with their count, all on the device.
+size_t failed_list_scratch_bytes(int64_t n);
+cudaError_t launch_failed_list(const uint32_t *order, const uint32_t *fail_flag, int64_t n, uint32_t *list,
+                               uint32_t *count, void *scratch, uint32_t *status, cudaStream_t st);
 // scratch holds query_order_scratch_bytes(n) bytes and owns *order.
 size_t query_order_scratch_bytes(int64_t n);
 cudaError_t launch_query_order(const TreeView &t, const float *pts, int64_t n, void *scratch, uint32_t **order,

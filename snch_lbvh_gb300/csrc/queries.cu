@@ -181,8 +181,8 @@ __global__ void __launch_bounds__(128) nearest_kernel(TreeView t, const float *_
         best = INFINITY;  // nothing within the seed radius: the fallback pass answers it
     out_idx[q] = nearest;
     out_dist[q] = sqrtf(best);
-    if (seed.fail_list)
-        append_failed(seed.fail_list, seed.fail_count, (uint32_t)q, nearest == kInvalid);
+    if (seed.fail_flag)
+        seed.fail_flag[q] = nearest == kInvalid ? 1u : 0u;
 }
 
 // ------------------------------------------------------------------ silhouette
@@ -544,8 +544,8 @@ __global__ void __launch_bounds__(128) silhouette_kernel(TreeView t, const float
     out_dist[q] = best;
     if (out_edge)
         out_edge[q] = best_edge;
-    if (seed.fail_list)
-        append_failed(seed.fail_list, seed.fail_count, (uint32_t)q, best_edge < 0);
+    if (seed.fail_flag)
+        seed.fail_flag[q] = best_edge < 0 ? 1u : 0u;
 }
 
 // ------------------------------------------------------------------ near-first forms
@@ -722,8 +722,8 @@ __global__ void __launch_bounds__(kBlock, 1280 / kBlock) nearest_fast_kernel(Tre
         best = INFINITY;  // nothing within the seed radius: the fallback pass answers it
     out_idx[q] = nearest == kInvalid ? kInvalid : nearest - qr.tri_off;
     out_dist[q] = sqrtf(best);
-    if (seed.fail_list)
-        append_failed(seed.fail_list, seed.fail_count, (uint32_t)q, failed);
+    if (seed.fail_flag)
+        seed.fail_flag[q] = failed ? 1u : 0u;
 }
 
 // one leaf of the silhouette query; key = rank * 4 + slot orders candidates
@@ -934,8 +934,8 @@ __global__ void __launch_bounds__(kBlock, 1152 / kBlock) silhouette_fast_kernel(
     out_dist[q] = best;
     if (out_edge)
         out_edge[q] = best_edge < 0 ? best_edge : best_edge - qr.edge_off;
-    if (seed.fail_list)
-        append_failed(seed.fail_list, seed.fail_count, (uint32_t)q, failed);
+    if (seed.fail_flag)
+        seed.fail_flag[q] = failed ? 1u : 0u;
     if (kStats)
     {
         stats[3 * q] = n_int;
@@ -1221,8 +1221,8 @@ __global__ void __launch_bounds__(128, SNCH_WIDE_MIN_BLOCKS)
         best = INFINITY;  // nothing within the seed radius: the fallback pass answers it
     out_idx[q] = nearest == kInvalid ? kInvalid : nearest - qr.tri_off;
     out_dist[q] = sqrtf(best);
-    if (seed.fail_list)
-        append_failed(seed.fail_list, seed.fail_count, (uint32_t)q, failed);
+    if (seed.fail_flag)
+        seed.fail_flag[q] = failed ? 1u : 0u;
 }
 
 template <int W, bool kStats>
@@ -1345,8 +1345,8 @@ __global__ void __launch_bounds__(128, SNCH_WIDE_MIN_BLOCKS)
     out_dist[q] = best;
     if (out_edge)
         out_edge[q] = best_edge < 0 ? best_edge : best_edge - qr.edge_off;
-    if (seed.fail_list)
-        append_failed(seed.fail_list, seed.fail_count, (uint32_t)q, failed);
+    if (seed.fail_flag)
+        seed.fail_flag[q] = failed ? 1u : 0u;
     if (kStats)
     {
         stats[3 * q] = n_int;
@@ -1511,8 +1511,8 @@ __global__ void __launch_bounds__(128, 10) nearest_packet_kernel(TreeView t, con
         best = INFINITY;  // nothing within the seed radius: the fallback pass answers it
     out_idx[q] = nearest == kInvalid ? kInvalid : nearest - qr.tri_off;
     out_dist[q] = sqrtf(best);
-    if (seed.fail_list)
-        append_failed(seed.fail_list, seed.fail_count, (uint32_t)q, failed);
+    if (seed.fail_flag)
+        seed.fail_flag[q] = failed ? 1u : 0u;
 }
 
 template <bool kStats>
@@ -1651,8 +1651,8 @@ __global__ void __launch_bounds__(128, 9) silhouette_packet_kernel(TreeView t, c
     out_dist[q] = best;
     if (out_edge)
         out_edge[q] = best_edge < 0 ? best_edge : best_edge - qr.edge_off;
-    if (seed.fail_list)
-        append_failed(seed.fail_list, seed.fail_count, (uint32_t)q, failed);
+    if (seed.fail_flag)
+        seed.fail_flag[q] = failed ? 1u : 0u;
     if (kStats)
     {
         stats[3 * q] = n_int;
@@ -1851,8 +1851,8 @@ __global__ void __launch_bounds__(128) silhouette_persistent_kernel(TreeView t, 
             out_dist[s.q] = s.best;
             if (out_edge)
                 out_edge[s.q] = s.best_edge < 0 ? s.best_edge : s.best_edge - s.edge_off;
-            if (kSeed && seed.fail_list)
-                append_failed(seed.fail_list, seed.fail_count, (uint32_t)s.q, s.best_edge < 0);
+            if (kSeed && seed.fail_flag)
+                seed.fail_flag[s.q] = s.best_edge < 0 ? 1u : 0u;
             active = false;
         }
     }
@@ -1969,8 +1969,8 @@ __global__ void __launch_bounds__(128) nearest_persistent_kernel(TreeView t, con
                 best = INFINITY;  // nothing within the seed radius: the fallback pass answers it
             out_idx[q] = nearest == kInvalid ? kInvalid : nearest - tri_off;
             out_dist[q] = sqrtf(best);
-            if (kSeed && seed.fail_list)
-                append_failed(seed.fail_list, seed.fail_count, (uint32_t)q, nearest == kInvalid);
+            if (kSeed && seed.fail_flag)
+                seed.fail_flag[q] = nearest == kInvalid ? 1u : 0u;
             active = false;
         }
     }
@@ -2694,6 +2694,43 @@ cudaError_t launch_query_order(const TreeView &t, const float *pts, int64_t n, v
     return e;
 }
 size_t query_order_scratch_bytes(int64_t n) { return 16 * (size_t)n + sort_scratch_bytes((uint32_t)n, 32) + 256; }
+
+// ---- the fallback list of a seeded batch, in the batch's own order
+// g[i] = fail_flag of the i-th query in batch order; list = those queries, in order
+__global__ void gather_fail_flags_kernel(const uint32_t *__restrict__ order, const uint32_t *__restrict__ flag,
+                                         uint32_t n, uint32_t *__restrict__ g)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n)
+        g[i] = flag[order ? order[i] : i];
+}
+__global__ void compact_failed_kernel(const uint32_t *__restrict__ order, const uint32_t *__restrict__ g,
+                                      const uint32_t *__restrict__ pos, uint32_t n, uint32_t *__restrict__ list)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n && g[i])
+        list[pos[i]] = order ? order[i] : i;
+}
+size_t failed_list_scratch_bytes(int64_t n) { return 8 * (size_t)n + scan_flags_scratch_bytes((uint64_t)n) + 256; }
+cudaError_t launch_failed_list(const uint32_t *order, const uint32_t *fail_flag, int64_t n, uint32_t *list,
+                               uint32_t *count, void *scratch, uint32_t *status, cudaStream_t st)
+{
+    if (n <= 0)
+        return cudaMemsetAsync(count, 0, 4, st);
+    uint32_t *g = static_cast<uint32_t *>(scratch), *pos = g + n;
+    void *scan_scratch = pos + n;
+    const unsigned grid = (unsigned)((n + 255) / 256);
+    gather_fail_flags_kernel<<<grid, 256, 0, st>>>(order, fail_flag, (uint32_t)n, g);
+    note_launch();
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess)
+        e = scan_flags(g, pos, (uint32_t)n, count, scan_scratch, status, st);
+    if (e != cudaSuccess)
+        return e;
+    compact_failed_kernel<<<grid, 256, 0, st>>>(order, g, pos, (uint32_t)n, list);
+    note_launch();
+    return cudaGetLastError();
+}
 
 cudaError_t launch_sample_point(const float *verts, const int32_t *tris, uint32_t num_tris, const int32_t *idx,
                                 const float *u, const float *v, int64_t n, float *out, cudaStream_t st)
