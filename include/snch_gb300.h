@@ -318,7 +318,7 @@ int snch_batch_query_silhouette(snch_scene_t scene, const int32_t *mesh, const f
 
 /* Autotuner (no reference counterpart): times this scene's nearest and
  * silhouette searches in SNCH_AUTOTUNE_CONFIGS configurations -- (node width,
- * threads per block, SNCH_OPT_PACKET, SNCH_OPT_PERSISTENT) = (2, 128, 2, 0)
+ * threads per block, SNCH_OPT_PACKET, SNCH_OPT_PERSISTENT) = (2, 128, 1, 0)
  * [warp packets: 32 queries per traversal], (2, 128, 0, 0), (4, 128, 0, 0),
  * (8, 128, 0, 0), (2, 64, 0, 0), (2, 256, 0, 0) [one query per traversal],
  * (2, 128, 0, 1) [persistent work-stealing lanes] -- on caller sample batches

@@ -261,7 +261,7 @@ class Scene:
 
     # (node width, threads per block, OPT_PACKET, OPT_PERSISTENT): warp packets, one query
     # per traversal, persistent work-stealing lanes
-    AUTOTUNE_CONFIGS = ((2, 128, 2, 0), (2, 128, 0, 0), (4, 128, 0, 0), (8, 128, 0, 0), (2, 64, 0, 0),
+    AUTOTUNE_CONFIGS = ((2, 128, 1, 0), (2, 128, 0, 0), (4, 128, 0, 0), (8, 128, 0, 0), (2, 64, 0, 0),
                         (2, 256, 0, 0), (2, 128, 0, 1))
 
     def autotune(self, near_points=None, sil_points=None, sil_flip=None, near_mesh=None, sil_mesh=None,

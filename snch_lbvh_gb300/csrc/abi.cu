@@ -101,6 +101,13 @@ struct snch_scene_s
     int32_t *mesh_edge_start = nullptr;
     cudaStream_t pipe[2] = {nullptr, nullptr};
     HostStage stage;
+    // Fallback fraction of the last seeded nearest [0] / silhouette [1] call,
+    // read back without a synchronisation: the count is copied to pinned host
+    // memory behind an event and taken at a later call once the event is done.
+    float fallback_frac[2] = {0.0f, 0.0f};
+    uint32_t *fallback_host = nullptr;  // pinned: [kind] = fallback count
+    cudaEvent_t fallback_event[2] = {nullptr, nullptr};
+    int64_t fallback_pending[2] = {0, 0};  // batch size whose count is in flight
     // node width of the near-first nearest / silhouette searches (2, 4 or 8)
     // and the wide records of the built tree: [0] 4-way, [1] 8-way
     int width_near = 2, width_sil = 2;
@@ -323,6 +330,11 @@ void free_scene(snch_scene_s *s)
     for (cudaStream_t st : s->pipe)
         if (st)
             cudaStreamDestroy(st);
+    for (cudaEvent_t ev : s->fallback_event)
+        if (ev)
+            cudaEventDestroy(ev);
+    if (s->fallback_host)
+        cudaFreeHost(s->fallback_host);
     delete s;
 }
 
@@ -616,6 +628,51 @@ cudaError_t batch_view(const snch_scene_s *s, const float *keys_from, int64_t n,
     return e;
 }
 
+// Fallback lists of at least this fraction of their batch run as warp packets
+// (when the batch itself qualifies): measured on the 2M-triangle scene (3.3 %
+// silhouette fallbacks: packets x1.08) and the 20,480-triangle sphere (5.5 %:
+// x1.5), against a walk-on-stars trace (0.08 %: packets x0.86 overall).
+constexpr float kPacketFallbackMinFrac = 0.01f;
+
+// Takes the count of an earlier seeded call of this kind if it has arrived
+// (never waits for it).
+void refresh_fallback_frac(snch_scene_s *s, int kind)
+{
+    if (s->fallback_pending[kind] <= 0)
+        return;
+    if (cudaEventQuery(s->fallback_event[kind]) != cudaSuccess)
+    {
+        cudaGetLastError();  // cudaErrorNotReady is not an error
+        return;
+    }
+    s->fallback_frac[kind] = (float)s->fallback_host[kind] / (float)s->fallback_pending[kind];
+    s->fallback_pending[kind] = 0;
+}
+
+// Queues the copy of this call's fallback count to pinned host memory (not
+// under stream capture, and not while an earlier copy is still in flight).
+cudaError_t queue_fallback_count(snch_scene_s *s, int kind, const uint32_t *count, int64_t n, cudaStream_t st)
+{
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaError_t e = cudaStreamIsCapturing(st, &cs);
+    if (e != cudaSuccess || cs != cudaStreamCaptureStatusNone || n <= 0 || s->fallback_pending[kind] > 0)
+        return e;
+    if (!s->fallback_host)
+    {
+        if ((e = cudaHostAlloc(reinterpret_cast<void **>(&s->fallback_host), 2 * sizeof(uint32_t),
+                               cudaHostAllocDefault)) != cudaSuccess)
+            return e;
+        s->fallback_host[0] = s->fallback_host[1] = 0;
+    }
+    if (!s->fallback_event[kind] &&
+        (e = cudaEventCreateWithFlags(&s->fallback_event[kind], cudaEventDisableTiming)) != cudaSuccess)
+        return e;
+    if ((e = cudaMemcpyAsync(s->fallback_host + kind, count, 4, cudaMemcpyDeviceToHost, st)) != cudaSuccess)
+        return e;
+    s->fallback_pending[kind] = n;
+    return cudaEventRecord(s->fallback_event[kind], st);
+}
+
 // One nearest / silhouette batch in up to three passes:
 //   1. the batch (Morton-ordered), seeded with `radius` if given, near-first
 //      searches capped at tail_cap expansions (the long ones are deferred with
@@ -683,14 +740,24 @@ int run_query(snch_scene_s *s, int kind, const float *pts, const float *radius, 
     }
     if (e == cudaSuccess && radius)
     {
-        // the fallback pass runs the failed queries in the batch's own (Morton)
-        // order, so its warps stay as coherent as the batch's
+        // The fallback pass runs the failed queries in the batch's own (Morton)
+        // order. Failures that cluster (a few percent of a batch, e.g. points
+        // far inside a closed mesh) keep neighbouring queries in a warp and run
+        // as warp packets; sparse ones (a fraction of a percent spread over the
+        // batch) run one search per lane, where packets lose. The fraction is
+        // the previous seeded call's of this kind (the current one is known
+        // only on the device).
         e = launch_failed_list(b.t.order, fail_flag, n, fail_list, fail_count, list_scratch, b.t.status, st);
         TreeView t3 = b.t;
         t3.order = fail_list;
         t3.order_count = fail_count;
+        refresh_fallback_frac(s, kind);
+        if (s->fallback_frac[kind] < kPacketFallbackMinFrac)
+            t3.order_coherent = 0;
         if (e == cudaSuccess)
             e = launch(t3, SeedArgs());
+        if (e == cudaSuccess)
+            e = queue_fallback_count(s, kind, fail_count, n, st);
     }
     if (e == cudaSuccess && num_fallback)
         e = cudaMemcpyAsync(num_fallback, fail_count, 4, cudaMemcpyDeviceToDevice, st);
@@ -1735,12 +1802,12 @@ int snch_autotune(snch_scene_t s, const int32_t *near_mesh, const float *near_pt
         return rc;
     cudaStream_t st = S(stream);
     // candidates (node width, threads per block, SNCH_OPT_PACKET, SNCH_OPT_PERSISTENT):
-    // warp packets (2: for Morton-ordered batches, as the sample is), one search
-    // per lane, or persistent work-stealing lanes; the block size applies to the
-    // per-lane binary searches
+    // warp packets (1: whatever the sample's size), one search per lane, or
+    // persistent work-stealing lanes; the block size applies to the per-lane
+    // binary searches
     constexpr int kConfigs = SNCH_AUTOTUNE_CONFIGS;
     const int cw[kConfigs] = {2, 2, 4, 8, 2, 2, 2}, cb[kConfigs] = {128, 128, 128, 128, 64, 256, 128},
-              cp[kConfigs] = {2, 0, 0, 0, 0, 0, 0}, cr[kConfigs] = {0, 0, 0, 0, 0, 0, 1};
+              cp[kConfigs] = {1, 0, 0, 0, 0, 0, 0}, cr[kConfigs] = {0, 0, 0, 0, 0, 0, 1};
     float ms[2][kConfigs] = {};
     char *out = nullptr;
     const int64_t nmax = std::max<int64_t>(1, std::max(n_near, n_sil));
