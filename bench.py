@@ -801,6 +801,13 @@ def run_ours(args):
                                   dev["smp_u"][:m["smp"]]).mean(0),
     }
 
+    # ---- the occlusion form of the ray query (ray_intersect<TestOnly = true>) on the
+    # same rays, outside the timed step; its hit flags equal the timed step's
+    ray_test_ms = time_events(lambda: scene.query_ray_test(dev["ray_o"], dev["ray_d"], dev["ray_tmax"]), 3, stream)
+    ray_test = {"qps": counts["ray"] / (ray_test_ms / 1e3), "ms": ray_test_ms,
+                "same_hits": bool(torch.equal(scene.query_ray_test(dev["ray_o"], dev["ray_d"], dev["ray_tmax"]),
+                                              out["ray"][0]))}
+
     # ---- learned radius vs plain on the same batches (outside the timed step)
     learned = None
     if not args.no_learned:
@@ -923,6 +930,7 @@ def run_ours(args):
                    "l2": "inputs larger than L2: 192 MB per 16M-query array, >1 GB of tree records",
                    "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
         "per_type_qps": {k: float(v) for k, v in per_type.items()},
+        "ray_test": ray_test,
         "phase_ms": {"build": float(phase_ms[0]), **{k: float(phase_ms[1 + i]) for i, k in enumerate(kinds)}},
         "gpu_launches": int(launches),
         "device_status": int(status),

@@ -266,6 +266,11 @@ int snch_query_line(snch_scene_t scene, const float *origins, const float *dirs,
 int snch_query_ray(snch_scene_t scene, const float *origins_xyz, const float *dirs_xyz, const float *tmax,
                    int64_t n, uint8_t *out_hit, float *out_t, float *out_uv, uint32_t *out_index,
                    snch_stream_t stream);
+/* the same with ray_intersect<TestOnly = true> (query.cuh:117-121): an occlusion
+ * test that stops at the first hit it accepts -> out_hit only (equal to
+ * snch_query_ray's hit flag) */
+int snch_query_ray_test(snch_scene_t scene, const float *origins_xyz, const float *dirs_xyz, const float *tmax,
+                        int64_t n, uint8_t *out_hit, snch_stream_t stream);
 
 /* sample_object_in_sphere(bvh, sphere_intersect(sphere(c, r)), intersect_sphere(),
  * measurement_getter(), green_weight(), u) sample.cuh:26-91 -> (object index or -1,
@@ -394,6 +399,8 @@ int snch_scene2_query_silhouette(snch_scene2_t scene, const float *points_xy, co
 int snch_scene2_query_ray(snch_scene2_t scene, const float *origins_xy, const float *dirs_xy, const float *tmax,
                           int64_t n, uint8_t *out_hit, float *out_t, float *out_segment_param, uint32_t *out_index,
                           snch_stream_t stream);
+int snch_scene2_query_ray_test(snch_scene2_t scene, const float *origins_xy, const float *dirs_xy, const float *tmax,
+                               int64_t n, uint8_t *out_hit, snch_stream_t stream);
 int snch_scene2_sample_in_circle(snch_scene2_t scene, const float *centers_xy, const float *radii, const float *u,
                                  int64_t n, int32_t *out_index, float *out_pdf, snch_stream_t stream);
 int snch_scene2_sample_on_object(snch_scene2_t scene, const int32_t *index, const float *u, int64_t n,

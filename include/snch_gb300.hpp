@@ -110,6 +110,12 @@ class scene3
     {
         check(snch_query_ray(h_, origins_xyz, dirs_xyz, tmax, n, hit, t, uv, index, stream));
     }
+    // ray_intersect<TestOnly = true>: occlusion test, hit flags only
+    void query_ray_test(const float *origins_xyz, const float *dirs_xyz, const float *tmax, int64_t n, uint8_t *hit,
+                        snch_stream_t stream = nullptr) const
+    {
+        check(snch_query_ray_test(h_, origins_xyz, dirs_xyz, tmax, n, hit, stream));
+    }
     void sample_in_sphere(const float *centers_xyz, const float *radii, const float *u, int64_t n, int32_t *index,
                           float *pdf, snch_stream_t stream = nullptr) const
     {
@@ -258,6 +264,11 @@ class scene2
                    float *t, float *segment_param, uint32_t *index, snch_stream_t stream = nullptr) const
     {
         check(snch_scene2_query_ray(h_, origins_xy, dirs_xy, tmax, n, hit, t, segment_param, index, stream));
+    }
+    void query_ray_test(const float *origins_xy, const float *dirs_xy, const float *tmax, int64_t n, uint8_t *hit,
+                        snch_stream_t stream = nullptr) const
+    {
+        check(snch_scene2_query_ray_test(h_, origins_xy, dirs_xy, tmax, n, hit, stream));
     }
     void sample_in_circle(const float *centers_xy, const float *radii, const float *u, int64_t n, int32_t *index,
                           float *pdf, snch_stream_t stream = nullptr) const

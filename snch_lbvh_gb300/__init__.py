@@ -370,6 +370,16 @@ class Scene:
                                    _stream(stream)))
         return hit, t, uv, idx
 
+    def query_ray_test(self, origins, dirs, tmax, stream=None, out=None):
+        """ray_intersect<TestOnly = true> query.cuh:117-121: occlusion test -> hit uint8."""
+        torch = _torch()
+        o, d = _dev(origins, torch.float32, 3), _dev(dirs, torch.float32, 3)
+        tm = _dev(tmax, torch.float32)
+        n = o.shape[0]
+        hit = out if out is not None else torch.empty(n, dtype=torch.uint8, device="cuda")
+        check(lib().snch_query_ray_test(self._h, _ptr(o), _ptr(d), _ptr(tm), n, _ptr(hit), _stream(stream)))
+        return hit
+
     def sample_in_sphere(self, centers, radii, u, stream=None, out=None):
         """sample_object_in_sphere sample.cuh:26 -> (index or -1, pdf)."""
         torch = _torch()
@@ -625,6 +635,15 @@ class Scene2:
         check(lib().snch_scene2_query_ray(self._h, _ptr(o), _ptr(d), _ptr(tm), n, _ptr(hit), _ptr(t), _ptr(sp),
                                           _ptr(idx), _stream(stream)))
         return hit, t, sp, idx
+
+    def query_ray_test(self, origins, dirs, tmax, stream=None):
+        """ray_intersect<TestOnly = true> over segments -> hit uint8."""
+        torch = _torch()
+        o, d, tm = _dev(origins, torch.float32, 2), _dev(dirs, torch.float32, 2), _dev(tmax, torch.float32)
+        hit = torch.empty(o.shape[0], dtype=torch.uint8, device="cuda")
+        check(lib().snch_scene2_query_ray_test(self._h, _ptr(o), _ptr(d), _ptr(tm), o.shape[0], _ptr(hit),
+                                               _stream(stream)))
+        return hit
 
     def sample_in_circle(self, centers, radii, u, stream=None):
         torch = _torch()

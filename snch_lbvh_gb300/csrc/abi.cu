@@ -1301,6 +1301,20 @@ int snch_query_ray(snch_scene_t s, const float *o, const float *d, const float *
     return SNCH_OK;
 }
 
+int snch_query_ray_test(snch_scene_t s, const float *o, const float *d, const float *tmax, int64_t n, uint8_t *hit,
+                        snch_stream_t stream)
+{
+    int rc = check_built(s);
+    if (rc == SNCH_OK)
+        rc = check_n(n, {o, d, tmax, hit});
+    if (rc != SNCH_OK)
+        return rc;
+    BatchView b;
+    SNCH_CUDA(batch_view(s, o, n, S(stream), b));
+    SNCH_CUDA(launch_ray_test(b.t, o, d, tmax, n, hit, S(stream)));
+    return SNCH_OK;
+}
+
 int snch_sample_in_sphere(snch_scene_t s, const float *c, const float *r, const float *u, int64_t n, int32_t *idx,
                           float *pdf, snch_stream_t stream)
 {

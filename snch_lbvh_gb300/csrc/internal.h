@@ -130,6 +130,8 @@ cudaError_t launch_silhouette(const TreeView &t, const float *pts, const uint8_t
 cudaError_t launch_cone_filter_check(int64_t n, uint64_t seed, unsigned long long *counts, cudaStream_t st);
 cudaError_t launch_ray(const TreeView &t, const float *o, const float *d, const float *tmax, int64_t n, uint8_t *hit,
                        float *tt, float *uv, uint32_t *idx, cudaStream_t st, uint32_t *stats = nullptr);
+cudaError_t launch_ray_test(const TreeView &t, const float *o, const float *d, const float *tmax, int64_t n,
+                            uint8_t *hit, cudaStream_t st);
 cudaError_t launch_sample(const TreeView &t, const float *c, const float *r, const float *u, int64_t n, int32_t *idx,
                           float *pdf, cudaStream_t st, uint32_t *stats = nullptr);
 // overlap (line = false: q0 = boxes, lower xyz + upper xyz) / line (q0 = origins,

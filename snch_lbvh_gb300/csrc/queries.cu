@@ -2026,7 +2026,11 @@ SNCH_DEV bool ray_triangle(f3 o, f3 dir, f3 v0, f3 v1, f3 v2, float &t, float &u
     return false;
 }
 
-template <bool kStats>
+// kAny: query_ray_intersect<TestOnly = true> (query.cuh:117-121): stop at the
+// first accepted hit of the same traversal and report only whether there is one
+// (always the hit flag of the closest-hit search: both take the same path up to
+// that hit); t, uv and idx are not written.
+template <bool kStats, bool kAny = false>
 __global__ void __launch_bounds__(128) ray_kernel(TreeView t, const float *__restrict__ origins,
                                                   const float *__restrict__ dirs, const float *__restrict__ tmaxs,
                                                   int64_t n, uint8_t *__restrict__ out_hit, float *__restrict__ out_t,
@@ -2073,6 +2077,8 @@ __global__ void __launch_bounds__(128) ray_kernel(TreeView t, const float *__res
                     bu = uu;
                     bv = vv;
                     nearest = orig;
+                    if (kAny)
+                        break;
                 }
                 next = false;
             }
@@ -2129,6 +2135,8 @@ __global__ void __launch_bounds__(128) ray_kernel(TreeView t, const float *__res
         }
     }
     out_hit[q] = found ? 1 : 0;
+    if (kAny)
+        return;
     out_t[q] = min_dist;
     out_uv[2 * q] = bu;
     out_uv[2 * q + 1] = bv;
@@ -2657,6 +2665,16 @@ cudaError_t launch_ray(const TreeView &t, const float *o, const float *d, const 
         ray_kernel<true><<<grid_for(n, 128), 128, 0, st>>>(t, o, d, tmax, n, hit, tt, uv, idx, stats);
     else
         ray_kernel<false><<<grid_for(n, 128), 128, 0, st>>>(t, o, d, tmax, n, hit, tt, uv, idx, nullptr);
+    note_launch();
+    return cudaGetLastError();
+}
+cudaError_t launch_ray_test(const TreeView &t, const float *o, const float *d, const float *tmax, int64_t n,
+                            uint8_t *hit, cudaStream_t st)
+{
+    if (n <= 0)
+        return cudaSuccess;
+    ray_kernel<false, true><<<grid_for(n, 128), 128, 0, st>>>(t, o, d, tmax, n, hit, nullptr, nullptr, nullptr,
+                                                               nullptr);
     note_launch();
     return cudaGetLastError();
 }

@@ -702,7 +702,10 @@ SNCH_DEV bool ray_segment(float2 o, float2 dir, float2 p0, float2 p1, float &t, 
     }
     return false;
 }
-// query_device(ray_intersect) query.cuh:82-169 over segments, the reference's order
+// query_device(ray_intersect) query.cuh:82-169 over segments, the reference's order;
+// kAny: TestOnly = true (query.cuh:117-121), stop at the first accepted hit and
+// write only the hit flag
+template <bool kAny = false>
 __global__ void __launch_bounds__(128) ray2_kernel(Tree2 t, const float *__restrict__ origins,
                                                    const float *__restrict__ dirs, const float *__restrict__ tmaxs,
                                                    int64_t n, uint8_t *__restrict__ out_hit, float *__restrict__ out_t,
@@ -742,6 +745,8 @@ __global__ void __launch_bounds__(128) ray2_kernel(Tree2 t, const float *__restr
                     found = true;
                     bs = ss;
                     nearest = obj;
+                    if (kAny)
+                        break;
                 }
                 continue;
             }
@@ -786,6 +791,8 @@ __global__ void __launch_bounds__(128) ray2_kernel(Tree2 t, const float *__restr
         } while (sp > 0);
     }
     out_hit[q] = found ? 1 : 0;
+    if (kAny)
+        return;
     out_t[q] = min_dist;
     out_s[q] = bs;
     out_idx[q] = nearest;
@@ -1146,6 +1153,19 @@ int snch_scene2_query_ray(snch_scene2_t s, const float *origins, const float *di
     if (rc != SNCH_OK || n == 0)
         return rc;
     ray2_kernel<<<blocks(n, 128), 128, 0, S2(stream)>>>(s->tree(), origins, dirs, tmax, n, hit, t, seg_param, idx);
+    note_launch();
+    SNCH2_CUDA(cudaGetLastError());
+    return SNCH_OK;
+}
+
+int snch_scene2_query_ray_test(snch_scene2_t s, const float *origins, const float *dirs, const float *tmax,
+                               int64_t n, uint8_t *hit, snch_stream_t stream)
+{
+    int rc = check2(s, n, {origins, dirs, tmax, hit});
+    if (rc != SNCH_OK || n == 0)
+        return rc;
+    ray2_kernel<true><<<blocks(n, 128), 128, 0, S2(stream)>>>(s->tree(), origins, dirs, tmax, n, hit, nullptr,
+                                                               nullptr, nullptr);
     note_launch();
     SNCH2_CUDA(cudaGetLastError());
     return SNCH_OK;

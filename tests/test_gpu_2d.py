@@ -145,6 +145,7 @@ def test_2d_large_scene_against_oracle(snch, oracle_mod):
     h, t, sp, ri = s.query_ray(p, dirs, tm)
     oh, ot, osp, ori = orc.ray(p, dirs, tm)
     np.testing.assert_array_equal(h.cpu().numpy(), oh)
+    np.testing.assert_array_equal(s.query_ray_test(p, dirs, tm).cpu().numpy(), oh)  # TestOnly = true
     np.testing.assert_array_equal(bits(t.cpu().numpy()), bits(ot))
     np.testing.assert_array_equal(ri.cpu().numpy().view(np.uint32), ori)
     rr = np.exp(rng.uniform(np.log(1e-2), np.log(3), n)).astype(np.float32)

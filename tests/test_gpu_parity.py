@@ -173,6 +173,9 @@ def test_queries_match_reference(snch, name):
         check_silhouette(sd.cpu().numpy(), g["ref_sil_dist"])
     hit, t, uv, ri = s.query_ray(g["ray_o"], g["ray_d"], g["ray_tmax"])
     np.testing.assert_array_equal(hit.cpu().numpy(), g["ref_ray_hit"])
+    # ray_intersect<TestOnly = true>: the same hit flags, from the first accepted hit
+    np.testing.assert_array_equal(s.query_ray_test(g["ray_o"], g["ray_d"], g["ray_tmax"]).cpu().numpy(),
+                                  g["ref_ray_hit"])
     np.testing.assert_array_equal(bits(t.cpu().numpy()), bits(g["ref_ray_t"]))
     np.testing.assert_array_equal(bits(uv.cpu().numpy()), bits(g["ref_ray_uv"]))
     np.testing.assert_array_equal(ri.cpu().numpy().view(np.uint32), g["ref_ray_idx"])
@@ -251,6 +254,8 @@ def test_empty_and_single_triangle(snch):
     assert np.all(idx.cpu().numpy() == -1) and np.all(np.isinf(dist.cpu().numpy()))
     hit, t, _, ri = empty.query_ray(np.zeros((2, 3), np.float32), np.ones((2, 3), np.float32), np.ones(2, np.float32))
     assert not hit.cpu().numpy().any()
+    assert not empty.query_ray_test(np.zeros((2, 3), np.float32), np.ones((2, 3), np.float32),
+                                    np.ones(2, np.float32)).cpu().numpy().any()
     one = built_scene(snch, np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], np.float32), np.array([[0, 1, 2]], np.int32))
     idx, dist = one.query_nearest(np.array([[0.2, 0.2, 1.0], [2.0, 0.0, 0.0]], np.float32))
     np.testing.assert_array_equal(idx.cpu().numpy(), [0, 0])

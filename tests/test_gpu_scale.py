@@ -81,6 +81,7 @@ def test_queries_against_oracle_subset(big):
     hit, t, uv, ri = s.query_ray(q["ray_o"], q["ray_d"], q["ray_tmax"])
     oh, ot, ouv, oi = orc.ray(q["ray_o"], q["ray_d"], q["ray_tmax"])
     np.testing.assert_array_equal(hit.cpu().numpy(), oh)
+    np.testing.assert_array_equal(s.query_ray_test(q["ray_o"], q["ray_d"], q["ray_tmax"]).cpu().numpy(), oh)
     np.testing.assert_array_equal(bits(t.cpu().numpy()), bits(ot))
     np.testing.assert_array_equal(ri.cpu().numpy().view(np.uint32), oi)
     si, sp = s.sample_in_sphere(q["smp_c"], q["smp_r"], q["smp_u"])
