@@ -162,12 +162,14 @@ int snch_set_traversal(snch_scene_t scene, int mode);
 #define SNCH_OPT_QUERY_ORDER 2
 #define SNCH_OPT_ORDER_MIN_BATCH 3
 /*   SNCH_OPT_PERSISTENT       1: near-first nearest/silhouette batches (plain or batched
- *                             scenes) run as persistent work-stealing kernels: a warp
- *                             takes 32 queries at a time from a batch-wide counter and a
- *                             lane takes the next query when its own is done; 0
- *                             (default): one thread per query. Same results; on the
- *                             2M-triangle scene with Morton-ordered batches the refilled
- *                             lanes lose their warp's coherence and run slower.
+ *                             scenes) searched one query per lane run as persistent
+ *                             work-stealing kernels: a warp takes 32 queries at a time
+ *                             from a batch-wide counter and a lane takes the next query
+ *                             when its own is done; 0 (default): one thread per query.
+ *                             Same results; on the 2M-triangle scene with Morton-ordered
+ *                             batches the refilled lanes lose their warp's coherence and
+ *                             run slower. (Warp packets always run persistent: a warp
+ *                             takes the next 32 queries when its packet is done.)
  *   SNCH_OPT_PERSISTENT_NEAREST / _SILHOUETTE  the same for one query type. */
 #define SNCH_OPT_PERSISTENT 4
 #define SNCH_OPT_PERSISTENT_NEAREST 16

@@ -273,7 +273,9 @@ void trim_pools()
             cudaMemPoolTrimTo(pool, 0);
 }
 
-cudaError_t scratch_alloc_raw(void **pp, size_t bytes, cudaStream_t st)
+}  // namespace
+
+cudaError_t snch::scratch_alloc_raw(void **pp, size_t bytes, cudaStream_t st)
 {
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
     if (cudaStreamIsCapturing(st, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone)
@@ -297,6 +299,9 @@ cudaError_t scratch_alloc_raw(void **pp, size_t bytes, cudaStream_t st)
     return e;
 }
 
+
+namespace
+{
 template <typename T>
 cudaError_t scratch_alloc(T **p, size_t bytes, cudaStream_t st)
 {

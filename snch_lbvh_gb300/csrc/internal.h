@@ -139,6 +139,10 @@ cudaError_t launch_sample(const TreeView &t, const float *c, const float *r, con
 cudaError_t launch_enumerate(const TreeView &t, bool line, const float *q0, const float *q1, int64_t n,
                              uint32_t max_out, uint32_t *idx, float *tt, uint32_t *count, cudaStream_t st);
 // Morton-sorted order of a query batch (thread i answers query order[i]);
+// Stream-ordered scratch from the library's memory pool on the current device
+// (kept mapped between calls; cudaMallocAsync under stream capture). Free with
+// cudaFreeAsync on the same stream.
+cudaError_t scratch_alloc_raw(void **p, size_t bytes, cudaStream_t st);
 // The queries of a seeded batch whose fail_flag is set, listed in batch order
 // (order[i], or i without an order) with their count, all on the device.
 size_t failed_list_scratch_bytes(int64_t n);
