@@ -168,8 +168,9 @@ int snch_set_traversal(snch_scene_t scene, int mode);
  *                             when its own is done; 0 (default): one thread per query.
  *                             Same results; on the 2M-triangle scene with Morton-ordered
  *                             batches the refilled lanes lose their warp's coherence and
- *                             run slower. (Warp packets always run persistent: a warp
- *                             takes the next 32 queries when its packet is done.)
+ *                             run slower. (Warp packets of batches of 2^23 queries or
+ *                             more always run persistent: a warp takes the next 32
+ *                             queries when its packet is done.)
  *   SNCH_OPT_PERSISTENT_NEAREST / _SILHOUETTE  the same for one query type. */
 #define SNCH_OPT_PERSISTENT 4
 #define SNCH_OPT_PERSISTENT_NEAREST 16

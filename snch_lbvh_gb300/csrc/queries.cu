@@ -2590,6 +2590,9 @@ inline bool packet_ok(const TreeView &t, int packet, int width, const SeedArgs &
 // 1,280-triangle spheres: packets faster from 13 queries per triangle up).
 // Silhouette packets won at every measured density (0.26 queries per triangle up).
 constexpr uint64_t kPacketNearestMinQueriesPerTri = 3;
+// Packets run persistent from this batch size (measured faster at 16M and 166M
+// queries, slower at 1M: a walk-on-stars step and a 1M-point sphere batch)
+constexpr int64_t kPersistentPacketMinBatch = int64_t(1) << 23;
 inline bool packet_dense(const TreeView &t, int packet, int64_t n)
 {
     return packet == 1 || (uint64_t)n >= kPacketNearestMinQueriesPerTri * t.num_tris;
@@ -2641,13 +2644,15 @@ cudaError_t launch_nearest(const TreeView &t, const float *pts, int64_t n, uint3
     const bool persistent = (t.persistent & 1) != 0;
     if (packet_ok(t, t.packet_near, t.width_near, seed) && packet_dense(t, t.packet_near, n))
     {
-        // persistent packets: the same packets and answers, 2-7 % faster (no warp
-        // slot waits for the slowest packet of its block); the counters' pass
-        // keeps the one-launch-per-batch form
+        // persistent packets for large batches: the same packets and answers, 2-7 %
+        // faster there (no warp slot waits for the slowest packet of its block);
+        // 6 % slower on 1M-query batches. The counters' pass keeps the grid form.
         if (stats)
             nearest_packet_kernel<true><<<grid_for(n, 128), 128, 0, st>>>(t, pts, n, idx, dist, stats, seed);
-        else
+        else if (n >= kPersistentPacketMinBatch)
             return launch_persistent(nearest_packet_persistent_kernel, n, st, t, pts, n, idx, dist, seed);
+        else
+            nearest_packet_kernel<false><<<grid_for(n, 128), 128, 0, st>>>(t, pts, n, idx, dist, nullptr, seed);
     }
     else if (wide_ok(t, t.width_near, persistent, seed))
     {
@@ -2688,8 +2693,11 @@ cudaError_t launch_silhouette(const TreeView &t, const float *pts, const uint8_t
         if (stats)
             silhouette_packet_kernel<true>
                 <<<grid_for(n, 128), 128, 0, st>>>(t, pts, flip, n, dist, edge, stats, seed);
-        else
+        else if (n >= kPersistentPacketMinBatch)
             return launch_persistent(silhouette_packet_persistent_kernel, n, st, t, pts, flip, n, dist, edge, seed);
+        else
+            silhouette_packet_kernel<false>
+                <<<grid_for(n, 128), 128, 0, st>>>(t, pts, flip, n, dist, edge, nullptr, seed);
     }
     else if (wide_ok(t, t.width_sil, persistent, seed))
     {
