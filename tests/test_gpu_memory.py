@@ -110,3 +110,22 @@ def test_reused_blocks_give_the_same_answers(snch):
     small.close()
     snch.release_cached_memory()
     assert snch.cached_memory_bytes() == 0
+
+
+def test_options_read_back(snch):
+    """snch_get_option returns what snch_set_option set, per query type."""
+    v, t = mesh()
+    s = snch.Scene(v, t)
+    s.build_bvh()
+    assert s.get_option(snch.OPT_HOST_CHUNK) == 0  # automatic per query type
+    s.set_option(snch.OPT_HOST_CHUNK, 1 << 20)
+    assert s.get_option(snch.OPT_HOST_CHUNK) == 1 << 20
+    s.set_option(snch.OPT_PACKET_SILHOUETTE, 0)
+    assert s.get_option(snch.OPT_PACKET_NEAREST) == 2 and s.get_option(snch.OPT_PACKET_SILHOUETTE) == 0
+    s.set_option(snch.OPT_PERSISTENT_NEAREST, 1)
+    assert s.search_config("nearest")[3] == 1 and s.search_config("silhouette")[3] == 0
+    s.set_option(snch.OPT_NODE_WIDTH_SILHOUETTE, 4)
+    assert s.search_config("silhouette")[0] == 4 and s.search_config("nearest")[0] == 2
+    with pytest.raises(snch.SnchError):
+        s.get_option(99)
+    s.close()
