@@ -1692,12 +1692,17 @@ SNCH_DEV void silhouette_packet_chunk(const TreeView &t, const float *__restrict
         stats[3 * q + 2] = n_edge;
     }}
 
+// blocks per SM the silhouette packet kernels are compiled for (9: 56 registers;
+// measured on the 2M-triangle scene: 8 blocks / 64 registers within 1 %, 10 / 48
+// registers 6-12 % slower)
+#ifndef SNCH_SIL_PACKET_MIN_BLOCKS
+#define SNCH_SIL_PACKET_MIN_BLOCKS 9
+#endif
 template <bool kStats>
-__global__ void __launch_bounds__(128, 9) silhouette_packet_kernel(TreeView t, const float *__restrict__ pts,
-                                                               const uint8_t *__restrict__ flips, int64_t n,
-                                                               float *__restrict__ out_dist,
-                                                               int32_t *__restrict__ out_edge,
-                                                               uint32_t *__restrict__ stats, SeedArgs seed)
+__global__ void __launch_bounds__(128, SNCH_SIL_PACKET_MIN_BLOCKS)
+    silhouette_packet_kernel(TreeView t, const float *__restrict__ pts, const uint8_t *__restrict__ flips, int64_t n,
+                             float *__restrict__ out_dist, int32_t *__restrict__ out_edge,
+                             uint32_t *__restrict__ stats, SeedArgs seed)
 {
     __shared__ uint32_t st_node[kPacketWarps][kStackDepth];
     __shared__ uint32_t st_mask[kPacketWarps][kStackDepth];
@@ -1709,7 +1714,7 @@ __global__ void __launch_bounds__(128, 9) silhouette_packet_kernel(TreeView t, c
 // the same packets, persistent: each warp takes the next 32 queries of the
 // batch from a batch-wide counter when its packet is done, so no warp slot
 // waits for the slowest packet of its block
-__global__ void __launch_bounds__(128, 9)
+__global__ void __launch_bounds__(128, SNCH_SIL_PACKET_MIN_BLOCKS)
     silhouette_packet_persistent_kernel(TreeView t, const float *__restrict__ pts, const uint8_t *__restrict__ flips,
                                         int64_t n, float *__restrict__ out_dist, int32_t *__restrict__ out_edge,
                                         SeedArgs seed, unsigned long long *counter)
