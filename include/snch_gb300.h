@@ -323,6 +323,15 @@ int snch_batch_query_nearest(snch_scene_t scene, const int32_t *mesh, const floa
 int snch_batch_query_silhouette(snch_scene_t scene, const int32_t *mesh, const float *points,
                                 const uint8_t *flip_or_null, int64_t n, float *distance, int32_t *edge_or_null,
                                 snch_stream_t stream);
+/* the same seeded with a per-query radius (DEVICE float), as snch_query_*_seeded:
+ * identical results whatever the radii; num_fallback (DEVICE uint32, may be NULL)
+ * receives how many queries found nothing inside their radius */
+int snch_batch_query_nearest_seeded(snch_scene_t scene, const int32_t *mesh, const float *points,
+                                    const float *radius, int64_t n, int32_t *index, float *distance,
+                                    uint32_t *num_fallback, snch_stream_t stream);
+int snch_batch_query_silhouette_seeded(snch_scene_t scene, const int32_t *mesh, const float *points,
+                                       const float *radius, const uint8_t *flip_or_null, int64_t n, float *distance,
+                                       int32_t *edge_or_null, uint32_t *num_fallback, snch_stream_t stream);
 
 /* Autotuner (no reference counterpart): times this scene's nearest and
  * silhouette searches in SNCH_AUTOTUNE_CONFIGS configurations -- (node width,

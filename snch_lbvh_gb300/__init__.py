@@ -554,6 +554,29 @@ class BatchedScene(Scene):
                                                 _stream(stream)))
         return dist, edge
 
+    def query_nearest_batch_seeded(self, mesh, points, radius, stream=None, num_fallback=None):
+        """query_nearest_batch seeded with per-query radii (same results)."""
+        torch = _torch()
+        p, m, r = _dev(points, torch.float32, 3), _dev(mesh, torch.int32), _dev(radius, torch.float32)
+        n = p.shape[0]
+        idx = torch.empty(n, dtype=torch.int32, device="cuda")
+        dist = torch.empty(n, dtype=torch.float32, device="cuda")
+        check(lib().snch_batch_query_nearest_seeded(self._h, _ptr(m), _ptr(p), _ptr(r), n, _ptr(idx), _ptr(dist),
+                                                    _ptr(num_fallback), _stream(stream)))
+        return idx, dist
+
+    def query_silhouette_batch_seeded(self, mesh, points, radius, flip=None, stream=None, num_fallback=None):
+        """query_silhouette_batch seeded with per-query radii (same results)."""
+        torch = _torch()
+        p, m, r = _dev(points, torch.float32, 3), _dev(mesh, torch.int32), _dev(radius, torch.float32)
+        n = p.shape[0]
+        f = None if flip is None else _dev(flip, torch.uint8)
+        dist = torch.empty(n, dtype=torch.float32, device="cuda")
+        edge = torch.empty(n, dtype=torch.int32, device="cuda")
+        check(lib().snch_batch_query_silhouette_seeded(self._h, _ptr(m), _ptr(p), _ptr(r), _ptr(f), n, _ptr(dist),
+                                                       _ptr(edge), _ptr(num_fallback), _stream(stream)))
+        return dist, edge
+
 
 class Scene2:
     """lbvh::scene<2> (scene.cuh:287-703): line segments with silhouette vertices

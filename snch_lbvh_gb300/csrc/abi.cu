@@ -1806,6 +1806,56 @@ int snch_batch_query_silhouette(snch_scene_t s, const int32_t *mesh, const float
         reinterpret_cast<const uint32_t *>(mesh));
 }
 
+int snch_batch_query_nearest_seeded(snch_scene_t s, const int32_t *mesh, const float *pts, const float *radius,
+                                    int64_t n, int32_t *idx, float *dist, uint32_t *num_fallback,
+                                    snch_stream_t stream)
+{
+    int rc = check_built(s);
+    if (rc == SNCH_OK && !s->num_meshes)
+        rc = fail(SNCH_ERR_INVALID_ARGUMENT, "not a batched scene");
+    if (rc == SNCH_OK)
+        rc = check_n(n, {mesh, pts, radius, idx, dist});
+    if (rc != SNCH_OK)
+        return rc;
+    if (n == 0)
+    {
+        if (num_fallback)
+            SNCH_CUDA(cudaMemsetAsync(num_fallback, 0, 4, S(stream)));
+        return SNCH_OK;
+    }
+    return run_query(
+        s, 0, pts, radius, n, num_fallback, S(stream),
+        [&](const TreeView &t, const SeedArgs &seed) {
+            return launch_nearest(t, pts, n, reinterpret_cast<uint32_t *>(idx), dist, S(stream), nullptr, seed);
+        },
+        reinterpret_cast<const uint32_t *>(mesh));
+}
+
+int snch_batch_query_silhouette_seeded(snch_scene_t s, const int32_t *mesh, const float *pts, const float *radius,
+                                       const uint8_t *flip, int64_t n, float *dist, int32_t *edge,
+                                       uint32_t *num_fallback, snch_stream_t stream)
+{
+    int rc = check_built(s);
+    if (rc == SNCH_OK && !s->num_meshes)
+        rc = fail(SNCH_ERR_INVALID_ARGUMENT, "not a batched scene");
+    if (rc == SNCH_OK)
+        rc = check_n(n, {mesh, pts, radius, dist});
+    if (rc != SNCH_OK)
+        return rc;
+    if (n == 0)
+    {
+        if (num_fallback)
+            SNCH_CUDA(cudaMemsetAsync(num_fallback, 0, 4, S(stream)));
+        return SNCH_OK;
+    }
+    return run_query(
+        s, 1, pts, radius, n, num_fallback, S(stream),
+        [&](const TreeView &t, const SeedArgs &seed) {
+            return launch_silhouette(t, pts, flip, n, dist, edge, S(stream), nullptr, seed);
+        },
+        reinterpret_cast<const uint32_t *>(mesh));
+}
+
 int snch_autotune(snch_scene_t s, const int32_t *near_mesh, const float *near_pts, int64_t n_near,
                   const int32_t *sil_mesh, const float *sil_pts, const uint8_t *sil_flip, int64_t n_sil, float *out_ms,
                   snch_stream_t stream)

@@ -144,6 +144,43 @@ def test_batched_persistent_work_stealing(snch_mod):
     b.close()
 
 
+def test_batched_seeded_equals_plain(snch_mod):
+    """Seeded batched searches (per-query radii: exact, too small, large, zero)
+    return the plain batched results bit for bit and count the fallbacks."""
+    import torch
+    snch = snch_mod
+    rng = np.random.default_rng(4)
+    ms = mixed_meshes(rng, 12)
+    b = snch.BatchedScene(ms)
+    b.compute_silhouettes()
+    b.build_bvh()
+    n = 200_000
+    mesh = torch.from_numpy(rng.integers(0, len(ms), n).astype(np.int32)).cuda()
+    pts = torch.from_numpy(rng.uniform(-3, 3, (n, 3)).astype(np.float32)).cuda()
+    flip = torch.from_numpy((rng.random(n) < 0.5).astype(np.uint8)).cuda()
+    i0, d0 = b.query_nearest_batch(mesh, pts)
+    s0, e0 = b.query_silhouette_batch(mesh, pts, flip)
+    for scale in (1.0, 0.5, 4.0, 0.0):
+        rn = torch.where(torch.isfinite(d0), d0 * scale, torch.full_like(d0, 1.0))
+        rs = torch.where(torch.isfinite(s0), s0 * scale, torch.full_like(s0, 1.0))
+        nf = torch.zeros(2, dtype=torch.int32, device="cuda")
+        i1, d1 = b.query_nearest_batch_seeded(mesh, pts, rn, num_fallback=nf[0:1])
+        s1, e1 = b.query_silhouette_batch_seeded(mesh, pts, rs, flip, num_fallback=nf[1:2])
+        assert torch.equal(d1.view(torch.int32), d0.view(torch.int32)), scale
+        assert torch.equal(s1.view(torch.int32), s0.view(torch.int32)), scale
+        same_i = (i1 == i0) | torch.isinf(d0)
+        same_e = (e1 == e0) | torch.isinf(s0)
+        # indices: equal up to exact ties on a rounding boundary (warp packets)
+        assert same_i.float().mean().item() > 0.9999 and same_e.float().mean().item() > 0.9999, scale
+        fb = nf.cpu().numpy()
+        if scale < 1.0:
+            assert fb[0] > 0  # radii below the answer: those queries fall back
+        if scale > 1.0:
+            assert fb[0] < n // 100 and fb[1] < n // 100
+    assert b.device_status() == 0
+    b.close()
+
+
 def test_batched_rejects_bad_input(snch_mod):
     snch = snch_mod
     v = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], np.float32)
