@@ -32,6 +32,7 @@ OPT_BLOCK, OPT_BLOCK_NEAREST, OPT_BLOCK_SILHOUETTE = 9, 10, 11
 OPT_PACKET, OPT_PACKET_NEAREST, OPT_PACKET_SILHOUETTE = 12, 13, 14
 OPT_HOST_CHUNK = 15
 OPT_PERSISTENT_NEAREST, OPT_PERSISTENT_SILHOUETTE = 16, 17
+OPT_PERSISTENT_RAY = 18
 
 
 def _torch():

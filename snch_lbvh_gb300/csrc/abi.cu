@@ -93,6 +93,7 @@ struct snch_scene_s
     int64_t order_min = 65536;
     int64_t host_chunk = 0;  // queries per pipelined host-form chunk; 0: per query type
     int persistent_near = 0, persistent_sil = 0;  // lane-refill (work-stealing) searches
+    int persistent_ray = 0;
     int64_t tail_cap = 0;            // near-first expansions before a query is deferred (0: off; measured slower)
     // batched scene (num_meshes > 0): independent meshes, one build, per-mesh queries
     uint32_t num_meshes = 0;
@@ -130,7 +131,7 @@ struct snch_scene_s
         t.edges = edges;
         t.status = small + kWStatus;
         t.near_first = traversal == SNCH_TRAVERSAL_NEAR_FIRST ? 1 : 0;
-        t.persistent = (persistent_near ? 1 : 0) | (persistent_sil ? 2 : 0);
+        t.persistent = (persistent_near ? 1 : 0) | (persistent_sil ? 2 : 0) | (persistent_ray ? 4 : 0);
         t.width_near = width_near;
         t.width_sil = width_sil;
         t.block_near = block_near;
@@ -1049,6 +1050,11 @@ int snch_set_option(snch_scene_t s, int option, int64_t value)
         if (value < 0)
             return fail(SNCH_ERR_INVALID_ARGUMENT, "SNCH_OPT_ORDER_MIN_BATCH must be >= 0");
         s->order_min = value;
+        return SNCH_OK;
+    case SNCH_OPT_PERSISTENT_RAY:
+        if (value != 0 && value != 1)
+            return fail(SNCH_ERR_INVALID_ARGUMENT, "SNCH_OPT_PERSISTENT_RAY takes 0 or 1");
+        s->persistent_ray = (int)value;
         return SNCH_OK;
     case SNCH_OPT_HOST_CHUNK:
         if (value != 0 && (value < 1024 || value >= (int64_t(1) << 30)))
@@ -2240,6 +2246,7 @@ int snch_get_option(snch_scene_t s, int option, int64_t *value)
     case SNCH_OPT_PACKET_NEAREST: *value = s->packet_near; break;
     case SNCH_OPT_PACKET_SILHOUETTE: *value = s->packet_sil; break;
     case SNCH_OPT_HOST_CHUNK: *value = s->host_chunk; break;
+    case SNCH_OPT_PERSISTENT_RAY: *value = s->persistent_ray; break;
     default: return fail(SNCH_ERR_INVALID_ARGUMENT, "unknown option " + std::to_string(option));
     }
     return SNCH_OK;

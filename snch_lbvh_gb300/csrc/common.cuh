@@ -135,7 +135,7 @@ struct TreeView
     int near_first = 1;               // 1: near-first nearest/silhouette traversal, 0: the reference's stack order
     const uint32_t *order = nullptr;  // optional: thread i answers query order[i] (Morton-sorted batches)
     const uint32_t *order_count = nullptr;  // optional: device count of valid entries of order
-    int persistent = 0;  // persistent lane-refill kernels (same results): bit 0 nearest, bit 1 silhouette
+    int persistent = 0;  // persistent lane-refill kernels (same results): bit 0 nearest, bit 1 silhouette, bit 2 ray
     // batched queries over a batched scene: the mesh of each query (input position)
     // selects the subtree it searches; results are reported per mesh
     const uint32_t *query_mesh = nullptr;

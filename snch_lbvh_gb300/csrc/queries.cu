@@ -2225,6 +2225,154 @@ __global__ void __launch_bounds__(128) ray_kernel(TreeView t, const float *__res
     }
 }
 
+// The same ray traversal, persistent (lane refill): a lane takes the next ray
+// of the batch when its own is done (warp-chunked counter, take_query). Rays
+// with tmax log-uniform over three decades differ in cost by orders of
+// magnitude, so a one-ray-per-thread warp waits for its longest ray; here the
+// finished lanes start new rays instead. Each iteration is one step of the
+// reference's near-first order (same visits, same answers).
+template <bool kAny>
+__global__ void __launch_bounds__(128) ray_persistent_kernel(TreeView t, const float *__restrict__ origins,
+                                                             const float *__restrict__ dirs,
+                                                             const float *__restrict__ tmaxs, int64_t n,
+                                                             uint8_t *__restrict__ out_hit, float *__restrict__ out_t,
+                                                             float *__restrict__ out_uv,
+                                                             uint32_t *__restrict__ out_idx,
+                                                             unsigned long long *counter)
+{
+    const unsigned long long total = (unsigned long long)query_count(t, n);
+    const uint32_t ni = t.num_tris - 1;
+    uint32_t sn[kStackDepth];
+    float sd[kStackDepth];
+    int sp = 0;
+    int64_t q = -1;
+    f3 o = mk(0.f, 0.f, 0.f), dir = o, inv = o;
+    float max_dist = 0.f, min_dist = INFINITY, bu = 0.f, bv = 0.f, nd = INFINITY;
+    bool found = false, active = false;
+    uint32_t nearest = kInvalid, node = 0;
+    WarpQueue wq;
+    for (;;)
+    {
+        const int64_t qi = take_query(wq, total, counter, !active);
+        bool done = false;
+        if (qi >= 0)
+        {
+            q = query_index(t, qi);
+            o = load_point(origins, q);
+            dir = load_point(dirs, q);
+            inv = mk(1 / dir.x, 1 / dir.y, 1 / dir.z);  // ray ctor aabb.cuh:305-312
+            max_dist = __ldg(tmaxs + q);
+            min_dist = INFINITY;
+            bu = bv = 0.f;
+            found = false;
+            nearest = kInvalid;
+            node = 0;
+            nd = INFINITY;
+            sp = 0;
+            active = true;
+            done = t.num_tris == 0;
+        }
+        if (!__any_sync(0xFFFFFFFFu, active))
+        {
+            if (wq.exhausted)
+                break;
+            continue;
+        }
+        if (!active)
+            continue;
+        if (!done)
+        {
+            bool next = !(nd > min_dist);
+            if (next && node >= ni)
+            {
+                f3 pa, pb, pc;
+                uint32_t orig, n_owned;
+                load_leaf(t.leaves + (node - ni), pa, pb, pc, orig, n_owned);
+                float tt, uu, vv;
+                if (ray_triangle(o, dir, pa, pb, pc, tt, uu, vv) && tt < max_dist && tt < min_dist)
+                {
+                    min_dist = tt;
+                    found = true;
+                    bu = uu;
+                    bv = vv;
+                    nearest = orig;
+                    if (kAny)
+                        done = true;
+                }
+                next = false;
+            }
+            else if (next)
+            {
+                if (sp > kStackDepth - 2)
+                {
+                    atomicOr(t.status, kStatusStackOverflow);
+                    found = false;
+                    nearest = kInvalid;
+                    min_dist = NAN;
+                    done = true;
+                }
+                else
+                {
+                    Box lb, rb;
+                    uint32_t L, R;
+                    unpack_inner(load_inner(t.inner + node), lb, rb, L, R);
+                    float Ld = 0.0f, Rd = 0.0f;
+                    const bool Lh = ray_box(o, inv, lb, max_dist, Ld);
+                    const bool Rh = ray_box(o, inv, rb, max_dist, Rd);
+                    if (Lh && Rh)
+                    {
+                        uint32_t closer = L, other = R;
+                        if (Rd < Ld)
+                        {
+                            const float tmp = Ld;
+                            Ld = Rd;
+                            Rd = tmp;
+                            closer = R;
+                            other = L;
+                        }
+                        sn[sp] = other;
+                        sd[sp] = Rd;
+                        ++sp;
+                        node = closer;
+                        nd = Ld;
+                    }
+                    else if (Lh || Rh)
+                    {
+                        node = Lh ? L : R;
+                        nd = Lh ? Ld : Rd;
+                    }
+                    else
+                        next = false;
+                }
+            }
+            if (!done && !next)
+            {
+                // pop (the reference's stack order)
+                if (sp == 0)
+                    done = true;
+                else
+                {
+                    --sp;
+                    node = sn[sp];
+                    nd = sd[sp];
+                }
+            }
+        }
+        if (done)
+        {
+            out_hit[q] = found ? 1 : 0;
+            if (!kAny)
+            {
+                out_t[q] = min_dist;
+                out_uv[2 * q] = bu;
+                out_uv[2 * q + 1] = bv;
+                out_idx[q] = nearest;
+            }
+            active = false;
+        }
+    }
+}
+
 // ------------------------------------------------------------------ sampling
 // intersect_sphere(sphere, aabb) aabb.cuh:433-449
 SNCH_DEV bool sphere_box(f3 c, float r, const Box &b)
@@ -2749,6 +2897,8 @@ cudaError_t launch_ray(const TreeView &t, const float *o, const float *d, const 
         return cudaSuccess;
     if (stats)
         ray_kernel<true><<<grid_for(n, 128), 128, 0, st>>>(t, o, d, tmax, n, hit, tt, uv, idx, stats);
+    else if (t.persistent & 4)
+        return launch_persistent(ray_persistent_kernel<false>, n, st, t, o, d, tmax, n, hit, tt, uv, idx);
     else
         ray_kernel<false><<<grid_for(n, 128), 128, 0, st>>>(t, o, d, tmax, n, hit, tt, uv, idx, nullptr);
     note_launch();
@@ -2759,6 +2909,9 @@ cudaError_t launch_ray_test(const TreeView &t, const float *o, const float *d, c
 {
     if (n <= 0)
         return cudaSuccess;
+    if (t.persistent & 4)
+        return launch_persistent(ray_persistent_kernel<true>, n, st, t, o, d, tmax, n, hit, (float *)nullptr,
+                                 (float *)nullptr, (uint32_t *)nullptr);
     ray_kernel<false, true><<<grid_for(n, 128), 128, 0, st>>>(t, o, d, tmax, n, hit, nullptr, nullptr, nullptr,
                                                                nullptr);
     note_launch();

@@ -238,6 +238,41 @@ def test_host_forms_equal_device_forms(snch):
     np.testing.assert_array_equal(bits(p1[1].cpu().numpy()), bits(p2[1]))
 
 
+@pytest.mark.parametrize("name", golden_names())
+def test_persistent_rays_match_reference(snch, name):
+    """Lane-refill ray kernels (closest hit and occlusion) give the reference's answers."""
+    g = load_golden(name)
+    s = built_scene(snch, g["verts"], g["tris"])
+    s.set_option(snch.OPT_PERSISTENT_RAY, 1)
+    hit, t, uv, ri = s.query_ray(g["ray_o"], g["ray_d"], g["ray_tmax"])
+    np.testing.assert_array_equal(hit.cpu().numpy(), g["ref_ray_hit"])
+    np.testing.assert_array_equal(bits(t.cpu().numpy()), bits(g["ref_ray_t"]))
+    np.testing.assert_array_equal(bits(uv.cpu().numpy()), bits(g["ref_ray_uv"]))
+    np.testing.assert_array_equal(ri.cpu().numpy().view(np.uint32), g["ref_ray_idx"])
+    np.testing.assert_array_equal(s.query_ray_test(g["ray_o"], g["ray_d"], g["ray_tmax"]).cpu().numpy(),
+                                  g["ref_ray_hit"])
+    assert s.device_status() == 0
+
+
+def test_persistent_rays_full_scene(snch):
+    """Lane-refill rays equal one-thread-per-ray rays bit for bit on 2M rays of the
+    two-million-triangle scene (tmax log-uniform over three decades)."""
+    from snch_lbvh_gb300 import meshes
+    sc = meshes.wost_scene(seed=0)
+    q = meshes.wost_queries(1, 1, 2_000_000, 1, seed=21)
+    s = built_scene(snch, sc.verts, sc.faces)
+    a = [x.cpu().numpy() for x in s.query_ray(q["ray_o"], q["ray_d"], q["ray_tmax"])]
+    at = s.query_ray_test(q["ray_o"], q["ray_d"], q["ray_tmax"]).cpu().numpy()
+    s.set_option(snch.OPT_PERSISTENT_RAY, 1)
+    b = [x.cpu().numpy() for x in s.query_ray(q["ray_o"], q["ray_d"], q["ray_tmax"])]
+    bt = s.query_ray_test(q["ray_o"], q["ray_d"], q["ray_tmax"]).cpu().numpy()
+    for x, y in zip(a, b):
+        np.testing.assert_array_equal(x.view(np.uint8), y.view(np.uint8))
+    np.testing.assert_array_equal(at, bt)
+    np.testing.assert_array_equal(bt, a[0])
+    assert s.device_status() == 0
+
+
 def test_query_before_build_raises(snch):
     import torch
     s = snch.Scene(np.eye(3, dtype=np.float32), np.array([[0, 1, 2]], np.int32))
