@@ -502,9 +502,10 @@ int snch_gemm_bf16(const void *A, const void *B, float *C, int64_t M, int64_t N,
 
 /* Host-buffer forms of the four queries: copy in, run, copy out in pipelined
  * chunks on the scene's own streams; return when results are in host memory.
- * The scene's streams are ordered after work queued on the legacy default
- * stream (stream 0, where a NULL snch_stream_t builds); a build queued on any
- * other stream must be complete before the call.
+ * The searches start after the work queued on the legacy default stream
+ * before the call (stream 0, where a NULL snch_stream_t builds; the input
+ * copies overlap it); a build queued on any other stream must be complete
+ * before the call.
  * This is the call shape of the reference's benchmark loop (benchmark.cu:395-409). */
 int snch_query_nearest_host(snch_scene_t scene, const float *points_xyz, int64_t n, uint32_t *out_index,
                             float *out_distance);

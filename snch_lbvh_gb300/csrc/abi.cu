@@ -101,6 +101,7 @@ struct snch_scene_s
              *mesh_root = nullptr, *perm = nullptr, *perm_tmp = nullptr, *mkey_tmp = nullptr;
     int32_t *mesh_edge_start = nullptr;
     cudaStream_t pipe[2] = {nullptr, nullptr};
+    cudaEvent_t pipe_ready = nullptr;  // legacy-stream work before a host-form call
     HostStage stage;
     // Fallback fraction of the last seeded nearest [0] / silhouette [1] call,
     // read back without a synchronisation: the count is copied to pinned host
@@ -339,6 +340,8 @@ void free_scene(snch_scene_s *s)
     for (cudaEvent_t ev : s->fallback_event)
         if (ev)
             cudaEventDestroy(ev);
+    if (s->pipe_ready)
+        cudaEventDestroy(s->pipe_ready);
     if (s->fallback_host)
         cudaFreeHost(s->fallback_host);
     delete s;
@@ -842,13 +845,16 @@ MlpWorkspace mlp_workspace(char *base, int64_t rows)
 }
 
 // ---- host-form pipeline: chunk i runs on pipe[i % 2]: H2D inputs, kernel, D2H outputs.
-// The pipes are blocking streams: their work starts after what is queued on the
-// legacy default stream (a build with a NULL stream) and needs no event.
+// The searches wait for an event recorded on the legacy default stream at the
+// start of the call (so a build queued there with a NULL stream is complete);
+// the input copies do not, so they overlap that build.
 int ensure_stage(snch_scene_s *s, size_t in_bytes, size_t out_bytes)
 {
     for (int k = 0; k < 2; ++k)
         if (!s->pipe[k])
-            SNCH_CUDA(cudaStreamCreateWithFlags(&s->pipe[k], cudaStreamDefault));
+            SNCH_CUDA(cudaStreamCreateWithFlags(&s->pipe[k], cudaStreamNonBlocking));
+    if (!s->pipe_ready)
+        SNCH_CUDA(cudaEventCreateWithFlags(&s->pipe_ready, cudaEventDisableTiming));
     if (in_bytes <= s->stage.in_bytes && out_bytes <= s->stage.out_bytes)
         return SNCH_OK;
     // a call that failed part-way may have left copies queued on the stage
@@ -904,6 +910,7 @@ int run_host_pipeline(snch_scene_s *s, int64_t n, int64_t auto_chunk, const Fiel
     int rc = ensure_stage(s, in_per * chunk + 256 * nin, out_per * chunk + 256 * nout);
     if (rc != SNCH_OK)
         return rc;
+    SNCH_CUDA(cudaEventRecord(s->pipe_ready, cudaStreamLegacy));
     for (int64_t b = 0, c = 0; b < n; b += chunk, ++c)
     {
         const int64_t m = std::min<int64_t>(chunk, n - b);
@@ -929,6 +936,7 @@ int run_host_pipeline(snch_scene_s *s, int64_t n, int64_t auto_chunk, const Fiel
             dev_out[i] = outs[i].host_out ? dout + off : nullptr;
             off += (outs[i].elem * chunk + 255) & ~size_t(255);
         }
+        SNCH_CUDA(cudaStreamWaitEvent(st, s->pipe_ready, 0));
         SNCH_CUDA(body(m, dev_in, dev_out, st));
         for (int i = 0; i < nout; ++i)
             if (outs[i].host_out)
