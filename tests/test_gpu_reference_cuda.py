@@ -34,7 +34,8 @@ def ref():
 def close(a, b, rtol=RTOL, atol=ATOL):
     a, b = a.astype(np.float64), b.astype(np.float64)
     both_inf = np.isinf(a) & np.isinf(b) & (np.sign(a) == np.sign(b))
-    return both_inf | (np.abs(a - b) <= np.maximum(rtol * np.abs(b), atol))
+    with np.errstate(invalid="ignore"):  # inf - inf where both are infinite
+        return both_inf | (np.abs(a - b) <= np.maximum(rtol * np.abs(b), atol))
 
 
 def compare_all(snch, ref, s, q, min_agree=0.999):
