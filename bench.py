@@ -75,6 +75,20 @@ def dist_env():
     return ws, int(os.environ.get("RANK", "0")), int(os.environ.get("LOCAL_RANK", "0"))
 
 
+def max_over_ranks(value: float, device=None) -> float:
+    """Maximum of a per-rank scalar (a step time) over the default process group.
+    The multi-GPU form runs replicas: every rank builds its own scene and answers
+    its own full batches (queries are independent), so this and the barrier are
+    the only collectives."""
+    import torch
+    import torch.distributed as dist
+    if not dist.is_available() or not dist.is_initialized() or dist.get_world_size() == 1:
+        return float(value)
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def workload_name(counts, ntri):
     return (f"wost_2m: {ntri:,} triangles (64 noisy tori + icospheres in the unit cube); step = silhouette "
             f"topology + LBVH build + {counts['near']:,} nearest + {counts['sil']:,} silhouette + "
@@ -779,11 +793,7 @@ def run_ours(args):
                       "smp_idx": out["smp"][0].cpu().numpy(), "smp_pdf": out["smp"][1].cpu().numpy()}
     status |= scene.device_status()
     elapsed_ms = t_start.elapsed_time(t_end)
-    if ws > 1:
-        import torch.distributed as dist
-        t = torch.tensor([elapsed_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed_ms = float(t.item())
+    elapsed_ms = max_over_ranks(elapsed_ms, "cuda")
     phase_ms = np.array([[e[i].elapsed_time(e[i + 1]) for i in range(5)] for e in evs]).mean(0)
     total_q = sum(counts.values())
     value = total_q * ws * args.steps / (elapsed_ms / 1e3)
@@ -873,11 +883,7 @@ def run_ours(args):
             e2e_step()
         barrier()
         e2e_s = time.perf_counter() - t0
-        if ws > 1:
-            import torch.distributed as dist
-            t = torch.tensor([e2e_s], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            e2e_s = float(t.item())
+        e2e_s = max_over_ranks(e2e_s, "cuda")
         h2d = sc.verts.nbytes + sc.faces.nbytes + sum(v.nbytes for v in q.values())
         d2h = sum(a.nbytes for v in hout.values() for a in v)
         host_answers = {"near_dist": hout["near"][1], "sil_dist": hout["sil"][0], "ray_hit": hout["ray"][0],

@@ -221,6 +221,12 @@ int snch_set_traversal(snch_scene_t scene, int mode);
 #define SNCH_OPT_PACKET 12
 #define SNCH_OPT_PACKET_NEAREST 13
 #define SNCH_OPT_PACKET_SILHOUETTE 14
+/*   SNCH_OPT_PACKET_PERSISTENT_MIN  smallest warp-packet batch (nearest and silhouette)
+ *                             that runs persistent: each warp takes the next 32 queries
+ *                             of the batch from a counter when its packet ends (same
+ *                             packets, same answers). Default 2^23 (measured faster from
+ *                             there, 6 % slower on 1M-query batches); >= 1. */
+#define SNCH_OPT_PACKET_PERSISTENT_MIN 19
 /*   SNCH_OPT_HOST_CHUNK       queries per chunk of the *_host forms (at most 29 bytes in
  *                             and 17 out per query on each of two streams): chunk i's
  *                             input copy, search and output copy run on stream i % 2, so
@@ -560,9 +566,15 @@ int snch_release_cached_memory(void);
  * exit. At most SNCH_SORT_NOALLOC_MAX_PAIRS pairs per call (larger n returns
  * SNCH_ERR_TOO_LARGE). Calls share that array: calls that overlap on the GPU
  * (other streams, other host threads) race and must be serialised by the
- * caller. The first call on each device looks up the array's device address
- * (cudaGetSymbolAddress) -- make it before any stream capture. device_status
- * (may be NULL) is a caller DEVICE word that receives SNCH_DEVICE_* bits. */
+ * caller. Each call outside a stream capture looks up the array's device
+ * address in the current CUDA context (cudaGetSymbolAddress; a context of the
+ * caller's own and a context re-created after cudaDeviceReset both work); a
+ * call during a capture reuses the address its context last looked up, so make
+ * the first call in each context before any stream capture. device_status
+ * (may be NULL) is a caller DEVICE word that receives SNCH_DEVICE_* bits; with
+ * NULL the bits go to a word inside the shared array that no caller can read,
+ * so a sort that gave up on a look-back wait (its output then incomplete) goes
+ * unnoticed: pass a status word wherever that matters. */
 #define SNCH_SORT_NOALLOC_MAX_PAIRS 1048576
 int snch_sort_pairs_noalloc(const uint32_t *keys_in, const uint32_t *values_in, uint32_t *keys_out,
                             uint32_t *values_out, int64_t n, int key_bits, uint32_t *device_status,

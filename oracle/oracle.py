@@ -19,9 +19,17 @@ REF_HARNESS = os.path.join(HERE, "_ref", "ref_harness")
 _lib = None
 
 
+# where the reference checkout lies in the container that generates the golden
+# vectors (the GPU machines have none); SNCH_REFERENCE overrides it
+REFERENCE_CHECKOUT = "/root/reference"
+
+
 def build(verbose: bool = False) -> None:
     """Compile the oracle (and, where the reference checkout exists, the reference harness)."""
-    out = subprocess.run(["make", "-s", "-C", HERE], capture_output=True, text=True)
+    env = dict(os.environ)
+    if not env.get("SNCH_REFERENCE") and os.path.isdir(REFERENCE_CHECKOUT):
+        env["SNCH_REFERENCE"] = REFERENCE_CHECKOUT
+    out = subprocess.run(["make", "-s", "-C", HERE], capture_output=True, text=True, env=env)
     if out.returncode != 0:
         raise RuntimeError("oracle build failed:\n" + out.stdout + out.stderr)
     if verbose:

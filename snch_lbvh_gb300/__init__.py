@@ -33,6 +33,7 @@ OPT_PACKET, OPT_PACKET_NEAREST, OPT_PACKET_SILHOUETTE = 12, 13, 14
 OPT_HOST_CHUNK = 15
 OPT_PERSISTENT_NEAREST, OPT_PERSISTENT_SILHOUETTE = 16, 17
 OPT_PERSISTENT_RAY = 18
+OPT_PACKET_PERSISTENT_MIN = 19
 
 
 def _torch():

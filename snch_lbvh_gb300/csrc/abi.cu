@@ -115,6 +115,7 @@ struct snch_scene_s
     int width_near = 2, width_sil = 2;
     int block_near = 128, block_sil = 128;  // threads per block of the binary searches
     int packet_near = 2, packet_sil = 2;    // warp packets: 0 never, 1 always, 2 Morton-ordered batches
+    int64_t packet_persistent_min = int64_t(1) << 23;  // packet batches this large run persistent
     float4 *wide[2] = {nullptr, nullptr};
     uint32_t *wide_idx[2] = {nullptr, nullptr};  // wide index of each wide-root binary node
     size_t wide_cap[2] = {0, 0};  // records allocated
@@ -139,6 +140,7 @@ struct snch_scene_s
         t.block_sil = block_sil;
         t.packet_near = packet_near;
         t.packet_sil = packet_sil;
+        t.packet_persistent_min = packet_persistent_min;
         if (wide_ready[0])
         {
             t.wide4 = wide[0];
@@ -911,40 +913,51 @@ int run_host_pipeline(snch_scene_s *s, int64_t n, int64_t auto_chunk, const Fiel
     if (rc != SNCH_OK)
         return rc;
     SNCH_CUDA(cudaEventRecord(s->pipe_ready, cudaStreamLegacy));
-    for (int64_t b = 0, c = 0; b < n; b += chunk, ++c)
-    {
-        const int64_t m = std::min<int64_t>(chunk, n - b);
-        const int k = (int)(c & 1);
-        cudaStream_t st = s->pipe[k];
-        char *din = static_cast<char *>(s->stage.in[k]);
-        char *dout = static_cast<char *>(s->stage.out[k]);
-        void *dev_in[4], *dev_out[4];
-        size_t off = 0;
-        for (int i = 0; i < nin; ++i)
+    // Every chunk is queued before the first wait. The pipe streams do not
+    // synchronise with the legacy default stream, so a call that fails part-way
+    // still waits for the chunks it queued: they read the tree and the stage,
+    // which a later NULL-stream build of this scene or the next call overwrites.
+    const int queued = [&]() -> int {
+        for (int64_t b = 0, c = 0; b < n; b += chunk, ++c)
         {
-            dev_in[i] = din + off;
-            if (ins[i].host_in)
-                SNCH_CUDA(cudaMemcpyAsync(din + off, static_cast<const char *>(ins[i].host_in) + b * ins[i].elem,
-                                          m * ins[i].elem, cudaMemcpyHostToDevice, st));
-            else
-                dev_in[i] = nullptr;
-            off += (ins[i].elem * chunk + 255) & ~size_t(255);
+            const int64_t m = std::min<int64_t>(chunk, n - b);
+            const int k = (int)(c & 1);
+            cudaStream_t st = s->pipe[k];
+            char *din = static_cast<char *>(s->stage.in[k]);
+            char *dout = static_cast<char *>(s->stage.out[k]);
+            void *dev_in[4], *dev_out[4];
+            size_t off = 0;
+            for (int i = 0; i < nin; ++i)
+            {
+                dev_in[i] = din + off;
+                if (ins[i].host_in)
+                    SNCH_CUDA(cudaMemcpyAsync(din + off, static_cast<const char *>(ins[i].host_in) + b * ins[i].elem,
+                                              m * ins[i].elem, cudaMemcpyHostToDevice, st));
+                else
+                    dev_in[i] = nullptr;
+                off += (ins[i].elem * chunk + 255) & ~size_t(255);
+            }
+            off = 0;
+            for (int i = 0; i < nout; ++i)
+            {
+                dev_out[i] = outs[i].host_out ? dout + off : nullptr;
+                off += (outs[i].elem * chunk + 255) & ~size_t(255);
+            }
+            SNCH_CUDA(cudaStreamWaitEvent(st, s->pipe_ready, 0));
+            SNCH_CUDA(body(m, dev_in, dev_out, st));
+            for (int i = 0; i < nout; ++i)
+                if (outs[i].host_out)
+                    SNCH_CUDA(cudaMemcpyAsync(static_cast<char *>(outs[i].host_out) + b * outs[i].elem, dev_out[i],
+                                              m * outs[i].elem, cudaMemcpyDeviceToHost, st));
         }
-        off = 0;
-        for (int i = 0; i < nout; ++i)
-        {
-            dev_out[i] = outs[i].host_out ? dout + off : nullptr;
-            off += (outs[i].elem * chunk + 255) & ~size_t(255);
-        }
-        SNCH_CUDA(cudaStreamWaitEvent(st, s->pipe_ready, 0));
-        SNCH_CUDA(body(m, dev_in, dev_out, st));
-        for (int i = 0; i < nout; ++i)
-            if (outs[i].host_out)
-                SNCH_CUDA(cudaMemcpyAsync(static_cast<char *>(outs[i].host_out) + b * outs[i].elem, dev_out[i],
-                                          m * outs[i].elem, cudaMemcpyDeviceToHost, st));
-    }
-    SNCH_CUDA(cudaStreamSynchronize(s->pipe[0]));
-    SNCH_CUDA(cudaStreamSynchronize(s->pipe[1]));
+        return SNCH_OK;
+    }();
+    const cudaError_t e0 = cudaStreamSynchronize(s->pipe[0]);
+    const cudaError_t e1 = cudaStreamSynchronize(s->pipe[1]);
+    if (queued != SNCH_OK)
+        return queued;
+    SNCH_CUDA(e0);
+    SNCH_CUDA(e1);
     return SNCH_OK;
 }
 
@@ -1058,6 +1071,11 @@ int snch_set_option(snch_scene_t s, int option, int64_t value)
         if (value < 0)
             return fail(SNCH_ERR_INVALID_ARGUMENT, "SNCH_OPT_ORDER_MIN_BATCH must be >= 0");
         s->order_min = value;
+        return SNCH_OK;
+    case SNCH_OPT_PACKET_PERSISTENT_MIN:
+        if (value < 1)
+            return fail(SNCH_ERR_INVALID_ARGUMENT, "SNCH_OPT_PACKET_PERSISTENT_MIN must be >= 1");
+        s->packet_persistent_min = value;
         return SNCH_OK;
     case SNCH_OPT_PERSISTENT_RAY:
         if (value != 0 && value != 1)
@@ -2255,6 +2273,7 @@ int snch_get_option(snch_scene_t s, int option, int64_t *value)
     case SNCH_OPT_PACKET_SILHOUETTE: *value = s->packet_sil; break;
     case SNCH_OPT_HOST_CHUNK: *value = s->host_chunk; break;
     case SNCH_OPT_PERSISTENT_RAY: *value = s->persistent_ray; break;
+    case SNCH_OPT_PACKET_PERSISTENT_MIN: *value = s->packet_persistent_min; break;
     default: return fail(SNCH_ERR_INVALID_ARGUMENT, "unknown option " + std::to_string(option));
     }
     return SNCH_OK;

@@ -151,6 +151,7 @@ struct TreeView
     // warp packets (a warp's 32 queries walk one shared traversal): 0 never,
     // 1 always, 2 when the batch is Morton-ordered (order_coherent)
     int packet_near = 0, packet_sil = 0;
+    int64_t packet_persistent_min = int64_t(1) << 23;  // packet batches this large run persistent
     int order_coherent = 0;  // order[] is the batch's Morton order (neighbours share warps)
     const float4 *wide4 = nullptr, *wide8 = nullptr;        // wide records
     const uint32_t *wide4_of = nullptr, *wide8_of = nullptr;  // wide index of each binary wide-root node

@@ -14,8 +14,11 @@
 // it (and clears what must start at zero), so two calls that overlap on the
 // GPU -- on different streams, or from different host threads -- race on it
 // and must be ordered by the caller.
+#include <cuda.h>
+
 #include <mutex>
 #include <string>
+#include <vector>
 
 #include "internal.h"
 
@@ -32,31 +35,70 @@ constexpr size_t kNoAllocBytes = 2 * kNoAllocTmpBytes + kNoAllocSortBytes + 256;
 // [tmp keys | tmp values | look-back flags, histograms, tile counters | status word]
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
-constexpr int kMaxDevices = 256;
-std::mutex g_setup_mutex;
-unsigned char *g_scratch_address[kMaxDevices] = {};
+// Device address of g_noalloc_scratch for the calling thread's current CUDA
+// context. In host code the array's name is only a host-side stand-in; the
+// address belongs to the module loaded in one context, not to a device
+// ordinal: a host plug-in may run under a context of its own, and after a
+// cudaDeviceReset the module is loaded again at a possibly different address.
+// So the address is looked up again (cudaGetSymbolAddress, which allocates
+// nothing) on every call whose stream is not being captured, and remembered per
+// context for calls made during a capture. A call under capture in a context
+// that has never made an uncaptured call looks it up too (the lookup can load
+// the module, which is why the first call belongs before any capture).
+using CtxGetCurrentFn = CUresult (*)(CUcontext *);
 
-// Device address of g_noalloc_scratch on the current device. In host code the
-// array's name is only a host-side stand-in, so the address is looked up once
-// per device (with that device current) and cached.
-cudaError_t scratch_address(unsigned char **out)
+CtxGetCurrentFn ctx_get_current()
 {
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
+    static CtxGetCurrentFn fn = [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            p = nullptr;
+        return reinterpret_cast<CtxGetCurrentFn>(p);
+    }();
+    return fn;
+}
+
+struct ContextAddress
+{
+    CUcontext ctx;
+    unsigned char *address;
+};
+std::mutex g_setup_mutex;
+std::vector<ContextAddress> g_scratch_address;  // one entry per context seen
+
+cudaError_t scratch_address(cudaStream_t st, unsigned char **out)
+{
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaError_t e = cudaStreamIsCapturing(st, &cs);
     if (e != cudaSuccess)
         return e;
-    if (dev < 0 || dev >= kMaxDevices)
-        return cudaErrorInvalidDevice;
+    CtxGetCurrentFn get = ctx_get_current();
+    CUcontext ctx = nullptr;
+    if (!get || get(&ctx) != CUDA_SUCCESS)
+        ctx = nullptr;
     std::lock_guard<std::mutex> lock(g_setup_mutex);
-    if (!g_scratch_address[dev])
+    ContextAddress *hit = nullptr;
+    if (ctx)
+        for (ContextAddress &c : g_scratch_address)
+            if (c.ctx == ctx)
+                hit = &c;
+    if (hit && cs != cudaStreamCaptureStatusNone)
     {
-        void *p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess)
-            return e;
-        g_scratch_address[dev] = static_cast<unsigned char *>(p);
+        *out = hit->address;
+        return cudaSuccess;
     }
-    *out = g_scratch_address[dev];
+    void *p = nullptr;
+    if ((e = cudaGetSymbolAddress(&p, g_noalloc_scratch)) != cudaSuccess)
+        return e;
+    if (!ctx && get && get(&ctx) != CUDA_SUCCESS)  // the lookup may have made the primary context current
+        ctx = nullptr;
+    if (hit)
+        hit->address = static_cast<unsigned char *>(p);
+    else if (ctx)
+        g_scratch_address.push_back({ctx, static_cast<unsigned char *>(p)});
+    *out = static_cast<unsigned char *>(p);
     return cudaSuccess;
 }
 
@@ -83,11 +125,11 @@ int snch_sort_pairs_noalloc(const uint32_t *keys_in, const uint32_t *values_in, 
         return SNCH_OK;
     if (sort_scratch_bytes((uint32_t)kNoAllocMaxPairs, 32) > kNoAllocSortBytes)
         return report_error(SNCH_ERR_TOO_LARGE, "internal: static sort scratch is too small");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
     unsigned char *base = nullptr;
-    cudaError_t e = scratch_address(&base);
+    cudaError_t e = scratch_address(st, &base);
     if (e != cudaSuccess)
         return report_error(SNCH_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-    cudaStream_t st = static_cast<cudaStream_t>(stream);
     uint32_t *tmp_keys = reinterpret_cast<uint32_t *>(base);
     uint32_t *tmp_vals = reinterpret_cast<uint32_t *>(base + kNoAllocTmpBytes);
     void *sort_scratch = base + 2 * kNoAllocTmpBytes;

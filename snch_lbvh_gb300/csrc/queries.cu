@@ -2743,9 +2743,6 @@ inline bool packet_ok(const TreeView &t, int packet, int width, const SeedArgs &
 // 1,280-triangle spheres: packets faster from 13 queries per triangle up).
 // Silhouette packets won at every measured density (0.26 queries per triangle up).
 constexpr uint64_t kPacketNearestMinQueriesPerTri = 3;
-// Packets run persistent from this batch size (measured faster at 16M and 166M
-// queries, slower at 1M: a walk-on-stars step and a 1M-point sphere batch)
-constexpr int64_t kPersistentPacketMinBatch = int64_t(1) << 23;
 inline bool packet_dense(const TreeView &t, int packet, int64_t n)
 {
     return packet == 1 || (uint64_t)n >= kPacketNearestMinQueriesPerTri * t.num_tris;
@@ -2802,7 +2799,7 @@ cudaError_t launch_nearest(const TreeView &t, const float *pts, int64_t n, uint3
         // 6 % slower on 1M-query batches. The counters' pass keeps the grid form.
         if (stats)
             nearest_packet_kernel<true><<<grid_for(n, 128), 128, 0, st>>>(t, pts, n, idx, dist, stats, seed);
-        else if (n >= kPersistentPacketMinBatch)
+        else if (n >= t.packet_persistent_min)
             return launch_persistent(nearest_packet_persistent_kernel, n, st, t, pts, n, idx, dist, seed);
         else
             nearest_packet_kernel<false><<<grid_for(n, 128), 128, 0, st>>>(t, pts, n, idx, dist, nullptr, seed);
@@ -2846,7 +2843,7 @@ cudaError_t launch_silhouette(const TreeView &t, const float *pts, const uint8_t
         if (stats)
             silhouette_packet_kernel<true>
                 <<<grid_for(n, 128), 128, 0, st>>>(t, pts, flip, n, dist, edge, stats, seed);
-        else if (n >= kPersistentPacketMinBatch)
+        else if (n >= t.packet_persistent_min)
             return launch_persistent(silhouette_packet_persistent_kernel, n, st, t, pts, flip, n, dist, edge, seed);
         else
             silhouette_packet_kernel<false>

@@ -5,7 +5,7 @@ properties of the tree."""
 import numpy as np
 import pytest
 
-from test_gpu_parity import bits, built_scene, check_cones, check_silhouette, check_tri_ids
+from test_gpu_parity import bits, built_scene, check_cones, check_edge_ids, check_silhouette, check_tri_ids
 
 pytestmark = pytest.mark.gpu
 
@@ -148,3 +148,65 @@ def test_tail_cap_full_scene(big):
         for x, y in zip(a, b):
             np.testing.assert_array_equal(x.view(np.uint8), y.view(np.uint8))
     assert s.device_status() == 0
+
+
+def _packet_answers(s, q, flip):
+    i, d = s.query_nearest(q)
+    sd, se = s.query_silhouette(q, flip)
+    return [x.cpu().numpy() for x in (i, d, sd, se)]
+
+
+def _check_persistent_packets(snch, sc, s, orc, pts, flip, n_oracle):
+    """Persistent warp packets (nearest_packet_persistent_kernel,
+    silhouette_packet_persistent_kernel) against the grid-launched packets
+    (bit for bit: the same packets walk the same traversals), the per-lane
+    searches (distances bit for bit, ids equal or an FP64 distance tie) and, on
+    a seeded subset of the same batch, the oracle (query.cuh:239-318, 326-423)."""
+    s.set_option(snch.OPT_PACKET, 0)
+    lane = _packet_answers(s, pts, flip)
+    s.set_option(snch.OPT_PACKET, 2)
+    s.set_option(snch.OPT_PACKET_PERSISTENT_MIN, 1 << 40)  # grid launch
+    grid = _packet_answers(s, pts, flip)
+    s.set_option(snch.OPT_PACKET_PERSISTENT_MIN, 1)  # persistent at any size
+    pers = _packet_answers(s, pts, flip)
+    s.set_option(snch.OPT_PACKET_PERSISTENT_MIN, 1 << 23)
+    assert s.get_option(snch.OPT_PACKET_PERSISTENT_MIN) == 1 << 23
+    assert s.device_status() == 0
+    for name, x, y in zip(("nearest idx", "nearest dist", "silhouette dist", "silhouette edge"), grid, pers):
+        np.testing.assert_array_equal(x.view(np.uint32), y.view(np.uint32), err_msg=name)
+    np.testing.assert_array_equal(bits(pers[1]), bits(lane[1]))
+    np.testing.assert_array_equal(bits(pers[2]), bits(lane[2]))
+    check_tri_ids(pers[0], lane[0], lane[1], pts, sc.verts, sc.faces)
+    check_edge_ids(pers[3], lane[3], lane[2], pts, sc.verts, s.export_topology()[2])
+    sub = np.random.default_rng(len(pts)).choice(len(pts), n_oracle, replace=False)
+    oi, od = orc.nearest(pts[sub])
+    np.testing.assert_array_equal(bits(pers[1][sub]), bits(od))
+    check_tri_ids(pers[0][sub], oi, od, pts[sub], sc.verts, sc.faces)
+    osd, ose = orc.silhouette(pts[sub], flip[sub])
+    check_silhouette(pers[2][sub], osd)
+    same = bits(pers[2][sub]) == bits(osd)
+    check_edge_ids(pers[3][sub][same], ose[same], osd[same], pts[sub][same], sc.verts, s.export_topology()[2])
+
+
+def test_persistent_packets_full_scene(big, oracle_mod):
+    """2M nearest + 2M silhouette queries on the 2M-triangle scene with the
+    persistent packet kernels forced below their default batch size."""
+    import snch_lbvh_gb300 as snch
+    sc, s, orc = big
+    rng = np.random.default_rng(31)
+    pts = rng.random((2_000_000, 3), dtype=np.float32)
+    flip = (rng.random(len(pts)) < 0.5).astype(np.uint8)
+    _check_persistent_packets(snch, sc, s, orc, pts, flip, 100_000)
+
+
+def test_persistent_packets_bench_size(big, oracle_mod):
+    """A batch above 2^23 queries (the size from which the persistent packet
+    kernels run by default, as in the 16M-query walk-on-stars step)."""
+    import snch_lbvh_gb300 as snch
+    from snch_lbvh_gb300 import meshes
+    sc, s, orc = big
+    n = (1 << 23) + 12_345
+    q = meshes.wost_queries(n, 1, 1, 1, seed=37)
+    pts = q["near_pts"]
+    flip = np.zeros(n, np.uint8)  # the step's silhouette queries carry flip = false
+    _check_persistent_packets(snch, sc, s, orc, pts, flip, 65_536)

@@ -77,6 +77,31 @@ def test_noalloc_sort_matches_allocating_sort_twice():
         np.testing.assert_array_equal(nv.cpu().numpy(), vals.cpu().numpy()[order])
 
 
+def test_noalloc_sort_in_place_and_without_status_word():
+    """keys_out == keys_in and values_out == values_in (documented as allowed),
+    and device_status NULL (the bits then go to the shared array's own word),
+    each against snch_sort_pairs, twice in a row."""
+    import torch
+    from snch_lbvh_gb300 import _ffi
+    L = _ffi.lib()
+    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    rng = np.random.default_rng(11)
+    for n, bits in ((300_001, 30), (65_536, 32)):
+        keys_np = rng.integers(0, 1 << bits, n, dtype=np.uint64).astype(np.uint32)
+        keys = torch.from_numpy(keys_np.view(np.int32)).cuda()
+        vals = torch.from_numpy(rng.permutation(n).astype(np.int32)).cuda()
+        ek, ev, _ = sort_existing(L, keys, vals, bits, stream)
+        k, v = keys.clone(), vals.clone()
+        rc = L.snch_sort_pairs_noalloc(ptr(k), ptr(v), ptr(k), ptr(v), n, bits, None, stream)
+        assert rc == 0, L.snch_last_error()
+        ko, vo = torch.empty_like(keys), torch.empty_like(vals)
+        rc = L.snch_sort_pairs_noalloc(ptr(keys), ptr(vals), ptr(ko), ptr(vo), n, bits, None, stream)
+        assert rc == 0, L.snch_last_error()
+        torch.cuda.synchronize()
+        for a, b in ((k, ek), (v, ev), (ko, ek), (vo, ev)):
+            np.testing.assert_array_equal(a.cpu().numpy(), b.cpu().numpy())
+
+
 def test_noalloc_sort_rejects_sizes_beyond_its_limit():
     import torch
     from snch_lbvh_gb300 import _ffi
