@@ -38,6 +38,8 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
+METRIC = ("queries/sec (walk-on-stars query set: nearest, silhouette, ray, sphere sample) on the 2M-triangle "
+          "scene")
 FULL = {"near": 16_000_000, "sil": 16_000_000, "ray": 16_000_000, "smp": 4_000_000}
 # kernels the default configuration runs for each query type (Morton-ordered
 # 16M-query batches, 8 queries per triangle: nearest and silhouette batches
@@ -67,6 +69,11 @@ def parse():
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-meshes leg")
     ap.add_argument("--no-wost", action="store_true", help="skip the walk-on-stars leg")
     ap.add_argument("--no-icosphere", action="store_true", help="skip the 20,480-triangle icosphere leg")
+    ap.add_argument("--output-scatter", type=int, default=-1, choices=[-1, 0, 1],
+                    help="SNCH_OPT_OUTPUT_SCATTER of the step's scene (-1: the library default)")
+    ap.add_argument("--persistent-min", type=int, default=0,
+                    help="SNCH_OPT_PACKET_PERSISTENT_MIN of the step's scene (0: the library default, 2^23); "
+                         "lets a reduced --scale run the persistent packet kernels of the full workload")
     return ap.parse_args()
 
 
@@ -102,6 +109,13 @@ def bit_mismatches(a, b):
         return -1
     w = {1: np.uint8, 2: np.uint16, 4: np.uint32, 8: np.uint64}[a.dtype.itemsize]
     return int(np.count_nonzero(a.view(w) != b.view(w)))
+
+
+def bench_config(counts, ntri, ws):
+    """The `config` of both arms' JSON lines (the same workload)."""
+    return {"workload": workload_name(counts, ntri),
+            "l2": "inputs larger than L2: 192 MB per 16M-query array, >1 GB of tree records",
+            "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"}
 
 
 def make_workload(scale, seed):
@@ -174,44 +188,64 @@ def traffic_of(kernel, workload_key):
     return None
 
 
+def issue_of(kernel):
+    """Issue-bound figures of `kernel` from the committed ncu summary, if any:
+    issue slots busy, active lanes per warp instruction, warp instructions per
+    query, DRAM % of peak (profiles/issue.txt)."""
+    path = os.path.join(ROOT, "profiles", "issue.txt")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        parts = line.split()
+        if len(parts) >= 6 and not line.startswith("#") and parts[0] == kernel:
+            return {"issue_slots_busy": float(parts[1]), "lanes_per_inst": float(parts[2]),
+                    "warp_inst_per_query": float(parts[3]), "dram_pct_of_peak": float(parts[4]),
+                    "profile": parts[5]}
+    return None
+
+
 # --------------------------------------------------------------------- CPU restatement
 def cpu_sample_counts(counts, frac):
     return {k: max(256, int(v * frac)) for k, v in counts.items()}
 
 
 def run_cpu(sc, q, counts, frac, nthreads):
-    """Times the CPU restatement: single-threaded build + a bounded sample of each
-    query batch on nthreads threads. Returns per-type q/s, build seconds, and
-    mean visit counts (for the algorithmic-bytes roofline)."""
+    """Times the CPU restatement on one bounded sample of the step: the
+    single-threaded build of the whole scene + the first `frac` of each query
+    batch on nthreads threads. value = sample queries / the wall time of that
+    sample (build included, so the build weighs 1/frac times more than in the
+    full step: a conservative figure). Also returns per-type q/s, the mean visit
+    counts (for the algorithmic-bytes roofline) and the tree."""
     from oracle import oracle
     oracle.build()
     t0 = time.perf_counter()
     tree = oracle.Tree(sc.verts, sc.faces)
     build_s = time.perf_counter() - t0
     sc_n = cpu_sample_counts(counts, frac)
-    out, stats = {}, {}
+    out, stats, secs = {}, {}, {}
     t0 = time.perf_counter()
     _, _, st = tree.nearest(q["near_pts"][:sc_n["near"]], stats=True, nthreads=nthreads)
-    out["near"] = sc_n["near"] / (time.perf_counter() - t0)
+    secs["near"] = time.perf_counter() - t0
     stats["near"] = st.mean(0)
     t0 = time.perf_counter()
     _, _, st = tree.silhouette(q["sil_pts"][:sc_n["sil"]], q["sil_flip"][:sc_n["sil"]], stats=True, nthreads=nthreads)
-    out["sil"] = sc_n["sil"] / (time.perf_counter() - t0)
+    secs["sil"] = time.perf_counter() - t0
     stats["sil"] = st.mean(0)
     t0 = time.perf_counter()
     *_, st = tree.ray(q["ray_o"][:sc_n["ray"]], q["ray_d"][:sc_n["ray"]], q["ray_tmax"][:sc_n["ray"]], stats=True,
                       nthreads=nthreads)
-    out["ray"] = sc_n["ray"] / (time.perf_counter() - t0)
+    secs["ray"] = time.perf_counter() - t0
     stats["ray"] = st.mean(0)
     t0 = time.perf_counter()
     *_, st = tree.sample(q["smp_c"][:sc_n["smp"]], q["smp_r"][:sc_n["smp"]], q["smp_u"][:sc_n["smp"]], stats=True,
                          nthreads=nthreads)
-    out["smp"] = sc_n["smp"] / (time.perf_counter() - t0)
+    secs["smp"] = time.perf_counter() - t0
     stats["smp"] = st.mean(0)
-    step_s = build_s + sum(counts[k] / out[k] for k in counts)
-    total = sum(counts.values())
-    return {"qps": out, "build_s": build_s, "step_s": step_s, "value": total / step_s, "stats": stats,
-            "sample": sc_n}
+    out = {k: sc_n[k] / secs[k] for k in secs}
+    wall_s = build_s + sum(secs.values())
+    n_sample = sum(sc_n.values())
+    return {"qps": out, "build_s": build_s, "wall_s": wall_s, "queries": n_sample, "value": n_sample / wall_s,
+            "stats": stats, "sample": sc_n, "tree": tree}
 
 
 def algorithmic_bytes(kind, st):
@@ -292,10 +326,41 @@ def learned_leg(scene, sc, dev, counts, out, steps, scale):
             best = (margin, r)
     res["best_margin"] = best[0]
     res["near_qps"], res["sil_qps"] = best[1]["near_qps"], best[1]["sil_qps"]
+    res["ceiling"] = radius_ceiling(scene, dev, counts, out, steps)
     res["identical_to_plain"] = all(r["identical_to_plain"] for r in res["margins"].values())
     res["reference_order"] = learned_on_reference_order(scene, model, dev, best[0], best[1]["mlp_ms"], counts)
     model.close()
     return res
+
+
+def radius_ceiling(scene, dev, counts, out, steps):
+    """What radius seeding can buy at most on the default traversal: every query
+    seeded with its own answer (the next float above the plain distance, so that
+    no query falls back), no MLP time, against the plain search on the same
+    batch. No predictor can prune more than the exact distance does."""
+    import torch
+    stream = torch.cuda.current_stream()
+    rn = torch.from_numpy(np.nextafter(out["near"][1].cpu().numpy(), np.float32(np.inf))).cuda()
+    rs = torch.from_numpy(np.nextafter(out["sil"][0].cpu().numpy(), np.float32(np.inf))).cuda()
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(5)] for _ in range(steps + 1)]
+    for k in range(steps + 1):  # the first round is a warm-up
+        e = ev[k]
+        e[0].record(stream)
+        scene.query_nearest(dev["near_pts"])
+        e[1].record(stream)
+        scene.query_nearest_seeded(dev["near_pts"], rn)
+        e[2].record(stream)
+        scene.query_silhouette(dev["sil_pts"], dev["sil_flip"])
+        e[3].record(stream)
+        scene.query_silhouette_seeded(dev["sil_pts"], rs, dev["sil_flip"])
+        e[4].record(stream)
+    torch.cuda.synchronize()
+    ms = np.array([[e[i].elapsed_time(e[i + 1]) for i in range(4)] for e in ev[1:]]).mean(0)
+    return {"what": "seeded with each query's own distance (next float up), no MLP: the upper bound of any "
+                    "radius predictor on this traversal",
+            "plain_ms": {"near": float(ms[0]), "sil": float(ms[2])},
+            "exact_seeded_ms": {"near": float(ms[1]), "sil": float(ms[3])},
+            "speedup": {"near": float(ms[0] / ms[1]), "sil": float(ms[2] / ms[3])}}
 
 
 def learned_on_reference_order(scene, model, dev, margin, mlp_ms, counts, sub=2_000_000):
@@ -632,43 +697,50 @@ def wost_leg(scale, walkers=1_000_000, max_steps=128):
 
 # --------------------------------------------------------------------- reference arm
 def run_reference(args):
+    """The reference's own implementation of the step on this machine: the CPU
+    restatement of its build and queries (its documented CPU query path is
+    broken, README.md:39) on all host cores, each step one bounded sample of the
+    workload, timed as it runs; plus the reference's own CUDA queries (its
+    headers compiled for sm_103a) over a tree the restatement built."""
     ws, rank, _ = dist_env()
     if rank != 0:
         return
     sc, counts, q = make_workload(args.scale, seed=1)
     nthreads = cpu_threads()
-    frac = 0.01
-    # warmup steps are short: the build is the expensive part and is repeated
-    vals = []
+    frac, warm_frac = 0.01, 0.001
+    rows = []
     for i in range(args.warmup + args.steps):
-        r = run_cpu(sc, q, counts, frac if i >= args.warmup else 0.001, nthreads)
+        r = run_cpu(sc, q, counts, frac if i >= args.warmup else warm_frac, nthreads)
         if i >= args.warmup:
-            vals.append(r)
-    value = float(np.mean([r["value"] for r in vals]))
-    step_ms = float(np.mean([r["step_s"] for r in vals]) * 1e3)
-    smp = vals[-1]["sample"]
+            rows.append(r)
+    wall = sum(r["wall_s"] for r in rows)
+    value = sum(r["queries"] for r in rows) / wall
+    smp = rows[-1]["sample"]
     line = {
-        "impl": "reference", "metric": "queries/sec (walk-on-stars query set: nearest, silhouette, ray, sphere "
-        "sample) on the 2M-triangle scene", "value": value, "unit": "queries/s", "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
-        "config": {"workload": workload_name(counts, len(sc.faces)), "backend": "cpu"},
-        "per_type_qps": {k: float(np.mean([r["qps"][k] for r in vals])) for k in counts},
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "queries/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * wall / len(rows), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded meshes and queries)",
+        "config": bench_config(counts, len(sc.faces), ws),
+        "per_type_qps": {k: float(np.mean([r["qps"][k] for r in rows])) for k in counts},
+        "build_s": float(np.mean([r["build_s"] for r in rows])),
         "cpu_baseline": {"value": value, "unit": "queries/s", "cores": nthreads, "kind": "port",
-                         "sample": f"per step: single-thread build of the {len(sc.faces):,}-triangle scene + "
-                                   f"{smp['near']:,} nearest, {smp['sil']:,} silhouette, {smp['ray']:,} ray, "
-                                   f"{smp['smp']:,} sample queries on {nthreads} threads, each type "
-                                   f"extrapolated to its full batch"},
+                         "sample": f"per step: single-thread build of the whole {len(sc.faces):,}-triangle scene + "
+                                   f"the first {smp['near']:,} nearest, {smp['sil']:,} silhouette, {smp['ray']:,} "
+                                   f"ray and {smp['smp']:,} sample queries ({frac:.0%} of each batch) on {nthreads} "
+                                   f"threads; value = those queries / the step's wall time"},
         "e2e": {"value": value, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
-    line["reference_cuda"] = reference_cuda_leg(sc, q, counts)
+    line["reference_cuda"] = reference_cuda_leg(rows[-1]["tree"], q, counts)
     print(json.dumps(line), flush=True)
 
 
-def reference_cuda_leg(sc, q, counts, sample=2_000_000):
+def reference_cuda_leg(tree, q, counts, sample=2_000_000):
     """The reference's own query_device kernels (its headers compiled for sm_103a
-    with its flags, oracle/ref_gpu_kernels.cu) timed on this GPU over a tree
-    built by this library; queries only, a bounded sample of each batch."""
+    with its flags, oracle/ref_gpu_kernels.cu), timed on this GPU over a tree the
+    CPU restatement built (oracle/ref_gpu.py RefTree: the reference's device
+    layout, no code of this library); queries only, a bounded sample of each
+    batch. The reference's build runs Thrust from host code compiled with its
+    headers, which this GPU machine cannot compile (they are not on it)."""
     try:
         import torch
         if not torch.cuda.is_available():
@@ -677,16 +749,11 @@ def reference_cuda_leg(sc, q, counts, sample=2_000_000):
         ok, why = ref_gpu.available()
         if not ok:
             return {"unavailable": why}
-        import snch_lbvh_gb300 as snch
-        scene = snch.Scene(torch.from_numpy(sc.verts).cuda(), torch.from_numpy(sc.faces).cuda())
-        scene.compute_silhouettes()
-        scene.build_bvh()
-        R = ref_gpu.RefQueries(scene)
+        R = ref_gpu.RefQueries(ref_gpu.RefTree(tree))
         m = {k: min(sample, counts[k]) for k in counts}
-        d = {k: torch.from_numpy(np.ascontiguousarray(v[:m[{"near_pts": "near", "sil_pts": "sil", "sil_flip": "sil",
-                                                         "ray_o": "ray", "ray_d": "ray", "ray_tmax": "ray",
-                                                         "smp_c": "smp", "smp_r": "smp", "smp_u": "smp"}[k]]]))
-             .cuda() for k, v in q.items()}
+        kind = {"near_pts": "near", "sil_pts": "sil", "sil_flip": "sil", "ray_o": "ray", "ray_d": "ray",
+                "ray_tmax": "ray", "smp_c": "smp", "smp_r": "smp", "smp_u": "smp"}
+        d = {k: torch.from_numpy(np.ascontiguousarray(v[:m[kind[k]]])).cuda() for k, v in q.items()}
         calls = {"near": lambda: R.nearest(d["near_pts"]), "sil": lambda: R.silhouette(d["sil_pts"], d["sil_flip"]),
                  "ray": lambda: R.ray(d["ray_o"], d["ray_d"], d["ray_tmax"]),
                  "smp": lambda: R.sample(d["smp_c"], d["smp_r"], d["smp_u"])}
@@ -702,9 +769,9 @@ def reference_cuda_leg(sc, q, counts, sample=2_000_000):
             qps[k] = m[k] / (e0.elapsed_time(e1) / 1e3)
         t = sum(counts[k] / qps[k] for k in counts)
         return {"value": sum(counts.values()) / t, "unit": "queries/s", "per_type_qps": qps,
+                "tree": "built by the CPU restatement (oracle), reference device layout",
                 "sample": f"{m['near']:,} nearest, {m['sil']:,} silhouette, {m['ray']:,} ray, {m['smp']:,} sample "
-                          f"queries (input order), each extrapolated to its batch; queries only (the reference's "
-                          f"build is host Thrust code)"}
+                          f"queries (input order), each extrapolated to its batch; queries only"}
     except Exception as exc:  # reported, never fatal for the CPU arm
         return {"unavailable": f"{type(exc).__name__}: {exc}"}
 
@@ -738,6 +805,10 @@ def run_ours(args):
     verts_d = torch.from_numpy(sc.verts).cuda()
     faces_d = torch.from_numpy(sc.faces).cuda()
     scene = snch.Scene(verts_d, faces_d)
+    if args.persistent_min > 0:
+        scene.set_option(snch.OPT_PACKET_PERSISTENT_MIN, args.persistent_min)
+    if args.output_scatter >= 0:
+        scene.set_option(snch.OPT_OUTPUT_SCATTER, args.output_scatter)
     stream = torch.cuda.current_stream()
 
     def step(ev=None):
@@ -907,6 +978,7 @@ def run_ours(args):
     cpu = None
     if ws == 1 and not args.no_cpu_baseline:
         cpu = run_cpu(sc, q, counts, 0.005, cpu_threads())
+        cpu.pop("tree")
     kinds = ["near", "sil", "ray", "smp"]
     dom = kinds[int(np.argmax(phase_ms[1:]))]
     peak, peak_src = hbm_peak()
@@ -923,18 +995,33 @@ def run_ours(args):
             per_kernel[KERNEL_OF[k]]["reference_order_bytes_per_query"] = bref
             per_kernel[KERNEL_OF[k]]["effective_GB/s"] = bref * counts[k] / (ms / 1e3) / 1e9
     dk = per_kernel[KERNEL_OF[dom]]
-    roof = {"bound": "hbm", "kernel": KERNEL_OF[dom], "achieved": dk["GB/s"], "peak": peak, "unit": "GB/s",
-            "frac": dk["GB/s"] / peak, "peak_source": peak_src,
-            "algorithmic_bytes_per_query": dk["bytes_per_query"], "traffic": traffic_of(KERNEL_OF[dom], "wost_2m"),
+    dom_ms = float(phase_ms[1 + kinds.index(dom)])
+    traffic = traffic_of(KERNEL_OF[dom], "wost_2m")
+    issue = issue_of(KERNEL_OF[dom])
+    dram_gbs = traffic / (dom_ms / 1e3) / 1e9 if traffic else None
+    roof = {"bound": "issue" if issue else "hbm", "kernel": KERNEL_OF[dom],
+            "achieved": dram_gbs, "peak": peak, "unit": "GB/s",
+            "frac": dram_gbs / peak if dram_gbs else None, "peak_source": peak_src, "traffic": traffic,
+            "basis": "achieved = the kernel's measured DRAM bytes per launch (ncu, profiles/traffic.txt) / its "
+                     "event time; the warp-packet searches are bound by instruction issue, not by HBM",
+            "issue": issue,
+            "effective": {"achieved": dk.get("effective_GB/s"),
+                          "frac": dk["effective_GB/s"] / peak if "effective_GB/s" in dk else None,
+                          "algorithmic_bytes_per_query": dk.get("reference_order_bytes_per_query"),
+                          "basis": "reference record sizes x the visits of the reference's own traversal order "
+                                   "(CPU restatement on a sample) / this kernel's time: what the same answers "
+                                   "cost the reference's algorithm, per second of this kernel"},
+            "own_visits": {"achieved": dk["GB/s"], "frac": dk["GB/s"] / peak,
+                           "algorithmic_bytes_per_query": dk["bytes_per_query"],
+                           "basis": "reference record sizes x this kernel's own per-lane visits / its time; a "
+                                    "warp packet loads a shared record once for all its lanes, so this exceeds "
+                                    "the bytes it moves"},
             "per_kernel": per_kernel}
     line = {
-        "metric": "queries/sec (walk-on-stars query set: nearest, silhouette, ray, sphere sample) on the 2M-triangle "
-                  "scene", "value": value, "unit": "queries/s", "n_gpus": ws, "steps": args.steps,
+        "metric": METRIC, "value": value, "unit": "queries/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded meshes and queries)",
-        "config": {"workload": workload_name(counts, len(sc.faces)),
-                   "l2": "inputs larger than L2: 192 MB per 16M-query array, >1 GB of tree records",
-                   "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
+        "config": bench_config(counts, len(sc.faces), ws),
         "per_type_qps": {k: float(v) for k, v in per_type.items()},
         "ray_test": ray_test,
         "phase_ms": {"build": float(phase_ms[0]), **{k: float(phase_ms[1 + i]) for i, k in enumerate(kinds)}},
@@ -951,9 +1038,10 @@ def run_ours(args):
     if cpu is not None:
         smp = cpu["sample"]
         line["cpu_baseline"] = {"value": cpu["value"], "unit": "queries/s", "cores": cpu_threads(), "kind": "port",
-                                "sample": f"single-thread build of the {len(sc.faces):,}-triangle scene + "
-                                          f"{smp['near']:,} nearest, {smp['sil']:,} silhouette, {smp['ray']:,} ray, "
-                                          f"{smp['smp']:,} sample queries, each type extrapolated to its batch",
+                                "sample": f"single-thread build of the whole {len(sc.faces):,}-triangle scene + "
+                                          f"the first {smp['near']:,} nearest, {smp['sil']:,} silhouette, "
+                                          f"{smp['ray']:,} ray, {smp['smp']:,} sample queries (0.5 % of each batch); "
+                                          f"value = those queries / the wall time",
                                 "per_type_qps": {k: float(v) for k, v in cpu["qps"].items()},
                                 "build_s": cpu["build_s"]}
     print(json.dumps(line), flush=True)

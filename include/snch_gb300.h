@@ -97,6 +97,40 @@ int snch_build_bvh(snch_scene_t scene, snch_stream_t stream);
  * reference's device layout (device pointers owned by the scene). */
 int snch_get_bvh_view(snch_scene_t scene, snch_bvh_view *out_view);
 
+/* The built tree in this library's traversal layout, for the header-only
+ * device functions of snch_device.cuh (snch::query_device and friends, called
+ * per thread from a caller's own kernels). No reference counterpart: it plays
+ * the role of the reference's device view (bvh_device, bvh.cuh:36-72) for the
+ * device-side query_device of query.cuh:82-423 and sample.cuh:10-91. Device
+ * pointers owned by the scene, valid until it is rebuilt or destroyed. Records
+ * (32-bit floats; "bits" = a uint32 stored in a float slot):
+ *   inner[N-1], 64 B: (Lup.xyz, Llo.x) (Llo.yz, Rup.xy) (Rup.z, Rlo.xyz)
+ *                     (bits L, bits R, bits Linfo, bits Rinfo); children are
+ *                     node ids (internal < N-1 <= leaf N-1+j for sorted leaf j);
+ *                     a leaf child's info = depth-first rank | owned edges << 30
+ *   inner_cones[N-1], 48 B: (L.axis, L.half) (L.radius, R.axis) (R.half, R.radius, 0, 0)
+ *   leaves[N], 48 B:  (a.xyz, bits original index) (b.xyz, bits owned edges) (c.xyz, bits rank)
+ *   edges[3N], 64 B:  owned silhouette edge k of sorted leaf j at 3j+k:
+ *                     (p0.xyz, bits face flags) (p1.xyz, bits edge id) (n0.xyz, 0) (n1.xyz, 0)
+ *   root_box:         6 floats, upper xyz then lower xyz
+ *   vertices / triangles: the scene's own arrays (sample_on_object)
+ *   status:           the scene's device status word (stack overflow bit)
+ * Plain scenes only (a batched scene returns SNCH_ERR_INVALID_ARGUMENT). */
+typedef struct
+{
+    uint32_t num_triangles;
+    uint32_t reserved;
+    const float *root_box;
+    const void *inner;
+    const void *inner_cones;
+    const void *leaves;
+    const void *edges;
+    const float *vertices;
+    const int32_t *triangles;
+    uint32_t *status;
+} snch_traversal_view;
+int snch_get_traversal_view(snch_scene_t scene, snch_traversal_view *out_view);
+
 /* scene_loader<3>(filename) scene_loader.cuh:86-152, a host-side reader: "v x y z"
  * vertices and "f a b c" triangles (1-based in the file, 0-based out; the first
  * three indices of a longer face; every other line ignored), into caller HOST
@@ -227,6 +261,15 @@ int snch_set_traversal(snch_scene_t scene, int mode);
  *                             packets, same answers). Default 2^23 (measured faster from
  *                             there, 6 % slower on 1M-query batches); >= 1. */
 #define SNCH_OPT_PACKET_PERSISTENT_MIN 19
+/*   SNCH_OPT_OUTPUT_SCATTER   1 (default): the results of a Morton-ordered, unseeded
+ *                             batch are written in batch order to a temporary and then
+ *                             moved to input order by one scatter pass, so that each
+ *                             warp's stores fill whole sectors (written at input
+ *                             positions directly, neighbouring lanes store 4 bytes each
+ *                             to unrelated sectors and DRAM sees up to 8x the output
+ *                             bytes); 0: results written at input positions by the
+ *                             search kernels. Same results either way. */
+#define SNCH_OPT_OUTPUT_SCATTER 20
 /*   SNCH_OPT_HOST_CHUNK       queries per chunk of the *_host forms (at most 29 bytes in
  *                             and 17 out per query on each of two streams): chunk i's
  *                             input copy, search and output copy run on stream i % 2, so
@@ -530,6 +573,13 @@ int snch_sample_in_sphere_host(snch_scene_t scene, const float *centers_xyz, con
  * Used to count algorithmic bytes; no reference counterpart. */
 int snch_query_visits(snch_scene_t scene, int kind, const float *in0, const float *in1, const float *in2,
                       const uint8_t *flip, int64_t n, uint32_t *visits, snch_stream_t stream);
+/* The same counters for the first pass of a seeded nearest (kind 0) or
+ * silhouette (kind 1) search (snch_query_*_seeded): the search starts with the
+ * DEVICE radii `radius` as its bound; queries that find nothing inside their
+ * radius would then be answered by an unbounded pass, which is not counted
+ * here. Shows what a learned radius saves; no reference counterpart. */
+int snch_query_visits_seeded(snch_scene_t scene, int kind, const float *points, const uint8_t *flip,
+                             const float *radius, int64_t n, uint32_t *visits, snch_stream_t stream);
 
 /* ------------------------------------------------------------------ building blocks */
 

@@ -38,6 +38,8 @@ def lib():
         L.rg_load.argtypes = [C.c_char_p]
         L.rg_nearest.argtypes = [P, P, I, P, P, P]
         L.rg_silhouette.argtypes = [P, P, P, I, P, P]
+        L.rg_silhouette_edge.argtypes = [P, P, P, I, P, P, P]
+        L.rg_ray_uv.argtypes = [P, P, P, P, I, P, P, P, P, P]
         L.rg_ray.argtypes = [P, P, P, P, I, P, P, P, P]
         L.rg_sample.argtypes = [P, P, P, P, I, P, P, P]
         rc = L.rg_load(CUBIN.encode())
@@ -51,11 +53,56 @@ def _p(t):
     return None if t is None else C.c_void_p(t.data_ptr())
 
 
+class RefView(C.Structure):
+    """lbvh::bvh_device<float, 3, scene<3>::triangle> (bvh.cuh:36-72): counts, then
+    node / aabb / cone / object device pointers (40 bytes)."""
+    _fields_ = [("num_nodes", C.c_uint32), ("num_objects", C.c_uint32), ("nodes", C.c_void_p),
+                ("aabbs", C.c_void_p), ("cones", C.c_void_p), ("objects", C.c_void_p)]
+
+
+class RefTree:
+    """A tree built by the ORACLE (the CPU restatement of the reference's build,
+    bvh.cuh:380-613 with the silhouette topology of scene.cuh:1135-1229, equal bit
+    for bit to the reference's own build on every golden mesh), uploaded in the
+    reference's device layout -- nodes (bvh.cuh:27-33), aabbs upper-first,
+    cones, scene<3>::triangle objects (scene.cuh:826-840: vertex ids, owned
+    silhouette ids, vertex and edge pointers; 40 B) and silhouette_edge records
+    (scene.cuh:708-722: 4 vertex ids and the vertex pointer; 32 B) -- so that the
+    reference's own CUDA queries run on a tree this library never touched."""
+
+    def __init__(self, tree):
+        import numpy as np
+        import torch
+        n = tree.num_tris
+        dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+        self.verts = dev(tree.verts)
+        self.nodes = dev(tree.nodes.view(np.int32))
+        self.aabbs = dev(tree.aabbs)
+        self.cones = dev(tree.cones)
+        vptr = self.verts.data_ptr()
+        ne = len(tree.edge_verts)
+        e = np.zeros((max(ne, 1), 4), np.int64)  # 32 B per edge
+        if ne:
+            e[:, :2] = tree.edge_verts.astype(np.int32).view(np.int64)
+            e[:, 2] = vptr
+        self.edges = dev(e)
+        o = np.zeros((max(n, 1), 5), np.int64)  # 40 B per triangle
+        if n:
+            o[:, :3] = np.concatenate([tree.tris, tree.tri_owned], axis=1).astype(np.int32).view(np.int64)
+            o[:, 3] = vptr
+            o[:, 4] = self.edges.data_ptr()
+        self.objects = dev(o)
+        self.view = RefView(2 * n - 1 if n else 0, n, self.nodes.data_ptr(), self.aabbs.data_ptr(),
+                            self.cones.data_ptr(), self.objects.data_ptr())
+
+
 class RefQueries:
-    """The reference's query_device kernels over `scene` (an snch_lbvh_gb300.Scene)."""
+    """The reference's query_device kernels over a tree: an snch_lbvh_gb300.Scene
+    (through its byte-compatible snch_bvh_view) or a RefTree."""
 
     def __init__(self, scene):
-        self.view = scene.get_bvh_device_ptr()
+        self.view = scene.view if isinstance(scene, RefTree) else scene.get_bvh_device_ptr()
+        self._keep = scene
         self.L = lib()
 
     def _s(self, stream):
@@ -78,6 +125,16 @@ class RefQueries:
         assert rc == 0, rc
         return dist
 
+    def silhouette_edge(self, pts, flip=None, stream=None):
+        """Distance and the silhouette edge the reference's traversal ended on."""
+        import torch
+        n = pts.shape[0]
+        dist = torch.empty(n, device="cuda")
+        edge = torch.empty(n, dtype=torch.int32, device="cuda")
+        rc = self.L.rg_silhouette_edge(C.byref(self.view), _p(pts), _p(flip), n, _p(dist), _p(edge), self._s(stream))
+        assert rc == 0, rc
+        return dist, edge
+
     def ray(self, o, d, tmax, out=None, stream=None):
         import torch
         n = o.shape[0]
@@ -86,6 +143,19 @@ class RefQueries:
         rc = self.L.rg_ray(C.byref(self.view), _p(o), _p(d), _p(tmax), n, _p(hit), _p(t), _p(idx), self._s(stream))
         assert rc == 0, rc
         return hit, t, idx
+
+    def ray_uv(self, o, d, tmax, stream=None):
+        """Closest hit with its barycentric (u, v): hit, t, uv (n, 2), triangle index."""
+        import torch
+        n = o.shape[0]
+        hit = torch.empty(n, dtype=torch.uint8, device="cuda")
+        t = torch.empty(n, device="cuda")
+        uv = torch.empty((n, 2), device="cuda")
+        idx = torch.empty(n, dtype=torch.int32, device="cuda")
+        rc = self.L.rg_ray_uv(C.byref(self.view), _p(o), _p(d), _p(tmax), n, _p(hit), _p(t), _p(uv), _p(idx),
+                              self._s(stream))
+        assert rc == 0, rc
+        return hit, t, uv, idx
 
     def sample(self, c, r, u, out=None, stream=None):
         import torch

@@ -11,15 +11,16 @@
 #include <stdint.h>
 
 static cudaLibrary_t g_lib;
-static cudaKernel_t g_k[4];
-static const char *g_names[4] = {"ref_nearest", "ref_silhouette", "ref_ray", "ref_sample"};
+#define NK 6
+static cudaKernel_t g_k[NK];
+static const char *g_names[NK] = {"ref_nearest", "ref_silhouette", "ref_ray", "ref_sample", "ref_silhouette_edge", "ref_ray_uv"};
 
 /* returns 0 on success, else the cudaError_t */
 int rg_load(const char *cubin_path) {
     if (g_lib) return 0;
     cudaError_t e = cudaLibraryLoadFromFile(&g_lib, cubin_path, NULL, NULL, 0, NULL, NULL, 0);
     if (e != cudaSuccess) return (int)e;
-    for (int i = 0; i < 4; ++i) {
+    for (int i = 0; i < NK; ++i) {
         e = cudaLibraryGetKernel(&g_k[i], g_lib, g_names[i]);
         if (e != cudaSuccess) return (int)e;
     }
@@ -59,4 +60,18 @@ int rg_sample(const void *view, const float *c, const float *r, const float *u, 
     view40 v = *(const view40 *)view;
     void *args[] = {&v, &c, &r, &u, &n, &idx, &pdf};
     return launch(3, n, args, stream);
+}
+
+int rg_silhouette_edge(const void *view, const float *pts, const unsigned char *flip, int n, float *dist, int *edge,
+                       void *stream) {
+    view40 v = *(const view40 *)view;
+    void *args[] = {&v, &pts, &flip, &n, &dist, &edge};
+    return launch(4, n, args, stream);
+}
+
+int rg_ray_uv(const void *view, const float *o, const float *d, const float *tmax, int n, unsigned char *hit, float *t,
+              float *uv, unsigned *idx, void *stream) {
+    view40 v = *(const view40 *)view;
+    void *args[] = {&v, &o, &d, &tmax, &n, &hit, &t, &uv, &idx};
+    return launch(5, n, args, stream);
 }

@@ -18,6 +18,7 @@ import os
 
 import numpy as np
 
+from . import _ffi
 from ._ffi import BvhView, SnchError, check, lib  # noqa: F401
 
 __all__ = ["Scene", "BatchedScene", "Scene2", "Graph", "SnchError", "BvhView", "lib", "read_obj",
@@ -34,6 +35,7 @@ OPT_HOST_CHUNK = 15
 OPT_PERSISTENT_NEAREST, OPT_PERSISTENT_SILHOUETTE = 16, 17
 OPT_PERSISTENT_RAY = 18
 OPT_PACKET_PERSISTENT_MIN = 19
+OPT_OUTPUT_SCATTER = 20
 
 
 def _torch():
@@ -155,6 +157,13 @@ class Scene:
         check(lib().snch_get_bvh_view(self._h, C.byref(v)))
         return v
 
+    def get_traversal_view(self):
+        """The tree in the traversal layout for snch_device.cuh's per-thread queries
+        (snch_traversal_view); valid until the scene is rebuilt or destroyed."""
+        v = _ffi.TraversalView()
+        check(lib().snch_get_traversal_view(self._h, C.byref(v)))
+        return v
+
     def set_traversal(self, mode: int):
         """TRAVERSAL_NEAR_FIRST (default) or TRAVERSAL_REFERENCE_ORDER; same results."""
         check(lib().snch_set_traversal(self._h, int(mode)))
@@ -224,6 +233,20 @@ class Scene:
         out = torch.empty((n, 3), dtype=torch.int32, device="cuda")
         check(lib().snch_query_visits(self._h, k, _ptr(ins[0]), _ptr(ins[1]), _ptr(ins[2]), _ptr(f), n, _ptr(out),
                                       _stream(stream)))
+        return out.cpu().numpy().view(np.uint32)
+
+    def query_visits_seeded(self, kind: str, points, radius, flip=None, stream=None):
+        """The same counters for the seeded first pass of a nearest / silhouette
+        search started at the given radii (queries with nothing inside their
+        radius would go to an unbounded pass, not counted here)."""
+        torch = _torch()
+        k = {"nearest": 0, "silhouette": 1}[kind]
+        p = _dev(points, torch.float32, 3)
+        r = _dev(radius, torch.float32)
+        f = None if flip is None else _dev(flip, torch.uint8)
+        n = p.shape[0]
+        out = torch.empty((n, 3), dtype=torch.int32, device="cuda")
+        check(lib().snch_query_visits_seeded(self._h, k, _ptr(p), _ptr(f), _ptr(r), n, _ptr(out), _stream(stream)))
         return out.cpu().numpy().view(np.uint32)
 
     def vertices(self):

@@ -31,6 +31,13 @@ class BvhView(C.Structure):
                 ("cones", P), ("objects", P)]
 
 
+class TraversalView(C.Structure):
+    """snch_traversal_view: the tree in this library's 64-byte record layout, read by
+    the header-only device functions of include/snch_device.cuh."""
+    _fields_ = [("num_triangles", C.c_uint32), ("reserved", C.c_uint32), ("root_box", P), ("inner", P),
+                ("inner_cones", P), ("leaves", P), ("edges", P), ("vertices", P), ("triangles", P), ("status", P)]
+
+
 # name -> (restype, argtypes), parsed from the public header so the binding
 # cannot drift from it
 def _header_signatures():

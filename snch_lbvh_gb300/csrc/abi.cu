@@ -116,6 +116,7 @@ struct snch_scene_s
     int block_near = 128, block_sil = 128;  // threads per block of the binary searches
     int packet_near = 2, packet_sil = 2;    // warp packets: 0 never, 1 always, 2 Morton-ordered batches
     int64_t packet_persistent_min = int64_t(1) << 23;  // packet batches this large run persistent
+    int output_scatter = 1;  // ordered batches: results in batch order, then one scatter pass
     float4 *wide[2] = {nullptr, nullptr};
     uint32_t *wide_idx[2] = {nullptr, nullptr};  // wide index of each wide-root binary node
     size_t wide_cap[2] = {0, 0};  // records allocated
@@ -141,6 +142,7 @@ struct snch_scene_s
         t.packet_near = packet_near;
         t.packet_sil = packet_sil;
         t.packet_persistent_min = packet_persistent_min;
+        t.out_batch_order_enabled = output_scatter;
         if (wide_ready[0])
         {
             t.wide4 = wide[0];
@@ -1072,6 +1074,11 @@ int snch_set_option(snch_scene_t s, int option, int64_t value)
             return fail(SNCH_ERR_INVALID_ARGUMENT, "SNCH_OPT_ORDER_MIN_BATCH must be >= 0");
         s->order_min = value;
         return SNCH_OK;
+    case SNCH_OPT_OUTPUT_SCATTER:
+        if (value != 0 && value != 1)
+            return fail(SNCH_ERR_INVALID_ARGUMENT, "SNCH_OPT_OUTPUT_SCATTER takes 0 or 1");
+        s->output_scatter = (int)value;
+        return SNCH_OK;
     case SNCH_OPT_PACKET_PERSISTENT_MIN:
         if (value < 1)
             return fail(SNCH_ERR_INVALID_ARGUMENT, "SNCH_OPT_PACKET_PERSISTENT_MIN must be >= 1");
@@ -1176,6 +1183,28 @@ int snch_get_bvh_view(snch_scene_t s, snch_bvh_view *out)
     out->aabbs = reinterpret_cast<const snch_aabb *>(s->aabbs);
     out->cones = reinterpret_cast<const snch_cone *>(s->cones);
     out->objects = s->ref_objects;
+    return SNCH_OK;
+}
+
+int snch_get_traversal_view(snch_scene_t s, snch_traversal_view *out)
+{
+    int rc = check_built(s);
+    if (rc != SNCH_OK)
+        return rc;
+    if (!out)
+        return fail(SNCH_ERR_INVALID_ARGUMENT, "out_view is NULL");
+    if (s->num_meshes > 0)
+        return fail(SNCH_ERR_INVALID_ARGUMENT, "snch_get_traversal_view serves plain scenes, not batched ones");
+    *out = snch_traversal_view{};
+    out->num_triangles = s->num_tris;
+    out->root_box = reinterpret_cast<const float *>(s->aabbs);
+    out->inner = s->inner;
+    out->inner_cones = s->inner_cones;
+    out->leaves = s->leaves;
+    out->edges = s->edges;
+    out->vertices = s->verts;
+    out->triangles = s->tris;
+    out->status = s->small + kWStatus;
     return SNCH_OK;
 }
 
@@ -1534,6 +1563,34 @@ int snch_query_visits(snch_scene_t s, int kind, const float *in0, const float *i
         cudaFreeAsync(scratch, st);
         return fail(SNCH_ERR_INVALID_ARGUMENT, "kind must be 0..3");
     }
+    cudaFreeAsync(scratch, st);
+    SNCH_CUDA(e);
+    return SNCH_OK;
+}
+
+int snch_query_visits_seeded(snch_scene_t s, int kind, const float *pts, const uint8_t *flip, const float *radius,
+                             int64_t n, uint32_t *visits, snch_stream_t stream)
+{
+    int rc = check_built(s);
+    if (rc == SNCH_OK)
+        rc = check_n(n, {pts, radius, visits});
+    if (rc != SNCH_OK)
+        return rc;
+    if (kind != 0 && kind != 1)
+        return fail(SNCH_ERR_INVALID_ARGUMENT, "kind must be 0 (nearest) or 1 (silhouette)");
+    if (n == 0)
+        return SNCH_OK;
+    cudaStream_t st = S(stream);
+    char *scratch = nullptr;
+    SNCH_CUDA(scratch_alloc(&scratch, 8 * (size_t)n + 256, st));
+    BatchView b;
+    cudaError_t e = batch_view(s, pts, n, st, b);
+    SeedArgs seed;
+    seed.radius = radius;
+    if (e == cudaSuccess)
+        e = kind == 0 ? launch_nearest(b.t, pts, n, (uint32_t *)scratch, (float *)(scratch + 4 * n), st, visits, seed)
+                      : launch_silhouette(b.t, pts, flip, n, (float *)scratch, (int32_t *)(scratch + 4 * n), st,
+                                          visits, seed);
     cudaFreeAsync(scratch, st);
     SNCH_CUDA(e);
     return SNCH_OK;
@@ -2274,6 +2331,7 @@ int snch_get_option(snch_scene_t s, int option, int64_t *value)
     case SNCH_OPT_HOST_CHUNK: *value = s->host_chunk; break;
     case SNCH_OPT_PERSISTENT_RAY: *value = s->persistent_ray; break;
     case SNCH_OPT_PACKET_PERSISTENT_MIN: *value = s->packet_persistent_min; break;
+    case SNCH_OPT_OUTPUT_SCATTER: *value = s->output_scatter; break;
     default: return fail(SNCH_ERR_INVALID_ARGUMENT, "unknown option " + std::to_string(option));
     }
     return SNCH_OK;

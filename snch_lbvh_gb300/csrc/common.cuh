@@ -153,6 +153,11 @@ struct TreeView
     int packet_near = 0, packet_sil = 0;
     int64_t packet_persistent_min = int64_t(1) << 23;  // packet batches this large run persistent
     int order_coherent = 0;  // order[] is the batch's Morton order (neighbours share warps)
+    // 1: results are written at their batch position i (coalesced) instead of at
+    // query order[i]; the launcher then scatters them to query order (unseeded,
+    // fully ordered batches of the kernels that support it)
+    int out_batch_order = 0;
+    int out_batch_order_enabled = 1;  // SNCH_OPT_OUTPUT_SCATTER
     const float4 *wide4 = nullptr, *wide8 = nullptr;        // wide records
     const uint32_t *wide4_of = nullptr, *wide8_of = nullptr;  // wide index of each binary wide-root node
 };
@@ -202,6 +207,8 @@ struct SeedArgs
 
 // index of the query answered by global thread i
 SNCH_DEV int64_t query_index(const TreeView &t, int64_t i) { return t.order ? (int64_t)__ldg(t.order + i) : i; }
+// where the result of the query at batch position i (query index q) is written
+SNCH_DEV int64_t out_pos(const TreeView &t, int64_t i, int64_t q) { return t.out_batch_order ? i : q; }
 // number of queries of this launch (the fallback pass reads it from the device)
 SNCH_DEV int64_t query_count(const TreeView &t, int64_t n) { return t.order_count ? (int64_t)*t.order_count : n; }
 

@@ -720,8 +720,8 @@ __global__ void __launch_bounds__(kBlock, 1280 / kBlock) nearest_fast_kernel(Tre
     const bool failed = seed.radius && nearest == kInvalid && r0 < INFINITY;
     if (seed.radius && nearest == kInvalid)
         best = INFINITY;  // nothing within the seed radius: the fallback pass answers it
-    out_idx[q] = nearest == kInvalid ? kInvalid : nearest - qr.tri_off;
-    out_dist[q] = sqrtf(best);
+    out_idx[out_pos(t, qi, q)] = nearest == kInvalid ? kInvalid : nearest - qr.tri_off;
+    out_dist[out_pos(t, qi, q)] = sqrtf(best);
     if (seed.fail_flag)
         seed.fail_flag[q] = failed ? 1u : 0u;
 }
@@ -931,9 +931,9 @@ __global__ void __launch_bounds__(kBlock, 1152 / kBlock) silhouette_fast_kernel(
     const bool failed = seed.radius && best_edge < 0 && r0 < INFINITY;
     if (seed.radius && best_edge < 0)
         best = INFINITY;  // nothing within the seed radius: the fallback pass answers it
-    out_dist[q] = best;
+    out_dist[out_pos(t, qi, q)] = best;
     if (out_edge)
-        out_edge[q] = best_edge < 0 ? best_edge : best_edge - qr.edge_off;
+        out_edge[out_pos(t, qi, q)] = best_edge < 0 ? best_edge : best_edge - qr.edge_off;
     if (seed.fail_flag)
         seed.fail_flag[q] = failed ? 1u : 0u;
     if (kStats)
@@ -1219,8 +1219,8 @@ __global__ void __launch_bounds__(128, SNCH_WIDE_MIN_BLOCKS)
     const bool failed = seed.radius && nearest == kInvalid && r0 < INFINITY;
     if (seed.radius && nearest == kInvalid)
         best = INFINITY;  // nothing within the seed radius: the fallback pass answers it
-    out_idx[q] = nearest == kInvalid ? kInvalid : nearest - qr.tri_off;
-    out_dist[q] = sqrtf(best);
+    out_idx[out_pos(t, qi, q)] = nearest == kInvalid ? kInvalid : nearest - qr.tri_off;
+    out_dist[out_pos(t, qi, q)] = sqrtf(best);
     if (seed.fail_flag)
         seed.fail_flag[q] = failed ? 1u : 0u;
 }
@@ -1342,9 +1342,9 @@ __global__ void __launch_bounds__(128, SNCH_WIDE_MIN_BLOCKS)
     const bool failed = seed.radius && best_edge < 0 && r0 < INFINITY;
     if (seed.radius && best_edge < 0)
         best = INFINITY;  // nothing within the seed radius: the fallback pass answers it
-    out_dist[q] = best;
+    out_dist[out_pos(t, qi, q)] = best;
     if (out_edge)
-        out_edge[q] = best_edge < 0 ? best_edge : best_edge - qr.edge_off;
+        out_edge[out_pos(t, qi, q)] = best_edge < 0 ? best_edge : best_edge - qr.edge_off;
     if (seed.fail_flag)
         seed.fail_flag[q] = failed ? 1u : 0u;
     if (kStats)
@@ -1507,8 +1507,8 @@ SNCH_DEV void nearest_packet_chunk(const TreeView &t, const float *__restrict__ 
     const bool failed = seed.radius && nearest == kInvalid && r0 < INFINITY;
     if (seed.radius && nearest == kInvalid)
         best = INFINITY;  // nothing within the seed radius: the fallback pass answers it
-    out_idx[q] = nearest == kInvalid ? kInvalid : nearest - qr.tri_off;
-    out_dist[q] = sqrtf(best);
+    out_idx[out_pos(t, qi, q)] = nearest == kInvalid ? kInvalid : nearest - qr.tri_off;
+    out_dist[out_pos(t, qi, q)] = sqrtf(best);
     if (seed.fail_flag)
         seed.fail_flag[q] = failed ? 1u : 0u;}
 
@@ -1680,9 +1680,9 @@ SNCH_DEV void silhouette_packet_chunk(const TreeView &t, const float *__restrict
     const bool failed = seed.radius && best_edge < 0 && r0 < INFINITY;
     if (seed.radius && best_edge < 0)
         best = INFINITY;  // nothing within the seed radius: the fallback pass answers it
-    out_dist[q] = best;
+    out_dist[out_pos(t, qi, q)] = best;
     if (out_edge)
-        out_edge[q] = best_edge < 0 ? best_edge : best_edge - qr.edge_off;
+        out_edge[out_pos(t, qi, q)] = best_edge < 0 ? best_edge : best_edge - qr.edge_off;
     if (seed.fail_flag)
         seed.fail_flag[q] = failed ? 1u : 0u;
     if (kStats)
@@ -2210,13 +2210,13 @@ __global__ void __launch_bounds__(128) ray_kernel(TreeView t, const float *__res
             nd = sd[sp];
         }
     }
-    out_hit[q] = found ? 1 : 0;
+    out_hit[out_pos(t, qi, q)] = found ? 1 : 0;
     if (kAny)
         return;
-    out_t[q] = min_dist;
-    out_uv[2 * q] = bu;
-    out_uv[2 * q + 1] = bv;
-    out_idx[q] = nearest;
+    out_t[out_pos(t, qi, q)] = min_dist;
+    out_uv[2 * out_pos(t, qi, q)] = bu;
+    out_uv[2 * out_pos(t, qi, q) + 1] = bv;
+    out_idx[out_pos(t, qi, q)] = nearest;
     if (kStats)
     {
         stats[3 * q] = n_int;
@@ -2494,8 +2494,8 @@ __global__ void __launch_bounds__(128) sample_kernel(TreeView t, const float *__
             }
         }
     }
-    out_idx[q] = oi;
-    out_pdf[q] = opdf;
+    out_idx[out_pos(t, qi, q)] = oi;
+    out_pdf[out_pos(t, qi, q)] = opdf;
     if (kStats)
     {
         stats[3 * q] = n_int;
@@ -2784,15 +2784,109 @@ cudaError_t launch_persistent(void (*kernel)(KArgs...), int64_t n, cudaStream_t 
     const cudaError_t f = cudaFreeAsync(counter, st);
     return e != cudaSuccess ? e : f;
 }
+// Results of an unseeded, fully Morton-ordered batch are written at their batch
+// position into a stream-ordered temporary (warp-contiguous, coalesced stores)
+// and moved to query order by one scatter pass per batch. Written at query
+// order[i] directly, neighbouring lanes store to unrelated 4-byte slots: each
+// store dirties a 32-byte sector that L2 evicts long before the other seven
+// slots arrive (the search streams the tree through L2), so DRAM sees about 8x
+// the output bytes (16M nearest queries: 1.07 GB written for 128 MB of results).
+// The scatter pass touches only the output arrays, which stay in L2 while
+// their sectors fill.
+inline bool batch_order_ok(const TreeView &t, const SeedArgs &seed, const uint32_t *stats)
+{
+    return t.order && !t.order_count && t.out_batch_order_enabled && !stats && !seed.radius && !seed.fail_flag &&
+           !seed.cap;
+}
+
+// out[order[i]] = tmp[i] for two 4-byte result arrays (streaming loads keep L2
+// for the scattered stores)
+__global__ void scatter2_kernel(const uint32_t *__restrict__ order, int64_t n, const uint32_t *__restrict__ a,
+                                uint32_t *__restrict__ A, const uint32_t *__restrict__ b, uint32_t *__restrict__ B)
+{
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    const uint32_t q = __ldcs(order + i);
+    A[q] = __ldcs(a + i);
+    if (B)
+        B[q] = __ldcs(b + i);
+}
+// the ray's four result arrays; uv as one 8-byte store when the caller's array allows it
+__global__ void scatter_ray_kernel(const uint32_t *__restrict__ order, int64_t n, const uint8_t *__restrict__ th,
+                                   const float *__restrict__ tt, const float2 *__restrict__ tuv,
+                                   const uint32_t *__restrict__ ti, uint8_t *__restrict__ hit, float *__restrict__ t,
+                                   float *__restrict__ uv, uint32_t *__restrict__ idx, int uv_aligned)
+{
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    const uint32_t q = __ldcs(order + i);
+    hit[q] = __ldcs(th + i);
+    t[q] = __ldcs(tt + i);
+    const float2 w = __ldcs(tuv + i);
+    if (uv_aligned)
+        reinterpret_cast<float2 *>(uv)[q] = w;
+    else
+    {
+        uv[2 * (int64_t)q] = w.x;
+        uv[2 * (int64_t)q + 1] = w.y;
+    }
+    idx[q] = __ldcs(ti + i);
+}
+
+// stream-ordered temporary for one batch's results in batch order
+struct BatchOut
+{
+    char *base = nullptr;
+    cudaStream_t st = nullptr;
+    cudaError_t alloc(int64_t n, size_t bytes_per_query, cudaStream_t s)
+    {
+        st = s;
+        return scratch_alloc_raw(reinterpret_cast<void **>(&base), bytes_per_query * (size_t)n + 1024, s);
+    }
+    // the k-th array of `elem` bytes per query, 256-byte aligned after the previous ones
+    template <typename T>
+    T *at(size_t offset_bytes) const
+    {
+        return reinterpret_cast<T *>(base + offset_bytes);
+    }
+    ~BatchOut()
+    {
+        if (base)
+            cudaFreeAsync(base, st);
+    }
+};
+inline size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 }  // namespace
 
-cudaError_t launch_nearest(const TreeView &t, const float *pts, int64_t n, uint32_t *idx, float *dist, cudaStream_t st,
-                           uint32_t *stats, const SeedArgs &seed)
+cudaError_t launch_nearest(const TreeView &t0, const float *pts, int64_t n, uint32_t *idx_out, float *dist_out,
+                           cudaStream_t st, uint32_t *stats, const SeedArgs &seed)
 {
     if (n <= 0)
         return cudaSuccess;
+    TreeView t = t0;
     const bool persistent = (t.persistent & 1) != 0;
-    if (packet_ok(t, t.packet_near, t.width_near, seed) && packet_dense(t, t.packet_near, n))
+    const bool packets = packet_ok(t, t.packet_near, t.width_near, seed) && packet_dense(t, t.packet_near, n);
+    const bool wide = !packets && wide_ok(t, t.width_near, persistent, seed);
+    const bool lane_persistent = !packets && !wide && !stats && t.near_first && t.num_tris > 1 && persistent;
+    // the kernels below that write at out_pos() (all but the lane-refill and reference-order ones)
+    const bool supports = packets || wide || (t.near_first && !lane_persistent);
+    BatchOut tmp;
+    uint32_t *idx = idx_out;
+    float *dist = dist_out;
+    if (supports && batch_order_ok(t, seed, stats))
+    {
+        cudaError_t e = tmp.alloc(n, 8, st);
+        if (e != cudaSuccess)
+            return e;
+        idx = tmp.at<uint32_t>(0);
+        dist = tmp.at<float>(align256(4 * (size_t)n));
+        t.out_batch_order = 1;
+    }
+    cudaError_t e = cudaSuccess;
+    bool launched = false;
+    if (packets)
     {
         // persistent packets for large batches: the same packets and answers, 2-7 %
         // faster there (no warp slot waits for the slowest packet of its block);
@@ -2800,11 +2894,14 @@ cudaError_t launch_nearest(const TreeView &t, const float *pts, int64_t n, uint3
         if (stats)
             nearest_packet_kernel<true><<<grid_for(n, 128), 128, 0, st>>>(t, pts, n, idx, dist, stats, seed);
         else if (n >= t.packet_persistent_min)
-            return launch_persistent(nearest_packet_persistent_kernel, n, st, t, pts, n, idx, dist, seed);
+        {
+            e = launch_persistent(nearest_packet_persistent_kernel, n, st, t, pts, n, idx, dist, seed);
+            launched = true;
+        }
         else
             nearest_packet_kernel<false><<<grid_for(n, 128), 128, 0, st>>>(t, pts, n, idx, dist, nullptr, seed);
     }
-    else if (wide_ok(t, t.width_near, persistent, seed))
+    else if (wide)
     {
         const unsigned g = grid_for(n, 128);
         if (t.width_near == 4)
@@ -2816,10 +2913,11 @@ cudaError_t launch_nearest(const TreeView &t, const float *pts, int64_t n, uint3
     }
     else if (stats)
         nearest_fast_kernel<true><<<grid_for(n, 128), 128, 0, st>>>(t, pts, n, idx, dist, stats, seed);
-    else if (t.near_first && t.num_tris > 1 && persistent)
+    else if (lane_persistent)
     {
-        return seed.radius ? launch_persistent(nearest_persistent_kernel<true>, n, st, t, pts, n, idx, dist, seed)
-                           : launch_persistent(nearest_persistent_kernel<false>, n, st, t, pts, n, idx, dist, seed);
+        e = seed.radius ? launch_persistent(nearest_persistent_kernel<true>, n, st, t, pts, n, idx, dist, seed)
+                        : launch_persistent(nearest_persistent_kernel<false>, n, st, t, pts, n, idx, dist, seed);
+        launched = true;
     }
     else if (t.near_first && t.block_near == 64)
         nearest_fast_kernel<false, 64><<<grid_for(n, 64), 64, 0, st>>>(t, pts, n, idx, dist, nullptr, seed);
@@ -2829,27 +2927,61 @@ cudaError_t launch_nearest(const TreeView &t, const float *pts, int64_t n, uint3
         nearest_fast_kernel<false><<<grid_for(n, 128), 128, 0, st>>>(t, pts, n, idx, dist, nullptr, seed);
     else
         nearest_kernel<<<grid_for(n, 128), 128, 0, st>>>(t, pts, n, idx, dist, seed);
-    note_launch();
-    return cudaGetLastError();
+    if (!launched)
+    {
+        note_launch();
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess && t.out_batch_order)
+    {
+        scatter2_kernel<<<grid_for(n, 256), 256, 0, st>>>(t.order, n, idx, idx_out,
+                                                         reinterpret_cast<const uint32_t *>(dist),
+                                                         reinterpret_cast<uint32_t *>(dist_out));
+        note_launch();
+        e = cudaGetLastError();
+    }
+    return e;
 }
-cudaError_t launch_silhouette(const TreeView &t, const float *pts, const uint8_t *flip, int64_t n, float *dist,
-                              int32_t *edge, cudaStream_t st, uint32_t *stats, const SeedArgs &seed)
+cudaError_t launch_silhouette(const TreeView &t0, const float *pts, const uint8_t *flip, int64_t n, float *dist_out,
+                              int32_t *edge_out, cudaStream_t st, uint32_t *stats, const SeedArgs &seed)
 {
     if (n <= 0)
         return cudaSuccess;
+    TreeView t = t0;
     const bool persistent = (t.persistent & 2) != 0;
-    if (packet_ok(t, t.packet_sil, t.width_sil, seed))
+    const bool packets = packet_ok(t, t.packet_sil, t.width_sil, seed);
+    const bool wide = !packets && wide_ok(t, t.width_sil, persistent, seed);
+    const bool lane_persistent = !packets && !wide && !stats && t.near_first && t.num_tris > 1 && persistent;
+    const bool supports = packets || wide || (t.near_first && !lane_persistent);
+    BatchOut tmp;
+    float *dist = dist_out;
+    int32_t *edge = edge_out;
+    if (supports && batch_order_ok(t, seed, stats))
+    {
+        cudaError_t e = tmp.alloc(n, 8, st);
+        if (e != cudaSuccess)
+            return e;
+        dist = tmp.at<float>(0);
+        edge = edge_out ? tmp.at<int32_t>(align256(4 * (size_t)n)) : nullptr;
+        t.out_batch_order = 1;
+    }
+    cudaError_t e = cudaSuccess;
+    bool launched = false;
+    if (packets)
     {
         if (stats)
             silhouette_packet_kernel<true>
                 <<<grid_for(n, 128), 128, 0, st>>>(t, pts, flip, n, dist, edge, stats, seed);
         else if (n >= t.packet_persistent_min)
-            return launch_persistent(silhouette_packet_persistent_kernel, n, st, t, pts, flip, n, dist, edge, seed);
+        {
+            e = launch_persistent(silhouette_packet_persistent_kernel, n, st, t, pts, flip, n, dist, edge, seed);
+            launched = true;
+        }
         else
             silhouette_packet_kernel<false>
                 <<<grid_for(n, 128), 128, 0, st>>>(t, pts, flip, n, dist, edge, nullptr, seed);
     }
-    else if (wide_ok(t, t.width_sil, persistent, seed))
+    else if (wide)
     {
         const unsigned g = grid_for(n, 128);
         if (t.width_sil == 4)
@@ -2861,11 +2993,12 @@ cudaError_t launch_silhouette(const TreeView &t, const float *pts, const uint8_t
     }
     else if (stats)
         silhouette_fast_kernel<true><<<grid_for(n, 128), 128, 0, st>>>(t, pts, flip, n, dist, edge, stats, seed);
-    else if (t.near_first && t.num_tris > 1 && persistent)
+    else if (lane_persistent)
     {
-        return seed.radius
-                   ? launch_persistent(silhouette_persistent_kernel<true>, n, st, t, pts, flip, n, dist, edge, seed)
-                   : launch_persistent(silhouette_persistent_kernel<false>, n, st, t, pts, flip, n, dist, edge, seed);
+        e = seed.radius
+                ? launch_persistent(silhouette_persistent_kernel<true>, n, st, t, pts, flip, n, dist, edge, seed)
+                : launch_persistent(silhouette_persistent_kernel<false>, n, st, t, pts, flip, n, dist, edge, seed);
+        launched = true;
     }
     else if (t.near_first && t.block_sil == 64)
         silhouette_fast_kernel<false, 64><<<grid_for(n, 64), 64, 0, st>>>(t, pts, flip, n, dist, edge, nullptr, seed);
@@ -2876,8 +3009,21 @@ cudaError_t launch_silhouette(const TreeView &t, const float *pts, const uint8_t
         silhouette_fast_kernel<false><<<grid_for(n, 128), 128, 0, st>>>(t, pts, flip, n, dist, edge, nullptr, seed);
     else
         silhouette_kernel<<<grid_for(n, 128), 128, 0, st>>>(t, pts, flip, n, dist, edge, seed);
-    note_launch();
-    return cudaGetLastError();
+    if (!launched)
+    {
+        note_launch();
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess && t.out_batch_order)
+    {
+        scatter2_kernel<<<grid_for(n, 256), 256, 0, st>>>(t.order, n, reinterpret_cast<const uint32_t *>(dist),
+                                                         reinterpret_cast<uint32_t *>(dist_out),
+                                                         reinterpret_cast<const uint32_t *>(edge),
+                                                         reinterpret_cast<uint32_t *>(edge_out));
+        note_launch();
+        e = cudaGetLastError();
+    }
+    return e;
 }
 cudaError_t launch_cone_filter_check(int64_t n, uint64_t seed, unsigned long long *counts, cudaStream_t st)
 {
@@ -2887,17 +3033,39 @@ cudaError_t launch_cone_filter_check(int64_t n, uint64_t seed, unsigned long lon
     note_launch();
     return cudaGetLastError();
 }
-cudaError_t launch_ray(const TreeView &t, const float *o, const float *d, const float *tmax, int64_t n, uint8_t *hit,
-                       float *tt, float *uv, uint32_t *idx, cudaStream_t st, uint32_t *stats)
+cudaError_t launch_ray(const TreeView &t0, const float *o, const float *d, const float *tmax, int64_t n,
+                       uint8_t *hit_out, float *t_out, float *uv_out, uint32_t *idx_out, cudaStream_t st,
+                       uint32_t *stats)
 {
     if (n <= 0)
         return cudaSuccess;
+    TreeView t = t0;
     if (stats)
-        ray_kernel<true><<<grid_for(n, 128), 128, 0, st>>>(t, o, d, tmax, n, hit, tt, uv, idx, stats);
+        ray_kernel<true><<<grid_for(n, 128), 128, 0, st>>>(t, o, d, tmax, n, hit_out, t_out, uv_out, idx_out, stats);
     else if (t.persistent & 4)
-        return launch_persistent(ray_persistent_kernel<false>, n, st, t, o, d, tmax, n, hit, tt, uv, idx);
+        return launch_persistent(ray_persistent_kernel<false>, n, st, t, o, d, tmax, n, hit_out, t_out, uv_out,
+                                 idx_out);
+    else if (batch_order_ok(t, SeedArgs(), nullptr))
+    {
+        BatchOut tmp;
+        const size_t a_t = align256((size_t)n), a_uv = a_t + align256(4 * (size_t)n),
+                     a_idx = a_uv + align256(8 * (size_t)n);
+        cudaError_t e = tmp.alloc(n, 17, st);
+        if (e != cudaSuccess)
+            return e;
+        t.out_batch_order = 1;
+        ray_kernel<false><<<grid_for(n, 128), 128, 0, st>>>(t, o, d, tmax, n, tmp.at<uint8_t>(0), tmp.at<float>(a_t),
+                                                            tmp.at<float>(a_uv), tmp.at<uint32_t>(a_idx), nullptr);
+        note_launch();
+        if ((e = cudaGetLastError()) != cudaSuccess)
+            return e;
+        scatter_ray_kernel<<<grid_for(n, 256), 256, 0, st>>>(
+            t.order, n, tmp.at<uint8_t>(0), tmp.at<float>(a_t), tmp.at<float2>(a_uv), tmp.at<uint32_t>(a_idx),
+            hit_out, t_out, uv_out, idx_out, (reinterpret_cast<uintptr_t>(uv_out) & 7) == 0);
+    }
     else
-        ray_kernel<false><<<grid_for(n, 128), 128, 0, st>>>(t, o, d, tmax, n, hit, tt, uv, idx, nullptr);
+        ray_kernel<false><<<grid_for(n, 128), 128, 0, st>>>(t, o, d, tmax, n, hit_out, t_out, uv_out, idx_out,
+                                                            nullptr);
     note_launch();
     return cudaGetLastError();
 }
@@ -2914,15 +3082,34 @@ cudaError_t launch_ray_test(const TreeView &t, const float *o, const float *d, c
     note_launch();
     return cudaGetLastError();
 }
-cudaError_t launch_sample(const TreeView &t, const float *c, const float *r, const float *u, int64_t n, int32_t *idx,
-                          float *pdf, cudaStream_t st, uint32_t *stats)
+cudaError_t launch_sample(const TreeView &t0, const float *c, const float *r, const float *u, int64_t n,
+                          int32_t *idx_out, float *pdf_out, cudaStream_t st, uint32_t *stats)
 {
     if (n <= 0)
         return cudaSuccess;
+    TreeView t = t0;
     if (stats)
-        sample_kernel<true><<<grid_for(n, 128), 128, 0, st>>>(t, c, r, u, n, idx, pdf, stats);
+        sample_kernel<true><<<grid_for(n, 128), 128, 0, st>>>(t, c, r, u, n, idx_out, pdf_out, stats);
+    else if (batch_order_ok(t, SeedArgs(), nullptr))
+    {
+        BatchOut tmp;
+        cudaError_t e = tmp.alloc(n, 8, st);
+        if (e != cudaSuccess)
+            return e;
+        t.out_batch_order = 1;
+        int32_t *ti = tmp.at<int32_t>(0);
+        float *tp = tmp.at<float>(align256(4 * (size_t)n));
+        sample_kernel<false><<<grid_for(n, 128), 128, 0, st>>>(t, c, r, u, n, ti, tp, nullptr);
+        note_launch();
+        if ((e = cudaGetLastError()) != cudaSuccess)
+            return e;
+        scatter2_kernel<<<grid_for(n, 256), 256, 0, st>>>(t.order, n, reinterpret_cast<const uint32_t *>(ti),
+                                                         reinterpret_cast<uint32_t *>(idx_out),
+                                                         reinterpret_cast<const uint32_t *>(tp),
+                                                         reinterpret_cast<uint32_t *>(pdf_out));
+    }
     else
-        sample_kernel<false><<<grid_for(n, 128), 128, 0, st>>>(t, c, r, u, n, idx, pdf, nullptr);
+        sample_kernel<false><<<grid_for(n, 128), 128, 0, st>>>(t, c, r, u, n, idx_out, pdf_out, nullptr);
     note_launch();
     return cudaGetLastError();
 }

@@ -35,3 +35,13 @@ def test_cxx_api_runs_on_gpu():
     exe = compile_example()
     r = subprocess.run([exe], capture_output=True, text=True)
     assert r.returncode == 0, r.stdout + r.stderr
+
+
+def test_device_header_compiles_with_default_nvcc_flags(tmp_path):
+    """include/snch_device.cuh in a caller's kernels (tests/cxx/device_shim_kernels.cu),
+    compiled for sm_103a with nvcc's defaults; the GPU comparison is
+    tests/test_gpu_device_shim.py."""
+    cmd = [build.nvcc(), "-c", *build.ARCH, "-O3", "-std=c++17", "-I", os.path.join(ROOT, "include"),
+           os.path.join(ROOT, "tests", "cxx", "device_shim_kernels.cu"), "-o", str(tmp_path / "shim.o")]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr

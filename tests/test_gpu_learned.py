@@ -166,3 +166,55 @@ def test_learned_radius_queries_identical(trained):
     frac_sil = int(nf.item()) / len(pts)
     assert frac_near < 0.5 and frac_sil < 0.5, (frac_near, frac_sil)
     assert s.device_status() == 0
+
+
+def _seeded_cost(s, kind, pts, radius, flip, plain, plain_dist):
+    """Node expansions + leaves per query of a seeded search: its first pass,
+    plus the unbounded pass for the queries with nothing inside their radius."""
+    v = s.query_visits_seeded(kind, pts, radius, flip=flip).astype(np.int64)
+    failed = ~(plain_dist <= radius.cpu().numpy())
+    cost = v[:, 0] + v[:, 1]
+    cost[failed] += plain[failed, 0] + plain[failed, 1]
+    return cost, failed
+
+
+def test_trained_radius_saves_expansions(trained):
+    """What the trained network gains over the search without it, on held-out
+    points: node expansions + leaf tests per query (the search's work, which a
+    timing would only blur), for the library's default traversal (near-first,
+    Morton-ordered warp packets), fallback passes included. The untrained
+    network (the same model before training) sets the floor of what a radius
+    alone, without learning, gives."""
+    import torch
+    from snch_lbvh_gb300.learned import LearnedRadius
+    s, m, _, _ = trained
+    rng = np.random.default_rng(1234)  # held out: the training points came from seed 21
+    pts = torch.from_numpy(rng.random((400_000, 3), dtype=np.float32)).cuda()
+    flip = torch.zeros(len(pts), dtype=torch.uint8, device="cuda")
+    untrained = LearnedRadius(np.zeros(3), np.ones(3), seed=1)
+    res = {}
+    for kind, col in (("nearest", 0), ("silhouette", 1)):
+        plain = s.query_visits(kind, pts, flip=flip if col else None).astype(np.int64)
+        if col == 0:
+            _, d = s.query_nearest(pts)
+        else:
+            d, _ = s.query_silhouette(pts, flip)
+        d = d.cpu().numpy()
+        base = (plain[:, 0] + plain[:, 1]).mean()
+        r_tr = m.predict(pts, margin=1.25)[col]
+        r_un = untrained.predict(pts, margin=1.25)[col]
+        r_ex = torch.from_numpy(np.nextafter(d, np.float32(np.inf))).cuda()
+        c_tr, f_tr = _seeded_cost(s, kind, pts, r_tr, flip if col else None, plain, d)
+        c_un, _ = _seeded_cost(s, kind, pts, r_un, flip if col else None, plain, d)
+        c_ex, _ = _seeded_cost(s, kind, pts, r_ex, flip if col else None, plain, d)
+        res[kind] = {"plain": base, "trained": c_tr.mean(), "untrained": c_un.mean(), "exact": c_ex.mean(),
+                     "fallback": f_tr.mean()}
+    print("expansions + leaves per query:", res)
+    untrained.close()
+    for kind, r in res.items():
+        # the trained radius removes work the plain search does ...
+        assert r["trained"] < 0.95 * r["plain"], (kind, r)
+        # ... more than an untrained network's radius does
+        assert r["trained"] < r["untrained"], (kind, r)
+        # and no radius can beat the answers themselves as radii
+        assert r["exact"] <= r["trained"], (kind, r)
