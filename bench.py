@@ -71,6 +71,8 @@ def parse():
     ap.add_argument("--no-icosphere", action="store_true", help="skip the 20,480-triangle icosphere leg")
     ap.add_argument("--output-scatter", type=int, default=-1, choices=[-1, 0, 1],
                     help="SNCH_OPT_OUTPUT_SCATTER of the step's scene (-1: the library default)")
+    ap.add_argument("--top-levels", type=int, default=-1,
+                    help="SNCH_OPT_TOP_LEVELS of the step's scene (-1: the library default)")
     ap.add_argument("--persistent-min", type=int, default=0,
                     help="SNCH_OPT_PACKET_PERSISTENT_MIN of the step's scene (0: the library default, 2^23); "
                          "lets a reduced --scale run the persistent packet kernels of the full workload")
@@ -809,6 +811,8 @@ def run_ours(args):
         scene.set_option(snch.OPT_PACKET_PERSISTENT_MIN, args.persistent_min)
     if args.output_scatter >= 0:
         scene.set_option(snch.OPT_OUTPUT_SCATTER, args.output_scatter)
+    if args.top_levels >= 0:
+        scene.set_option(snch.OPT_TOP_LEVELS, args.top_levels)
     stream = torch.cuda.current_stream()
 
     def step(ev=None):

@@ -46,6 +46,7 @@ typedef enum
 #define SNCH_DEVICE_LOOKBACK_TIMEOUT 2u /* a bounded cross-block wait gave up (results invalid) */
 #define SNCH_DEVICE_HASH_FULL 4u        /* the edge hash table overflowed (results invalid)    */
 #define SNCH_DEVICE_TREE_DEPTH 16u      /* a wide-record pass met a tree deeper than its bound  */
+#define SNCH_DEVICE_COPY_TIMEOUT 32u    /* a bulk copy into shared memory did not complete in time */
 
 /* Reference-layout records, byte-compatible with the reference's device view
  * (bvh.cuh:27-33 node, aabb.cuh:12-16 aabb<float,3>, cone.cuh:11-16 cone<float,3>,
@@ -261,15 +262,25 @@ int snch_set_traversal(snch_scene_t scene, int mode);
  *                             packets, same answers). Default 2^23 (measured faster from
  *                             there, 6 % slower on 1M-query batches); >= 1. */
 #define SNCH_OPT_PACKET_PERSISTENT_MIN 19
-/*   SNCH_OPT_OUTPUT_SCATTER   1 (default): the results of a Morton-ordered, unseeded
- *                             batch are written in batch order to a temporary and then
- *                             moved to input order by one scatter pass, so that each
- *                             warp's stores fill whole sectors (written at input
- *                             positions directly, neighbouring lanes store 4 bytes each
- *                             to unrelated sectors and DRAM sees up to 8x the output
- *                             bytes); 0: results written at input positions by the
- *                             search kernels. Same results either way. */
+/*   SNCH_OPT_OUTPUT_SCATTER   1: the results of a Morton-ordered, unseeded batch are
+ *                             written in batch order to a temporary and then moved to
+ *                             input order by one scatter pass, so that each warp's stores
+ *                             fill whole sectors (written at input positions directly,
+ *                             neighbouring lanes store 4 bytes each to unrelated sectors
+ *                             and DRAM sees 5-9x the output bytes). 0 (default): results
+ *                             written at input positions by the search kernels, which are
+ *                             bound by instruction issue and latency, not by DRAM: the
+ *                             extra pass costs more time than the writes it saves. Same
+ *                             results either way. */
 #define SNCH_OPT_OUTPUT_SCATTER 20
+/*   SNCH_OPT_TOP_LEVELS       0 (default) to 7: the persistent warp-packet searches
+ *                             (nearest and silhouette batches of at least
+ *                             SNCH_OPT_PACKET_PERSISTENT_MIN queries, plain scenes) copy
+ *                             the records of the top levels of the tree (2^levels - 1
+ *                             nodes, 112 bytes each) into each block's shared memory
+ *                             once, with a bulk copy, and read those nodes from there.
+ *                             Same results. */
+#define SNCH_OPT_TOP_LEVELS 21
 /*   SNCH_OPT_HOST_CHUNK       queries per chunk of the *_host forms (at most 29 bytes in
  *                             and 17 out per query on each of two streams): chunk i's
  *                             input copy, search and output copy run on stream i % 2, so

@@ -36,6 +36,7 @@ OPT_PERSISTENT_NEAREST, OPT_PERSISTENT_SILHOUETTE = 16, 17
 OPT_PERSISTENT_RAY = 18
 OPT_PACKET_PERSISTENT_MIN = 19
 OPT_OUTPUT_SCATTER = 20
+OPT_TOP_LEVELS = 21
 
 
 def _torch():

@@ -116,7 +116,12 @@ struct snch_scene_s
     int block_near = 128, block_sil = 128;  // threads per block of the binary searches
     int packet_near = 2, packet_sil = 2;    // warp packets: 0 never, 1 always, 2 Morton-ordered batches
     int64_t packet_persistent_min = int64_t(1) << 23;  // packet batches this large run persistent
-    int output_scatter = 1;  // ordered batches: results in batch order, then one scatter pass
+    int output_scatter = 0;  // ordered batches: results in batch order, then one scatter pass (measured slower)
+    // top tree levels staged in shared memory by the persistent packet searches:
+    // the first 2^levels - 1 of kTopSlots heap slots, gathered after every build
+    int top_levels = 0;
+    InnerRec *top_inner = nullptr;
+    InnerConeRec *top_cones = nullptr;
     float4 *wide[2] = {nullptr, nullptr};
     uint32_t *wide_idx[2] = {nullptr, nullptr};  // wide index of each wide-root binary node
     size_t wide_cap[2] = {0, 0};  // records allocated
@@ -143,6 +148,12 @@ struct snch_scene_s
         t.packet_sil = packet_sil;
         t.packet_persistent_min = packet_persistent_min;
         t.out_batch_order_enabled = output_scatter;
+        if (top_levels > 0 && num_meshes == 0)
+        {
+            t.top_inner = top_inner;
+            t.top_cones = top_cones;
+            t.top_slots = (1u << top_levels) - 1u;
+        }
         if (wide_ready[0])
         {
             t.wide4 = wide[0];
@@ -159,6 +170,7 @@ struct snch_scene_s
 
 namespace
 {
+constexpr uint32_t kTopSlots = 127;  // seven levels: 8 KB of records + 6 KB of cones
 // Scene arrays and host-form staging buffers come from a cache of released
 // device blocks: a scene created and destroyed once per batch of work reuses
 // the previous scene's blocks instead of paying cudaMalloc / cudaFree (and the
@@ -334,7 +346,7 @@ void free_scene(snch_scene_s *s)
                     s->stage.in[0], s->stage.in[1], s->stage.out[0], s->stage.out[1],
                     s->tri_mesh, s->mesh_tri_start, s->mesh_box, s->sorted_mesh, s->mesh_root, s->perm,
                     s->perm_tmp, s->mkey_tmp, s->mesh_edge_start, s->wide[0], s->wide[1], s->wide_idx[0],
-                    s->wide_idx[1]};
+                    s->wide_idx[1], s->top_inner, s->top_cones};
     cudaDeviceSynchronize();  // the scene's queued work ends before its blocks are reused
     for (void *p : ptrs)
         cache_release(p);
@@ -376,6 +388,8 @@ int allocate(snch_scene_s *s)
     SNCH_CUDA(dalloc(&s->small, kSmallWords));
     SNCH_CUDA(dalloc(&s->ref_objects, n));
     SNCH_CUDA(dalloc(&s->ref_edges, 3 * n));
+    SNCH_CUDA(dalloc(&s->top_inner, kTopSlots));
+    SNCH_CUDA(dalloc(&s->top_cones, kTopSlots));
     const size_t scratch = std::max(topology_scratch_bytes((uint32_t)n), sort_scratch_bytes((uint32_t)n, 30));
     SNCH_CUDA(cache_alloc(&s->scratch, scratch));
     SNCH_CUDA(cudaMemset(s->small, 0, kSmallWords * 4));
@@ -1040,6 +1054,9 @@ int snch_build_bvh(snch_scene_t s, snch_stream_t stream)
         SNCH_CUDA(launch_build_back(a, st));
         SNCH_CUDA(launch_ref_objects(s->verts, s->tris, s->tri_owned, s->edge_verts, s->num_tris, s->ref_objects,
                                      s->ref_edges, st));
+        if (s->num_meshes == 0)
+            SNCH_CUDA(launch_top_levels(s->inner, s->inner_cones, s->num_tris, kTopSlots, s->top_inner,
+                                        s->top_cones, st));
     }
     s->wide_ready[0] = s->wide_ready[1] = false;
     s->built = true;
@@ -1073,6 +1090,11 @@ int snch_set_option(snch_scene_t s, int option, int64_t value)
         if (value < 0)
             return fail(SNCH_ERR_INVALID_ARGUMENT, "SNCH_OPT_ORDER_MIN_BATCH must be >= 0");
         s->order_min = value;
+        return SNCH_OK;
+    case SNCH_OPT_TOP_LEVELS:
+        if (value < 0 || value > 7)
+            return fail(SNCH_ERR_INVALID_ARGUMENT, "SNCH_OPT_TOP_LEVELS must be in [0, 7]");
+        s->top_levels = (int)value;
         return SNCH_OK;
     case SNCH_OPT_OUTPUT_SCATTER:
         if (value != 0 && value != 1)
@@ -2282,6 +2304,8 @@ int snch_scene_load(const char *path, snch_scene_t *out, snch_stream_t stream)
             e = launch_ref_objects(s->verts, s->tris, s->tri_owned, s->edge_verts, s->num_tris, s->ref_objects,
                                    s->ref_edges, st);
         if (e == cudaSuccess)
+            e = launch_top_levels(s->inner, s->inner_cones, s->num_tris, kTopSlots, s->top_inner, s->top_cones, st);
+        if (e == cudaSuccess)
             e = cudaStreamSynchronize(st);
         if (e != cudaSuccess)
             rc = fail(SNCH_ERR_CUDA, std::string("scene load: ") + cudaGetErrorString(e));
@@ -2332,6 +2356,7 @@ int snch_get_option(snch_scene_t s, int option, int64_t *value)
     case SNCH_OPT_PERSISTENT_RAY: *value = s->persistent_ray; break;
     case SNCH_OPT_PACKET_PERSISTENT_MIN: *value = s->packet_persistent_min; break;
     case SNCH_OPT_OUTPUT_SCATTER: *value = s->output_scatter; break;
+    case SNCH_OPT_TOP_LEVELS: *value = s->top_levels; break;
     default: return fail(SNCH_ERR_INVALID_ARGUMENT, "unknown option " + std::to_string(option));
     }
     return SNCH_OK;

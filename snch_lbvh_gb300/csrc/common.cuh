@@ -29,6 +29,7 @@ enum : uint32_t
     kStatusHashFull = 4u,          // the edge hash table had no free slot
     kStatusRefitTimeout = 8u,      // reserved
     kStatusTreeDepth = 16u,        // a wide-record pass met a tree deeper than its bound
+    kStatusCopyTimeout = 32u,      // a bulk copy into shared memory did not complete in time
 };
 
 struct f3
@@ -153,11 +154,17 @@ struct TreeView
     int packet_near = 0, packet_sil = 0;
     int64_t packet_persistent_min = int64_t(1) << 23;  // packet batches this large run persistent
     int order_coherent = 0;  // order[] is the batch's Morton order (neighbours share warps)
+    // the internal nodes of the top tree levels in heap order (slot 0 the root,
+    // the children of slot i at 2i+1 / 2i+2), staged in shared memory by the
+    // persistent packet searches; top_slots = 2^levels - 1, 0 = off
+    const InnerRec *top_inner = nullptr;
+    const InnerConeRec *top_cones = nullptr;
+    uint32_t top_slots = 0;
     // 1: results are written at their batch position i (coalesced) instead of at
     // query order[i]; the launcher then scatters them to query order (unseeded,
     // fully ordered batches of the kernels that support it)
     int out_batch_order = 0;
-    int out_batch_order_enabled = 1;  // SNCH_OPT_OUTPUT_SCATTER
+    int out_batch_order_enabled = 0;  // SNCH_OPT_OUTPUT_SCATTER
     const float4 *wide4 = nullptr, *wide8 = nullptr;        // wide records
     const uint32_t *wide4_of = nullptr, *wide8_of = nullptr;  // wide index of each binary wide-root node
 };

@@ -148,6 +148,9 @@ cudaError_t scratch_alloc_raw(void **p, size_t bytes, cudaStream_t st);
 size_t failed_list_scratch_bytes(int64_t n);
 cudaError_t launch_failed_list(const uint32_t *order, const uint32_t *fail_flag, int64_t n, uint32_t *list,
                                uint32_t *count, void *scratch, uint32_t *status, cudaStream_t st);
+// the top `slots` (2^levels - 1) heap slots of the tree's internal-node records
+cudaError_t launch_top_levels(const InnerRec *inner, const InnerConeRec *cones, uint32_t num_tris, uint32_t slots,
+                              InnerRec *top, InnerConeRec *topc, cudaStream_t st);
 // scratch holds query_order_scratch_bytes(n) bytes and owns *order.
 size_t query_order_scratch_bytes(int64_t n);
 cudaError_t launch_query_order(const TreeView &t, const float *pts, int64_t n, void *scratch, uint32_t **order,

@@ -253,10 +253,20 @@ SNCH_DEV bool cone_overlap(const Cone &bc, f3 o, const Box &b, float dist_to_box
 constexpr float kConeTol = 4.0e-4f;
 constexpr float kIllCond = 0.999f;
 
+// Hardware approximations (MUFU) and fused multiply-adds: the filter only needs
+// its angles to within its margin kConeTol = 4e-4 rad, and these add a few 1e-7
+// relative (amplified at most 22.4x through arccos below kIllCond), against the
+// multi-instruction IEEE sqrtf / __frcp_rn sequences the exact path needs.
+SNCH_DEV float sqrt_approx(float x)
+{
+    float r;
+    asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
 SNCH_DEV float acos_as(float x)  // 0 <= x <= 1
 {
     const float a0 = 1.5707288f, a1 = -0.2121144f, a2 = 0.0742610f, a3 = -0.0187293f;
-    return sqrtf(1.0f - x) * (a0 + x * (a1 + x * (a2 + x * a3)));
+    return sqrt_approx(1.0f - x) * __fmaf_rn(x, __fmaf_rn(x, __fmaf_rn(x, a3, a2), a1), a0);
 }
 
 // 1: overlap, 0: no overlap, -1: undecided (take cone_overlap)
@@ -266,10 +276,12 @@ SNCH_DEV int cone_overlap_fast(const Cone &bc, f3 o, const Box &b, float dist_to
         return 1;  // the same first test as cone_overlap
     const f3 c = centroid(b);
     const f3 v = mk(c.x - o.x, c.y - o.y, c.z - o.z);
-    const float l = len3(v);  // bit-identical to cone_overlap's l (the l > radius branch)
+    // approximate l: the asin branch below is taken only when radius / l <= kIllCond,
+    // i.e. l exceeds the radius by 0.1 %, so the exact l > radius holds there too
+    const float l = sqrt_approx(__fmaf_rn(v.x, v.x, __fmaf_rn(v.y, v.y, v.z * v.z)));
     if (!(l > 0.0f))
         return -1;
-    const float ax = fabsf(dot3(bc.axis, v)) * __frcp_rn(l);
+    const float ax = __fdividef(fabsf(__fmaf_rn(bc.axis.x, v.x, __fmaf_rn(bc.axis.y, v.y, bc.axis.z * v.z))), l);
     if (!(ax <= kIllCond))
         return -1;
     const float dev = kPi2 - acos_as(ax);
@@ -1382,11 +1394,22 @@ struct PacketLane
 };
 
 // one warp's packet: the 32 queries qi .. qi + 31 (lane order) of the batch
-template <bool kStats>
+// Top levels (kTop): the node's heap slot travels with it (slot of a child:
+// 2 s + 1 / 2 s + 2), and a node whose slot is below top_slots is read from the
+// shared-memory copy s_top instead of global memory; kNoSlot below the top.
+constexpr uint32_t kNoSlot = 0xFFu;
+SNCH_DEV uint32_t child_slot(uint32_t slot, uint32_t k, uint32_t top_slots)
+{
+    const uint32_t c = 2u * slot + 1u + k;
+    return slot < top_slots && c < top_slots ? c : kNoSlot;
+}
+
+template <bool kStats, bool kTop = false>
 SNCH_DEV void nearest_packet_chunk(const TreeView &t, const float *__restrict__ pts, int64_t n,
                                    uint32_t *__restrict__ out_idx, float *__restrict__ out_dist,
                                    uint32_t *__restrict__ stats, const SeedArgs &seed, int64_t qi, uint32_t *st_node,
-                                   uint32_t *st_mask)
+                                   uint32_t *st_mask, uint8_t *st_slot = nullptr, const InnerRec *s_top = nullptr,
+                                   uint32_t top_slots = 0)
 {
     const int lane = threadIdx.x & 31;
     const bool valid = qi < query_count(t, n);
@@ -1418,6 +1441,7 @@ SNCH_DEV void nearest_packet_chunk(const TreeView &t, const float *__restrict__ 
             in = !(mindist(load_root_box(t.aabbs + root), p) > best);
         uint32_t mask = __ballot_sync(0xffffffffu, in);
         uint32_t node = root;
+        uint32_t slot = kTop && root == 0u && !t.query_mesh ? 0u : kNoSlot;
         int sp = 0;
         while (true)
         {
@@ -1428,12 +1452,14 @@ SNCH_DEV void nearest_packet_chunk(const TreeView &t, const float *__restrict__ 
                 --sp;
                 node = st_node[sp];
                 mask = st_mask[sp];
+                if (kTop)
+                    slot = st_slot[sp];
                 continue;
             }
             const bool act = (mask >> lane) & 1u;
             Box lb, rb;
             uint32_t L, R;
-            unpack_inner(load_inner(t.inner + node), lb, rb, L, R);
+            unpack_inner(kTop && slot < top_slots ? s_top[slot] : load_inner(t.inner + node), lb, rb, L, R);
             float Lmd = INFINITY, Rmd = INFINITY;
             bool aL = false, aR = false;
             if (act)
@@ -1472,16 +1498,22 @@ SNCH_DEV void nearest_packet_chunk(const TreeView &t, const float *__restrict__ 
                 {
                     st_node[sp] = l_first ? R : L;
                     st_mask[sp] = l_first ? pR : pL;
+                    if (kTop)
+                        st_slot[sp] = (uint8_t)child_slot(slot, l_first ? 1u : 0u, top_slots);
                 }
                 __syncwarp();
                 ++sp;
                 node = l_first ? L : R;
                 mask = l_first ? pL : pR;
+                if (kTop)
+                    slot = child_slot(slot, l_first ? 0u : 1u, top_slots);
             }
             else if (pL | pR)
             {
                 node = pL ? L : R;
                 mask = pL ? pL : pR;
+                if (kTop)
+                    slot = child_slot(slot, pL ? 0u : 1u, top_slots);
             }
             else
                 mask = 0u;
@@ -1525,15 +1557,86 @@ __global__ void __launch_bounds__(128, 10) nearest_packet_kernel(TreeView t, con
                                  blockIdx.x * (int64_t)blockDim.x + threadIdx.x, st_node[w], st_mask[w]);
 }
 
+// ---- top tree levels staged in shared memory (TMA bulk copies)
+// The block's first thread copies the heap-ordered top-level records (and, for
+// silhouettes, their cones) from global memory with cp.async.bulk, completing on
+// an mbarrier that every thread waits on with a bounded poll. If the copy does
+// not complete in time the block sets kStatusCopyTimeout, waits once more
+// (bounded) for it, and searches from global memory (same answers).
+constexpr uint32_t kCopyPolls = 1u << 22;
+SNCH_DEV uint32_t smem_addr(const void *p) { return static_cast<uint32_t>(__cvta_generic_to_shared(p)); }
+SNCH_DEV void bulk_copy_to_smem(void *dst, const void *src, uint32_t bytes, uint64_t *mbar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_addr(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_addr(mbar))
+                 : "memory");
+}
+SNCH_DEV bool mbar_wait_parity(uint64_t *mbar, uint32_t parity, uint32_t polls)
+{
+    for (uint32_t i = 0; i < polls; ++i)
+    {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(smem_addr(mbar)), "r"(parity)
+            : "memory");
+        if (done)
+            return true;
+    }
+    return false;
+}
+// returns the number of top slots this block may read from shared memory (0 on a timeout)
+SNCH_DEV uint32_t stage_top_levels(const TreeView &t, InnerRec *s_top, InnerConeRec *s_topc, uint64_t *mbar)
+{
+    if (threadIdx.x == 0)
+    {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(mbar)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    const uint32_t bi = t.top_slots * (uint32_t)sizeof(InnerRec);
+    const uint32_t bc = s_topc ? t.top_slots * (uint32_t)sizeof(InnerConeRec) : 0u;
+    if (threadIdx.x == 0)
+    {
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(mbar)), "r"(bi + bc)
+                     : "memory");
+        bulk_copy_to_smem(s_top, t.top_inner, bi, mbar);
+        if (bc)
+            bulk_copy_to_smem(s_topc, t.top_cones, bc, mbar);
+    }
+    const bool ok = __syncthreads_and(mbar_wait_parity(mbar, 0, kCopyPolls));
+    if (ok)
+        return t.top_slots;
+    if (threadIdx.x == 0)
+        atomicOr(t.status, kStatusCopyTimeout);
+    __syncthreads_and(mbar_wait_parity(mbar, 0, kCopyPolls));  // the copy must not outlive the block
+    return 0;
+}
+inline size_t top_smem_bytes(uint32_t slots, bool cones)
+{
+    return (size_t)slots * (sizeof(InnerRec) + (cones ? sizeof(InnerConeRec) : 0));
+}
+
 // the same packets, persistent: each warp takes the next 32 queries of the
 // batch from a batch-wide counter when its packet is done, so no warp slot
-// waits for the slowest packet of its block
+// waits for the slowest packet of its block. kTop: the top tree levels are read
+// from a shared-memory copy (dynamic shared memory, top_smem_bytes).
+template <bool kTop>
 __global__ void __launch_bounds__(128, 10)
     nearest_packet_persistent_kernel(TreeView t, const float *__restrict__ pts, int64_t n, uint32_t *__restrict__ out_idx,
                                      float *__restrict__ out_dist, SeedArgs seed, unsigned long long *counter)
 {
     __shared__ uint32_t st_node[kPacketWarps][kStackDepth];
     __shared__ uint32_t st_mask[kPacketWarps][kStackDepth];
+    __shared__ uint8_t st_slot[kPacketWarps][kStackDepth];
+    __shared__ uint64_t mbar;
+    extern __shared__ __align__(128) unsigned char s_dyn[];
+    InnerRec *s_top = reinterpret_cast<InnerRec *>(s_dyn);
+    const uint32_t top_slots = kTop ? stage_top_levels(t, s_top, nullptr, &mbar) : 0u;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const unsigned long long total = (unsigned long long)query_count(t, n);
     for (;;)
@@ -1544,18 +1647,20 @@ __global__ void __launch_bounds__(128, 10)
         base = __shfl_sync(0xffffffffu, base, 0);
         if (base >= total)
             break;
-        nearest_packet_chunk<false>(t, pts, n, out_idx, out_dist, nullptr, seed, (int64_t)base + lane, st_node[w],
-                                    st_mask[w]);
+        nearest_packet_chunk<false, kTop>(t, pts, n, out_idx, out_dist, nullptr, seed, (int64_t)base + lane,
+                                          st_node[w], st_mask[w], st_slot[w], s_top, top_slots);
         __syncwarp();
     }
 }
 
 // one warp's packet: the 32 queries qi .. qi + 31 (lane order) of the batch
-template <bool kStats>
+template <bool kStats, bool kTop = false>
 SNCH_DEV void silhouette_packet_chunk(const TreeView &t, const float *__restrict__ pts, const uint8_t *__restrict__ flips,
                                       int64_t n, float *__restrict__ out_dist, int32_t *__restrict__ out_edge,
                                       uint32_t *__restrict__ stats, const SeedArgs &seed, int64_t qi,
-                                      uint32_t *st_node, uint32_t *st_mask)
+                                      uint32_t *st_node, uint32_t *st_mask, uint8_t *st_slot = nullptr,
+                                      const InnerRec *s_top = nullptr, const InnerConeRec *s_topc = nullptr,
+                                      uint32_t top_slots = 0)
 {
     const int lane = threadIdx.x & 31;
     const bool valid = qi < query_count(t, n);
@@ -1585,6 +1690,7 @@ SNCH_DEV void silhouette_packet_chunk(const TreeView &t, const float *__restrict
             in = !(mindist(load_root_box(t.aabbs + root), p) > best * best);
         uint32_t mask = __ballot_sync(0xffffffffu, in);
         uint32_t node = root;
+        uint32_t slot = kTop && root == 0u && !t.query_mesh ? 0u : kNoSlot;
         int sp = 0;
         while (true)
         {
@@ -1595,12 +1701,15 @@ SNCH_DEV void silhouette_packet_chunk(const TreeView &t, const float *__restrict
                 --sp;
                 node = st_node[sp];
                 mask = st_mask[sp];
+                if (kTop)
+                    slot = st_slot[sp];
                 continue;
             }
             const bool act = (mask >> lane) & 1u;
+            const bool in_top = kTop && slot < top_slots;
             Box lb, rb;
             uint32_t L, R, Linfo, Rinfo;
-            const InnerRec rec = load_inner(t.inner + node);
+            const InnerRec rec = in_top ? s_top[slot] : load_inner(t.inner + node);
             unpack_inner(rec, lb, rb, L, R);
             unpack_leaf_info(rec, Linfo, Rinfo);
             float Lmd = INFINITY, Rmd = INFINITY;
@@ -1609,11 +1718,16 @@ SNCH_DEV void silhouette_packet_chunk(const TreeView &t, const float *__restrict
             {
                 if (kStats)
                     ++n_int;
-                const float4 *cr = reinterpret_cast<const float4 *>(t.inner_cones + node);
                 InnerConeRec icr;
-                icr.a = __ldg(cr);
-                icr.b = __ldg(cr + 1);
-                icr.c = __ldg(cr + 2);
+                if (in_top)
+                    icr = s_topc[slot];
+                else
+                {
+                    const float4 *cr = reinterpret_cast<const float4 *>(t.inner_cones + node);
+                    icr.a = __ldg(cr);
+                    icr.b = __ldg(cr + 1);
+                    icr.c = __ldg(cr + 2);
+                }
                 Cone lc, rc;
                 unpack_cones(icr, lc, rc);
                 Lmd = mindist(lb, p);
@@ -1651,16 +1765,22 @@ SNCH_DEV void silhouette_packet_chunk(const TreeView &t, const float *__restrict
                 {
                     st_node[sp] = l_first ? R : L;
                     st_mask[sp] = l_first ? pR : pL;
+                    if (kTop)
+                        st_slot[sp] = (uint8_t)child_slot(slot, l_first ? 1u : 0u, top_slots);
                 }
                 __syncwarp();
                 ++sp;
                 node = l_first ? L : R;
                 mask = l_first ? pL : pR;
+                if (kTop)
+                    slot = child_slot(slot, l_first ? 0u : 1u, top_slots);
             }
             else if (pL | pR)
             {
                 node = pL ? L : R;
                 mask = pL ? pL : pR;
+                if (kTop)
+                    slot = child_slot(slot, pL ? 0u : 1u, top_slots);
             }
             else
                 mask = 0u;
@@ -1711,9 +1831,8 @@ __global__ void __launch_bounds__(128, SNCH_SIL_PACKET_MIN_BLOCKS)
                                     blockIdx.x * (int64_t)blockDim.x + threadIdx.x, st_node[w], st_mask[w]);
 }
 
-// the same packets, persistent: each warp takes the next 32 queries of the
-// batch from a batch-wide counter when its packet is done, so no warp slot
-// waits for the slowest packet of its block
+// the same packets, persistent (see nearest_packet_persistent_kernel)
+template <bool kTop>
 __global__ void __launch_bounds__(128, SNCH_SIL_PACKET_MIN_BLOCKS)
     silhouette_packet_persistent_kernel(TreeView t, const float *__restrict__ pts, const uint8_t *__restrict__ flips,
                                         int64_t n, float *__restrict__ out_dist, int32_t *__restrict__ out_edge,
@@ -1721,6 +1840,12 @@ __global__ void __launch_bounds__(128, SNCH_SIL_PACKET_MIN_BLOCKS)
 {
     __shared__ uint32_t st_node[kPacketWarps][kStackDepth];
     __shared__ uint32_t st_mask[kPacketWarps][kStackDepth];
+    __shared__ uint8_t st_slot[kPacketWarps][kStackDepth];
+    __shared__ uint64_t mbar;
+    extern __shared__ __align__(128) unsigned char s_dyn[];
+    InnerRec *s_top = reinterpret_cast<InnerRec *>(s_dyn);
+    InnerConeRec *s_topc = reinterpret_cast<InnerConeRec *>(s_dyn + (kTop ? t.top_slots : 0u) * sizeof(InnerRec));
+    const uint32_t top_slots = kTop ? stage_top_levels(t, s_top, s_topc, &mbar) : 0u;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const unsigned long long total = (unsigned long long)query_count(t, n);
     for (;;)
@@ -1731,8 +1856,8 @@ __global__ void __launch_bounds__(128, SNCH_SIL_PACKET_MIN_BLOCKS)
         base = __shfl_sync(0xffffffffu, base, 0);
         if (base >= total)
             break;
-        silhouette_packet_chunk<false>(t, pts, flips, n, out_dist, out_edge, nullptr, seed, (int64_t)base + lane,
-                                       st_node[w], st_mask[w]);
+        silhouette_packet_chunk<false, kTop>(t, pts, flips, n, out_dist, out_edge, nullptr, seed, (int64_t)base + lane,
+                                             st_node[w], st_mask[w], st_slot[w], s_top, s_topc, top_slots);
         __syncwarp();
     }
 }
@@ -2373,6 +2498,46 @@ __global__ void __launch_bounds__(128) ray_persistent_kernel(TreeView t, const f
     }
 }
 
+// ------------------------------------------------------------------ top levels
+// Heap slot i (children 2i+1, 2i+2) of the top levels: the internal node reached
+// from the root by the bits of i + 1 below its leading one (0 = left); a slot
+// under a leaf is left zero (the searches never read it).
+__global__ void top_levels_kernel(const InnerRec *__restrict__ inner, const InnerConeRec *__restrict__ cones,
+                                  uint32_t num_tris, uint32_t slots, InnerRec *__restrict__ top,
+                                  InnerConeRec *__restrict__ topc)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= slots)
+        return;
+    const uint32_t ni = num_tris - 1, h = i + 1;
+    uint32_t node = 0;
+    bool ok = num_tris > 1;
+    for (int b = 30 - __clz(h); b >= 0 && ok; --b)
+    {
+        const float4 d = __ldg(reinterpret_cast<const float4 *>(inner + node) + 3);
+        node = ((h >> b) & 1u) ? __float_as_uint(d.y) : __float_as_uint(d.x);
+        ok = node < ni;
+    }
+    InnerRec r{};
+    InnerConeRec c{};
+    if (ok)
+    {
+        r = inner[node];
+        c = cones[node];
+    }
+    top[i] = r;
+    topc[i] = c;
+}
+cudaError_t launch_top_levels(const InnerRec *inner, const InnerConeRec *cones, uint32_t num_tris, uint32_t slots,
+                              InnerRec *top, InnerConeRec *topc, cudaStream_t st)
+{
+    if (slots == 0 || num_tris < 2)
+        return cudaSuccess;
+    top_levels_kernel<<<1, 256, 0, st>>>(inner, cones, num_tris, slots, top, topc);
+    note_launch();
+    return cudaGetLastError();
+}
+
 // ------------------------------------------------------------------ sampling
 // intersect_sphere(sphere, aabb) aabb.cuh:433-449
 SNCH_DEV bool sphere_box(f3 c, float r, const Box &b)
@@ -2759,14 +2924,14 @@ inline bool wide_ok(const TreeView &t, int width, bool persistent, const SeedArg
 // small batches), and a zeroed 64-bit work counter of its own (stream-ordered
 // allocation, so concurrent calls on other streams do not share it)
 template <typename... KArgs, typename... Args>
-cudaError_t launch_persistent(void (*kernel)(KArgs...), int64_t n, cudaStream_t st, Args... args)
+cudaError_t launch_persistent_smem(void (*kernel)(KArgs...), size_t smem, int64_t n, cudaStream_t st, Args... args)
 {
     int dev = 0, sms = 0, per_sm = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e == cudaSuccess)
         e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (e == cudaSuccess)
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 128, 0);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 128, smem);
     if (e != cudaSuccess)
         return e;
     const int64_t need = (n + 127) / 128;
@@ -2777,12 +2942,17 @@ cudaError_t launch_persistent(void (*kernel)(KArgs...), int64_t n, cudaStream_t 
     e = cudaMemsetAsync(counter, 0, sizeof(unsigned long long), st);
     if (e == cudaSuccess)
     {
-        kernel<<<grid, 128, 0, st>>>(args..., counter);
+        kernel<<<grid, 128, smem, st>>>(args..., counter);
         note_launch();
         e = cudaGetLastError();
     }
     const cudaError_t f = cudaFreeAsync(counter, st);
     return e != cudaSuccess ? e : f;
+}
+template <typename... KArgs, typename... Args>
+cudaError_t launch_persistent(void (*kernel)(KArgs...), int64_t n, cudaStream_t st, Args... args)
+{
+    return launch_persistent_smem(kernel, 0, n, st, args...);
 }
 // Results of an unseeded, fully Morton-ordered batch are written at their batch
 // position into a stream-ordered temporary (warp-contiguous, coalesced stores)
@@ -2895,7 +3065,10 @@ cudaError_t launch_nearest(const TreeView &t0, const float *pts, int64_t n, uint
             nearest_packet_kernel<true><<<grid_for(n, 128), 128, 0, st>>>(t, pts, n, idx, dist, stats, seed);
         else if (n >= t.packet_persistent_min)
         {
-            e = launch_persistent(nearest_packet_persistent_kernel, n, st, t, pts, n, idx, dist, seed);
+            e = t.top_slots && !t.query_mesh
+                    ? launch_persistent_smem(nearest_packet_persistent_kernel<true>, top_smem_bytes(t.top_slots, false),
+                                             n, st, t, pts, n, idx, dist, seed)
+                    : launch_persistent(nearest_packet_persistent_kernel<false>, n, st, t, pts, n, idx, dist, seed);
             launched = true;
         }
         else
@@ -2974,7 +3147,12 @@ cudaError_t launch_silhouette(const TreeView &t0, const float *pts, const uint8_
                 <<<grid_for(n, 128), 128, 0, st>>>(t, pts, flip, n, dist, edge, stats, seed);
         else if (n >= t.packet_persistent_min)
         {
-            e = launch_persistent(silhouette_packet_persistent_kernel, n, st, t, pts, flip, n, dist, edge, seed);
+            e = t.top_slots && !t.query_mesh
+                    ? launch_persistent_smem(silhouette_packet_persistent_kernel<true>,
+                                             top_smem_bytes(t.top_slots, true), n, st, t, pts, flip, n, dist, edge,
+                                             seed)
+                    : launch_persistent(silhouette_packet_persistent_kernel<false>, n, st, t, pts, flip, n, dist, edge,
+                                        seed);
             launched = true;
         }
         else

@@ -275,8 +275,12 @@ def test_reference_cuda_on_oracle_built_tree(ref, oracle_mod):
     b = ref.RefQueries(built_scene(snch, v, f))
     for x, y in zip(a.nearest(d["near_pts"]), b.nearest(d["near_pts"])):
         np.testing.assert_array_equal(x.cpu().numpy().view(np.uint32), y.cpu().numpy().view(np.uint32))
-    for x, y in zip(a.ray_uv(d["ray_o"], d["ray_d"], d["ray_tmax"]), b.ray_uv(d["ray_o"], d["ray_d"], d["ray_tmax"])):
-        np.testing.assert_array_equal(x.cpu().numpy().view(np.uint8), y.cpu().numpy().view(np.uint8))
+    ra = [x.cpu().numpy() for x in a.ray_uv(d["ray_o"], d["ray_d"], d["ray_tmax"])]
+    rb = [x.cpu().numpy() for x in b.ray_uv(d["ray_o"], d["ray_d"], d["ray_tmax"])]
+    for k in (0, 1, 3):  # hit, t, triangle
+        np.testing.assert_array_equal(ra[k].view(np.uint8), rb[k].view(np.uint8))
+    hit = ra[0] == 1  # the reference leaves (u, v) unset on a miss
+    np.testing.assert_array_equal(ra[2][hit].view(np.uint32), rb[2][hit].view(np.uint32))
     for x, y in zip(a.sample(d["smp_c"], d["smp_r"], d["smp_u"]), b.sample(d["smp_c"], d["smp_r"], d["smp_u"])):
         np.testing.assert_array_equal(x.cpu().numpy().view(np.uint32), y.cpu().numpy().view(np.uint32))
     sa = a.silhouette(d["sil_pts"], d["sil_flip"]).cpu().numpy()

@@ -227,11 +227,33 @@ def test_output_scatter_equals_direct_stores(big):
         r += list(s.sample_in_sphere(q["smp_c"], q["smp_r"], q["smp_u"]))
         return [x.cpu().numpy() for x in r]
 
-    assert s.get_option(snch.OPT_OUTPUT_SCATTER) == 1
+    assert s.get_option(snch.OPT_OUTPUT_SCATTER) == 0
     a = run()
-    s.set_option(snch.OPT_OUTPUT_SCATTER, 0)
-    b = run()
     s.set_option(snch.OPT_OUTPUT_SCATTER, 1)
+    b = run()
+    s.set_option(snch.OPT_OUTPUT_SCATTER, 0)
     for x, y in zip(a, b):
         np.testing.assert_array_equal(x.view(np.uint8), y.view(np.uint8))
+    assert s.device_status() == 0
+
+
+@pytest.mark.parametrize("levels", [1, 5, 7])
+def test_top_levels_in_shared_memory_equal(big, levels):
+    """SNCH_OPT_TOP_LEVELS: the persistent packet searches reading the top tree
+    levels from a shared-memory copy (bulk-copied per block) give the answers of
+    the searches reading them from global memory, bit for bit (2M queries each,
+    persistent packets forced at this size)."""
+    import snch_lbvh_gb300 as snch
+    sc, s, _ = big
+    rng = np.random.default_rng(47 + levels)
+    pts = rng.random((2_000_000, 3), dtype=np.float32)
+    flip = (rng.random(len(pts)) < 0.5).astype(np.uint8)
+    s.set_option(snch.OPT_PACKET_PERSISTENT_MIN, 1)
+    a = _packet_answers(s, pts, flip)
+    s.set_option(snch.OPT_TOP_LEVELS, levels)
+    b = _packet_answers(s, pts, flip)
+    s.set_option(snch.OPT_TOP_LEVELS, 0)
+    s.set_option(snch.OPT_PACKET_PERSISTENT_MIN, 1 << 23)
+    for x, y in zip(a, b):
+        np.testing.assert_array_equal(x.view(np.uint32), y.view(np.uint32))
     assert s.device_status() == 0
