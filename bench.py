@@ -886,6 +886,21 @@ def run_ours(args):
                                   dev["smp_u"][:m["smp"]]).mean(0),
     }
 
+    # ---- stack depth: a search pushes at most one entry per level it descends, so
+    # the tree's depth bounds every stack (64 entries binary); no tuning needed
+    nodes = scene.export_tree()["nodes"].astype(np.int64)
+    depth = np.zeros(len(nodes), np.int64)
+    frontier = np.array([0])
+    ni = (len(nodes) + 1) // 2 - 1
+    while len(frontier):
+        inner = frontier[frontier < ni]
+        kids = np.concatenate([nodes[inner, 1], nodes[inner, 2]])
+        depth[kids] = np.concatenate([depth[inner], depth[inner]]) + 1
+        frontier = kids
+    stack = {"tree_depth": int(depth.max()), "stack_entries": 64,
+             "overflowed": bool(status & 1), "note": "a search's stack holds at most one entry per level below "
+             "its current node, so the tree depth bounds it; the autotuner has no stack dimension"}
+
     # ---- the occlusion form of the ray query (ray_intersect<TestOnly = true>) on the
     # same rays, outside the timed step; its hit flags equal the timed step's
     ray_test_ms = time_events(lambda: scene.query_ray_test(dev["ray_o"], dev["ray_d"], dev["ray_tmax"]), 3, stream)
@@ -950,6 +965,21 @@ def run_ours(args):
             t.append(time.perf_counter())
             e2e_parts.append([1e3 * (b_ - a_) for a_, b_ in zip(t, t[1:])])
 
+        # what the host link delivers on this machine (other tenants share it): one pinned
+        # 192 MB input array each way, event-timed
+        probe = torch.empty(pin["near_pts"].shape, dtype=torch.float32, device="cuda")
+        src = torch.from_numpy(pin["near_pts"])
+        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        probe.copy_(src, non_blocking=True)
+        e0.record()
+        probe.copy_(src, non_blocking=True)
+        e1.record()
+        src.copy_(probe, non_blocking=True)
+        e2.record()
+        torch.cuda.synchronize()
+        link = {"h2d_gbs": src.numel() * 4 / (e0.elapsed_time(e1) / 1e3) / 1e9,
+                "d2h_gbs": src.numel() * 4 / (e1.elapsed_time(e2) / 1e3) / 1e9}
+        del probe
         e2e_steps = max(1, min(args.steps, 3))
         e2e_step()
         barrier()
@@ -966,7 +996,7 @@ def run_ours(args):
         mismatch = {k: bit_mismatches(v, device_answers[k]) for k, v in host_answers.items()}
         e2e = {"value": total_q * ws * e2e_steps / e2e_s, "unit": "queries/s", "h2d_bytes_per_step": int(h2d),
                "d2h_bytes_per_step": int(d2h), "steps": e2e_steps,
-               "mismatches_vs_device_forms": mismatch,
+               "mismatches_vs_device_forms": mismatch, "pinned_link": link,
                "phase_ms": dict(zip(["create+build", "near", "sil", "ray", "smp", "close"],
                                     np.round(np.mean(e2e_parts[1:], 0), 2).tolist())),
                "note": "scene upload + build + snch_*_host queries from pinned host memory, wall clock; "
@@ -1030,6 +1060,7 @@ def run_ours(args):
         "ray_test": ray_test,
         "phase_ms": {"build": float(phase_ms[0]), **{k: float(phase_ms[1 + i]) for i, k in enumerate(kinds)}},
         "gpu_launches": int(launches),
+        "stack": stack,
         "device_status": int(status),
         "clocks": clk,
         "roofline": roof,

@@ -176,6 +176,9 @@ cudaError_t set_mlp_scales(const float *scales);
 // splits > 1: split K, C holds one M x N slice per split (the caller reduces them)
 cudaError_t launch_gemm_bf16(const void *A, const void *B, float *C, int64_t M, int64_t N, int64_t K, int accumulate,
                              uint32_t *status, cudaStream_t st, int splits = 1);
+// the same with H non-null: H = bf16(max(A B^T + bias, 0)) (N = 64) instead of C
+cudaError_t launch_gemm_bf16_ex(const void *A, const void *B, float *C, const float *bias, void *H, int64_t M,
+                                int64_t N, int64_t K, int accumulate, uint32_t *status, cudaStream_t st, int splits);
 cudaError_t launch_mlp_radius(const float *params, const float *pts, int64_t n, const float center[3],
                               const float inv_half[3], float margin, float floor_, float *r_near, float *r_sil,
                               uint32_t *status, cudaStream_t st);

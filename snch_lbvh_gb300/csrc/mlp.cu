@@ -11,16 +11,19 @@
 //
 // Kernels:
 //   gemm_bf16_kernel   C[MxN] (+)= A[MxK] B[NxK]^T, tiles of 128 rows, operands
-//                      staged in shared memory in the core-matrix layout, one
-//                      thread issues the MMAs, the accumulator stays in TMEM
-//                      across the K loop; used by training (forward, input and
-//                      weight gradients)
+//                      loaded by TMA into a 4-stage shared-memory ring in the
+//                      core-matrix layout, one thread issues the MMAs, the
+//                      accumulator stays in TMEM across the K loop; optional
+//                      bias + ReLU -> BF16 epilogue; used by training (forward
+//                      layers, input and weight gradients)
 //   mlp_radius_kernel  fused inference: features -> 4 tensor-core layers -> head
 //                      -> radius, persistent CTAs with the weights resident in
 //                      shared memory
-//   small elementwise kernels for training (bias + ReLU, transposes, loss, Adam)
+//   small elementwise kernels for training (transposes, loss, ReLU backward, Adam)
+#include <cuda.h>
 #include <cuda_bf16.h>
 
+#include <algorithm>
 #include <cmath>
 
 #include "internal.h"
@@ -96,19 +99,37 @@ struct Octaves
 // row-major. M % 128 == 0, K % 64 == 0, N in {64, 128, 192, 256}.
 // Split K (blockIdx.y = split): split s sums K columns [s * k_split, (s + 1) * k_split)
 // into its own slice C + s * M * N, so a reduction over the slices follows.
+// With H non-null (forward layers, N = 64) the epilogue writes
+// H = bf16(max(C + bias, 0)) instead of C.
+//
+// Operands arrive by TMA (cp.async.bulk.tensor.2d) in 64-column K chunks through
+// a kStages-deep ring of shared-memory stages: thread 0 produces (waits until a
+// stage is free, then issues 8 boxes of 8 columns x R rows per operand, each box
+// landing as one column of 8 x 16-byte core matrices), thread 32 consumes (waits
+// for the stage's bytes, issues the four K=16 tcgen05.mma steps, and commits to
+// the stage's "empty" barrier, which the tensor core signals once it has read
+// the stage). Layout of an operand of R rows in a stage:
+//   byte(r, k) = (k / 8) * (R * 16) + r * 16 + (k % 8) * 2
+// i.e. core matrices with LBO = R * 16 (along K) and SBO = 128 (along rows).
+// Every wait is bounded: on a timeout the block sets kStatusLookbackTimeout,
+// lets the copies and MMAs it issued finish (bounded again) and writes nothing.
 template <int N>
-__global__ void __launch_bounds__(128) gemm_bf16_kernel(const __nv_bfloat16 *__restrict__ A,
-                                                        const __nv_bfloat16 *__restrict__ B, float *__restrict__ C,
-                                                        int K, int k_split, int accumulate, uint32_t *status)
+__global__ void __launch_bounds__(128) gemm_bf16_kernel(const __grid_constant__ CUtensorMap tm_a,
+                                                        const __grid_constant__ CUtensorMap tm_b,
+                                                        float *__restrict__ C, const float *__restrict__ bias,
+                                                        __nv_bfloat16 *__restrict__ H, int K, int k_split,
+                                                        int accumulate, uint32_t *status)
 {
     constexpr int kChunk = 64;
-    constexpr uint32_t kLbo = 128, kSbo = (kChunk / 8) * 128;
+    constexpr int kStages = 4;
+    constexpr uint32_t kABytes = 128 * kChunk * 2, kBBytes = N * kChunk * 2, kStageBytes = kABytes + kBBytes;
     constexpr uint32_t kCols = N <= 64 ? 64 : (N <= 128 ? 128 : 256);
-    extern __shared__ __align__(128) uint8_t smem[];
-    uint8_t *sa = smem;                    // 128 x 64 bf16 = 16 KB
-    uint8_t *sb = smem + 128 * kChunk * 2;  // N x 64 bf16
-    __shared__ uint64_t mbar;
+    extern __shared__ __align__(128) uint8_t gemm_dyn[];
+    // the stage ring, 1024-byte aligned inside the dynamic allocation (1 KB extra)
+    uint8_t *smem = gemm_dyn + ((1024u - (tc::smem_u32(gemm_dyn) & 1023u)) & 1023u);
+    __shared__ uint64_t full[kStages], empty[kStages], done;
     __shared__ uint32_t tmem_base;
+    __shared__ int issued_s;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     if (warp == 0)
     {
@@ -116,57 +137,85 @@ __global__ void __launch_bounds__(128) gemm_bf16_kernel(const __nv_bfloat16 *__r
         tc::tmem_relinquish();
     }
     if (tid == 0)
-        tc::mbar_init(&mbar, 1);
+    {
+        for (int s = 0; s < kStages; ++s)
+        {
+            tc::mbar_init(&full[s], 1);
+            tc::mbar_init(&empty[s], 1);
+        }
+        tc::mbar_init(&done, 1);
+        tc::fence_mbar_init();
+    }
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
     const uint32_t taddr = tmem_base;
-    const int64_t m0 = (int64_t)blockIdx.x * 128;
+    const int m0 = blockIdx.x * 128;
     const int k_begin = blockIdx.y * k_split, k_end = min(K, k_begin + k_split);
+    const int nk = (k_end - k_begin) / kChunk;
     C += (int64_t)blockIdx.y * gridDim.x * 128 * N;
-    uint32_t phase = 0;
     bool ok = true;
-    for (int kc = k_begin; kc < k_end && ok; kc += kChunk)
+    if (tid == 0)
     {
-        // stage A rows m0 .. m0+127 and B rows 0 .. N-1, columns kc .. kc+63
+        // producer
+        int issued = 0;
+        for (int i = 0; i < nk; ++i)
         {
-            const uint4 *src = reinterpret_cast<const uint4 *>(A + (m0 + tid) * (int64_t)K + kc);
+            const int s = i % kStages;
+            if (i >= kStages && !tc::mbar_wait(&empty[s], (uint32_t)((i / kStages - 1) & 1), kWaitPolls))
+            {
+                ok = false;
+                break;
+            }
+            uint8_t *sa = smem + s * kStageBytes, *sb = sa + kABytes;
+            tc::mbar_arrive_expect_tx(&full[s], kStageBytes);
+            const int kc = k_begin + i * kChunk;
 #pragma unroll
-            for (int j = 0; j < 8; ++j)
-                *reinterpret_cast<uint4 *>(sa + tc::core_offset(tid, 8 * j, kLbo, kSbo)) = src[j];
+            for (int j = 0; j < kChunk / 8; ++j)
+            {
+                tc::tma_load_2d(sa + j * (128 * 16), &tm_a, kc + 8 * j, m0, &full[s]);
+                tc::tma_load_2d(sb + j * (N * 16), &tm_b, kc + 8 * j, 0, &full[s]);
+            }
+            issued = i + 1;
         }
-        for (int r = tid; r < N; r += 128)
-        {
-            const uint4 *src = reinterpret_cast<const uint4 *>(B + (int64_t)r * K + kc);
-#pragma unroll
-            for (int j = 0; j < 8; ++j)
-                *reinterpret_cast<uint4 *>(sb + tc::core_offset(r, 8 * j, kLbo, kSbo)) = src[j];
-        }
-        tc::fence_proxy_async();
-        tc::fence_before_sync();
-        __syncthreads();
-        if (tid == 0)
-        {
-            tc::fence_after_sync();
-            constexpr uint32_t idesc = tc::idesc_bf16_f32(128, N);
-#pragma unroll
-            for (int s = 0; s < kChunk / 16; ++s)
-                tc::mma_bf16(taddr, tc::smem_desc(tc::smem_u32(sa) + 256 * s, kLbo, kSbo),
-                             tc::smem_desc(tc::smem_u32(sb) + 256 * s, kLbo, kSbo), idesc,
-                             (kc > k_begin || s > 0) ? 1u : 0u);
-            tc::commit(&mbar);
-        }
-        // the whole CTA takes the same branch even if one thread's wait gave up
-        ok = __syncthreads_and(tc::mbar_wait(&mbar, phase, kWaitPolls) ? 1 : 0) != 0;
-        if (ok)
-            phase ^= 1u;
-        tc::fence_after_sync();
+        issued_s = issued;
     }
+    else if (tid == 32)
+    {
+        // MMA issuer
+        constexpr uint32_t idesc = tc::idesc_bf16_f32(128, N);
+        for (int i = 0; i < nk; ++i)
+        {
+            const int s = i % kStages;
+            if (!tc::mbar_wait(&full[s], (uint32_t)((i / kStages) & 1), kWaitPolls))
+            {
+                ok = false;
+                break;
+            }
+            tc::fence_after_sync();
+            const uint32_t sa = tc::smem_u32(smem + s * kStageBytes), sb = sa + kABytes;
+#pragma unroll
+            for (int k16 = 0; k16 < kChunk / 16; ++k16)
+                tc::mma_bf16(taddr, tc::smem_desc(sa + k16 * 2 * (128 * 16), 128 * 16, 128),
+                             tc::smem_desc(sb + k16 * 2 * (N * 16), N * 16, 128), idesc,
+                             (i > 0 || k16 > 0) ? 1u : 0u);
+            tc::commit(&empty[s]);
+        }
+        tc::commit(&done);  // arrives when every MMA issued above has completed
+    }
+    ok = __syncthreads_and(ok ? 1 : 0) != 0;
+    // the accumulator is complete once `done` fires (after a failure: the MMAs in flight have ended)
+    ok = __syncthreads_and((tc::mbar_wait(&done, 0, kWaitPolls) && ok) ? 1 : 0) != 0;
+    tc::fence_after_sync();
     if (!ok)
     {
         if (tid == 0)
+        {
             atomicOr(status, kStatusLookbackTimeout);
-        tc::mbar_wait(&mbar, phase, kWaitPolls);  // let the MMAs in flight finish before freeing TMEM
+            // the copies of the last issued round of every stage must land before the block exits
+            for (int i = max(0, issued_s - kStages); i < issued_s; ++i)
+                tc::mbar_wait(&full[i % kStages], (uint32_t)((i / kStages) & 1), kWaitPolls);
+        }
     }
     else
     {
@@ -176,10 +225,20 @@ __global__ void __launch_bounds__(128) gemm_bf16_kernel(const __nv_bfloat16 *__r
         {
             float v[16];
             tc::tmem_ld16(taddr + ((uint32_t)(32 * warp) << 16) + 16 * c, v);
-            float *dst = C + row * N + 16 * c;
+            if (H)
+            {
+                __nv_bfloat16 *dst = H + row * N + 16 * c;
 #pragma unroll
-            for (int j = 0; j < 16; ++j)
-                dst[j] = accumulate ? dst[j] + v[j] : v[j];
+                for (int j = 0; j < 16; ++j)
+                    dst[j] = __float2bfloat16_rn(fmaxf(v[j] + bias[16 * c + j], 0.0f));
+            }
+            else
+            {
+                float *dst = C + row * N + 16 * c;
+#pragma unroll
+                for (int j = 0; j < 16; ++j)
+                    dst[j] = accumulate ? dst[j] + v[j] : v[j];
+            }
         }
     }
     tc::fence_before_sync();
@@ -409,14 +468,6 @@ __global__ void features_kernel(const float *__restrict__ pts, int64_t n, int64_
 }
 
 // H = relu(Z + b) (bf16) for a [B x 64] pre-activation
-__global__ void bias_relu_kernel(const float *__restrict__ Z, const float *__restrict__ b, int64_t total,
-                                 __nv_bfloat16 *__restrict__ H)
-{
-    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i < total)
-        H[i] = __float2bfloat16_rn(fmaxf(Z[i] + b[i % kHid], 0.0f));
-}
-
 // dst[c][r] = src[r][c] (bf16), dst has dst_rows >= cols rows (the rest zero)
 __global__ void transpose_bf16_kernel(const __nv_bfloat16 *__restrict__ src, int64_t rows, int cols, int dst_rows,
                                       __nv_bfloat16 *__restrict__ dst)
@@ -595,27 +646,71 @@ inline unsigned blocks(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
 // ------------------------------------------------------------------ host entry points (internal)
 size_t mlp_num_params() { return mlp::kNumParams; }
 
-cudaError_t launch_gemm_bf16(const void *A, const void *B, float *C, int64_t M, int64_t N, int64_t K, int accumulate,
-                             uint32_t *status, cudaStream_t st, int splits)
+namespace
+{
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no libcuda link)
+using EncodeTiledFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                   const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiledFn encode_tiled()
+{
+    static EncodeTiledFn fn = [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            p = nullptr;
+        return reinterpret_cast<EncodeTiledFn>(p);
+    }();
+    return fn;
+}
+// a rows x K bf16 row-major matrix, boxes of 8 columns (16 bytes) x box_rows rows
+cudaError_t bf16_map(CUtensorMap *m, const void *base, int64_t rows, int64_t K, uint32_t box_rows)
+{
+    EncodeTiledFn f = encode_tiled();
+    if (!f)
+        return cudaErrorNotSupported;
+    const cuuint64_t dims[2] = {(cuuint64_t)K, (cuuint64_t)rows};
+    const cuuint64_t strides[1] = {(cuuint64_t)K * 2};
+    const cuuint32_t box[2] = {8, box_rows};
+    const cuuint32_t estr[2] = {1, 1};
+    const CUresult r = f(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(base), dims, strides, box, estr,
+                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+}  // namespace
+
+cudaError_t launch_gemm_bf16_ex(const void *A, const void *B, float *C, const float *bias, void *H, int64_t M,
+                                int64_t N, int64_t K, int accumulate, uint32_t *status, cudaStream_t st, int splits)
 {
     using namespace mlp;
-    const size_t smem = 128 * 64 * 2 + (size_t)N * 64 * 2;
+    if (M <= 0 || M % 128 || K <= 0 || K % 64 || (H && (N != 64 || !bias)) ||
+        (reinterpret_cast<uintptr_t>(A) | reinterpret_cast<uintptr_t>(B)) % 16)
+        return cudaErrorInvalidValue;
+    constexpr int kStages = 4;
+    const size_t smem = kStages * ((size_t)128 * 64 * 2 + (size_t)N * 64 * 2) + 1024;
     // every split gets at least one 64-column chunk, so every slice is written
     const int64_t chunks = K / 64;
     splits = (int)std::max<int64_t>(1, std::min<int64_t>(splits, chunks));
     const int k_split = (int)((chunks + splits - 1) / splits * 64);
     splits = (int)((K + k_split - 1) / k_split);
     const dim3 grid((unsigned)(M / 128), (unsigned)splits);
-    const auto *a = static_cast<const __nv_bfloat16 *>(A);
-    const auto *b = static_cast<const __nv_bfloat16 *>(B);
-    cudaError_t e = cudaSuccess;
+    CUtensorMap ta, tb;
+    cudaError_t e = bf16_map(&ta, A, M, K, 128);
+    if (e == cudaSuccess)
+        e = bf16_map(&tb, B, N, K, (uint32_t)N);
+    if (e != cudaSuccess)
+        return e;
+    auto *h = static_cast<__nv_bfloat16 *>(H);
     switch (N)
     {
 #define SNCH_GEMM_CASE(NN)                                                                                          \
     case NN:                                                                                                        \
         e = cudaFuncSetAttribute(gemm_bf16_kernel<NN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);     \
         if (e == cudaSuccess)                                                                                       \
-            gemm_bf16_kernel<NN><<<grid, 128, smem, st>>>(a, b, C, (int)K, k_split, accumulate, status);            \
+            gemm_bf16_kernel<NN><<<grid, 128, smem, st>>>(ta, tb, C, bias, h, (int)K, k_split, accumulate, status); \
         break;
         SNCH_GEMM_CASE(64)
         SNCH_GEMM_CASE(128)
@@ -627,6 +722,12 @@ cudaError_t launch_gemm_bf16(const void *A, const void *B, float *C, int64_t M, 
     }
     note_launch();
     return e != cudaSuccess ? e : cudaGetLastError();
+}
+
+cudaError_t launch_gemm_bf16(const void *A, const void *B, float *C, int64_t M, int64_t N, int64_t K, int accumulate,
+                             uint32_t *status, cudaStream_t st, int splits)
+{
+    return launch_gemm_bf16_ex(A, B, C, nullptr, nullptr, M, N, K, accumulate, status, st, splits);
 }
 
 cudaError_t set_mlp_scales(const float *scales)
@@ -692,7 +793,7 @@ cudaError_t mlp_forward_backward(float *params, float *grad, const float *pts, c
     auto *Tb2 = static_cast<__nv_bfloat16 *>(ws.T2);
     auto *Wt = static_cast<__nv_bfloat16 *>(ws.Wt);
     auto *Wb = static_cast<__nv_bfloat16 *>(ws.Wb);
-    float *Z = ws.Z, *dH = ws.dH, *C = ws.C;
+    float *dH = ws.dH, *C = ws.C;
     if ((e = cudaMemsetAsync(grad, 0, sizeof(float) * kNumParams, st)) != cudaSuccess)
         return e;
     if ((e = cudaMemsetAsync(loss, 0, sizeof(float), st)) != cudaSuccess)
@@ -713,10 +814,10 @@ cudaError_t mlp_forward_backward(float *params, float *grad, const float *pts, c
     const __nv_bfloat16 *in = X;
     for (int l = 0; l < 4; ++l)
     {
-        if ((e = launch_gemm_bf16(in, Wb + wbo[l], Z, rows, 64, win[l], 0, status, st)) != cudaSuccess)
+        // H_l = bf16(max(in W_l^T + b_l, 0)), bias and ReLU in the GEMM's epilogue
+        if ((e = launch_gemm_bf16_ex(in, Wb + wbo[l], nullptr, params + boff[l], H[l], rows, 64, win[l], 0, status,
+                                     st, 1)) != cudaSuccess)
             return e;
-        bias_relu_kernel<<<blocks(rows * 64, T), T, 0, st>>>(Z, params + boff[l], rows * 64, H[l]);
-        note_launch();
         in = H[l];
     }
     head_loss_kernel<<<blocks(rows, 128), 128, 0, st>>>(H[3], params, target, n, rows, tau,

@@ -17,43 +17,53 @@
 namespace snch
 {
 
-// find_closest_point_triangle scene.cuh:34-110 (distance only)
-SNCH_DEV float closest_point_triangle(f3 pa, f3 pb, f3 pc, f3 x)
+// find_closest_point_triangle scene.cuh:34-110: the squared length whose square root
+// is the distance (the argument of len3's sqrtf, summed in the same order)
+SNCH_DEV float closest_point_triangle_sq(f3 pa, f3 pb, f3 pc, f3 x)
 {
     const f3 ab = sub(pb, pa), ac = sub(pc, pa), ax = sub(x, pa);
     const float d1 = dot3(ab, ax), d2 = dot3(ac, ax);
     if (d1 <= 0.0f && d2 <= 0.0f)
-        return len3(sub(x, pa));
+        return sqlen3(sub(x, pa));
     const f3 bx = sub(x, pb);
     const float d3 = dot3(ab, bx), d4 = dot3(ac, bx);
     if (d3 >= 0.0f && d4 <= d3)
-        return len3(sub(x, pb));
+        return sqlen3(sub(x, pb));
     const f3 cx = sub(x, pc);
     const float d5 = dot3(ab, cx), d6 = dot3(ac, cx);
     if (d6 >= 0.0f && d5 <= d6)
-        return len3(sub(x, pc));
+        return sqlen3(sub(x, pc));
     const float vc = d1 * d4 - d3 * d2;
     if (vc <= 0.0f && d1 >= 0.0f && d3 <= 0.0f)
     {
         const float v = d1 / (d1 - d3);
-        return len3(sub(x, mk(pa.x + ab.x * v, pa.y + ab.y * v, pa.z + ab.z * v)));
+        return sqlen3(sub(x, mk(pa.x + ab.x * v, pa.y + ab.y * v, pa.z + ab.z * v)));
     }
     const float vb = d5 * d2 - d1 * d6;
     if (vb <= 0.0f && d2 >= 0.0f && d6 <= 0.0f)
     {
         const float w = d2 / (d2 - d6);
-        return len3(sub(x, mk(pa.x + ac.x * w, pa.y + ac.y * w, pa.z + ac.z * w)));
+        return sqlen3(sub(x, mk(pa.x + ac.x * w, pa.y + ac.y * w, pa.z + ac.z * w)));
     }
     const float va = d3 * d6 - d5 * d4;
     if (va <= 0.0f && (d4 - d3) >= 0.0f && (d5 - d6) >= 0.0f)
     {
         const float w = (d4 - d3) / ((d4 - d3) + (d5 - d6));
-        return len3(sub(x, mk(pb.x + (pc.x - pb.x) * w, pb.y + (pc.y - pb.y) * w, pb.z + (pc.z - pb.z) * w)));
+        return sqlen3(sub(x, mk(pb.x + (pc.x - pb.x) * w, pb.y + (pc.y - pb.y) * w, pb.z + (pc.z - pb.z) * w)));
     }
     const float denom = 1.0f / (va + vb + vc);
     const float v = vb * denom, w = vc * denom;
-    return len3(sub(x, mk(pa.x + ab.x * v + ac.x * w, pa.y + ab.y * v + ac.y * w, pa.z + ab.z * v + ac.z * w)));
+    return sqlen3(sub(x, mk(pa.x + ab.x * v + ac.x * w, pa.y + ab.y * v + ac.y * w, pa.z + ab.z * v + ac.z * w)));
 }
+
+SNCH_DEV float closest_point_triangle(f3 pa, f3 pb, f3 pc, f3 x) { return sqrtf(closest_point_triangle_sq(pa, pb, pc, x)); }
+
+// A candidate whose squared length s exceeds beyond(b) cannot pass a test
+// "sqrtf(s) <= b" (silhouette: b a distance) nor "sqrtf(s)^2 <= b" (nearest: b a
+// squared distance): b (1 + 2^-19), rounded twice, exceeds b (1 + 2^-20), and
+// both rounded forms of s then exceed b. So the IEEE square root is taken only
+// for candidates the exact test could accept; the answers do not change.
+SNCH_DEV float beyond_sq(float best_sq) { return best_sq * 1.0000019073486328125f; }
 
 SNCH_DEV Box load_root_box(const Box *p)
 {
@@ -373,26 +383,29 @@ __global__ void cone_filter_check_kernel(int64_t n, uint64_t seed, unsigned long
         atomicAdd(counts + threadIdx.x, s_c[threadIdx.x]);
 }
 
-// find_closest_point_line_segment(float3) scene.cuh:230-255
-SNCH_DEV float closest_point_segment(f3 pa, f3 pb, f3 x, f3 &pt)
+// find_closest_point_line_segment(float3) scene.cuh:230-255: the closest point pt
+// and the squared length whose square root is the distance
+SNCH_DEV float closest_point_segment_sq(f3 pa, f3 pb, f3 x, f3 &pt)
 {
     const f3 u = sub(pb, pa), v = sub(x, pa);
     const float c1 = dot3(u, v);
     if (c1 <= 0.0f)
     {
         pt = pa;
-        return len3(sub(x, pt));
+        return sqlen3(sub(x, pt));
     }
     const float c2 = dot3(u, u);
     if (c2 <= c1)
     {
         pt = pb;
-        return len3(sub(x, pt));
+        return sqlen3(sub(x, pt));
     }
     const float tt = c1 / c2;
     pt = mk(pa.x + u.x * tt, pa.y + u.y * tt, pa.z + u.z * tt);
-    return len3(sub(x, pt));
+    return sqlen3(sub(x, pt));
 }
+
+SNCH_DEV float closest_point_segment(f3 pa, f3 pb, f3 x, f3 &pt) { return sqrtf(closest_point_segment_sq(pa, pb, x, pt)); }
 
 // is_silhouette_edge scene.cuh:143-174 (view_dir left unnormalised, as there)
 SNCH_DEV bool is_silhouette_edge(f3 pa, f3 pb, f3 n0, f3 n1, f3 view_dir, float d, bool flip)
@@ -581,7 +594,10 @@ SNCH_DEV void leaf_nearest_fast(const TreeView &t, uint32_t pos, f3 p, float &be
 {
     const float4 *q = reinterpret_cast<const float4 *>(t.leaves + pos);
     const float4 a = __ldg(q), b = __ldg(q + 1), c = __ldg(q + 2);
-    float d = closest_point_triangle(mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), mk(c.x, c.y, c.z), p);
+    const float sq = closest_point_triangle_sq(mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), mk(c.x, c.y, c.z), p);
+    if (sq > beyond_sq(best))
+        return;  // d > best: not a candidate
+    float d = sqrtf(sq);
     d *= d;
     const uint32_t rank = __float_as_uint(c.w);
     if (d < best || (d == best && (nearest == kInvalid || rank > best_rank)))
@@ -753,7 +769,10 @@ SNCH_DEV void leaf_silhouette_fast(const TreeView &t, uint32_t pos, f3 o, bool f
         const float4 ea = __ldg(e), eb = __ldg(e + 1);
         const f3 pa = mk(ea.x, ea.y, ea.z), pb = mk(eb.x, eb.y, eb.z);
         f3 cp;
-        const float d = closest_point_segment(pa, pb, o, cp);
+        const float sq = closest_point_segment_sq(pa, pb, o, cp);
+        if (sq > beyond_sq(best * best))
+            continue;  // d > best
+        const float d = sqrtf(sq);
         if (d > best)
             continue;
         const uint32_t flags = __float_as_uint(ea.w);
@@ -790,7 +809,10 @@ SNCH_DEV void leaf_silhouette_info(const TreeView &t, uint32_t pos, uint32_t inf
         const float4 ea = __ldg(e), eb = __ldg(e + 1);
         const f3 pa = mk(ea.x, ea.y, ea.z), pb = mk(eb.x, eb.y, eb.z);
         f3 cp;
-        const float d = closest_point_segment(pa, pb, o, cp);
+        const float sq = closest_point_segment_sq(pa, pb, o, cp);
+        if (sq > beyond_sq(best * best))
+            continue;  // d > best
+        const float d = sqrtf(sq);
         if (d > best)
             continue;
         const uint32_t flags = __float_as_uint(ea.w);
@@ -1625,8 +1647,14 @@ inline size_t top_smem_bytes(uint32_t slots, bool cones)
 // batch from a batch-wide counter when its packet is done, so no warp slot
 // waits for the slowest packet of its block. kTop: the top tree levels are read
 // from a shared-memory copy (dynamic shared memory, top_smem_bytes).
+// blocks per SM the persistent nearest packet kernel is compiled for (9: 56
+// registers; measured on 16M-query batches of the 2M-triangle scene: 12.10 ms,
+// against 12.40 ms at 10 blocks / 48 registers, where its loop state spills)
+#ifndef SNCH_NEAR_PACKET_MIN_BLOCKS
+#define SNCH_NEAR_PACKET_MIN_BLOCKS 9
+#endif
 template <bool kTop>
-__global__ void __launch_bounds__(128, 10)
+__global__ void __launch_bounds__(128, SNCH_NEAR_PACKET_MIN_BLOCKS)
     nearest_packet_persistent_kernel(TreeView t, const float *__restrict__ pts, int64_t n, uint32_t *__restrict__ out_idx,
                                      float *__restrict__ out_dist, SeedArgs seed, unsigned long long *counter)
 {
@@ -1812,11 +1840,11 @@ SNCH_DEV void silhouette_packet_chunk(const TreeView &t, const float *__restrict
         stats[3 * q + 2] = n_edge;
     }}
 
-// blocks per SM the silhouette packet kernels are compiled for (9: 56 registers;
-// measured on the 2M-triangle scene: 8 blocks / 64 registers within 1 %, 10 / 48
-// registers 6-12 % slower)
+// blocks per SM the silhouette packet kernels are compiled for (8: 64 registers;
+// measured on 16M-query batches of the 2M-triangle scene: 35.82 ms, against 36.03
+// at 9 blocks / 56 registers and 41.2 at 10 blocks / 48 registers)
 #ifndef SNCH_SIL_PACKET_MIN_BLOCKS
-#define SNCH_SIL_PACKET_MIN_BLOCKS 9
+#define SNCH_SIL_PACKET_MIN_BLOCKS 8
 #endif
 template <bool kStats>
 __global__ void __launch_bounds__(128, SNCH_SIL_PACKET_MIN_BLOCKS)

@@ -114,6 +114,28 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *mbar, uint32_t parity, uint3
     return false;
 }
 
+// make the mbarrier initialisations visible to the async proxy (TMA)
+__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+
+// one arrival that also expects `bytes` of asynchronous (TMA) transactions
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *mbar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(mbar)), "r"(bytes)
+                 : "memory");
+}
+
+// TMA: the box at (x, y) of a 2D tensor map (x innermost, in elements; x times
+// the element size must be a multiple of 16 bytes) into shared memory at dst
+// (128-byte aligned), completing `box bytes` transactions on mbar
+__device__ __forceinline__ void tma_load_2d(void *dst, const void *tmap, int x, int y, uint64_t *mbar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+            smem_u32(dst)),
+        "l"(tmap), "r"(x), "r"(y), "r"(smem_u32(mbar))
+        : "memory");
+}
+
 // 32 lanes x 16 consecutive 32-bit columns: thread t of the warp receives
 // lane (warp quarter base + t), columns col..col+15
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16])
