@@ -2259,8 +2259,13 @@ SNCH_DEV bool ray_triangle(f3 o, f3 dir, f3 v0, f3 v1, f3 v2, float &t, float &u
 // first accepted hit of the same traversal and report only whether there is one
 // (always the hit flag of the closest-hit search: both take the same path up to
 // that hit); t, uv and idx are not written.
+// minimum blocks per SM the ray kernel is compiled for (0: the compiler's choice, 48
+// registers and ten blocks)
+#ifndef SNCH_RAY_MIN_BLOCKS
+#define SNCH_RAY_MIN_BLOCKS 0
+#endif
 template <bool kStats, bool kAny = false>
-__global__ void __launch_bounds__(128) ray_kernel(TreeView t, const float *__restrict__ origins,
+__global__ void __launch_bounds__(128, SNCH_RAY_MIN_BLOCKS) ray_kernel(TreeView t, const float *__restrict__ origins,
                                                   const float *__restrict__ dirs, const float *__restrict__ tmaxs,
                                                   int64_t n, uint8_t *__restrict__ out_hit, float *__restrict__ out_t,
                                                   float *__restrict__ out_uv, uint32_t *__restrict__ out_idx,
