@@ -73,6 +73,8 @@ def parse():
                     help="SNCH_OPT_OUTPUT_SCATTER of the step's scene (-1: the library default)")
     ap.add_argument("--top-levels", type=int, default=-1,
                     help="SNCH_OPT_TOP_LEVELS of the step's scene (-1: the library default)")
+    ap.add_argument("--host-chunk", type=int, default=0,
+                    help="SNCH_OPT_HOST_CHUNK of the end-to-end leg's scenes (0: the library default)")
     ap.add_argument("--persistent-min", type=int, default=0,
                     help="SNCH_OPT_PACKET_PERSISTENT_MIN of the step's scene (0: the library default, 2^23); "
                          "lets a reduced --scale run the persistent packet kernels of the full workload")
@@ -950,6 +952,8 @@ def run_ours(args):
         def e2e_step():
             t = [time.perf_counter()]
             s = snch.Scene(pin_v, pin_f)
+            if args.host_chunk > 0:
+                s.set_option(snch.OPT_HOST_CHUNK, args.host_chunk)
             s.compute_silhouettes()
             s.build_bvh()
             t.append(time.perf_counter())

@@ -103,7 +103,7 @@ struct Octaves
 // H = bf16(max(C + bias, 0)) instead of C.
 //
 // Operands arrive by TMA (cp.async.bulk.tensor.2d) in 64-column K chunks through
-// a kStages-deep ring of shared-memory stages: thread 0 produces (waits until a
+// a ring of up to kStages of shared-memory stages: thread 0 produces (waits until a
 // stage is free, then issues 8 boxes of 8 columns x R rows per operand, each box
 // landing as one column of 8 x 16-byte core matrices), thread 32 consumes (waits
 // for the stage's bytes, issues the four K=16 tcgen05.mma steps, and commits to
@@ -153,6 +153,8 @@ __global__ void __launch_bounds__(128) gemm_bf16_kernel(const __grid_constant__ 
     const int m0 = blockIdx.x * 128;
     const int k_begin = blockIdx.y * k_split, k_end = min(K, k_begin + k_split);
     const int nk = (k_end - k_begin) / kChunk;
+    // ring depth: the K chunks a split has, at most kStages (the launch sizes shared memory the same way)
+    const int stages = max(1, min(kStages, k_split / kChunk));
     C += (int64_t)blockIdx.y * gridDim.x * 128 * N;
     bool ok = true;
     if (tid == 0)
@@ -161,8 +163,8 @@ __global__ void __launch_bounds__(128) gemm_bf16_kernel(const __grid_constant__ 
         int issued = 0;
         for (int i = 0; i < nk; ++i)
         {
-            const int s = i % kStages;
-            if (i >= kStages && !tc::mbar_wait(&empty[s], (uint32_t)((i / kStages - 1) & 1), kWaitPolls))
+            const int s = i % stages;
+            if (i >= stages && !tc::mbar_wait(&empty[s], (uint32_t)((i / stages - 1) & 1), kWaitPolls))
             {
                 ok = false;
                 break;
@@ -186,8 +188,8 @@ __global__ void __launch_bounds__(128) gemm_bf16_kernel(const __grid_constant__ 
         constexpr uint32_t idesc = tc::idesc_bf16_f32(128, N);
         for (int i = 0; i < nk; ++i)
         {
-            const int s = i % kStages;
-            if (!tc::mbar_wait(&full[s], (uint32_t)((i / kStages) & 1), kWaitPolls))
+            const int s = i % stages;
+            if (!tc::mbar_wait(&full[s], (uint32_t)((i / stages) & 1), kWaitPolls))
             {
                 ok = false;
                 break;
@@ -213,8 +215,8 @@ __global__ void __launch_bounds__(128) gemm_bf16_kernel(const __grid_constant__ 
         {
             atomicOr(status, kStatusLookbackTimeout);
             // the copies of the last issued round of every stage must land before the block exits
-            for (int i = max(0, issued_s - kStages); i < issued_s; ++i)
-                tc::mbar_wait(&full[i % kStages], (uint32_t)((i / kStages) & 1), kWaitPolls);
+            for (int i = max(0, issued_s - stages); i < issued_s; ++i)
+                tc::mbar_wait(&full[i % stages], (uint32_t)((i / stages) & 1), kWaitPolls);
         }
     }
     else
@@ -689,13 +691,15 @@ cudaError_t launch_gemm_bf16_ex(const void *A, const void *B, float *C, const fl
     if (M <= 0 || M % 128 || K <= 0 || K % 64 || (H && (N != 64 || !bias)) ||
         (reinterpret_cast<uintptr_t>(A) | reinterpret_cast<uintptr_t>(B)) % 16)
         return cudaErrorInvalidValue;
-    constexpr int kStages = 4;
-    const size_t smem = kStages * ((size_t)128 * 64 * 2 + (size_t)N * 64 * 2) + 1024;
     // every split gets at least one 64-column chunk, so every slice is written
     const int64_t chunks = K / 64;
     splits = (int)std::max<int64_t>(1, std::min<int64_t>(splits, chunks));
     const int k_split = (int)((chunks + splits - 1) / splits * 64);
     splits = (int)((K + k_split - 1) / k_split);
+    // a ring of min(4, chunks per split) stages (the kernel computes the same depth): one
+    // 24 KB stage for the K = 64 GEMMs, so eight blocks fit on an SM (as many as TMEM allows)
+    const int stages = std::max(1, std::min(4, k_split / 64));
+    const size_t smem = stages * ((size_t)128 * 64 * 2 + (size_t)N * 64 * 2) + 1024;
     const dim3 grid((unsigned)(M / 128), (unsigned)splits);
     CUtensorMap ta, tb;
     cudaError_t e = bf16_map(&ta, A, M, K, 128);
