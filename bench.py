@@ -73,6 +73,10 @@ def parse():
                     help="SNCH_OPT_OUTPUT_SCATTER of the step's scene (-1: the library default)")
     ap.add_argument("--top-levels", type=int, default=-1,
                     help="SNCH_OPT_TOP_LEVELS of the step's scene (-1: the library default)")
+    ap.add_argument("--ray-order", type=int, default=-1, choices=[-1, 0, 1],
+                    help="SNCH_OPT_RAY_ORDER of the step's scene (-1: the library default)")
+    ap.add_argument("--order-bits", type=int, default=0,
+                    help="SNCH_OPT_ORDER_BITS of the step's scene (0: the library default)")
     ap.add_argument("--host-chunk", type=int, default=0,
                     help="SNCH_OPT_HOST_CHUNK of the end-to-end leg's scenes (0: the library default)")
     ap.add_argument("--persistent-min", type=int, default=0,
@@ -815,6 +819,10 @@ def run_ours(args):
         scene.set_option(snch.OPT_OUTPUT_SCATTER, args.output_scatter)
     if args.top_levels >= 0:
         scene.set_option(snch.OPT_TOP_LEVELS, args.top_levels)
+    if args.ray_order >= 0:
+        scene.set_option(snch.OPT_RAY_ORDER, args.ray_order)
+    if args.order_bits > 0:
+        scene.set_option(snch.OPT_ORDER_BITS, args.order_bits)
     stream = torch.cuda.current_stream()
 
     def step(ev=None):
@@ -1003,6 +1011,7 @@ def run_ours(args):
                "mismatches_vs_device_forms": mismatch, "pinned_link": link,
                "phase_ms": dict(zip(["create+build", "near", "sil", "ray", "smp", "close"],
                                     np.round(np.mean(e2e_parts[1:], 0), 2).tolist())),
+               "step_phase_ms": [np.round(p, 2).tolist() for p in e2e_parts[1:]],
                "note": "scene upload + build + snch_*_host queries from pinned host memory, wall clock; "
                        "answers compared bit for bit with the device forms' answers of the timed step"}
 

@@ -281,6 +281,16 @@ int snch_set_traversal(snch_scene_t scene, int mode);
  *                             once, with a bulk copy, and read those nodes from there.
  *                             Same results. */
 #define SNCH_OPT_TOP_LEVELS 21
+/*   SNCH_OPT_RAY_ORDER        0 (default): ray batches are answered in the Morton order of
+ *                             their origins; 1: by length bucket first (floor(log2(tmax /
+ *                             the scene box's largest side)), 16 buckets), then by origin,
+ *                             so that the rays of a warp have similar lengths. Same results. */
+#define SNCH_OPT_RAY_ORDER 22
+/*   SNCH_OPT_ORDER_BITS       bits of a query's Morton code (plain scenes) that order a
+ *                             batch: 12 to 30, default 30; the order is sorted in
+ *                             ceil(bits / 8) radix passes, and only changes speed (queries
+ *                             of one cell keep their input order). */
+#define SNCH_OPT_ORDER_BITS 23
 /*   SNCH_OPT_HOST_CHUNK       queries per chunk of the *_host forms (at most 29 bytes in
  *                             and 17 out per query on each of two streams): chunk i's
  *                             input copy, search and output copy run on stream i % 2, so
@@ -556,7 +566,8 @@ int snch_mlp_predict_radius(snch_mlp_t mlp, const float *points, int64_t n, floa
 int snch_selfcheck_cone_filter(int64_t n, uint64_t seed, uint64_t *device_counts, snch_stream_t stream);
 
 /* building block: C[M x N] (+)= A[M x K] * B[N x K]^T, bf16 row-major A and B, fp32 C, on
- * tcgen05; M % 128 == 0, K % 64 == 0, N in {64, 128, 192, 256}; all DEVICE buffers */
+ * tcgen05 with TMA operand loads; M % 128 == 0, K % 64 == 0, N in {64, 128, 192, 256}; all
+ * DEVICE buffers, 16-byte aligned (SNCH_ERR_CUDA otherwise) */
 int snch_gemm_bf16(const void *A, const void *B, float *C, int64_t M, int64_t N, int64_t K, int accumulate,
                    uint32_t *device_status, snch_stream_t stream);
 

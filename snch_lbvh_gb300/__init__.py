@@ -37,6 +37,8 @@ OPT_PERSISTENT_RAY = 18
 OPT_PACKET_PERSISTENT_MIN = 19
 OPT_OUTPUT_SCATTER = 20
 OPT_TOP_LEVELS = 21
+OPT_RAY_ORDER = 22
+OPT_ORDER_BITS = 23
 
 
 def _torch():

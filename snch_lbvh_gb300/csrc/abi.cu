@@ -117,6 +117,8 @@ struct snch_scene_s
     int packet_near = 2, packet_sil = 2;    // warp packets: 0 never, 1 always, 2 Morton-ordered batches
     int64_t packet_persistent_min = int64_t(1) << 23;  // packet batches this large run persistent
     int output_scatter = 0;  // ordered batches: results in batch order, then one scatter pass (measured slower)
+    int ray_order = 0;       // ray batches ordered by length bucket, then origin
+    int order_bits = 30;     // Morton bits of the query-order key of plain scenes
     // top tree levels staged in shared memory by the persistent packet searches:
     // the first 2^levels - 1 of kTopSlots heap slots, gathered after every build
     int top_levels = 0;
@@ -148,6 +150,7 @@ struct snch_scene_s
         t.packet_sil = packet_sil;
         t.packet_persistent_min = packet_persistent_min;
         t.out_batch_order_enabled = output_scatter;
+        t.order_bits = order_bits;
         if (top_levels > 0 && num_meshes == 0)
         {
             t.top_inner = top_inner;
@@ -629,7 +632,7 @@ struct BatchView
     }
 };
 cudaError_t batch_view(const snch_scene_s *s, const float *keys_from, int64_t n, cudaStream_t st, BatchView &b,
-                       const uint32_t *query_mesh = nullptr)
+                       const uint32_t *query_mesh = nullptr, const float *ray_len = nullptr)
 {
     b.t = s->view();
     b.st = st;
@@ -649,7 +652,7 @@ cudaError_t batch_view(const snch_scene_s *s, const float *keys_from, int64_t n,
     if (e != cudaSuccess)
         return e;
     uint32_t *order = nullptr;
-    e = launch_query_order(b.t, keys_from, n, b.scratch, &order, st);
+    e = launch_query_order(b.t, keys_from, n, b.scratch, &order, st, s->ray_order ? ray_len : nullptr);
     b.t.order = order;
     b.t.order_coherent = 1;
     return e;
@@ -1096,6 +1099,16 @@ int snch_set_option(snch_scene_t s, int option, int64_t value)
             return fail(SNCH_ERR_INVALID_ARGUMENT, "SNCH_OPT_TOP_LEVELS must be in [0, 7]");
         s->top_levels = (int)value;
         return SNCH_OK;
+    case SNCH_OPT_ORDER_BITS:
+        if (value < 12 || value > 30)
+            return fail(SNCH_ERR_INVALID_ARGUMENT, "SNCH_OPT_ORDER_BITS must be in [12, 30]");
+        s->order_bits = (int)value;
+        return SNCH_OK;
+    case SNCH_OPT_RAY_ORDER:
+        if (value != 0 && value != 1)
+            return fail(SNCH_ERR_INVALID_ARGUMENT, "SNCH_OPT_RAY_ORDER takes 0 or 1");
+        s->ray_order = (int)value;
+        return SNCH_OK;
     case SNCH_OPT_OUTPUT_SCATTER:
         if (value != 0 && value != 1)
             return fail(SNCH_ERR_INVALID_ARGUMENT, "SNCH_OPT_OUTPUT_SCATTER takes 0 or 1");
@@ -1384,7 +1397,7 @@ int snch_query_ray(snch_scene_t s, const float *o, const float *d, const float *
     if (rc != SNCH_OK)
         return rc;
     BatchView b;
-    SNCH_CUDA(batch_view(s, o, n, S(stream), b));
+    SNCH_CUDA(batch_view(s, o, n, S(stream), b, nullptr, tmax));
     SNCH_CUDA(launch_ray(b.t, o, d, tmax, n, hit, t, uv, idx, S(stream)));
     return SNCH_OK;
 }
@@ -1398,7 +1411,7 @@ int snch_query_ray_test(snch_scene_t s, const float *o, const float *d, const fl
     if (rc != SNCH_OK)
         return rc;
     BatchView b;
-    SNCH_CUDA(batch_view(s, o, n, S(stream), b));
+    SNCH_CUDA(batch_view(s, o, n, S(stream), b, nullptr, tmax));
     SNCH_CUDA(launch_ray_test(b.t, o, d, tmax, n, hit, S(stream)));
     return SNCH_OK;
 }
@@ -1487,7 +1500,7 @@ int snch_query_ray_host(snch_scene_t s, const float *o, const float *d, const fl
     return run_host_pipeline(s, n, kHostChunkRay, ins, 3, outs, 4,
                              [&](int64_t m, void **di, void **dout, cudaStream_t st) {
         BatchView b;
-        cudaError_t e = batch_view(s, (const float *)di[0], m, st, b);
+        cudaError_t e = batch_view(s, (const float *)di[0], m, st, b, nullptr, (const float *)di[2]);
         return e != cudaSuccess ? e
                                 : launch_ray(b.t, (const float *)di[0], (const float *)di[1], (const float *)di[2], m,
                                              (uint8_t *)dout[0], (float *)dout[1], (float *)dout[2],
@@ -2357,6 +2370,8 @@ int snch_get_option(snch_scene_t s, int option, int64_t *value)
     case SNCH_OPT_PACKET_PERSISTENT_MIN: *value = s->packet_persistent_min; break;
     case SNCH_OPT_OUTPUT_SCATTER: *value = s->output_scatter; break;
     case SNCH_OPT_TOP_LEVELS: *value = s->top_levels; break;
+    case SNCH_OPT_RAY_ORDER: *value = s->ray_order; break;
+    case SNCH_OPT_ORDER_BITS: *value = s->order_bits; break;
     default: return fail(SNCH_ERR_INVALID_ARGUMENT, "unknown option " + std::to_string(option));
     }
     return SNCH_OK;

@@ -153,8 +153,9 @@ cudaError_t launch_top_levels(const InnerRec *inner, const InnerConeRec *cones, 
                               InnerRec *top, InnerConeRec *topc, cudaStream_t st);
 // scratch holds query_order_scratch_bytes(n) bytes and owns *order.
 size_t query_order_scratch_bytes(int64_t n);
+// len (optional, rays: tmax): order by length bucket, then by the origin's Morton code
 cudaError_t launch_query_order(const TreeView &t, const float *pts, int64_t n, void *scratch, uint32_t **order,
-                               cudaStream_t st);
+                               cudaStream_t st, const float *len = nullptr);
 cudaError_t launch_sample_point(const float *verts, const int32_t *tris, uint32_t num_tris, const int32_t *idx,
                                 const float *u, const float *v, int64_t n, float *out, cudaStream_t st);
 

@@ -103,7 +103,7 @@ struct Octaves
 // H = bf16(max(C + bias, 0)) instead of C.
 //
 // Operands arrive by TMA (cp.async.bulk.tensor.2d) in 64-column K chunks through
-// a ring of up to kStages of shared-memory stages: thread 0 produces (waits until a
+// a ring of kStages shared-memory stages: thread 0 produces (waits until a
 // stage is free, then issues 8 boxes of 8 columns x R rows per operand, each box
 // landing as one column of 8 x 16-byte core matrices), thread 32 consumes (waits
 // for the stage's bytes, issues the four K=16 tcgen05.mma steps, and commits to
@@ -153,8 +153,7 @@ __global__ void __launch_bounds__(128) gemm_bf16_kernel(const __grid_constant__ 
     const int m0 = blockIdx.x * 128;
     const int k_begin = blockIdx.y * k_split, k_end = min(K, k_begin + k_split);
     const int nk = (k_end - k_begin) / kChunk;
-    // ring depth: the K chunks a split has, at most kStages (the launch sizes shared memory the same way)
-    const int stages = max(1, min(kStages, k_split / kChunk));
+    constexpr int stages = kStages;
     C += (int64_t)blockIdx.y * gridDim.x * 128 * N;
     bool ok = true;
     if (tid == 0)
@@ -227,19 +226,34 @@ __global__ void __launch_bounds__(128) gemm_bf16_kernel(const __grid_constant__ 
         {
             float v[16];
             tc::tmem_ld16(taddr + ((uint32_t)(32 * warp) << 16) + 16 * c, v);
+            // 16-byte stores: a row's 16 columns are 64 (fp32) or 32 (bf16) contiguous bytes
             if (H)
             {
-                __nv_bfloat16 *dst = H + row * N + 16 * c;
+                __align__(16) __nv_bfloat16 h[16];
 #pragma unroll
                 for (int j = 0; j < 16; ++j)
-                    dst[j] = __float2bfloat16_rn(fmaxf(v[j] + bias[16 * c + j], 0.0f));
+                    h[j] = __float2bfloat16_rn(fmaxf(v[j] + bias[16 * c + j], 0.0f));
+                uint4 *dst = reinterpret_cast<uint4 *>(H + row * N + 16 * c);
+                dst[0] = reinterpret_cast<const uint4 *>(h)[0];
+                dst[1] = reinterpret_cast<const uint4 *>(h)[1];
             }
             else
             {
-                float *dst = C + row * N + 16 * c;
+                float4 *dst = reinterpret_cast<float4 *>(C + row * N + 16 * c);
 #pragma unroll
-                for (int j = 0; j < 16; ++j)
-                    dst[j] = accumulate ? dst[j] + v[j] : v[j];
+                for (int j = 0; j < 4; ++j)
+                {
+                    float4 o = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
+                    if (accumulate)
+                    {
+                        const float4 a = dst[j];
+                        o.x += a.x;
+                        o.y += a.y;
+                        o.z += a.z;
+                        o.w += a.w;
+                    }
+                    dst[j] = o;
+                }
             }
         }
     }
@@ -688,18 +702,19 @@ cudaError_t launch_gemm_bf16_ex(const void *A, const void *B, float *C, const fl
                                 int64_t N, int64_t K, int accumulate, uint32_t *status, cudaStream_t st, int splits)
 {
     using namespace mlp;
+    // TMA reads A and B, and the epilogue writes C / H, in 16-byte units
     if (M <= 0 || M % 128 || K <= 0 || K % 64 || (H && (N != 64 || !bias)) ||
-        (reinterpret_cast<uintptr_t>(A) | reinterpret_cast<uintptr_t>(B)) % 16)
+        (reinterpret_cast<uintptr_t>(A) | reinterpret_cast<uintptr_t>(B) | reinterpret_cast<uintptr_t>(C) |
+         reinterpret_cast<uintptr_t>(H)) % 16)
         return cudaErrorInvalidValue;
     // every split gets at least one 64-column chunk, so every slice is written
     const int64_t chunks = K / 64;
     splits = (int)std::max<int64_t>(1, std::min<int64_t>(splits, chunks));
     const int k_split = (int)((chunks + splits - 1) / splits * 64);
     splits = (int)((K + k_split - 1) / k_split);
-    // a ring of min(4, chunks per split) stages (the kernel computes the same depth): one
-    // 24 KB stage for the K = 64 GEMMs, so eight blocks fit on an SM (as many as TMEM allows)
-    const int stages = std::max(1, std::min(4, k_split / 64));
-    const size_t smem = stages * ((size_t)128 * 64 * 2 + (size_t)N * 64 * 2) + 1024;
+    // four stages (a ring sized to the chunks of a split, one stage for K = 64, measured
+    // slower: more resident blocks, slower per launch)
+    const size_t smem = 4 * ((size_t)128 * 64 * 2 + (size_t)N * 64 * 2) + 1024;
     const dim3 grid((unsigned)(M / 128), (unsigned)splits);
     CUtensorMap ta, tb;
     cudaError_t e = bf16_map(&ta, A, M, K, 128);

@@ -2739,9 +2739,14 @@ __global__ void sample_point_kernel(const float *__restrict__ verts, const int32
 // Morton code of the query point in the tree's root box; for batched queries
 // (mesh of each query given) in its mesh's root box, below the mesh id:
 // key = mesh << (32 - mesh_bits) | the code's top (32 - mesh_bits) bits
+// With lengths (rays: tmax), a plain scene's key is the ray's length bucket --
+// floor(log2(tmax / the root box's largest side)), 16 buckets from 2^-15 up --
+// above the top order_bits - 4 bits of the origin's code, so that a warp's rays have similar
+// lengths (a ray's work grows with its length) and, within a bucket, neighbouring
+// origins.
 __global__ void query_keys_kernel(const float *__restrict__ pts, int64_t n, const Box *__restrict__ root,
                                   uint32_t *__restrict__ keys, uint32_t *__restrict__ vals, TreeView t,
-                                  int mesh_bits)
+                                  int mesh_bits, const float *__restrict__ len)
 {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n)
@@ -2775,7 +2780,18 @@ __global__ void query_keys_kernel(const float *__restrict__ pts, int64_t n, cons
         return v;
     };
     const uint32_t code = expand(x) * 4 + expand(y) * 2 + expand(z);
-    keys[i] = t.query_mesh ? (m << (32 - mesh_bits)) | (code >> (mesh_bits - 2)) : code;
+    if (len && !t.query_mesh)
+    {
+        const float side = fmaxf(b.upper.x - b.lower.x, fmaxf(b.upper.y - b.lower.y, b.upper.z - b.lower.z));
+        const float r = __ldg(len + i) / side;
+        const int lb = r > 0.0f ? (isinf(r) ? 0 : ilogbf(r)) : -15;
+        const uint32_t bucket = (uint32_t)min(max(lb + 15, 0), 15);
+        keys[i] = (bucket << (t.order_bits - 4)) | (code >> (34 - t.order_bits));
+        vals[i] = (uint32_t)i;
+        return;
+    }
+    // plain scenes: the top order_bits of the 30-bit code (the sort takes that many bits)
+    keys[i] = t.query_mesh ? (m << (32 - mesh_bits)) | (code >> (mesh_bits - 2)) : code >> (30 - t.order_bits);
     vals[i] = (uint32_t)i;
 }
 
@@ -3338,7 +3354,7 @@ cudaError_t launch_enumerate(const TreeView &t, bool line, const float *q0, cons
 }
 
 cudaError_t launch_query_order(const TreeView &t, const float *pts, int64_t n, void *scratch, uint32_t **order,
-                               cudaStream_t st)
+                               cudaStream_t st, const float *len)
 {
     uint32_t *keys = static_cast<uint32_t *>(scratch);
     uint32_t *vals = keys + n, *keys_tmp = vals + n, *vals_tmp = keys_tmp + n;
@@ -3347,11 +3363,11 @@ cudaError_t launch_query_order(const TreeView &t, const float *pts, int64_t n, v
     int mesh_bits = 2;
     while (mesh_bits < 16 && (1u << mesh_bits) < t.num_meshes)
         ++mesh_bits;
-    query_keys_kernel<<<grid_for(n, 256), 256, 0, st>>>(pts, n, t.aabbs, keys, vals, t, mesh_bits);
+    query_keys_kernel<<<grid_for(n, 256), 256, 0, st>>>(pts, n, t.aabbs, keys, vals, t, mesh_bits, len);
     note_launch();
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess)
-        e = radix_sort_pairs(keys, vals, keys_tmp, vals_tmp, (uint32_t)n, t.query_mesh ? 32 : 30, nullptr,
+        e = radix_sort_pairs(keys, vals, keys_tmp, vals_tmp, (uint32_t)n, t.query_mesh ? 32 : t.order_bits, nullptr,
                              sort_scratch, t.status, st);
     *order = vals;
     return e;

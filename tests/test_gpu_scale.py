@@ -257,3 +257,54 @@ def test_top_levels_in_shared_memory_equal(big, levels):
     for x, y in zip(a, b):
         np.testing.assert_array_equal(x.view(np.uint32), y.view(np.uint32))
     assert s.device_status() == 0
+
+
+def test_ray_length_order_equal(big):
+    """SNCH_OPT_RAY_ORDER = 1 (rays ordered by length bucket, then origin) gives
+    the same closest hits and occlusion flags as the origin-ordered batch
+    (1M rays with tmax log-uniform over three decades)."""
+    import snch_lbvh_gb300 as snch
+    from snch_lbvh_gb300 import meshes
+    sc, s, _ = big
+    q = meshes.wost_queries(1, 1, 1_000_000, 1, seed=53)
+
+    def run():
+        r = [x.cpu().numpy() for x in s.query_ray(q["ray_o"], q["ray_d"], q["ray_tmax"])]
+        return r + [s.query_ray_test(q["ray_o"], q["ray_d"], q["ray_tmax"]).cpu().numpy()]
+
+    a = run()
+    s.set_option(snch.OPT_RAY_ORDER, 1)
+    b = run()
+    s.set_option(snch.OPT_RAY_ORDER, 0)
+    for x, y in zip(a, b):
+        np.testing.assert_array_equal(x.view(np.uint8), y.view(np.uint8))
+    assert s.device_status() == 0
+
+
+@pytest.mark.parametrize("bits", [24, 16])
+def test_order_bits_same_answers(big, bits):
+    """SNCH_OPT_ORDER_BITS: ordering batches by fewer Morton bits changes which
+    queries share a warp packet, not the answers: distances, ray hits and sphere
+    samples bit for bit, triangle indices / silhouette edge ids equal or an FP64
+    distance tie (1M queries per type)."""
+    import snch_lbvh_gb300 as snch
+    from snch_lbvh_gb300 import meshes
+    sc, s, _ = big
+    q = meshes.wost_queries(1_000_000, 1_000_000, 1_000_000, 1_000_000, seed=59)
+
+    def run():
+        r = list(s.query_nearest(q["near_pts"])) + list(s.query_silhouette(q["sil_pts"], q["sil_flip"]))
+        r += list(s.query_ray(q["ray_o"], q["ray_d"], q["ray_tmax"]))
+        r += list(s.sample_in_sphere(q["smp_c"], q["smp_r"], q["smp_u"]))
+        return [x.cpu().numpy() for x in r]
+
+    assert s.get_option(snch.OPT_ORDER_BITS) == 30
+    a = run()
+    s.set_option(snch.OPT_ORDER_BITS, bits)
+    b = run()
+    s.set_option(snch.OPT_ORDER_BITS, 30)
+    for k in (1, 2, 4, 5, 6, 7, 8, 9):  # distances, ray hit/t/uv/triangle, sample index/pdf
+        np.testing.assert_array_equal(a[k].view(np.uint8), b[k].view(np.uint8))
+    check_tri_ids(b[0], a[0], a[1], q["near_pts"], sc.verts, sc.faces)
+    check_edge_ids(b[3], a[3], a[2], q["sil_pts"], sc.verts, s.export_topology()[2])
+    assert s.device_status() == 0
