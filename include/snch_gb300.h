@@ -284,12 +284,16 @@ int snch_set_traversal(snch_scene_t scene, int mode);
 /*   SNCH_OPT_RAY_ORDER        0 (default): ray batches are answered in the Morton order of
  *                             their origins; 1: by length bucket first (floor(log2(tmax /
  *                             the scene box's largest side)), 16 buckets), then by origin,
- *                             so that the rays of a warp have similar lengths. Same results. */
+ *                             so that the rays of a warp have similar lengths (measured 1.6 %
+ *                             slower on 16M rays with tmax log-uniform over three decades:
+ *                             the lost spatial coherence costs more). Same results. */
 #define SNCH_OPT_RAY_ORDER 22
 /*   SNCH_OPT_ORDER_BITS       bits of a query's Morton code (plain scenes) that order a
- *                             batch: 12 to 30, default 30; the order is sorted in
- *                             ceil(bits / 8) radix passes, and only changes speed (queries
- *                             of one cell keep their input order). */
+ *                             batch: 12 to 30, default 24 (a 256^3 grid, sorted in three
+ *                             radix passes; measured on 16M-query batches of the
+ *                             2M-triangle scene: 0.4 % faster per step than 30 bits in four
+ *                             passes, 16 bits 52 % slower). Queries of one cell keep their
+ *                             input order; only the speed changes. */
 #define SNCH_OPT_ORDER_BITS 23
 /*   SNCH_OPT_HOST_CHUNK       queries per chunk of the *_host forms (at most 29 bytes in
  *                             and 17 out per query on each of two streams): chunk i's

@@ -163,7 +163,7 @@ struct TreeView
     // 1: results are written at their batch position i (coalesced) instead of at
     // query order[i]; the launcher then scatters them to query order (unseeded,
     // fully ordered batches of the kernels that support it)
-    int order_bits = 30;  // Morton bits of a plain scene's query-order key (sorted in ceil(bits / 8) passes)
+    int order_bits = 24;  // Morton bits of a plain scene's query-order key (sorted in ceil(bits / 8) passes)
     int out_batch_order = 0;
     int out_batch_order_enabled = 0;  // SNCH_OPT_OUTPUT_SCATTER
     const float4 *wide4 = nullptr, *wide8 = nullptr;        // wide records
