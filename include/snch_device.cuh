@@ -205,7 +205,7 @@ __device__ __forceinline__ inner load_inner(const snch_traversal_view &t, uint32
 }
 __device__ __forceinline__ void load_cones(const snch_traversal_view &t, uint32_t node, cone &l, cone &r)
 {
-    const float4 *q = static_cast<const float4 *>(t.inner_cones) + 4 * (size_t)node;
+    const float4 *q = static_cast<const float4 *>(t.inner_cones) + 3 * (size_t)node;
     const float4 a = __ldg(q), b = __ldg(q + 1), c = __ldg(q + 2);
     l.axis = mk(a.x, a.y, a.z);
     l.half_angle = a.w;

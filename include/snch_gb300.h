@@ -109,8 +109,7 @@ int snch_get_bvh_view(snch_scene_t scene, snch_bvh_view *out_view);
  *                     (bits L, bits R, bits Linfo, bits Rinfo); children are
  *                     node ids (internal < N-1 <= leaf N-1+j for sorted leaf j);
  *                     a leaf child's info = depth-first rank | owned edges << 30
- *   inner_cones[N-1], 64 B: (L.axis, L.half) (L.radius, R.axis) (R.half, R.radius, Lc.xy)
- *                     (Lc.z, Rc.xyz); Lc / Rc = the child boxes' centroids, (upper + lower) * 0.5
+ *   inner_cones[N-1], 48 B: (L.axis, L.half) (L.radius, R.axis) (R.half, R.radius, 0, 0)
  *   leaves[N], 48 B:  (a.xyz, bits original index) (b.xyz, bits owned edges) (c.xyz, bits rank)
  *   edges[3N], 64 B:  owned silhouette edge k of sorted leaf j at 3j+k:
  *                     (p0.xyz, bits face flags) (p1.xyz, bits edge id) (n0.xyz, 0) (n1.xyz, 0)

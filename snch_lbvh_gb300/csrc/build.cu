@@ -615,7 +615,7 @@ __global__ void __launch_bounds__(128) refit_kernel(BuildArgs a)
         a.aabbs[p] = m;
         a.cones[p] = cone_merge(lc, rc, centroid(lb), centroid(rb), centroid(m));
         a.inner[p] = pack_inner(lb, rb, L, R);
-        a.inner_cones[p] = pack_cones(lc, rc, lb, rb);
+        a.inner_cones[p] = pack_cones(lc, rc);
         cur = p;
     }
 }

@@ -67,15 +67,11 @@ struct alignas(64) InnerRec
     float4 a, b, c, d;
 };
 constexpr uint32_t kLeafRankMask = (1u << 30) - 1u;
-// Child cones of an internal node (silhouette traversal) and the centroids of the
-// child boxes the cone test measures from, 64 B (one line):
-//   a = (L.axis.xyz, L.half)  b = (L.radius, R.axis.xyz)
-//   c = (R.half, R.radius, Lc.x, Lc.y)  d = (Lc.z, Rc.xyz)
-// The centroids are computed by centroid() when the record is packed, so they are
-// the values a search would compute from the boxes.
-struct alignas(64) InnerConeRec
+// Child cones of an internal node (silhouette traversal), 48 B:
+//   a = (L.axis.xyz, L.half)  b = (L.radius, R.axis.xyz)  c = (R.half, R.radius, 0, 0)
+struct alignas(16) InnerConeRec
 {
-    float4 a, b, c, d;
+    float4 a, b, c;
 };
 // Leaf triangle in sorted order, vertices gathered: 48 B
 //   v0 = (pa.xyz, bits original index)  v1 = (pb.xyz, bits owned-edge count)  v2 = (pc.xyz, 0)
@@ -355,30 +351,13 @@ SNCH_DEV void unpack_cones(const InnerConeRec &r, Cone &l, Cone &rc)
     rc.half_angle = r.c.x;
     rc.radius = r.c.y;
 }
-SNCH_DEV void unpack_centroids(const InnerConeRec &r, f3 &lc, f3 &rc)
+SNCH_DEV InnerConeRec pack_cones(const Cone &l, const Cone &r)
 {
-    lc = mk(r.c.z, r.c.w, r.d.x);
-    rc = mk(r.d.y, r.d.z, r.d.w);
-}
-SNCH_DEV InnerConeRec pack_cones(const Cone &l, const Cone &r, const Box &lb, const Box &rb)
-{
-    const f3 lc = centroid(lb), rc = centroid(rb);
     InnerConeRec o;
     o.a = make_float4(l.axis.x, l.axis.y, l.axis.z, l.half_angle);
     o.b = make_float4(l.radius, r.axis.x, r.axis.y, r.axis.z);
-    o.c = make_float4(r.half_angle, r.radius, lc.x, lc.y);
-    o.d = make_float4(lc.z, rc.x, rc.y, rc.z);
+    o.c = make_float4(r.half_angle, r.radius, 0.0f, 0.0f);
     return o;
-}
-SNCH_DEV InnerConeRec load_cones(const InnerConeRec *p)
-{
-    const float4 *q = reinterpret_cast<const float4 *>(p);
-    InnerConeRec r;
-    r.a = __ldg(q);
-    r.b = __ldg(q + 1);
-    r.c = __ldg(q + 2);
-    r.d = __ldg(q + 3);
-    return r;
 }
 SNCH_DEV void load_leaf(const LeafRec *p, f3 &pa, f3 &pb, f3 &pc, uint32_t &orig, uint32_t &n_owned)
 {

@@ -210,11 +210,12 @@ SNCH_DEV float project_to_plane(f3 n, f3 e)
 }
 SNCH_DEV bool inrange(float v, float lo, float hi) { return v >= lo && v <= hi; }
 
-// overlap(cone<float,3>, ...) cone.cuh:168-212; c = centroid(b)
-SNCH_DEV bool cone_overlap(const Cone &bc, f3 c, f3 o, const Box &b, float dist_to_box)
+// overlap(cone<float,3>, ...) cone.cuh:168-212
+SNCH_DEV bool cone_overlap(const Cone &bc, f3 o, const Box &b, float dist_to_box)
 {
     if (bc.half_angle >= kPi2 || dist_to_box < kEps)
         return true;
+    const f3 c = centroid(b);
     f3 v = mk(c.x - o.x, c.y - o.y, c.z - o.z);
     const float l = len3(v);
     v.x /= l;
@@ -278,11 +279,12 @@ SNCH_DEV float acos_as(float x)  // 0 <= x <= 1
     return sqrt_approx(1.0f - x) * __fmaf_rn(x, __fmaf_rn(x, __fmaf_rn(x, a3, a2), a1), a0);
 }
 
-// 1: overlap, 0: no overlap, -1: undecided (take cone_overlap); c = centroid(b)
-SNCH_DEV int cone_overlap_fast(const Cone &bc, f3 c, f3 o, float dist_to_box)
+// 1: overlap, 0: no overlap, -1: undecided (take cone_overlap)
+SNCH_DEV int cone_overlap_fast(const Cone &bc, f3 o, const Box &b, float dist_to_box)
 {
     if (bc.half_angle >= kPi2 || dist_to_box < kEps)
         return 1;  // the same first test as cone_overlap
+    const f3 c = centroid(b);
     const f3 v = mk(c.x - o.x, c.y - o.y, c.z - o.z);
     // approximate l: the asin branch below is taken only when radius / l <= kIllCond,
     // i.e. l exceeds the radius by 0.1 %, so the exact l > radius holds there too
@@ -309,15 +311,10 @@ SNCH_DEV int cone_overlap_fast(const Cone &bc, f3 c, f3 o, float dist_to_box)
     return -1;
 }
 
-// c = centroid(b): precomputed in InnerConeRec for the binary searches
-SNCH_DEV bool cone_test(const Cone &bc, f3 c, f3 o, const Box &b, float dist_to_box)
-{
-    const int f = cone_overlap_fast(bc, c, o, dist_to_box);
-    return f >= 0 ? f == 1 : cone_overlap(bc, c, o, b, dist_to_box);
-}
 SNCH_DEV bool cone_test(const Cone &bc, f3 o, const Box &b, float dist_to_box)
 {
-    return cone_test(bc, centroid(b), o, b, dist_to_box);
+    const int f = cone_overlap_fast(bc, o, b, dist_to_box);
+    return f >= 0 ? f == 1 : cone_overlap(bc, o, b, dist_to_box);
 }
 
 // Self-check: counts where the fast form decides and agrees / disagrees with
@@ -377,8 +374,8 @@ __global__ void cone_filter_check_kernel(int64_t n, uint64_t seed, unsigned long
                           cosf(theta) * k.axis.z + sinf(theta) * pp.z);
         const f3 o = mk(c.x - l * dir.x, c.y - l * dir.y, c.z - l * dir.z);
         const float md = mindist(b, o);
-        const int f = cone_overlap_fast(k, centroid(b), o, md);
-        const int slot = f < 0 ? 2 : ((f == 1) == cone_overlap(k, centroid(b), o, b, md) ? 0 : 1);
+        const int f = cone_overlap_fast(k, o, b, md);
+        const int slot = f < 0 ? 2 : ((f == 1) == cone_overlap(k, o, b, md) ? 0 : 1);
         atomicAdd(&s_c[slot], 1ull);
     }
     __syncthreads();
@@ -517,14 +514,16 @@ __global__ void __launch_bounds__(128) silhouette_kernel(TreeView t, const float
             Box lb, rb;
             uint32_t L, R;
             unpack_inner(load_inner(t.inner + node), lb, rb, L, R);
-            const InnerConeRec icr = load_cones(t.inner_cones + node);
+            const float4 *cr = reinterpret_cast<const float4 *>(t.inner_cones + node);
+            InnerConeRec icr;
+            icr.a = __ldg(cr);
+            icr.b = __ldg(cr + 1);
+            icr.c = __ldg(cr + 2);
             Cone lc, rc;
             unpack_cones(icr, lc, rc);
-            f3 lcen, rcen;
-            unpack_centroids(icr, lcen, rcen);
             const float Lmd = mindist(lb, p), Rmd = mindist(rb, p);
-            const bool hitL = lc.half_angle >= 0.0f && cone_overlap(lc, lcen, p, lb, Lmd);
-            const bool hitR = rc.half_angle >= 0.0f && cone_overlap(rc, rcen, p, rb, Rmd);
+            const bool hitL = lc.half_angle >= 0.0f && cone_overlap(lc, p, lb, Lmd);
+            const bool hitR = rc.half_angle >= 0.0f && cone_overlap(rc, p, rb, Rmd);
             if (hitL)
             {
                 if (L >= ni)
@@ -883,15 +882,17 @@ __global__ void __launch_bounds__(kBlock, 1152 / kBlock) silhouette_fast_kernel(
             const InnerRec rec = load_inner(t.inner + node);
             unpack_inner(rec, lb, rb, L, R);
             unpack_leaf_info(rec, Linfo, Rinfo);
-            const InnerConeRec icr = load_cones(t.inner_cones + node);
+            const float4 *cr = reinterpret_cast<const float4 *>(t.inner_cones + node);
+            InnerConeRec icr;
+            icr.a = __ldg(cr);
+            icr.b = __ldg(cr + 1);
+            icr.c = __ldg(cr + 2);
             Cone lc, rc;
             unpack_cones(icr, lc, rc);
-            f3 lcen, rcen;
-            unpack_centroids(icr, lcen, rcen);
             const float Lmd = mindist(lb, p), Rmd = mindist(rb, p);
             const float b2 = best * best;
-            const bool hitL = Lmd <= b2 && lc.half_angle >= 0.0f && cone_test(lc, lcen, p, lb, Lmd);
-            const bool hitR = Rmd <= b2 && rc.half_angle >= 0.0f && cone_test(rc, rcen, p, rb, Rmd);
+            const bool hitL = Lmd <= b2 && lc.half_angle >= 0.0f && cone_test(lc, p, lb, Lmd);
+            const bool hitR = Rmd <= b2 && rc.half_angle >= 0.0f && cone_test(rc, p, rb, Rmd);
             if (kStats)
                 ++n_int;
             if (kPrefetchChildren)
@@ -1745,16 +1746,23 @@ SNCH_DEV void silhouette_packet_chunk(const TreeView &t, const float *__restrict
             {
                 if (kStats)
                     ++n_int;
-                const InnerConeRec icr = in_top ? s_topc[slot] : load_cones(t.inner_cones + node);
+                InnerConeRec icr;
+                if (in_top)
+                    icr = s_topc[slot];
+                else
+                {
+                    const float4 *cr = reinterpret_cast<const float4 *>(t.inner_cones + node);
+                    icr.a = __ldg(cr);
+                    icr.b = __ldg(cr + 1);
+                    icr.c = __ldg(cr + 2);
+                }
                 Cone lc, rc;
                 unpack_cones(icr, lc, rc);
-                f3 lcen, rcen;
-                unpack_centroids(icr, lcen, rcen);
                 Lmd = mindist(lb, p);
                 Rmd = mindist(rb, p);
                 const float b2 = best * best;
-                hitL = Lmd <= b2 && lc.half_angle >= 0.0f && cone_test(lc, lcen, p, lb, Lmd);
-                hitR = Rmd <= b2 && rc.half_angle >= 0.0f && cone_test(rc, rcen, p, rb, Rmd);
+                hitL = Lmd <= b2 && lc.half_angle >= 0.0f && cone_test(lc, p, lb, Lmd);
+                hitR = Rmd <= b2 && rc.half_angle >= 0.0f && cone_test(rc, p, rb, Rmd);
                 if (hitL && L >= ni)
                 {
                     leaf_silhouette_info(t, L - ni, Linfo, p, flip, best, best_key, best_edge, n_edge);
@@ -2029,16 +2037,18 @@ __global__ void __launch_bounds__(128) silhouette_persistent_kernel(TreeView t, 
                     Box lb, rb;
                     uint32_t L, R;
                     unpack_inner(load_inner(t.inner + node), lb, rb, L, R);
-                    const InnerConeRec icr = load_cones(t.inner_cones + node);
+                    const float4 *cr = reinterpret_cast<const float4 *>(t.inner_cones + node);
+                    InnerConeRec icr;
+                    icr.a = __ldg(cr);
+                    icr.b = __ldg(cr + 1);
+                    icr.c = __ldg(cr + 2);
                     Cone lc, rc;
                     unpack_cones(icr, lc, rc);
-                    f3 lcen, rcen;
-                    unpack_centroids(icr, lcen, rcen);
                     const f3 p = s.p;
                     const float Lmd = mindist(lb, p), Rmd = mindist(rb, p);
                     const float b2 = s.best * s.best;
-                    const bool hitL = Lmd <= b2 && lc.half_angle >= 0.0f && cone_test(lc, lcen, p, lb, Lmd);
-                    const bool hitR = Rmd <= b2 && rc.half_angle >= 0.0f && cone_test(rc, rcen, p, rb, Rmd);
+                    const bool hitL = Lmd <= b2 && lc.half_angle >= 0.0f && cone_test(lc, p, lb, Lmd);
+                    const bool hitR = Rmd <= b2 && rc.half_angle >= 0.0f && cone_test(rc, p, rb, Rmd);
                     if (hitL && L >= ni)
                         leaf_silhouette_fast(t, L - ni, p, s.flip, s.best, s.best_key, s.best_edge, dummy);
                     if (hitR && R >= ni)
