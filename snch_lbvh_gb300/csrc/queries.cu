@@ -1425,60 +1425,6 @@ __global__ void __launch_bounds__(128, SNCH_WIDE_MIN_BLOCKS)
 
 constexpr int kPacketWarps = 4;  // 128-thread blocks
 
-// ---- paired float arithmetic (f32x2)
-// sm_100-family instructions that apply one IEEE round-to-nearest add, sub or
-// mul to two floats at once, in one issue slot: a packet step puts its node's
-// two children through the same operations, each element rounded exactly as
-// the scalar operation rounds it.
-#ifndef SNCH_PAIRED_F32X2
-#define SNCH_PAIRED_F32X2 1
-#endif
-constexpr bool kPairedF32x2 = SNCH_PAIRED_F32X2 != 0;
-typedef unsigned long long f2x;
-SNCH_DEV f2x f2_pack(float a, float b)
-{
-    f2x r;
-    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
-    return r;
-}
-SNCH_DEV void f2_unpack(f2x v, float &a, float &b) { asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v)); }
-SNCH_DEV f2x f2_add(f2x a, f2x b)
-{
-    f2x r;
-    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
-SNCH_DEV f2x f2_sub(f2x a, f2x b)
-{
-    f2x r;
-    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
-SNCH_DEV f2x f2_mul(f2x a, f2x b)
-{
-    f2x r;
-    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
-// mindist (aabb.cuh mindist, squared) of the two children at once: the
-// clamps per element, then (dx dx + dy dy) + dz dz in pairs (nearest packets:
-// 11.67 against 12.01 ms per 16M queries of the 2M-triangle scene)
-SNCH_DEV void mindist2(const Box &a, const Box &b, f3 p, float &ma, float &mb)
-{
-    if (!kPairedF32x2)
-    {
-        ma = mindist(a, p);
-        mb = mindist(b, p);
-        return;
-    }
-    const f2x dx = f2_sub(f2_pack(fminf(a.upper.x, fmaxf(a.lower.x, p.x)), fminf(b.upper.x, fmaxf(b.lower.x, p.x))),
-                          f2_pack(p.x, p.x));
-    const f2x dy = f2_sub(f2_pack(fminf(a.upper.y, fmaxf(a.lower.y, p.y)), fminf(b.upper.y, fmaxf(b.lower.y, p.y))),
-                          f2_pack(p.y, p.y));
-    const f2x dz = f2_sub(f2_pack(fminf(a.upper.z, fmaxf(a.lower.z, p.z)), fminf(b.upper.z, fmaxf(b.lower.z, p.z))),
-                          f2_pack(p.z, p.z));
-    f2_unpack(f2_add(f2_add(f2_mul(dx, dx), f2_mul(dy, dy)), f2_mul(dz, dz)), ma, mb);
-}
 
 // per-lane start of a packet: lanes of a batched query set may search
 // different meshes; the warp runs one packet per distinct root
@@ -1563,7 +1509,8 @@ SNCH_DEV void nearest_packet_chunk(const TreeView &t, const float *__restrict__ 
             {
                 if (kStats)
                     ++n_int;
-                mindist2(lb, rb, p, Lmd, Rmd);
+                Lmd = mindist(lb, p);
+                Rmd = mindist(rb, p);
                 aL = aR = true;  // no minmaxdist sibling test: as nearest_fast_kernel
                 // two branches: one loop over both leaves (as the silhouette packets
                 // run them) measured 12 % slower here (16M queries, 13.43 vs 12.02 ms)
@@ -1834,8 +1781,6 @@ SNCH_DEV void silhouette_packet_chunk(const TreeView &t, const float *__restrict
                 }
                 Cone lc, rc;
                 unpack_cones(icr, lc, rc);
-                // scalar: the paired form measured 1.2 % slower here (35.97 vs 35.55 ms
-                // per 16M queries; it costs this kernel registers it spills)
                 Lmd = mindist(lb, p);
                 Rmd = mindist(rb, p);
                 const float b2 = best * best;
