@@ -47,6 +47,7 @@ typedef enum
 #define SNCH_DEVICE_HASH_FULL 4u        /* the edge hash table overflowed (results invalid)    */
 #define SNCH_DEVICE_TREE_DEPTH 16u      /* a wide-record pass met a tree deeper than its bound  */
 #define SNCH_DEVICE_COPY_TIMEOUT 32u    /* a bulk copy into shared memory did not complete in time */
+#define SNCH_DEVICE_WORK_TIMEOUT 64u    /* a persistent search stopped taking work (results invalid) */
 
 /* Reference-layout records, byte-compatible with the reference's device view
  * (bvh.cuh:27-33 node, aabb.cuh:12-16 aabb<float,3>, cone.cuh:11-16 cone<float,3>,

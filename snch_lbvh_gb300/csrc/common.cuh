@@ -30,6 +30,7 @@ enum : uint32_t
     kStatusRefitTimeout = 8u,      // reserved
     kStatusTreeDepth = 16u,        // a wide-record pass met a tree deeper than its bound
     kStatusCopyTimeout = 32u,      // a bulk copy into shared memory did not complete in time
+    kStatusWorkTimeout = 64u,      // a persistent search stopped taking work (results incomplete)
 };
 
 struct f3
