@@ -259,9 +259,11 @@ int snch_set_traversal(snch_scene_t scene, int mode);
 #define SNCH_OPT_PACKET_SILHOUETTE 14
 /*   SNCH_OPT_PACKET_PERSISTENT_MIN  smallest warp-packet batch (nearest and silhouette)
  *                             that runs persistent: each warp takes the next 32 queries
- *                             of the batch from a counter when its packet ends (same
- *                             packets, same answers). Default 2^23 (measured faster from
- *                             there, 6 % slower on 1M-query batches); >= 1. */
+ *                             of the batch when its packet ends, from a pool per SM
+ *                             refilled with 32 consecutive packets at a time (same
+ *                             packets, same answers); ray batches this large run the same
+ *                             way, 32 rays (one per lane) per take. Default 2^23 (measured
+ *                             faster from there, 6 % slower on 1M-query batches); >= 1. */
 #define SNCH_OPT_PACKET_PERSISTENT_MIN 19
 /*   SNCH_OPT_OUTPUT_SCATTER   1: the results of a Morton-ordered, unseeded batch are
  *                             written in batch order to a temporary and then moved to

@@ -2390,15 +2390,19 @@ SNCH_DEV bool ray_triangle(f3 o, f3 dir, f3 v0, f3 v1, f3 v2, float &t, float &u
 #ifndef SNCH_RAY_MIN_BLOCKS
 #define SNCH_RAY_MIN_BLOCKS 0
 #endif
-template <bool kStats, bool kAny = false>
-__global__ void __launch_bounds__(128, SNCH_RAY_MIN_BLOCKS) ray_kernel(TreeView t, const float *__restrict__ origins,
-                                                  const float *__restrict__ dirs, const float *__restrict__ tmaxs,
-                                                  int64_t n, uint8_t *__restrict__ out_hit, float *__restrict__ out_t,
-                                                  float *__restrict__ out_uv, uint32_t *__restrict__ out_idx,
-                                                  uint32_t *__restrict__ stats)
+// ray batches of at least SNCH_OPT_PACKET_PERSISTENT_MIN rays use ray_pool_kernel
+#ifndef SNCH_RAY_POOLS
+#define SNCH_RAY_POOLS 1
+#endif
+constexpr bool kRayPools = SNCH_RAY_POOLS != 0;
+// one ray of the batch (batch position qi)
+template <bool kStats, bool kAny>
+SNCH_DEV void ray_query(const TreeView &t, const float *__restrict__ origins, const float *__restrict__ dirs,
+                        const float *__restrict__ tmaxs, int64_t n, uint8_t *__restrict__ out_hit,
+                        float *__restrict__ out_t, float *__restrict__ out_uv, uint32_t *__restrict__ out_idx,
+                        uint32_t *__restrict__ stats, int64_t qi)
 {
     uint32_t n_int = 0, n_leaf = 0;
-    const int64_t qi = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (qi >= query_count(t, n))
         return;
     const int64_t q = query_index(t, qi);
@@ -2506,6 +2510,55 @@ __global__ void __launch_bounds__(128, SNCH_RAY_MIN_BLOCKS) ray_kernel(TreeView 
         stats[3 * q] = n_int;
         stats[3 * q + 1] = n_leaf;
         stats[3 * q + 2] = 0;
+    }
+}
+template <bool kStats, bool kAny = false>
+__global__ void __launch_bounds__(128, SNCH_RAY_MIN_BLOCKS) ray_kernel(TreeView t, const float *__restrict__ origins,
+                                                  const float *__restrict__ dirs, const float *__restrict__ tmaxs,
+                                                  int64_t n, uint8_t *__restrict__ out_hit, float *__restrict__ out_t,
+                                                  float *__restrict__ out_uv, uint32_t *__restrict__ out_idx,
+                                                  uint32_t *__restrict__ stats)
+{
+    ray_query<kStats, kAny>(t, origins, dirs, tmaxs, n, out_hit, out_t, out_uv, out_idx, stats,
+                            blockIdx.x * (int64_t)blockDim.x + threadIdx.x);
+}
+// The same rays, one per thread, handed out 32 at a time through the per-SM
+// pools of the packet searches (take_packet): a warp takes the next 32 rays of
+// its SM's chunk when its last ray ends, so the warps of an SM trace rays from
+// neighbouring origins (the batch is Morton-ordered by origin) and share the
+// tree records in its L1, and no warp waits for the slowest ray of its block.
+template <bool kAny>
+__global__ void __launch_bounds__(128, SNCH_RAY_MIN_BLOCKS)
+    ray_pool_kernel(TreeView t, const float *__restrict__ origins, const float *__restrict__ dirs,
+                    const float *__restrict__ tmaxs, int64_t n, uint8_t *__restrict__ out_hit,
+                    float *__restrict__ out_t, float *__restrict__ out_uv, uint32_t *__restrict__ out_idx,
+                    unsigned long long *work)
+{
+    const int lane = threadIdx.x & 31;
+    const unsigned long long total = (unsigned long long)query_count(t, n), packets = (total + 31ull) / 32ull;
+    uint32_t empty_takes = 0;
+    for (;;)
+    {
+        unsigned long long packet = 0;
+        if (lane == 0)
+            packet = take_packet(work, packets);
+        packet = __shfl_sync(0xffffffffu, packet, 0);
+        if (packet == ~0ull)
+            break;
+        if (packet >= packets)
+        {
+            if (++empty_takes > kPoolSpins)  // cannot happen: see take_packet
+            {
+                if (lane == 0)
+                    atomicOr(t.status, kStatusWorkTimeout);
+                break;
+            }
+            continue;
+        }
+        empty_takes = 0;
+        ray_query<false, kAny>(t, origins, dirs, tmaxs, n, out_hit, out_t, out_uv, out_idx, nullptr,
+                               (int64_t)(packet * 32ull) + lane);
+        __syncwarp();
     }
 }
 
@@ -3418,6 +3471,8 @@ cudaError_t launch_ray(const TreeView &t0, const float *o, const float *d, const
             t.order, n, tmp.at<uint8_t>(0), tmp.at<float>(a_t), tmp.at<float2>(a_uv), tmp.at<uint32_t>(a_idx),
             hit_out, t_out, uv_out, idx_out, (reinterpret_cast<uintptr_t>(uv_out) & 7) == 0);
     }
+    else if (kRayPools && n >= t.packet_persistent_min)
+        return launch_persistent(ray_pool_kernel<false>, n, st, t, o, d, tmax, n, hit_out, t_out, uv_out, idx_out);
     else
         ray_kernel<false><<<grid_for(n, 128), 128, 0, st>>>(t, o, d, tmax, n, hit_out, t_out, uv_out, idx_out,
                                                             nullptr);
@@ -3431,6 +3486,9 @@ cudaError_t launch_ray_test(const TreeView &t, const float *o, const float *d, c
         return cudaSuccess;
     if (t.persistent & 4)
         return launch_persistent(ray_persistent_kernel<true>, n, st, t, o, d, tmax, n, hit, (float *)nullptr,
+                                 (float *)nullptr, (uint32_t *)nullptr);
+    if (kRayPools && n >= t.packet_persistent_min)
+        return launch_persistent(ray_pool_kernel<true>, n, st, t, o, d, tmax, n, hit, (float *)nullptr,
                                  (float *)nullptr, (uint32_t *)nullptr);
     ray_kernel<false, true><<<grid_for(n, 128), 128, 0, st>>>(t, o, d, tmax, n, hit, nullptr, nullptr, nullptr,
                                                                nullptr);

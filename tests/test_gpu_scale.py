@@ -308,3 +308,29 @@ def test_order_bits_same_answers(big, bits):
     check_tri_ids(b[0], a[0], a[1], q["near_pts"], sc.verts, sc.faces)
     check_edge_ids(b[3], a[3], a[2], q["sil_pts"], sc.verts, s.export_topology()[2])
     assert s.device_status() == 0
+
+
+def test_ray_pools_equal_grid_launch(big):
+    """Ray batches of at least SNCH_OPT_PACKET_PERSISTENT_MIN rays run as warps
+    that take 32 rays at a time from per-SM pools (ray_pool_kernel): the same
+    per-ray traversal as the one-thread-per-ray grid launch, so hit flags, t, uv,
+    triangle indices and occlusion flags are identical (2M rays, 2M-triangle
+    scene, ordered and unordered batches)."""
+    import snch_lbvh_gb300 as snch
+    from snch_lbvh_gb300 import meshes
+    sc, s, _ = big
+    q = meshes.wost_queries(1, 1, 2_000_003, 1, seed=73)
+    args = (q["ray_o"], q["ray_d"], q["ray_tmax"])
+    try:
+        for ordered in (1, 0):
+            s.set_option(snch.OPT_QUERY_ORDER, ordered)
+            s.set_option(snch.OPT_PACKET_PERSISTENT_MIN, 1 << 40)  # grid launch
+            grid = [x.cpu().numpy() for x in s.query_ray(*args)] + [s.query_ray_test(*args).cpu().numpy()]
+            s.set_option(snch.OPT_PACKET_PERSISTENT_MIN, 1)  # pools at any size
+            pool = [x.cpu().numpy() for x in s.query_ray(*args)] + [s.query_ray_test(*args).cpu().numpy()]
+            for name, x, y in zip(("hit", "t", "uv", "triangle", "occluded"), grid, pool):
+                np.testing.assert_array_equal(x.view(np.uint8), y.view(np.uint8), err_msg=name)
+    finally:
+        s.set_option(snch.OPT_QUERY_ORDER, 1)
+        s.set_option(snch.OPT_PACKET_PERSISTENT_MIN, 1 << 23)
+    assert s.device_status() == 0
