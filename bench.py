@@ -992,7 +992,7 @@ def run_ours(args):
         link = {"h2d_gbs": src.numel() * 4 / (e0.elapsed_time(e1) / 1e3) / 1e9,
                 "d2h_gbs": src.numel() * 4 / (e1.elapsed_time(e2) / 1e3) / 1e9}
         del probe
-        e2e_steps = max(1, min(args.steps, 3))
+        e2e_steps = max(1, min(args.steps, 5))
         e2e_step()
         barrier()
         t0 = time.perf_counter()
