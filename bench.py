@@ -43,9 +43,9 @@ METRIC = ("queries/sec (walk-on-stars query set: nearest, silhouette, ray, spher
 FULL = {"near": 16_000_000, "sil": 16_000_000, "ray": 16_000_000, "smp": 4_000_000}
 # kernels the default configuration runs for each query type (Morton-ordered
 # 16M-query batches, 8 queries per triangle: nearest and silhouette batches
-# run as persistent warp packets)
+# run as persistent warp packets, rays as warps taking 32 rays at a time)
 KERNEL_OF = {"near": "nearest_packet_persistent_kernel", "sil": "silhouette_packet_persistent_kernel",
-             "ray": "ray_kernel", "smp": "sample_kernel"}
+             "ray": "ray_pool_kernel", "smp": "sample_kernel"}
 # algorithmic bytes per query, reference record sizes: input + output + per
 # expanded internal node (2 child boxes + 2 child refs [+ 2 cones]) + per leaf
 # (vertex ids + vertices [silhouette: owned-edge ids]) + per silhouette edge
