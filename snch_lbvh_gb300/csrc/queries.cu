@@ -1728,11 +1728,12 @@ inline size_t top_smem_bytes(uint32_t slots, bool cones)
 // batch from a batch-wide counter when its packet is done, so no warp slot
 // waits for the slowest packet of its block. kTop: the top tree levels are read
 // from a shared-memory copy (dynamic shared memory, top_smem_bytes).
-// blocks per SM the persistent nearest packet kernel is compiled for (9: 56
-// registers; measured on 16M-query batches of the 2M-triangle scene: 12.10 ms,
-// against 12.40 ms at 10 blocks / 48 registers, where its loop state spills)
+// blocks per SM the persistent nearest packet kernel is compiled for (8: 64
+// registers; measured on 16M-query batches of the 2M-triangle scene with the
+// per-SM packet pools: 11.05 ms, against 11.27 at 9 blocks / 56 registers and
+// 11.82 at 10 blocks / 48 registers, where its loop state spills)
 #ifndef SNCH_NEAR_PACKET_MIN_BLOCKS
-#define SNCH_NEAR_PACKET_MIN_BLOCKS 9
+#define SNCH_NEAR_PACKET_MIN_BLOCKS 8
 #endif
 template <bool kTop>
 __global__ void __launch_bounds__(128, SNCH_NEAR_PACKET_MIN_BLOCKS)
