@@ -1444,7 +1444,10 @@ constexpr int kPacketWarps = 4;  // 128-thread blocks
 #endif
 constexpr bool kPacketPools = SNCH_PACKET_POOLS != 0;  // 0: every packet straight from the counter
 constexpr uint32_t kPoolSlots = 1024;                  // pools (SM id modulo kPoolSlots)
-constexpr uint64_t kPoolChunk = 32;
+#ifndef SNCH_POOL_CHUNK
+#define SNCH_POOL_CHUNK 32
+#endif
+constexpr uint64_t kPoolChunk = SNCH_POOL_CHUNK;  // packets per refill
 constexpr unsigned long long kPoolDone = (1ull << 40) - 1ull;
 constexpr uint32_t kPoolSpins = 1u << 16;
 // work[0]: the batch-wide packet counter, work[1 + s]: pool s (zeroed before
@@ -1728,12 +1731,12 @@ inline size_t top_smem_bytes(uint32_t slots, bool cones)
 // batch from a batch-wide counter when its packet is done, so no warp slot
 // waits for the slowest packet of its block. kTop: the top tree levels are read
 // from a shared-memory copy (dynamic shared memory, top_smem_bytes).
-// blocks per SM the persistent nearest packet kernel is compiled for (8: 64
+// blocks per SM the persistent nearest packet kernel is compiled for (7: 72
 // registers; measured on 16M-query batches of the 2M-triangle scene with the
-// per-SM packet pools: 11.05 ms, against 11.27 at 9 blocks / 56 registers and
-// 11.82 at 10 blocks / 48 registers, where its loop state spills)
+// per-SM packet pools: 10.83 ms, against 11.05 at 8 blocks / 64 registers,
+// 11.27 at 9 / 56 and 11.82 at 10 / 48, where its loop state spills)
 #ifndef SNCH_NEAR_PACKET_MIN_BLOCKS
-#define SNCH_NEAR_PACKET_MIN_BLOCKS 8
+#define SNCH_NEAR_PACKET_MIN_BLOCKS 7
 #endif
 template <bool kTop>
 __global__ void __launch_bounds__(128, SNCH_NEAR_PACKET_MIN_BLOCKS)
