@@ -204,9 +204,10 @@ int snch_set_traversal(snch_scene_t scene, int mode);
  *                             when its own is done; 0 (default): one thread per query.
  *                             Same results; on the 2M-triangle scene with Morton-ordered
  *                             batches the refilled lanes lose their warp's coherence and
- *                             run slower. (Warp packets of batches of 2^23 queries or
- *                             more always run persistent: a warp takes the next 32
- *                             queries when its packet is done.)
+ *                             run slower. (Warp packets of batches of at least
+ *                             SNCH_OPT_PACKET_PERSISTENT_MIN queries always run
+ *                             persistent: a warp takes the next 32 queries when its
+ *                             packet is done.)
  *   SNCH_OPT_PERSISTENT_NEAREST / _SILHOUETTE  the same for one query type. */
 #define SNCH_OPT_PERSISTENT 4
 #define SNCH_OPT_PERSISTENT_NEAREST 16
@@ -261,9 +262,10 @@ int snch_set_traversal(snch_scene_t scene, int mode);
  *                             that runs persistent: each warp takes the next 32 queries
  *                             of the batch when its packet ends, from a pool per SM
  *                             refilled with 32 consecutive packets at a time (same
- *                             packets, same answers); ray batches this large run the same
- *                             way, 32 rays (one per lane) per take. Default 2^23 (measured
- *                             faster from there, 6 % slower on 1M-query batches); >= 1. */
+ *                             packets, same answers); ray batches of at least 4 times
+ *                             this run the same way, 32 rays (one per lane) per take.
+ *                             Default 2^19 (measured: silhouette packets faster from
+ *                             524,288 queries, rays from about 2M); >= 1. */
 #define SNCH_OPT_PACKET_PERSISTENT_MIN 19
 /*   SNCH_OPT_OUTPUT_SCATTER   1: the results of a Morton-ordered, unseeded batch are
  *                             written in batch order to a temporary and then moved to

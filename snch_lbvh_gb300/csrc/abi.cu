@@ -115,7 +115,7 @@ struct snch_scene_s
     int width_near = 2, width_sil = 2;
     int block_near = 128, block_sil = 128;  // threads per block of the binary searches
     int packet_near = 2, packet_sil = 2;    // warp packets: 0 never, 1 always, 2 Morton-ordered batches
-    int64_t packet_persistent_min = int64_t(1) << 23;  // packet batches this large run persistent
+    int64_t packet_persistent_min = int64_t(1) << 19;  // packet batches this large run persistent (rays: 4x)
     int output_scatter = 0;  // ordered batches: results in batch order, then one scatter pass (measured slower)
     int ray_order = 0;       // ray batches ordered by length bucket, then origin
     int order_bits = 24;     // Morton bits of the query-order key of plain scenes (3 sort passes; faster than 30)

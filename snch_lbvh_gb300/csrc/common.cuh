@@ -153,7 +153,7 @@ struct TreeView
     // warp packets (a warp's 32 queries walk one shared traversal): 0 never,
     // 1 always, 2 when the batch is Morton-ordered (order_coherent)
     int packet_near = 0, packet_sil = 0;
-    int64_t packet_persistent_min = int64_t(1) << 23;  // packet batches this large run persistent
+    int64_t packet_persistent_min = int64_t(1) << 19;  // packet batches this large run persistent (rays: 4x)
     int order_coherent = 0;  // order[] is the batch's Morton order (neighbours share warps)
     // the internal nodes of the top tree levels in heap order (slot 0 the root,
     // the children of slot i at 2i+1 / 2i+2), staged in shared memory by the

@@ -2394,7 +2394,7 @@ SNCH_DEV bool ray_triangle(f3 o, f3 dir, f3 v0, f3 v1, f3 v2, float &t, float &u
 #ifndef SNCH_RAY_MIN_BLOCKS
 #define SNCH_RAY_MIN_BLOCKS 0
 #endif
-// ray batches of at least SNCH_OPT_PACKET_PERSISTENT_MIN rays use ray_pool_kernel
+// ray batches of at least 4 x SNCH_OPT_PACKET_PERSISTENT_MIN rays use ray_pool_kernel
 #ifndef SNCH_RAY_POOLS
 #define SNCH_RAY_POOLS 1
 #endif
@@ -3475,7 +3475,7 @@ cudaError_t launch_ray(const TreeView &t0, const float *o, const float *d, const
             t.order, n, tmp.at<uint8_t>(0), tmp.at<float>(a_t), tmp.at<float2>(a_uv), tmp.at<uint32_t>(a_idx),
             hit_out, t_out, uv_out, idx_out, (reinterpret_cast<uintptr_t>(uv_out) & 7) == 0);
     }
-    else if (kRayPools && n >= t.packet_persistent_min)
+    else if (kRayPools && n / 4 >= t.packet_persistent_min)
         return launch_persistent(ray_pool_kernel<false>, n, st, t, o, d, tmax, n, hit_out, t_out, uv_out, idx_out);
     else
         ray_kernel<false><<<grid_for(n, 128), 128, 0, st>>>(t, o, d, tmax, n, hit_out, t_out, uv_out, idx_out,
@@ -3491,7 +3491,7 @@ cudaError_t launch_ray_test(const TreeView &t, const float *o, const float *d, c
     if (t.persistent & 4)
         return launch_persistent(ray_persistent_kernel<true>, n, st, t, o, d, tmax, n, hit, (float *)nullptr,
                                  (float *)nullptr, (uint32_t *)nullptr);
-    if (kRayPools && n >= t.packet_persistent_min)
+    if (kRayPools && n / 4 >= t.packet_persistent_min)
         return launch_persistent(ray_pool_kernel<true>, n, st, t, o, d, tmax, n, hit, (float *)nullptr,
                                  (float *)nullptr, (uint32_t *)nullptr);
     ray_kernel<false, true><<<grid_for(n, 128), 128, 0, st>>>(t, o, d, tmax, n, hit, nullptr, nullptr, nullptr,

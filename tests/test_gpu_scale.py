@@ -7,6 +7,8 @@ import pytest
 
 from test_gpu_parity import bits, built_scene, check_cones, check_edge_ids, check_silhouette, check_tri_ids
 
+PERSISTENT_MIN_DEFAULT = 1 << 19  # SNCH_OPT_PACKET_PERSISTENT_MIN's default (include/snch_gb300.h)
+
 pytestmark = pytest.mark.gpu
 
 
@@ -169,8 +171,8 @@ def _check_persistent_packets(snch, sc, s, orc, pts, flip, n_oracle):
     grid = _packet_answers(s, pts, flip)
     s.set_option(snch.OPT_PACKET_PERSISTENT_MIN, 1)  # persistent at any size
     pers = _packet_answers(s, pts, flip)
-    s.set_option(snch.OPT_PACKET_PERSISTENT_MIN, 1 << 23)
-    assert s.get_option(snch.OPT_PACKET_PERSISTENT_MIN) == 1 << 23
+    s.set_option(snch.OPT_PACKET_PERSISTENT_MIN, PERSISTENT_MIN_DEFAULT)
+    assert s.get_option(snch.OPT_PACKET_PERSISTENT_MIN) == PERSISTENT_MIN_DEFAULT
     assert s.device_status() == 0
     for name, x, y in zip(("nearest idx", "nearest dist", "silhouette dist", "silhouette edge"), grid, pers):
         np.testing.assert_array_equal(x.view(np.uint32), y.view(np.uint32), err_msg=name)
@@ -200,8 +202,8 @@ def test_persistent_packets_full_scene(big, oracle_mod):
 
 
 def test_persistent_packets_bench_size(big, oracle_mod):
-    """A batch above 2^23 queries (the size from which the persistent packet
-    kernels run by default, as in the 16M-query walk-on-stars step)."""
+    """A batch above 2^23 queries, run with the default settings as the
+    16M-query walk-on-stars step runs (persistent packets from per-SM pools)."""
     import snch_lbvh_gb300 as snch
     from snch_lbvh_gb300 import meshes
     sc, s, orc = big
@@ -253,7 +255,7 @@ def test_top_levels_in_shared_memory_equal(big, levels):
     s.set_option(snch.OPT_TOP_LEVELS, levels)
     b = _packet_answers(s, pts, flip)
     s.set_option(snch.OPT_TOP_LEVELS, 0)
-    s.set_option(snch.OPT_PACKET_PERSISTENT_MIN, 1 << 23)
+    s.set_option(snch.OPT_PACKET_PERSISTENT_MIN, PERSISTENT_MIN_DEFAULT)
     for x, y in zip(a, b):
         np.testing.assert_array_equal(x.view(np.uint32), y.view(np.uint32))
     assert s.device_status() == 0
@@ -332,5 +334,5 @@ def test_ray_pools_equal_grid_launch(big):
                 np.testing.assert_array_equal(x.view(np.uint8), y.view(np.uint8), err_msg=name)
     finally:
         s.set_option(snch.OPT_QUERY_ORDER, 1)
-        s.set_option(snch.OPT_PACKET_PERSISTENT_MIN, 1 << 23)
+        s.set_option(snch.OPT_PACKET_PERSISTENT_MIN, PERSISTENT_MIN_DEFAULT)
     assert s.device_status() == 0
