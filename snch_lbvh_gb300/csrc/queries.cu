@@ -290,6 +290,8 @@ SNCH_DEV int cone_overlap_fast(const Cone &bc, f3 o, const Box &b, float dist_to
 {
     if (bc.half_angle >= kPi2 || dist_to_box < kEps)
         return 1;  // the same first test as cone_overlap
+    // (computing centroid - o as one fused multiply-add per axis, the same value,
+    // measured 2 % slower: 34.44 against 33.70 ms per 16M silhouette queries)
     const f3 c = centroid(b);
     const f3 v = mk(c.x - o.x, c.y - o.y, c.z - o.z);
     // approximate l: the asin branch below is taken only when radius / l <= kIllCond,
