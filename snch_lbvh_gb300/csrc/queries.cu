@@ -2409,6 +2409,8 @@ SNCH_DEV bool ray_triangle(f3 o, f3 dir, f3 v0, f3 v1, f3 v2, float &t, float &u
 #define SNCH_RAY_MIN_BLOCKS 0
 #endif
 // ray batches of at least 4 x SNCH_OPT_PACKET_PERSISTENT_MIN rays use ray_pool_kernel
+// (sphere draws, whose single descent is short, measured 3 % slower that way and
+// keep one thread per draw)
 #ifndef SNCH_RAY_POOLS
 #define SNCH_RAY_POOLS 1
 #endif
