@@ -1745,10 +1745,11 @@ inline size_t top_smem_bytes(uint32_t slots, bool cones)
 // batch from a batch-wide counter when its packet is done, so no warp slot
 // waits for the slowest packet of its block. kTop: the top tree levels are read
 // from a shared-memory copy (dynamic shared memory, top_smem_bytes).
-// blocks per SM the persistent nearest packet kernel is compiled for (7: 72
-// registers; measured on 16M-query batches of the 2M-triangle scene with the
-// per-SM packet pools: 10.83 ms, against 11.05 at 8 blocks / 64 registers,
-// 11.27 at 9 / 56 and 11.82 at 10 / 48, where its loop state spills)
+// blocks per SM the persistent nearest packet kernel is compiled for (at least
+// 7: the compiler then takes 63 registers, so 8 blocks fit; measured on
+// 16M-query batches of the 2M-triangle scene with the per-SM packet pools:
+// 10.83 ms, against 11.05 compiled for 8 blocks (64 registers), 11.27 for 9 /
+// 56 and 11.82 for 10 / 48, where its loop state spills)
 #ifndef SNCH_NEAR_PACKET_MIN_BLOCKS
 #define SNCH_NEAR_PACKET_MIN_BLOCKS 7
 #endif
