@@ -17,6 +17,7 @@ SNCH_OK = 0
 STATUS_NAMES = {0: "SNCH_OK", 1: "SNCH_ERR_INVALID_ARGUMENT", 2: "SNCH_ERR_CUDA", 3: "SNCH_ERR_NOT_BUILT",
                 4: "SNCH_ERR_OUT_OF_MEMORY", 5: "SNCH_ERR_DEVICE_STATUS", 6: "SNCH_ERR_TOO_LARGE"}
 DEVICE_STACK_OVERFLOW, DEVICE_LOOKBACK_TIMEOUT, DEVICE_HASH_FULL = 1, 2, 4
+DEVICE_TREE_DEPTH, DEVICE_COPY_TIMEOUT, DEVICE_WORK_TIMEOUT = 16, 32, 64
 
 
 class SnchError(RuntimeError):

@@ -67,3 +67,18 @@ def test_argument_errors_before_any_cuda_call():
 def test_snch_error_carries_the_message():
     with pytest.raises(_ffi.SnchError, match="scene is NULL"):
         _ffi.check(_ffi.lib().snch_build_bvh(None, None))
+
+
+def test_python_constants_match_the_header():
+    """Every SNCH_OPT_* and SNCH_DEVICE_* value the header defines has the same
+    value under the Python package's name for it (OPT_* in snch_lbvh_gb300,
+    DEVICE_* in its _ffi module)."""
+    import snch_lbvh_gb300 as snch
+    text = open(os.path.join(build.INCLUDE, "snch_gb300.h")).read()
+    opts = dict(re.findall(r"#define SNCH_(OPT_\w+) (\d+)\b", text))
+    devs = dict(re.findall(r"#define SNCH_(DEVICE_\w+) (\d+)u\b", text))
+    assert len(opts) >= 20 and len(devs) >= 6
+    for name, value in opts.items():
+        assert getattr(snch, name) == int(value), name
+    for name, value in devs.items():
+        assert getattr(_ffi, name) == int(value), name
