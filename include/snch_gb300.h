@@ -248,7 +248,7 @@ int snch_set_traversal(snch_scene_t scene, int mode);
  *                             silhouette searches: a warp's 32 queries walk one shared
  *                             traversal, each lane applying its own tests and keeping its
  *                             own answer. 2 (default): for Morton-ordered batches (nearest
- *                             batches also need at least 3 queries per triangle); 1:
+ *                             batches also need at least 1 query per triangle); 1:
  *                             always; 0: never (each lane walks its own). Same distances;
  *                             the silhouette edge id / nearest index equals the per-lane
  *                             one except on an exact distance tie that falls on a

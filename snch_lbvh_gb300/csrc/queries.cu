@@ -3151,12 +3151,13 @@ inline bool packet_ok(const TreeView &t, int packet, int width, const SeedArgs &
     return on && width == 2 && t.near_first && !seed.cap && t.num_tris > 1;
 }
 // Automatic packets for nearest searches need a dense batch: a warp's 32
-// neighbours must share most of their traversal. Measured crossover: about 3
-// queries per triangle (2M-triangle scene: per lane x1.57 faster at 0.26 and
-// x1.09 at 1 query per triangle, packets x1.21 faster at 4; 20,480- and
-// 1,280-triangle spheres: packets faster from 13 queries per triangle up).
-// Silhouette packets won at every measured density (0.26 queries per triangle up).
-constexpr uint64_t kPacketNearestMinQueriesPerTri = 3;
+// neighbours must share most of their traversal. Measured crossover, with the
+// persistent packets drawing from per-SM pools: about 1 query per triangle
+// (2M-triangle scene: per lane x1.56 faster at 0.26 and x1.23 at 0.5 queries per
+// triangle; at 1 / 2 / 3 packets take 2.80 / 4.15 / 5.45 ms against 2.87 / 4.99 /
+// 7.07 per lane; before the pools the crossover was near 3). Silhouette packets
+// won at every measured density (0.26 queries per triangle up).
+constexpr uint64_t kPacketNearestMinQueriesPerTri = 1;
 inline bool packet_dense(const TreeView &t, int packet, int64_t n)
 {
     return packet == 1 || (uint64_t)n >= kPacketNearestMinQueriesPerTri * t.num_tris;
