@@ -860,14 +860,10 @@ SNCH_DEV void leaf_silhouette_info(const TreeView &t, uint32_t pos, uint32_t inf
 }
 
 // The silhouette packets run the leaf work of a node's two children as one loop
-// (the left leaf's edges, then the right leaf's, per lane: the same order as two
-// loops), so a lane with only the right leaf to test runs in the same
-// iterations as a lane with only the left one (16M queries of the 2M-triangle
-// scene: 35.61 against 35.78 ms).
-#ifndef SNCH_MERGED_LEAF_LOOP
-#define SNCH_MERGED_LEAF_LOOP 1
-#endif
-constexpr bool kMergedLeafLoop = SNCH_MERGED_LEAF_LOOP != 0;
+// of edge_candidate calls (the left leaf's edges, then the right leaf's, per
+// lane: the same order as two leaf_silhouette_info calls), so a lane with only
+// the right leaf to test runs in the same iterations as a lane with only the
+// left one (16M queries of the 2M-triangle scene: 35.61 against 35.78 ms).
 
 template <bool kStats, int kBlock = 128>
 __global__ void __launch_bounds__(kBlock, 1152 / kBlock) silhouette_fast_kernel(TreeView t, const float *__restrict__ pts,
@@ -1876,36 +1872,19 @@ SNCH_DEV void silhouette_packet_chunk(const TreeView &t, const float *__restrict
                 const float b2 = best * best;
                 hitL = Lmd <= b2 && lc.half_angle >= 0.0f && cone_test(lc, p, lb, Lmd);
                 hitR = Rmd <= b2 && rc.half_angle >= 0.0f && cone_test(rc, p, rb, Rmd);
-                if (kMergedLeafLoop)
+                // both leaf children's edges in one loop (see edge_candidate)
+                const uint32_t nL = hitL && L >= ni ? Linfo >> 30 : 0u;
+                const uint32_t nR = hitR && R >= ni ? Rinfo >> 30 : 0u;
+                if (kStats)
                 {
-                    const uint32_t nL = hitL && L >= ni ? Linfo >> 30 : 0u;
-                    const uint32_t nR = hitR && R >= ni ? Rinfo >> 30 : 0u;
-                    if (kStats)
-                    {
-                        n_leaf += (hitL && L >= ni ? 1u : 0u) + (hitR && R >= ni ? 1u : 0u);
-                        n_edge += nL + nR;
-                    }
-                    for (uint32_t k = 0; k < nL + nR; ++k)
-                    {
-                        const bool right = k >= nL;
-                        edge_candidate(t, right ? R - ni : L - ni, right ? k - nL : k,
-                                       (right ? Rinfo : Linfo) & kLeafRankMask, p, flip, best, best_key, best_edge);
-                    }
+                    n_leaf += (hitL && L >= ni ? 1u : 0u) + (hitR && R >= ni ? 1u : 0u);
+                    n_edge += nL + nR;
                 }
-                else
+                for (uint32_t k = 0; k < nL + nR; ++k)
                 {
-                    if (hitL && L >= ni)
-                    {
-                        leaf_silhouette_info(t, L - ni, Linfo, p, flip, best, best_key, best_edge, n_edge);
-                        if (kStats)
-                            ++n_leaf;
-                    }
-                    if (hitR && R >= ni)
-                    {
-                        leaf_silhouette_info(t, R - ni, Rinfo, p, flip, best, best_key, best_edge, n_edge);
-                        if (kStats)
-                            ++n_leaf;
-                    }
+                    const bool right = k >= nL;
+                    edge_candidate(t, right ? R - ni : L - ni, right ? k - nL : k,
+                                   (right ? Rinfo : Linfo) & kLeafRankMask, p, flip, best, best_key, best_edge);
                 }
             }
             const float b2n = best * best;
