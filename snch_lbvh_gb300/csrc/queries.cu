@@ -74,8 +74,30 @@ SNCH_DEV Box load_root_box(const Box *p)
     return b;
 }
 
+// Query inputs are read once and results written once: with streaming hints
+// (ld.global.cs / st.global.cs) their lines leave L2 first, and the tree
+// records the traversals re-read stay cached longer.
+#ifndef SNCH_STREAM_HINTS
+#define SNCH_STREAM_HINTS 1
+#endif
+constexpr bool kStreamHints = SNCH_STREAM_HINTS != 0;
+template <typename T>
+SNCH_DEV T ld_in(const T *p)
+{
+    return kStreamHints ? __ldcs(p) : __ldg(p);
+}
+template <typename T>
+SNCH_DEV void st_out(T *p, T v)
+{
+    if (kStreamHints)
+        __stcs(p, v);
+    else
+        *p = v;
+}
 SNCH_DEV f3 load_point(const float *__restrict__ p, int64_t q)
 {
+    if (kStreamHints)
+        return mk(__ldcs(p + 3 * q), __ldcs(p + 3 * q + 1), __ldcs(p + 3 * q + 2));
     return mk(__ldg(p + 3 * q), __ldg(p + 3 * q + 1), __ldg(p + 3 * q + 2));
 }
 
@@ -490,7 +512,7 @@ __global__ void __launch_bounds__(128) silhouette_kernel(TreeView t, const float
         return;
     const int64_t q = query_index(t, qi);
     const f3 p = load_point(pts, q);
-    const bool flip = flips ? __ldg(flips + q) != 0 : false;
+    const bool flip = flips ? ld_in(flips + q) != 0 : false;
     float best = seed.radius ? __ldg(seed.radius + q) : INFINITY;
     int32_t best_edge = -1;
     const uint32_t ni = t.num_tris - 1;
@@ -766,8 +788,8 @@ __global__ void __launch_bounds__(kBlock, 1280 / kBlock) nearest_fast_kernel(Tre
     const bool failed = seed.radius && nearest == kInvalid && r0 < INFINITY;
     if (seed.radius && nearest == kInvalid)
         best = INFINITY;  // nothing within the seed radius: the fallback pass answers it
-    out_idx[out_pos(t, qi, q)] = nearest == kInvalid ? kInvalid : nearest - qr.tri_off;
-    out_dist[out_pos(t, qi, q)] = sqrtf(best);
+    st_out(out_idx + out_pos(t, qi, q), nearest == kInvalid ? kInvalid : nearest - qr.tri_off);
+    st_out(out_dist + out_pos(t, qi, q), sqrtf(best));
     if (seed.fail_flag)
         seed.fail_flag[q] = failed ? 1u : 0u;
 }
@@ -878,7 +900,7 @@ __global__ void __launch_bounds__(kBlock, 1152 / kBlock) silhouette_fast_kernel(
         return;
     const int64_t q = query_index(t, qi);
     const f3 p = load_point(pts, q);
-    const bool flip = flips ? __ldg(flips + q) != 0 : false;
+    const bool flip = flips ? ld_in(flips + q) != 0 : false;
     const float r0 = seed.radius ? __ldg(seed.radius + q) : INFINITY;
     float best = r0;
     uint32_t best_key = 0;
@@ -995,9 +1017,9 @@ __global__ void __launch_bounds__(kBlock, 1152 / kBlock) silhouette_fast_kernel(
     const bool failed = seed.radius && best_edge < 0 && r0 < INFINITY;
     if (seed.radius && best_edge < 0)
         best = INFINITY;  // nothing within the seed radius: the fallback pass answers it
-    out_dist[out_pos(t, qi, q)] = best;
+    st_out(out_dist + out_pos(t, qi, q), best);
     if (out_edge)
-        out_edge[out_pos(t, qi, q)] = best_edge < 0 ? best_edge : best_edge - qr.edge_off;
+        st_out(out_edge + out_pos(t, qi, q), best_edge < 0 ? best_edge : best_edge - qr.edge_off);
     if (seed.fail_flag)
         seed.fail_flag[q] = failed ? 1u : 0u;
     if (kStats)
@@ -1283,8 +1305,8 @@ __global__ void __launch_bounds__(128, SNCH_WIDE_MIN_BLOCKS)
     const bool failed = seed.radius && nearest == kInvalid && r0 < INFINITY;
     if (seed.radius && nearest == kInvalid)
         best = INFINITY;  // nothing within the seed radius: the fallback pass answers it
-    out_idx[out_pos(t, qi, q)] = nearest == kInvalid ? kInvalid : nearest - qr.tri_off;
-    out_dist[out_pos(t, qi, q)] = sqrtf(best);
+    st_out(out_idx + out_pos(t, qi, q), nearest == kInvalid ? kInvalid : nearest - qr.tri_off);
+    st_out(out_dist + out_pos(t, qi, q), sqrtf(best));
     if (seed.fail_flag)
         seed.fail_flag[q] = failed ? 1u : 0u;
 }
@@ -1302,7 +1324,7 @@ __global__ void __launch_bounds__(128, SNCH_WIDE_MIN_BLOCKS)
         return;
     const int64_t q = query_index(t, qi);
     const f3 p = load_point(pts, q);
-    const bool flip = flips ? __ldg(flips + q) != 0 : false;
+    const bool flip = flips ? ld_in(flips + q) != 0 : false;
     const float r0 = seed.radius ? __ldg(seed.radius + q) : INFINITY;
     float best = r0;
     uint32_t best_key = 0;
@@ -1406,9 +1428,9 @@ __global__ void __launch_bounds__(128, SNCH_WIDE_MIN_BLOCKS)
     const bool failed = seed.radius && best_edge < 0 && r0 < INFINITY;
     if (seed.radius && best_edge < 0)
         best = INFINITY;  // nothing within the seed radius: the fallback pass answers it
-    out_dist[out_pos(t, qi, q)] = best;
+    st_out(out_dist + out_pos(t, qi, q), best);
     if (out_edge)
-        out_edge[out_pos(t, qi, q)] = best_edge < 0 ? best_edge : best_edge - qr.edge_off;
+        st_out(out_edge + out_pos(t, qi, q), best_edge < 0 ? best_edge : best_edge - qr.edge_off);
     if (seed.fail_flag)
         seed.fail_flag[q] = failed ? 1u : 0u;
     if (kStats)
@@ -1655,8 +1677,8 @@ SNCH_DEV void nearest_packet_chunk(const TreeView &t, const float *__restrict__ 
     const bool failed = seed.radius && nearest == kInvalid && r0 < INFINITY;
     if (seed.radius && nearest == kInvalid)
         best = INFINITY;  // nothing within the seed radius: the fallback pass answers it
-    out_idx[out_pos(t, qi, q)] = nearest == kInvalid ? kInvalid : nearest - qr.tri_off;
-    out_dist[out_pos(t, qi, q)] = sqrtf(best);
+    st_out(out_idx + out_pos(t, qi, q), nearest == kInvalid ? kInvalid : nearest - qr.tri_off);
+    st_out(out_dist + out_pos(t, qi, q), sqrtf(best));
     if (seed.fail_flag)
         seed.fail_flag[q] = failed ? 1u : 0u;}
 
@@ -1805,7 +1827,7 @@ SNCH_DEV void silhouette_packet_chunk(const TreeView &t, const float *__restrict
         return;
     const int64_t q = valid ? query_index(t, qi) : 0;
     const f3 p = valid ? load_point(pts, q) : mk(0.0f, 0.0f, 0.0f);
-    const bool flip = valid && flips ? __ldg(flips + q) != 0 : false;
+    const bool flip = valid && flips ? ld_in(flips + q) != 0 : false;
     const float r0 = valid && seed.radius ? __ldg(seed.radius + q) : INFINITY;
     float best = r0;
     uint32_t best_key = 0, n_int = 0, n_leaf = 0, n_edge = 0;
@@ -1939,9 +1961,9 @@ SNCH_DEV void silhouette_packet_chunk(const TreeView &t, const float *__restrict
     const bool failed = seed.radius && best_edge < 0 && r0 < INFINITY;
     if (seed.radius && best_edge < 0)
         best = INFINITY;  // nothing within the seed radius: the fallback pass answers it
-    out_dist[out_pos(t, qi, q)] = best;
+    st_out(out_dist + out_pos(t, qi, q), best);
     if (out_edge)
-        out_edge[out_pos(t, qi, q)] = best_edge < 0 ? best_edge : best_edge - qr.edge_off;
+        st_out(out_edge + out_pos(t, qi, q), best_edge < 0 ? best_edge : best_edge - qr.edge_off);
     if (seed.fail_flag)
         seed.fail_flag[q] = failed ? 1u : 0u;
     if (kStats)
@@ -2408,7 +2430,7 @@ SNCH_DEV void ray_query(const TreeView &t, const float *__restrict__ origins, co
     const int64_t q = query_index(t, qi);
     const f3 o = load_point(origins, q), dir = load_point(dirs, q);
     const f3 inv = mk(1 / dir.x, 1 / dir.y, 1 / dir.z);  // ray ctor aabb.cuh:305-312
-    const float max_dist = __ldg(tmaxs + q);
+    const float max_dist = ld_in(tmaxs + q);
     float min_dist = INFINITY, bu = 0.0f, bv = 0.0f;
     bool found = false;
     uint32_t nearest = kInvalid;
@@ -2498,13 +2520,13 @@ SNCH_DEV void ray_query(const TreeView &t, const float *__restrict__ origins, co
             nd = sd[sp];
         }
     }
-    out_hit[out_pos(t, qi, q)] = found ? 1 : 0;
+    st_out(out_hit + out_pos(t, qi, q), (uint8_t)(found ? 1 : 0));
     if (kAny)
         return;
-    out_t[out_pos(t, qi, q)] = min_dist;
-    out_uv[2 * out_pos(t, qi, q)] = bu;
-    out_uv[2 * out_pos(t, qi, q) + 1] = bv;
-    out_idx[out_pos(t, qi, q)] = nearest;
+    st_out(out_t + out_pos(t, qi, q), min_dist);
+    st_out(out_uv + 2 * out_pos(t, qi, q), bu);
+    st_out(out_uv + 2 * out_pos(t, qi, q) + 1, bv);
+    st_out(out_idx + out_pos(t, qi, q), nearest);
     if (kStats)
     {
         stats[3 * q] = n_int;
@@ -2598,7 +2620,7 @@ __global__ void __launch_bounds__(128) ray_persistent_kernel(TreeView t, const f
             o = load_point(origins, q);
             dir = load_point(dirs, q);
             inv = mk(1 / dir.x, 1 / dir.y, 1 / dir.z);  // ray ctor aabb.cuh:305-312
-            max_dist = __ldg(tmaxs + q);
+            max_dist = ld_in(tmaxs + q);
             min_dist = INFINITY;
             bu = bv = 0.f;
             found = false;
@@ -2817,8 +2839,8 @@ __global__ void __launch_bounds__(128) sample_kernel(TreeView t, const float *__
         return;
     const int64_t q = query_index(t, qi);
     const f3 c = load_point(centers, q);
-    const float rad = __ldg(radii + q);
-    float u = __ldg(us + q);
+    const float rad = ld_in(radii + q);
+    float u = ld_in(us + q);
     int32_t oi = -1;
     float opdf = 0.0f;
     const uint32_t ni = t.num_tris - 1;
@@ -2871,8 +2893,8 @@ __global__ void __launch_bounds__(128) sample_kernel(TreeView t, const float *__
             }
         }
     }
-    out_idx[out_pos(t, qi, q)] = oi;
-    out_pdf[out_pos(t, qi, q)] = opdf;
+    st_out(out_idx + out_pos(t, qi, q), oi);
+    st_out(out_pdf + out_pos(t, qi, q), opdf);
     if (kStats)
     {
         stats[3 * q] = n_int;
@@ -2899,7 +2921,7 @@ __global__ void sample_point_kernel(const float *__restrict__ verts, const int32
     }
     const int32_t *tr = tris + 3 * (int64_t)k;
     const f3 pa = load_vert(verts, __ldg(tr)), pb = load_vert(verts, __ldg(tr + 1)), pc = load_vert(verts, __ldg(tr + 2));
-    float u = __ldg(us + q), v = __ldg(vs + q);
+    float u = ld_in(us + q), v = __ldg(vs + q);
     if (u + v > 1.0f)
     {
         u = 1.0f - u;
