@@ -25,6 +25,7 @@ walk-on-stars trace.
 from __future__ import annotations
 
 import argparse
+import gc
 import json
 import math
 import os
@@ -994,11 +995,19 @@ def run_ours(args):
         del probe
         e2e_steps = max(1, min(args.steps, 5))
         e2e_step()
+        # Python's cyclic garbage collector off while the host-form calls are timed
+        # (as timeit does): a full collection over this process's objects can pause
+        # the calling thread for milliseconds between two enqueues
+        gc.collect()
+        gc.disable()
         barrier()
         t0 = time.perf_counter()
-        for _ in range(e2e_steps):
-            e2e_step()
-        barrier()
+        try:
+            for _ in range(e2e_steps):
+                e2e_step()
+            barrier()
+        finally:
+            gc.enable()
         e2e_s = time.perf_counter() - t0
         e2e_s = max_over_ranks(e2e_s, "cuda")
         h2d = sc.verts.nbytes + sc.faces.nbytes + sum(v.nbytes for v in q.values())
@@ -1012,8 +1021,9 @@ def run_ours(args):
                "phase_ms": dict(zip(["create+build", "near", "sil", "ray", "smp", "close"],
                                     np.round(np.mean(e2e_parts[1:], 0), 2).tolist())),
                "step_phase_ms": [np.round(p, 2).tolist() for p in e2e_parts[1:]],
-               "note": "scene upload + build + snch_*_host queries from pinned host memory, wall clock; "
-                       "answers compared bit for bit with the device forms' answers of the timed step"}
+               "note": "scene upload + build + snch_*_host queries from pinned host memory, wall clock, "
+                       "Python's garbage collector off while timed; answers compared bit for bit with the "
+                       "device forms' answers of the timed step"}
 
     if rank != 0:
         if ws > 1:
