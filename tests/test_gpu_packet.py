@@ -121,3 +121,39 @@ def test_packet_batched_and_seeded(snch):
     np.testing.assert_array_equal(bits(sd1.cpu().numpy()), bits(sd0.cpu().numpy()))
     check_edge_ids(se1.cpu().numpy(), se0.cpu().numpy(), sd0.cpu().numpy(), q, sc.verts, s.export_topology()[2])
     assert s.device_status() == 0
+
+
+@pytest.mark.parametrize("n", [1, 31, 32, 33, 1025, 2 * 32 * 32 + 7, 70_001])
+def test_pooled_persistent_kernels_at_small_sizes(snch, n):
+    """The persistent packet searches and the pooled rays forced on at any size
+    (SNCH_OPT_PACKET_PERSISTENT_MIN = 1): batches smaller than one pool chunk, a
+    partly filled last packet and last chunk give the per-lane searches'
+    answers (nearest, silhouette, closest hit, occlusion) on the config-1 sphere,
+    and every warp stops (no work-timeout status)."""
+    from snch_lbvh_gb300 import meshes
+    v, f = meshes.noisy_icosphere(5, 1.0, 0.01, seed=0)
+    s = built_scene(snch, v, f)
+    rng = np.random.default_rng(n)
+    pts = meshes.box_queries(v, n, 1.2, seed=n)
+    flip = (rng.random(n) < 0.5).astype(np.uint8)
+    d = rng.standard_normal((n, 3)).astype(np.float32)
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    tmax = np.full(n, 3.0, np.float32)
+
+    def run():
+        i, nd = s.query_nearest(pts)
+        sd, se = s.query_silhouette(pts, flip)
+        h, t, uv, ri = s.query_ray(pts, d, tmax)
+        occ = s.query_ray_test(pts, d, tmax)
+        return [x.cpu().numpy() for x in (i, nd, sd, se, h, t, uv, ri, occ)]
+
+    s.set_option(snch.OPT_PACKET, 0)
+    base = run()
+    s.set_option(snch.OPT_PACKET, 1)
+    s.set_option(snch.OPT_PACKET_PERSISTENT_MIN, 1)
+    got = run()
+    assert s.device_status() == 0
+    for k in (1, 2, 4, 5, 6, 7, 8):  # distances, ray hit / t / uv / triangle, occlusion
+        np.testing.assert_array_equal(got[k].view(np.uint8), base[k].view(np.uint8))
+    check_tri_ids(got[0], base[0], base[1].view(np.float32), pts, v, f)
+    check_edge_ids(got[3], base[3], base[2].view(np.float32), pts, v, s.export_topology()[2])
