@@ -70,6 +70,9 @@ def parse():
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-meshes leg")
     ap.add_argument("--no-wost", action="store_true", help="skip the walk-on-stars leg")
     ap.add_argument("--no-icosphere", action="store_true", help="skip the 20,480-triangle icosphere leg")
+    ap.add_argument("--no-sort", action="store_true", help="skip the radix-sort leg")
+    ap.add_argument("--sort-only", action="store_true",
+                    help="run only the radix-sort leg (16M pairs) and print its object (for profiling)")
     ap.add_argument("--output-scatter", type=int, default=-1, choices=[-1, 0, 1],
                     help="SNCH_OPT_OUTPUT_SCATTER of the step's scene (-1: the library default)")
     ap.add_argument("--top-levels", type=int, default=-1,
@@ -173,6 +176,50 @@ class ClockSampler:
         reasons = sorted({names[i] for r in self.rows if len(r) >= 9 for i in range(4) if r[5 + i] == "Active"})
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
                 "reasons": reasons, "samples": len(sm)}
+
+
+# --------------------------------------------------------------------- radix sort
+def sort_leg(reps=6):
+    """The onesweep radix sort alone (row a3: the build's Morton sort and each
+    query batch's Morton ordering), through snch_sort_pairs on 16M random
+    (key, value) uint32 pairs: 24-bit keys (the query-order width, 3 passes) and
+    30-bit keys (the build's Morton codes, 4 passes); event-timed median. Bytes
+    counted: the histogram pass reads the keys (4 B per pair), each digit pass
+    reads and writes key and value (16 B per pair), and a sort with an odd pass
+    count copies the pairs back (16 B per pair)."""
+    import ctypes as C
+    import torch
+    import snch_lbvh_gb300 as snch
+    L = snch.lib()
+    n = 16_000_000
+    peak, _ = hbm_peak()
+    gen = torch.Generator(device="cuda").manual_seed(11)
+    raw = torch.randint(0, 2**31 - 1, (n,), dtype=torch.int64, device="cuda", generator=gen)
+    vals = torch.arange(n, dtype=torch.int32, device="cuda")
+    kt, vt = torch.empty_like(vals), torch.empty_like(vals)
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    res = {"pairs": n}
+    for bits in (24, 30):
+        keys = (raw & ((1 << bits) - 1)).to(torch.int32)
+        scratch = torch.empty(L.snch_sort_scratch_bytes(n, bits), dtype=torch.uint8, device="cuda")
+        ts = []
+        for _ in range(reps + 2):
+            kk, vv = keys.clone(), vals.clone()
+            a, z = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            snch.check(L.snch_sort_pairs(C.c_void_p(kk.data_ptr()), C.c_void_p(vv.data_ptr()),
+                                         C.c_void_p(kt.data_ptr()), C.c_void_p(vt.data_ptr()), n, bits,
+                                         C.c_void_p(scratch.data_ptr()), C.c_void_p(status.data_ptr()), None))
+            z.record()
+            torch.cuda.synchronize()
+            ts.append(a.elapsed_time(z))
+        ms = float(np.median(ts[2:]))
+        passes = (bits + 7) // 8
+        byts = n * (4 + 16 * passes + (16 if passes % 2 else 0))
+        ok = bool((kk[1:].to(torch.int64) >= kk[:-1].to(torch.int64)).all()) and int(status.item()) == 0
+        res[f"bits{bits}"] = {"ms": ms, "passes": passes, "GB/s": byts / ms / 1e6, "frac": byts / ms / 1e6 / peak,
+                              "sorted": ok}
+    return res
 
 
 # --------------------------------------------------------------------- peaks
@@ -929,7 +976,9 @@ def run_ours(args):
         learned["status"] = int(scene.device_status())
 
     # ---- icosphere, batched meshes and walk-on-stars (single GPU only; outside the timed step)
-    batched = wost_res = ico = None
+    batched = wost_res = ico = sort_res = None
+    if ws == 1 and not args.no_sort:
+        sort_res = sort_leg()
     if ws == 1 and not args.no_icosphere:
         ico = icosphere_leg(args.scale)
     if ws == 1 and not args.no_batched:
@@ -1090,6 +1139,7 @@ def run_ours(args):
         "e2e": e2e,
         "learned": learned,
         "icosphere": ico,
+        "sort": sort_res,
         "batched": batched,
         "wost": wost_res,
     }
@@ -1112,6 +1162,8 @@ def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.sort_only:
+        print(json.dumps({"sort": sort_leg()}), flush=True)
     else:
         run_ours(args)
 

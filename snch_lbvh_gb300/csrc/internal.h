@@ -197,12 +197,20 @@ cudaError_t scan_flags(const uint32_t *in, uint32_t *out, uint32_t n, uint32_t *
 // Stable LSD radix sort of (key, value) pairs on the low key_bits bits,
 // onesweep style: one histogram pass then one scatter pass per 8-bit digit.
 // Data ping-pongs between (keys, vals) and (keys_tmp, vals_tmp); the result
-// is written back to (keys, vals). If hist is non-null it already holds the
-// per-pass digit counts (passes x 256) and the histogram pass is skipped.
+// is written back to (keys, vals), unless result is non-null: then *result
+// receives the buffer pair that holds it ((keys, vals) or (keys_tmp,
+// vals_tmp), after an odd number of passes) and nothing is copied back. If
+// hist is non-null it already holds the per-pass digit counts (passes x 256)
+// and the histogram pass is skipped.
 constexpr int kSortTile = 4096;
 size_t sort_scratch_bytes(uint32_t n, int key_bits);
+struct SortResult
+{
+    uint32_t *keys, *vals;
+};
 cudaError_t radix_sort_pairs(uint32_t *keys, uint32_t *vals, uint32_t *keys_tmp, uint32_t *vals_tmp, uint32_t n,
-                             int key_bits, const uint32_t *hist, void *scratch, uint32_t *status, cudaStream_t st);
+                             int key_bits, const uint32_t *hist, void *scratch, uint32_t *status, cudaStream_t st,
+                             SortResult *result = nullptr);
 inline int sort_passes(int key_bits) { return (key_bits + 7) / 8; }
 
 // ---- topology.cu (scene.cuh:1135-1225 on the device)

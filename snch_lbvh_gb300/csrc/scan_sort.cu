@@ -155,6 +155,9 @@ __global__ void radix_hist_kernel(const uint32_t *__restrict__ keys, uint32_t n,
 // rounds of 32 with __match_any_sync, which keeps equal digits in input order;
 // the block then stages the tile in shared memory in digit order and writes
 // each digit run to its global position.
+// (The compiler's 80 registers allow 3 blocks per SM. Compiled for 4 or 5 blocks,
+// with the largest shared-memory carveout so that the 42 KB of shared memory
+// per block fit, the 16M-pair sort took 0.576 / 0.586 against 0.570 ms.)
 __global__ void __launch_bounds__(kThreads) onesweep_pass_kernel(
     const uint32_t *__restrict__ keys_in, const uint32_t *__restrict__ vals_in, uint32_t *__restrict__ keys_out,
     uint32_t *__restrict__ vals_out, uint32_t n, int shift, const uint32_t *__restrict__ hist, uint32_t *lookback,
@@ -260,6 +263,7 @@ __global__ void __launch_bounds__(kThreads) onesweep_pass_kernel(
 
 inline uint32_t num_tiles(uint64_t n) { return (uint32_t)((n + kSortTile - 1) / kSortTile); }
 
+
 }  // namespace
 
 size_t scan_flags_scratch_bytes(uint64_t n) { return 4 * (size_t)(num_tiles(n) + 1); }
@@ -288,8 +292,11 @@ size_t sort_scratch_bytes(uint32_t n, int key_bits)
 }
 
 cudaError_t radix_sort_pairs(uint32_t *keys, uint32_t *vals, uint32_t *keys_tmp, uint32_t *vals_tmp, uint32_t n,
-                             int key_bits, const uint32_t *hist, void *scratch, uint32_t *status, cudaStream_t st)
+                             int key_bits, const uint32_t *hist, void *scratch, uint32_t *status, cudaStream_t st,
+                             SortResult *result)
 {
+    if (result)
+        *result = SortResult{keys, vals};
     if (n <= 1)
         return cudaSuccess;
     const int passes = sort_passes(key_bits);
@@ -321,7 +328,9 @@ cudaError_t radix_sort_pairs(uint32_t *keys, uint32_t *vals, uint32_t *keys_tmp,
         vo = t;
     }
     e = cudaGetLastError();
-    if (e == cudaSuccess && ki != keys)
+    if (result)
+        *result = SortResult{ki, vi};
+    else if (e == cudaSuccess && ki != keys)
     {
         e = cudaMemcpyAsync(keys, ki, 4 * (size_t)n, cudaMemcpyDeviceToDevice, st);
         if (e == cudaSuccess)
