@@ -190,9 +190,12 @@ int snch_set_traversal(snch_scene_t scene, int mode);
 
 /* Scene options (snch_set_option):
  *   SNCH_OPT_TRAVERSAL        SNCH_TRAVERSAL_NEAR_FIRST (default) / _REFERENCE_ORDER
- *   SNCH_OPT_QUERY_ORDER      1 (default): batches are answered in the Morton order
- *                             of their query points (results still land at their
- *                             input positions and do not change); 0: input order
+ *   SNCH_OPT_QUERY_ORDER      1 (default): nearest, silhouette and ray batches are
+ *                             answered in the Morton order of their query points
+ *                             (results still land at their input positions and do not
+ *                             change); 0: input order. Sphere draws always run in input
+ *                             order: their single descent gains less from the order
+ *                             than the sort costs (4M draws: 0.77 ms against 0.93).
  *   SNCH_OPT_ORDER_MIN_BATCH  smallest batch that is reordered (default 65536) */
 #define SNCH_OPT_TRAVERSAL 1
 #define SNCH_OPT_QUERY_ORDER 2

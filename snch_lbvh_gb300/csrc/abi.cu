@@ -632,7 +632,7 @@ struct BatchView
     }
 };
 cudaError_t batch_view(const snch_scene_s *s, const float *keys_from, int64_t n, cudaStream_t st, BatchView &b,
-                       const uint32_t *query_mesh = nullptr, const float *ray_len = nullptr)
+                       const uint32_t *query_mesh = nullptr, const float *ray_len = nullptr, bool ordered = true)
 {
     b.t = s->view();
     b.st = st;
@@ -646,7 +646,7 @@ cudaError_t batch_view(const snch_scene_s *s, const float *keys_from, int64_t n,
         b.t.num_meshes = s->num_meshes;
         b.t.near_first = 1;
     }
-    if (!s->query_order || n < s->order_min || n >= (int64_t(1) << 30) || s->num_tris < 2)
+    if (!ordered || !s->query_order || n < s->order_min || n >= (int64_t(1) << 30) || s->num_tris < 2)
         return cudaSuccess;
     cudaError_t e = scratch_alloc(&b.scratch, query_order_scratch_bytes(n), st);
     if (e != cudaSuccess)
@@ -1424,8 +1424,11 @@ int snch_sample_in_sphere(snch_scene_t s, const float *c, const float *r, const 
         rc = check_n(n, {c, r, u, idx, pdf});
     if (rc != SNCH_OK)
         return rc;
+    // sphere draws run in input order: a draw is one short descent, and the
+    // Morton sort costs more than the coherence it gives (4M draws on the
+    // 2M-triangle scene: 0.77 ms unordered, 0.93 ms sorted first)
     BatchView b;
-    SNCH_CUDA(batch_view(s, c, n, S(stream), b));
+    SNCH_CUDA(batch_view(s, c, n, S(stream), b, nullptr, nullptr, false));
     SNCH_CUDA(launch_sample(b.t, c, r, u, n, idx, pdf, S(stream)));
     return SNCH_OK;
 }
@@ -1521,7 +1524,7 @@ int snch_sample_in_sphere_host(snch_scene_t s, const float *c, const float *r, c
     return run_host_pipeline(s, n, kHostChunkRay, ins, 3, outs, 2,
                              [&](int64_t m, void **di, void **dout, cudaStream_t st) {
         BatchView b;
-        cudaError_t e = batch_view(s, (const float *)di[0], m, st, b);
+        cudaError_t e = batch_view(s, (const float *)di[0], m, st, b, nullptr, nullptr, false);
         return e != cudaSuccess ? e : launch_sample(b.t, (const float *)di[0], (const float *)di[1],
                                                     (const float *)di[2], m, (int32_t *)dout[0], (float *)dout[1], st);
     });
