@@ -881,12 +881,6 @@ SNCH_DEV void leaf_silhouette_info(const TreeView &t, uint32_t pos, uint32_t inf
         edge_candidate(t, pos, k, rank, o, flip, best, best_key, best_edge);
 }
 
-// The silhouette packets run the leaf work of a node's two children as one loop
-// of edge_candidate calls (the left leaf's edges, then the right leaf's, per
-// lane: the same order as two leaf_silhouette_info calls), so a lane with only
-// the right leaf to test runs in the same iterations as a lane with only the
-// left one (16M queries of the 2M-triangle scene: 35.61 against 35.78 ms).
-
 template <bool kStats, int kBlock = 128>
 __global__ void __launch_bounds__(kBlock, 1152 / kBlock) silhouette_fast_kernel(TreeView t, const float *__restrict__ pts,
                                                               const uint8_t *__restrict__ flips, int64_t n,
@@ -1518,7 +1512,6 @@ __device__ __noinline__ unsigned long long take_packet(unsigned long long *work,
     return p < total_packets ? p : ~0ull;
 }
 
-
 // per-lane start of a packet: lanes of a batched query set may search
 // different meshes; the warp runs one packet per distinct root
 struct PacketLane
@@ -1759,9 +1752,9 @@ inline size_t top_smem_bytes(uint32_t slots, bool cones)
     return (size_t)slots * (sizeof(InnerRec) + (cones ? sizeof(InnerConeRec) : 0));
 }
 
-// the same packets, persistent: each warp takes the next 32 queries of the
-// batch from a batch-wide counter when its packet is done, so no warp slot
-// waits for the slowest packet of its block. kTop: the top tree levels are read
+// the same packets, persistent: each warp takes its next packet (32 queries
+// of the batch) from its SM's pool (take_packet) when its packet is done, so no
+// warp slot waits for the slowest packet of its block. kTop: the top tree levels are read
 // from a shared-memory copy (dynamic shared memory, top_smem_bytes).
 // blocks per SM the persistent nearest packet kernel is compiled for (at least
 // 7: the compiler then takes 63 registers, so 8 blocks fit; measured on
@@ -1894,7 +1887,11 @@ SNCH_DEV void silhouette_packet_chunk(const TreeView &t, const float *__restrict
                 const float b2 = best * best;
                 hitL = Lmd <= b2 && lc.half_angle >= 0.0f && cone_test(lc, p, lb, Lmd);
                 hitR = Rmd <= b2 && rc.half_angle >= 0.0f && cone_test(rc, p, rb, Rmd);
-                // both leaf children's edges in one loop (see edge_candidate)
+                // the leaf work of both children as one loop of edge_candidate calls
+                // (the left leaf's edges, then the right leaf's, per lane: the order of
+                // two leaf_silhouette_info calls), so a lane with only the right leaf
+                // to test runs in the same iterations as a lane with only the left one
+                // (16M queries of the 2M-triangle scene: 35.61 against 35.78 ms)
                 const uint32_t nL = hitL && L >= ni ? Linfo >> 30 : 0u;
                 const uint32_t nR = hitR && R >= ni ? Rinfo >> 30 : 0u;
                 if (kStats)
