@@ -263,7 +263,6 @@ __global__ void __launch_bounds__(kThreads) onesweep_pass_kernel(
 
 inline uint32_t num_tiles(uint64_t n) { return (uint32_t)((n + kSortTile - 1) / kSortTile); }
 
-
 }  // namespace
 
 size_t scan_flags_scratch_bytes(uint64_t n) { return 4 * (size_t)(num_tiles(n) + 1); }
