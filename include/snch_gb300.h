@@ -152,10 +152,13 @@ int snch_obj_read(const char *path, float *verts, int64_t vert_capacity, int32_t
 int snch_scene_save(snch_scene_t scene, const char *path, snch_stream_t stream);
 int snch_scene_load(const char *path, snch_scene_t *out_scene, snch_stream_t stream);
 
-/* ~scene: frees every device buffer of the scene. */
+/* ~scene<3>: frees every device buffer of the scene (the reference's scene owns
+ * its device vectors and a unique_ptr to its bvh, scene.cuh:1254-1268). */
 int snch_scene_destroy(snch_scene_t scene);
 
-/* Sizes (synchronises the scene's build stream for num_edges). */
+/* Sizes: vertices_h.size(), indices_h.size() and silhouettes_h.size() of the
+ * reference's scene (scene.cuh:1255-1264); synchronises the scene's build
+ * stream for num_edges. */
 int snch_scene_info(snch_scene_t scene, int64_t *num_vertices, int64_t *num_triangles, int64_t *num_edges);
 /* The scene's DEVICE vertex buffer (3 floats per vertex, the scene's own copy;
  * no reference counterpart): a caller that moves the vertices writes them here
@@ -164,18 +167,27 @@ int snch_scene_info(snch_scene_t scene, int64_t *num_vertices, int64_t *num_tria
 int snch_scene_vertices(snch_scene_t scene, float **out_device_xyz);
 
 /* Device status word of the scene (OR of SNCH_DEVICE_* bits set by its
- * kernels since the last reset); synchronises the given stream. */
+ * kernels since the last reset); synchronises the given stream. No reference
+ * counterpart: the reference's device code has asserts only, while these
+ * kernels finish every bounded wait and report here instead. */
 int snch_get_device_status(snch_scene_t scene, uint32_t *out_bits, int reset, snch_stream_t stream);
 
-/* Thread-local description of the last failure. */
+/* Thread-local description of the last failure: the message the reference
+ * throws as an exception ("BVH is not built yet.", scene.cuh:1250; Thrust's
+ * system_error on a CUDA failure), returned here since no exception crosses
+ * the C ABI. */
 const char *snch_last_error(void);
 
-/* Copies of the build products into caller DEVICE buffers (parity checks):
- * morton codes sorted (N), sorted original indices (N), nodes ((2N-1)*4),
- * aabbs ((2N-1)*6), cones ((2N-1)*5); any pointer may be NULL. */
+/* Copies of the build products into caller DEVICE buffers (parity checks; the
+ * reference's bvh keeps them as its device vectors, bvh.cuh:624-633, and its
+ * sort inputs, bvh.cuh:436-454): morton codes sorted (N), sorted original
+ * indices (N), nodes ((2N-1)*4), aabbs ((2N-1)*6), cones ((2N-1)*5); any
+ * pointer may be NULL. */
 int snch_export_tree(snch_scene_t scene, uint32_t *sorted_morton, uint32_t *sorted_indices, uint32_t *nodes,
                      float *aabbs, float *cones, snch_stream_t stream);
-/* tri_edges (N*3), tri_owned (N*3), edge_verts (E*4) into caller DEVICE buffers. */
+/* The silhouette topology (compute_silhouettes, scene.cuh:1135-1229: each
+ * triangle's edge ids, its owned edges, each edge's 4 vertex ids) into caller
+ * DEVICE buffers: tri_edges (N*3), tri_owned (N*3), edge_verts (E*4). */
 int snch_export_topology(snch_scene_t scene, int32_t *tri_edges, int32_t *tri_owned, int32_t *edge_verts,
                          snch_stream_t stream);
 
@@ -188,7 +200,9 @@ int snch_export_topology(snch_scene_t scene, int32_t *tri_edges, int32_t *tri_ow
 #define SNCH_TRAVERSAL_REFERENCE_ORDER 1
 int snch_set_traversal(snch_scene_t scene, int mode);
 
-/* Scene options (snch_set_option):
+/* Scene options (snch_set_option; no reference counterpart: the reference has
+ * one fixed search per query type, which the defaults reproduce result for
+ * result, and every option below changes only how fast an answer comes):
  *   SNCH_OPT_TRAVERSAL        SNCH_TRAVERSAL_NEAR_FIRST (default) / _REFERENCE_ORDER
  *   SNCH_OPT_QUERY_ORDER      1 (default): nearest, silhouette and ray batches are
  *                             answered in the Morton order of their query points
